@@ -1,0 +1,920 @@
+// bf_abi.cu -- the C ABI of include/bf_lbm.h: solver state, initialisation,
+// the per-step driver (LBM::_iterate_time / _collide / _stream /
+// _stream_thermal, BoltzmannFluids/Source/LBM/LBM.cpp:1484-1773) and readback.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/bf_lbm.h"
+#include "lbm_common.cuh"
+
+using namespace bf;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+#define BF_CUDA(call)                                                                          \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess)                                                                 \
+            return fail(e_ == cudaErrorMemoryAllocation ? BF_ERR_OUT_OF_MEMORY : BF_ERR_CUDA,  \
+                        std::string(#call " failed: ") + cudaGetErrorString(e_));              \
+    } while (0)
+
+constexpr int kMaxObjects = 256;  // ids 0..255 (LBM.h:29)
+constexpr int kGraphSteps = 16;   // steps per captured graph (even: the AA state has period 2)
+
+struct DeviceBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaError_t alloc(size_t n) {
+        release();
+        if (n == 0) return cudaSuccess;
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e == cudaSuccess) bytes = n; else p = nullptr;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+int q_of(int vs) {
+    switch (vs) {
+    case BF_D2Q9: return 9;
+    case BF_D3Q15: return 15;
+    case BF_D3Q19: return 19;
+    case BF_D3Q27: return 27;
+    }
+    return 0;
+}
+size_t storage_bytes(int st) { return st == BF_STORE_FP32 ? 4 : 2; }
+
+// LBM.cpp:569 / :606: bits per id = exp2(ceil(log2(ceil(log2(count))))), 0 for one object
+int bits_per_boundry(int count) {
+    if (count <= 1) return 0;
+    return (int)std::exp2(std::ceil(std::log2f(std::ceil(std::log2f((float)count)))));
+}
+
+}  // namespace
+
+struct bf_solver {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool initialized = false;
+    bf_init_desc desc{};
+    int Q = 0, QT = 0, dims = 0;
+    uint32_t N = 0;
+    // host copies of the object table (slot 0 = fluid)
+    std::vector<bf_object> objects;
+    // derived switches (LBM.cpp:523-556)
+    bool forcing = false, constant_force = true, thermal = false, boundaries = false;
+    float fconst[3] = {0, 0, 0};
+    int bits = 0;
+    size_t bnd_words = 0;
+    bool has_eq_objects = false;
+    // device memory
+    DeviceBuf lat[2], bnd, objs, kinds, force, bvals, th[2], psi[2];
+    DeviceBuf vel_den, force_temp, bnd_tex, partials, red_out, err, decode_tmp;
+    uint32_t n_blocks = 0;
+    // buffer roles (LBM.h:280-291)
+    int lat0_src = 1, th0_src = 1, psi0_src = 1;
+    int64_t ticks = 0;
+    bool last_saved = false;
+    // graphs keyed by the state that repeats every two steps
+    std::map<int, cudaGraphExec_t> graphs;
+    bool graphs_enabled = true;
+};
+
+namespace {
+
+void clear_graphs(bf_solver* s) {
+    for (auto& kv : s->graphs) cudaGraphExecDestroy(kv.second);
+    s->graphs.clear();
+}
+
+void release_all(bf_solver* s) {
+    clear_graphs(s);
+    DeviceBuf* bufs[] = {&s->lat[0], &s->lat[1], &s->bnd, &s->objs, &s->kinds, &s->force, &s->bvals,
+                         &s->th[0], &s->th[1], &s->psi[0], &s->psi[1], &s->vel_den, &s->force_temp,
+                         &s->bnd_tex, &s->partials, &s->red_out, &s->err, &s->decode_tmp};
+    for (auto* b : bufs) b->release();
+    s->initialized = false;
+}
+
+void* lat_src(bf_solver* s) { return s->lat[s->lat0_src ? 0 : 1].p; }
+void* lat_tgt(bf_solver* s) { return s->lat[s->lat0_src ? 1 : 0].p; }
+float* th_src(bf_solver* s) { return s->th[s->th0_src ? 0 : 1].as<float>(); }
+float* th_tgt(bf_solver* s) { return s->th[s->th0_src ? 1 : 0].as<float>(); }
+float* psi_src(bf_solver* s) { return s->psi[s->psi0_src ? 0 : 1].as<float>(); }
+float* psi_tgt(bf_solver* s) { return s->psi[s->psi0_src ? 1 : 0].as<float>(); }
+
+cudaError_t dispatch_step(bf_solver* s, const StepParams& p, int mode, bool generic) {
+    switch (s->Q) {
+    case 9: return launch_step<9>(p, s->desc.storage, mode, generic, s->stream);
+    case 15: return launch_step<15>(p, s->desc.storage, mode, generic, s->stream);
+    case 19: return launch_step<19>(p, s->desc.storage, mode, generic, s->stream);
+    case 27: return launch_step<27>(p, s->desc.storage, mode, generic, s->stream);
+    }
+    return cudaErrorInvalidValue;
+}
+
+uint32_t base_flags(bf_solver* s) {
+    uint32_t fl = 0;
+    if (s->desc.periodic[0]) fl |= F_PERIODIC_X;
+    if (s->desc.periodic[1]) fl |= F_PERIODIC_Y;
+    if (s->desc.periodic[2]) fl |= F_PERIODIC_Z;
+    if (s->boundaries) fl |= F_BOUNDARIES;
+    if (s->boundaries && s->desc.esoteric && s->desc.boundary_mode == BF_BOUNDARY_BOUNCE_BACK) fl |= F_BOUNCE_BACK;
+    if (s->forcing && s->constant_force) fl |= F_FORCE_CONST;
+    if (s->forcing && !s->constant_force) fl |= F_FORCE_FIELD;
+    if (s->thermal) fl |= F_THERMAL;
+    if (s->desc.multiphase) fl |= F_MULTIPHASE;
+    if (s->desc.collision == BF_COLLISION_TRT) fl |= F_TRT;
+    if (s->has_eq_objects) fl |= F_EQ_BOUNDARIES;
+    // collide.comp:609: the source term is compiled in with forcing, multiphase or thermal flow
+    if (s->forcing || s->desc.multiphase || s->thermal) fl |= F_SOURCE;
+    return fl;
+}
+
+void fill_constants(bf_solver* s, StepParams& p) {
+    // the reference's FP32 constants: cs = float(1/sqrt(3)) (LBM.cpp:1587)
+    const float cs = (float)(1.0 / std::sqrt(3.0));
+    const float cs2 = cs * cs, cs4 = cs2 * cs2;
+    const float tau = s->desc.relaxation_time;
+    p.inv_tau = 1.0f / tau;
+    p.src_pref = 1.0f - 1.0f / (2.0f * tau);
+    p.inv_cs2 = 1.0f / cs2;
+    p.half_inv_cs4 = 1.0f / (2.0f * cs4);
+    p.half_inv_cs2 = 1.0f / (2.0f * cs2);
+    p.inv_cs4 = 1.0f / cs4;
+    const float tau_minus = s->desc.trt_magic / (tau - 0.5f) + 0.5f;
+    p.trt_inv_tau_minus = 1.0f / tau_minus;
+    p.vlim = s->desc.velocity_limit;
+    p.vlim_ext = s->desc.velocity_limit_extreme;
+    p.fconst[0] = s->fconst[0]; p.fconst[1] = s->fconst[1]; p.fconst[2] = s->fconst[2];
+    p.inv_tau_t = 1.0f / s->desc.thermal_relaxation_time;
+    p.beta = s->desc.thermal_expansion_coefficient;
+    p.G = s->desc.intermolecular_interaction_strength;
+}
+
+// LBM::_collide (LBM.cpp:1557-1653): one launch of the fused AA step, then the swaps
+cudaError_t collide(bf_solver* s, bool save, bool update, bool reduce, bool measure) {
+    StepParams p{};
+    p.f = lat_src(s);
+    p.stride = s->N;
+    p.nx = s->desc.resolution[0]; p.ny = s->desc.resolution[1]; p.nz = s->desc.resolution[2];
+    p.n_cells = s->N;
+    p.flags = base_flags(s);
+    if (save) p.flags |= F_SAVE;
+    if (update) p.flags |= F_UPDATE;
+    if (reduce) p.flags |= F_REDUCE;
+    if (measure) p.flags |= F_MEASURE;
+    p.bits = s->bits;
+    fill_constants(s, p);
+    p.force = s->force.as<float4>();
+    p.bnd = s->bnd.as<uint32_t>();
+    p.objects = s->objs.as<float4>();
+    p.obj_kind = s->kinds.as<uint8_t>();
+    p.bvals = s->bvals.as<float4>();
+    if (s->thermal) { p.th_src = th_src(s); p.th_tgt = th_tgt(s); }
+    if (s->desc.multiphase) { p.psi_src = psi_src(s); p.psi_tgt = psi_tgt(s); }
+    p.vel_den = s->vel_den.as<float4>();
+    p.force_temp = s->force_temp.as<float4>();
+    p.bnd_tex = nullptr;  // the boundary-id field is written once at initialisation
+    p.red_partials = s->partials.as<double>();
+    p.err = s->err.as<unsigned int>();
+
+    int mode = s->desc.esoteric ? ((s->ticks % 2 == 1) ? AA_ODD : AA_EVEN) : AA_LOCAL;
+    const uint32_t heavy = F_BOUNDARIES | F_FORCE_FIELD | F_THERMAL | F_MULTIPHASE | F_EQ_BOUNDARIES;
+    const bool all_periodic = (p.flags & (F_PERIODIC_X | F_PERIODIC_Y | F_PERIODIC_Z)) ==
+                              (F_PERIODIC_X | F_PERIODIC_Y | F_PERIODIC_Z);
+    const bool generic = mode == AA_LOCAL || (p.flags & heavy) || !all_periodic;
+    cudaError_t e = dispatch_step(s, p, mode, generic);
+    if (e != cudaSuccess) return e;
+    if (measure) return cudaSuccess;
+    if (!s->desc.esoteric && update && !s->desc.two_buffer_fixed) s->lat0_src = !s->lat0_src;
+    if (s->desc.multiphase) s->psi0_src = !s->psi0_src;
+    s->th0_src = !s->th0_src;
+    return cudaSuccess;
+}
+
+// LBM::_stream (LBM.cpp:1495-1555)
+cudaError_t stream(bf_solver* s) {
+    StreamParams p{};
+    p.src = lat_src(s);
+    p.dst = lat_tgt(s);
+    p.stride = s->N;
+    p.nx = s->desc.resolution[0]; p.ny = s->desc.resolution[1]; p.nz = s->desc.resolution[2];
+    p.flags = base_flags(s);
+    p.bits = s->bits;
+    p.bnd = s->bnd.as<uint32_t>();
+    p.objects = s->objs.as<float4>();
+    p.obj_kind = s->kinds.as<uint8_t>();
+    cudaError_t e;
+    switch (s->Q) {
+    case 9: e = launch_stream<9>(p, s->desc.storage, s->stream); break;
+    case 15: e = launch_stream<15>(p, s->desc.storage, s->stream); break;
+    case 19: e = launch_stream<19>(p, s->desc.storage, s->stream); break;
+    default: e = launch_stream<27>(p, s->desc.storage, s->stream); break;
+    }
+    s->lat0_src = !s->lat0_src;
+    return e;
+}
+
+// LBM::_stream_thermal (LBM.cpp:1728-1773)
+cudaError_t stream_thermal(bf_solver* s) {
+    ThermalStreamParams p{};
+    p.src = th_src(s);
+    p.dst = th_tgt(s);
+    p.stride = s->N;
+    p.nx = s->desc.resolution[0]; p.ny = s->desc.resolution[1]; p.nz = s->desc.resolution[2];
+    p.flags = base_flags(s);
+    p.bits = s->bits;
+    p.bnd = s->bnd.as<uint32_t>();
+    p.objects = s->objs.as<float4>();
+    p.obj_kind = s->kinds.as<uint8_t>();
+    cudaError_t e = s->QT == 5 ? launch_stream_thermal<5>(p, s->stream) : launch_stream_thermal<7>(p, s->stream);
+    s->th0_src = !s->th0_src;
+    return e;
+}
+
+// LBM::_iterate_time (LBM.cpp:1484-1493)
+cudaError_t iterate_once(bf_solver* s, bool save, bool update, bool reduce) {
+    cudaError_t e = collide(s, save, update, reduce, false);
+    if (e != cudaSuccess) return e;
+    if (!s->desc.esoteric) { e = stream(s); if (e != cudaSuccess) return e; }
+    if (s->thermal) { e = stream_thermal(s); if (e != cudaSuccess) return e; }
+    return cudaSuccess;
+}
+
+int state_key(bf_solver* s) {
+    return (int)(s->ticks & 1) | (s->lat0_src << 1) | (s->th0_src << 2) | (s->psi0_src << 3);
+}
+
+int run_steps(bf_solver* s, int n, bool save_last) {
+    int remaining = n;
+    while (remaining > 0) {
+        const bool need_save_here = save_last && remaining == 1;
+        if (s->graphs_enabled && remaining - (save_last ? 1 : 0) >= kGraphSteps) {
+            const int key = state_key(s);
+            auto it = s->graphs.find(key);
+            if (it == s->graphs.end()) {
+                const int saved_key = key;
+                const int64_t t0 = s->ticks;
+                const int l0 = s->lat0_src, h0 = s->th0_src, p0 = s->psi0_src;
+                BF_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+                cudaError_t e = cudaSuccess;
+                for (int k = 0; k < kGraphSteps && e == cudaSuccess; k++) {
+                    e = iterate_once(s, false, true, false);
+                    s->ticks++;
+                }
+                cudaGraph_t g = nullptr;
+                cudaError_t e2 = cudaStreamEndCapture(s->stream, &g);
+                // restore the state: the captured work has not run yet
+                s->ticks = t0; s->lat0_src = l0; s->th0_src = h0; s->psi0_src = p0;
+                if (e != cudaSuccess) { if (g) cudaGraphDestroy(g); return fail(BF_ERR_CUDA, std::string("step capture: ") + cudaGetErrorString(e)); }
+                if (e2 != cudaSuccess) return fail(BF_ERR_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e2));
+                cudaGraphExec_t ex = nullptr;
+                cudaError_t e3 = cudaGraphInstantiate(&ex, g, 0);
+                cudaGraphDestroy(g);
+                if (e3 != cudaSuccess) return fail(BF_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e3));
+                it = s->graphs.emplace(saved_key, ex).first;
+            }
+            BF_CUDA(cudaGraphLaunch(it->second, s->stream));
+            // every buffer role has period two in steps and kGraphSteps is
+            // even, so only the tick counter moves
+            s->ticks += kGraphSteps;
+            remaining -= kGraphSteps;
+            s->last_saved = false;
+            continue;
+        }
+        cudaError_t e = iterate_once(s, need_save_here, true, false);
+        if (e != cudaSuccess) return fail(BF_ERR_CUDA, std::string("step launch: ") + cudaGetErrorString(e));
+        s->ticks++;
+        s->last_saved = need_save_here;
+        remaining--;
+    }
+    return BF_OK;
+}
+
+}  // namespace
+
+template <int Q>
+static void table_of(float* out) {
+    for (int i = 0; i < Q; i++) {
+        const Dir c = Lattice<Q>::c(i);
+        out[4 * i + 0] = (float)c.x; out[4 * i + 1] = (float)c.y; out[4 * i + 2] = (float)c.z;
+        out[4 * i + 3] = Lattice<Q>::w(i);
+    }
+}
+template <int QT>
+static void thermal_table_of(float* out) {
+    for (int i = 0; i < QT; i++) {
+        const Dir c = ThermalLattice<QT>::c(i);
+        out[4 * i + 0] = (float)c.x; out[4 * i + 1] = (float)c.y; out[4 * i + 2] = (float)c.z;
+        out[4 * i + 3] = ThermalLattice<QT>::w(i);
+    }
+}
+
+// ===========================================================================
+extern "C" {
+
+void bf_init_desc_default(bf_init_desc* d) {
+    if (!d) return;
+    std::memset(d, 0, sizeof(*d));
+    d->resolution[0] = d->resolution[1] = d->resolution[2] = 1;
+    d->relaxation_time = 0.53f;
+    d->periodic[0] = d->periodic[1] = d->periodic[2] = 1;
+    d->velocity_set = BF_D2Q9;
+    d->storage = BF_STORE_FP32;
+    d->multiphase = 0;
+    d->esoteric = 0;
+    d->boundary_mode = BF_BOUNDARY_SKIP;
+    d->collision = BF_COLLISION_BGK;
+    d->trt_magic = 0.25f;
+    d->velocity_limit = 0.25f;
+    d->velocity_limit_extreme = 0.30f;
+    d->intermolecular_interaction_strength = -6.0f;
+    d->thermal_relaxation_time = 2.0f;
+    d->thermal_expansion_coefficient = 0.5f;
+    d->thermal_init_equilibrium = 0;
+    d->two_buffer_fixed = 0;
+}
+
+const char* bf_last_error(void) { return g_last_error.c_str(); }
+
+int bf_get_velosity_vectors(int32_t vs, int32_t thermal, float* out, int32_t* count) {
+    const int Q = q_of(vs);
+    if (!Q || !count) return fail(BF_ERR_INVALID_ARGUMENT, "get_velosity_vectors(): velocity_set is not supported");
+    const int n = thermal ? (vs == BF_D2Q9 ? 5 : 7) : Q;
+    *count = n;
+    if (!out) return BF_OK;
+    if (thermal) { if (n == 5) thermal_table_of<5>(out); else thermal_table_of<7>(out); return BF_OK; }
+    switch (Q) {
+    case 9: table_of<9>(out); break;
+    case 15: table_of<15>(out); break;
+    case 19: table_of<19>(out); break;
+    default: table_of<27>(out); break;
+    }
+    return BF_OK;
+}
+
+int bf_bits_per_boundry(int32_t object_count, int32_t* bits) {
+    if (!bits || object_count < 0) return fail(BF_ERR_INVALID_ARGUMENT, "bits_per_boundry(): bad argument");
+    *bits = bits_per_boundry(object_count);
+    return BF_OK;
+}
+
+int bf_pack_boundries(const uint32_t* ids, size_t cells, int32_t bits, uint32_t* out, size_t cap, size_t* words) {
+    if (!words || (bits != 1 && bits != 2 && bits != 4 && bits != 8))
+        return fail(BF_ERR_INVALID_ARGUMENT, "pack_boundries(): bits must be 1, 2, 4 or 8");
+    *words = (cells * (size_t)bits + 31) / 32;
+    if (!out) return BF_OK;
+    if (!ids || cap < *words) return fail(BF_ERR_INVALID_ARGUMENT, "pack_boundries(): destination too small");
+    std::memset(out, 0, *words * 4);
+    for (size_t c = 0; c < cells; c++) {
+        const uint64_t b = (uint64_t)c * (uint64_t)bits;
+        out[b / 32] |= (ids[c] << (b % 32));
+    }
+    return BF_OK;
+}
+int bf_abi_version(void) { return BF_ABI_VERSION; }
+
+int bf_create(bf_solver** out) {
+    if (!out) return fail(BF_ERR_INVALID_ARGUMENT, "bf_create: out is NULL");
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return fail(BF_ERR_NO_DEVICE, "bf_create: no CUDA device visible");
+    }
+    bf_solver* s = new bf_solver();
+    cudaGetDevice(&s->device);
+    cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { delete s; return fail(BF_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e)); }
+    bf_object fluid{};
+    fluid.temperature = 1.0f;
+    fluid.effective_density = 1.0f;
+    s->objects.push_back(fluid);
+    bf_init_desc_default(&s->desc);
+    *out = s;
+    return BF_OK;
+}
+
+int bf_destroy(bf_solver* s) {
+    if (!s) return BF_OK;
+    cudaSetDevice(s->device);
+    cudaStreamSynchronize(s->stream);
+    release_all(s);
+    cudaStreamDestroy(s->stream);
+    delete s;
+    return BF_OK;
+}
+
+int bf_set_boundry_properties(bf_solver* s, uint32_t id, const bf_object* o) {
+    if (!s || !o) return fail(BF_ERR_INVALID_ARGUMENT, "bf_set_boundry_properties: NULL argument");
+    if (id > 255) return fail(BF_ERR_INVALID_ARGUMENT, "set_boundry_properties: boundry_id(" + std::to_string(id) + ") is greater than maximum(255)");
+    if (id == 0) return fail(BF_ERR_INVALID_ARGUMENT, "set_boundry_properties: boundry_id(0) is defined to be fluid, it cannot be treated as an object");
+    if (o->kind < BF_OBJECT_SOLID || o->kind > BF_OBJECT_EQ_DENSITY) return fail(BF_ERR_INVALID_ARGUMENT, "set_boundry_properties: unknown object kind");
+    if (id >= s->objects.size()) {
+        bf_object def{};
+        def.temperature = 1.0f; def.effective_density = 1.0f;
+        s->objects.resize(id + 1, def);
+    }
+    s->objects[id] = *o;
+    return BF_OK;
+}
+
+int bf_clear_boundry_properties(bf_solver* s) {
+    if (!s) return fail(BF_ERR_INVALID_ARGUMENT, "NULL solver");
+    s->objects.clear();  // LBM.cpp:1067-1070
+    return BF_OK;
+}
+
+int bf_initialize_fields(bf_solver* s, const bf_init_desc* d, const float* density, const float* velocity,
+                         const float* force, const float* temperature, const uint32_t* ids) {
+    if (!s || !d) return fail(BF_ERR_INVALID_ARGUMENT, "bf_initialize_fields: NULL argument");
+    cudaSetDevice(s->device);
+    const int rx = d->resolution[0], ry = d->resolution[1], rz = d->resolution[2];
+    if (rx <= 0 || ry <= 0 || rz <= 0)
+        return fail(BF_ERR_INVALID_ARGUMENT, "initialize_fields() is called but given resolution is not valid, all components must be greater than zero");
+    const int Q = q_of(d->velocity_set);
+    if (!Q) return fail(BF_ERR_INVALID_ARGUMENT, "initialize_fields(): velocity set is not supported");
+    const int dims = d->velocity_set == BF_D2Q9 ? 2 : 3;
+    if (dims == 2 && rz != 1)
+        return fail(BF_ERR_INVALID_ARGUMENT, "initialize_fields() is called but given velocity set dimention doesn't match the resolution dimention");
+    const uint64_t N64 = (uint64_t)rx * ry * rz;
+    if (N64 >= (1ull << 32) || ry > 65535 || rz > 65535)
+        return fail(BF_ERR_INVALID_ARGUMENT, "initialize_fields(): at most 2^32-1 cells and 65535 cells along y and z");
+    if (d->storage < BF_STORE_FP32 || d->storage > BF_STORE_FP16C) return fail(BF_ERR_INVALID_ARGUMENT, "initialize_fields(): unknown storage");
+    if (!(d->relaxation_time > 0.5f)) return fail(BF_ERR_INVALID_ARGUMENT, "initialize_fields(): relaxation_time must exceed 0.5");
+    if (d->collision == BF_COLLISION_TRT && !(d->trt_magic > 0.f)) return fail(BF_ERR_INVALID_ARGUMENT, "initialize_fields(): TRT magic parameter must be positive");
+
+    cudaStreamSynchronize(s->stream);
+    release_all(s);
+    s->desc = *d;
+    s->Q = Q; s->dims = dims; s->QT = dims == 2 ? 5 : 7;
+    s->N = (uint32_t)N64;
+    const uint32_t N = s->N;
+
+    // object table: slot 0 reset to fluid (LBM.cpp:439-441)
+    bf_object fluid{};
+    fluid.temperature = 1.0f; fluid.effective_density = 1.0f;
+    if (s->objects.empty()) s->objects.resize(1);
+    s->objects[0] = fluid;
+    // LBM.cpp:523-556 -- one host pass over the lambda results
+    uint32_t maxid = 0;
+    if (ids) for (uint32_t c = 0; c < N; c++) maxid = std::max(maxid, ids[c]);
+    if (maxid > 255) return fail(BF_ERR_INVALID_ARGUMENT, "initialize_fields(): boundry ids above 255");
+    if (maxid + 1 > s->objects.size()) {
+        bf_object def{};
+        def.temperature = 1.0f; def.effective_density = 1.0f;
+        s->objects.resize(maxid + 1, def);
+    }
+    const int nobj = (int)s->objects.size();
+    s->constant_force = true;
+    s->fconst[0] = force ? force[0] : 0.f; s->fconst[1] = force ? force[1] : 0.f; s->fconst[2] = force ? force[2] : 0.f;
+    s->thermal = false;
+    const float T0 = temperature ? temperature[0] : 1.0f;
+    for (uint32_t c = 0; c < N; c++) {
+        if (force && (force[3 * (uint64_t)c] != s->fconst[0] || force[3 * (uint64_t)c + 1] != s->fconst[1] || force[3 * (uint64_t)c + 2] != s->fconst[2]))
+            s->constant_force = false;
+        if (temperature && temperature[c] != T0) s->thermal = true;
+        const uint32_t id = ids ? ids[c] : 0u;
+        if (id != 0 && s->objects[id].temperature != T0) s->thermal = true;
+    }
+    s->forcing = !(s->constant_force && s->fconst[0] == 0.f && s->fconst[1] == 0.f && s->fconst[2] == 0.f);
+    s->boundaries = nobj > 1;
+    s->bits = bits_per_boundry(nobj);
+    if (s->bits > 8) return fail(BF_ERR_INVALID_ARGUMENT, "too many objects are defined, maximum of 255 bits are possible but number of objets were: " + std::to_string(nobj));
+    s->has_eq_objects = false;
+    for (int k = 1; k < nobj; k++) if (s->objects[k].kind != BF_OBJECT_SOLID) s->has_eq_objects = true;
+
+    const size_t sb = storage_bytes(d->storage);
+    const size_t lat_bytes = (size_t)N * Q * sb;
+    BF_CUDA(s->lat[0].alloc(lat_bytes));
+    if (!d->esoteric) BF_CUDA(s->lat[1].alloc(lat_bytes));
+    s->lat0_src = 1; s->th0_src = 1; s->psi0_src = 1;
+    s->ticks = 0;
+
+    // boundary bits (LBM.cpp:634-659) and the object table (LBM.cpp:613-626)
+    std::vector<uint8_t> kinds_h(kMaxObjects, 0);
+    std::vector<float4> objs_h((size_t)kMaxObjects * 3, make_float4(0, 0, 0, 0));
+    for (int k = 0; k < nobj; k++) {
+        const bf_object& o = s->objects[k];
+        objs_h[3 * k + 0] = make_float4(o.velocity_translational[0], o.velocity_translational[1], o.velocity_translational[2], o.temperature);
+        objs_h[3 * k + 1] = make_float4(o.velocity_angular[0], o.velocity_angular[1], o.velocity_angular[2], 0.f);
+        objs_h[3 * k + 2] = make_float4(o.center_of_mass[0], o.center_of_mass[1], o.center_of_mass[2], o.effective_density);
+        kinds_h[k] = (uint8_t)(k == 0 ? 0 : o.kind);
+    }
+    BF_CUDA(s->objs.alloc(objs_h.size() * sizeof(float4)));
+    BF_CUDA(s->kinds.alloc(kinds_h.size()));
+    BF_CUDA(cudaMemcpy(s->objs.p, objs_h.data(), objs_h.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    BF_CUDA(cudaMemcpy(s->kinds.p, kinds_h.data(), kinds_h.size(), cudaMemcpyHostToDevice));
+    std::vector<uint8_t> tex_h(N, 0);
+    if (s->boundaries) {
+        s->bnd_words = ((uint64_t)N * s->bits + 31) / 32;
+        std::vector<uint32_t> words(s->bnd_words + 1, 0u);
+        if (ids) {
+            size_t nw = 0;
+            bf_pack_boundries(ids, N, s->bits, words.data(), words.size(), &nw);
+            for (uint64_t c = 0; c < N; c++) tex_h[c] = (uint8_t)ids[c];
+        }
+        BF_CUDA(s->bnd.alloc(words.size() * 4));
+        BF_CUDA(cudaMemcpy(s->bnd.p, words.data(), words.size() * 4, cudaMemcpyHostToDevice));
+    } else {
+        s->bnd_words = 0;
+    }
+    BF_CUDA(s->bnd_tex.alloc(N));
+    BF_CUDA(cudaMemcpy(s->bnd_tex.p, tex_h.data(), N, cudaMemcpyHostToDevice));
+
+    // host staging of the lambda results
+    DeviceBuf d_rho, d_u, d_ids, d_T;
+    BF_CUDA(d_rho.alloc((size_t)N * 4));
+    BF_CUDA(d_u.alloc((size_t)N * 12));
+    {
+        std::vector<float> tmp;
+        if (density) BF_CUDA(cudaMemcpy(d_rho.p, density, (size_t)N * 4, cudaMemcpyHostToDevice));
+        else { tmp.assign(N, 1.0f); BF_CUDA(cudaMemcpy(d_rho.p, tmp.data(), (size_t)N * 4, cudaMemcpyHostToDevice)); }
+        if (velocity) BF_CUDA(cudaMemcpy(d_u.p, velocity, (size_t)N * 12, cudaMemcpyHostToDevice));
+        else BF_CUDA(cudaMemset(d_u.p, 0, (size_t)N * 12));
+    }
+    if (ids) {
+        BF_CUDA(d_ids.alloc((size_t)N * 4));
+        BF_CUDA(cudaMemcpy(d_ids.p, ids, (size_t)N * 4, cudaMemcpyHostToDevice));
+    }
+    // force field (LBM.cpp:693-717), vec4 per cell
+    if (s->forcing && !s->constant_force) {
+        std::vector<float4> fh(N);
+        for (uint64_t c = 0; c < N; c++) fh[c] = make_float4(force[3 * c], force[3 * c + 1], force[3 * c + 2], 0.f);
+        BF_CUDA(s->force.alloc((size_t)N * 16));
+        BF_CUDA(cudaMemcpy(s->force.p, fh.data(), (size_t)N * 16, cudaMemcpyHostToDevice));
+    }
+    // equilibrium-boundary values (extension): initial (rho, u) of each cell
+    if (s->has_eq_objects) {
+        std::vector<float4> bh(N);
+        for (uint64_t c = 0; c < N; c++)
+            bh[c] = make_float4(density ? density[c] : 1.0f, velocity ? velocity[3 * c] : 0.f,
+                                velocity ? velocity[3 * c + 1] : 0.f, velocity ? velocity[3 * c + 2] : 0.f);
+        BF_CUDA(s->bvals.alloc((size_t)N * 16));
+        BF_CUDA(cudaMemcpy(s->bvals.p, bh.data(), (size_t)N * 16, cudaMemcpyHostToDevice));
+    }
+    // Shan-Chen pseudopotential textures (LBM.cpp:848-866), zero initial contents
+    if (d->multiphase) {
+        BF_CUDA(s->psi[0].alloc((size_t)N * 4));
+        BF_CUDA(s->psi[1].alloc((size_t)N * 4));
+        BF_CUDA(cudaMemset(s->psi[0].p, 0, (size_t)N * 4));
+        BF_CUDA(cudaMemset(s->psi[1].p, 0, (size_t)N * 4));
+    }
+    BF_CUDA(s->vel_den.alloc((size_t)N * 16));
+    BF_CUDA(s->force_temp.alloc((size_t)N * 16));
+    BF_CUDA(cudaMemset(s->vel_den.p, 0, (size_t)N * 16));
+    BF_CUDA(cudaMemset(s->force_temp.p, 0, (size_t)N * 16));
+    {
+        // same block shape as cell_grid() in lbm_kernels.cuh
+        const int block = rx >= kStepBlock ? kStepBlock : ((rx + 31) / 32) * 32;
+        s->n_blocks = (uint32_t)((rx + block - 1) / block) * (uint32_t)ry * (uint32_t)rz;
+    }
+    BF_CUDA(s->partials.alloc((size_t)s->n_blocks * 5 * sizeof(double)));
+    BF_CUDA(s->red_out.alloc(5 * sizeof(double)));
+    BF_CUDA(s->err.alloc(sizeof(unsigned int)));
+    BF_CUDA(cudaMemset(s->err.p, 0, sizeof(unsigned int)));
+
+    // set_equilibrium_populations (LBM.cpp:1702-1726)
+    InitParams ip{};
+    ip.f = s->lat[0].p;
+    ip.stride = N;
+    ip.n_cells = N;
+    ip.rho = d_rho.as<float>();
+    ip.u = d_u.as<float>();
+    ip.ids = d_ids.as<uint32_t>();
+    ip.obj_kind = s->kinds.as<uint8_t>();
+    cudaError_t e;
+    switch (Q) {
+    case 9: e = launch_init<9>(ip, d->storage, s->stream); break;
+    case 15: e = launch_init<15>(ip, d->storage, s->stream); break;
+    case 19: e = launch_init<19>(ip, d->storage, s->stream); break;
+    default: e = launch_init<27>(ip, d->storage, s->stream); break;
+    }
+    if (e != cudaSuccess) return fail(BF_ERR_CUDA, std::string("init kernel: ") + cudaGetErrorString(e));
+    if (s->thermal) {
+        BF_CUDA(s->th[0].alloc((size_t)N * s->QT * 4));
+        BF_CUDA(s->th[1].alloc((size_t)N * s->QT * 4));
+        BF_CUDA(cudaMemsetAsync(s->th[0].p, 0, (size_t)N * s->QT * 4, s->stream));
+        BF_CUDA(cudaMemsetAsync(s->th[1].p, 0, (size_t)N * s->QT * 4, s->stream));
+        if (d->thermal_init_equilibrium) {
+            DeviceBuf d_Tb;
+            BF_CUDA(d_Tb.alloc((size_t)N * 4));
+            std::vector<float> tmp;
+            if (temperature) BF_CUDA(cudaMemcpy(d_Tb.p, temperature, (size_t)N * 4, cudaMemcpyHostToDevice));
+            else { tmp.assign(N, 1.0f); BF_CUDA(cudaMemcpy(d_Tb.p, tmp.data(), (size_t)N * 4, cudaMemcpyHostToDevice)); }
+            InitParams tp = ip;
+            tp.th = th_src(s);
+            tp.T = d_Tb.as<float>();
+            tp.stride = N;
+            e = s->QT == 5 ? launch_init_thermal<5>(tp, s->stream) : launch_init_thermal<7>(tp, s->stream);
+            if (e != cudaSuccess) return fail(BF_ERR_CUDA, std::string("thermal init kernel: ") + cudaGetErrorString(e));
+            BF_CUDA(cudaStreamSynchronize(s->stream));
+        }
+        // As the reference reads it, set_equilibrium_populations_thermal.comp:101-107
+        // writes past the end of the thermal buffer, which keeps its zero contents.
+    }
+    // LBM.cpp:502: _iterate_time(true, false)
+    e = iterate_once(s, true, false, false);
+    if (e != cudaSuccess) return fail(BF_ERR_CUDA, std::string("first pass: ") + cudaGetErrorString(e));
+    BF_CUDA(cudaStreamSynchronize(s->stream));
+    s->last_saved = true;
+    s->initialized = true;
+    return BF_OK;
+}
+
+int bf_iterate_time(bf_solver* s, int32_t n_steps, int32_t save_fields) {
+    if (!s) return fail(BF_ERR_INVALID_ARGUMENT, "NULL solver");
+    if (!s->initialized) return fail(BF_ERR_NOT_INITIALIZED, "iterate_time(): initialize_fields has not run");
+    if (n_steps < 0) return fail(BF_ERR_INVALID_ARGUMENT, "iterate_time(): negative step count");
+    cudaSetDevice(s->device);
+    return run_steps(s, n_steps, save_fields != 0);
+}
+
+int bf_synchronize(bf_solver* s, int32_t timeout_ms) {
+    if (!s) return fail(BF_ERR_INVALID_ARGUMENT, "NULL solver");
+    cudaSetDevice(s->device);
+    if (timeout_ms > 0) {
+        const auto t0 = std::chrono::steady_clock::now();
+        for (;;) {
+            cudaError_t q = cudaStreamQuery(s->stream);
+            if (q == cudaSuccess) break;
+            if (q != cudaErrorNotReady) return fail(BF_ERR_CUDA, std::string("cudaStreamQuery: ") + cudaGetErrorString(q));
+            if (std::chrono::steady_clock::now() - t0 > std::chrono::milliseconds(timeout_ms))
+                return fail(BF_ERR_TIMEOUT, "bf_synchronize: stream still busy after the time limit");
+            std::this_thread::sleep_for(std::chrono::microseconds(200));
+        }
+    } else {
+        BF_CUDA(cudaStreamSynchronize(s->stream));
+    }
+    if (s->initialized) {
+        unsigned int h = 0;
+        BF_CUDA(cudaMemcpy(&h, s->err.p, sizeof(h), cudaMemcpyDeviceToHost));
+        if (h & 1u) return fail(BF_ERR_UNSTABLE, "a step computed a NaN density (simulation unstable)");
+    }
+    return BF_OK;
+}
+
+int bf_get_total_ticks_elapsed(bf_solver* s, int64_t* t) {
+    if (!s || !t) return fail(BF_ERR_INVALID_ARGUMENT, "NULL argument");
+    *t = s->ticks;
+    return BF_OK;
+}
+int bf_get_resolution(bf_solver* s, int32_t r[3]) {
+    if (!s || !r) return fail(BF_ERR_INVALID_ARGUMENT, "NULL argument");
+    r[0] = s->desc.resolution[0]; r[1] = s->desc.resolution[1]; r[2] = s->desc.resolution[2];
+    return BF_OK;
+}
+int bf_get_velocity_set_vector_count(bf_solver* s, int32_t* q) {
+    if (!s || !q) return fail(BF_ERR_INVALID_ARGUMENT, "NULL argument");
+    *q = q_of(s->desc.velocity_set);
+    return BF_OK;
+}
+int bf_get_relaxation_time(bf_solver* s, float* tau) {
+    if (!s || !tau) return fail(BF_ERR_INVALID_ARGUMENT, "NULL argument");
+    *tau = s->desc.relaxation_time;
+    return BF_OK;
+}
+int bf_set_relaxation_time(bf_solver* s, float tau) {
+    if (!s) return fail(BF_ERR_INVALID_ARGUMENT, "NULL solver");
+    if (!(tau > 0.5f)) return fail(BF_ERR_INVALID_ARGUMENT, "set_relaxation_time(): tau must exceed 0.5");
+    s->desc.relaxation_time = tau;
+    clear_graphs(s);
+    return BF_OK;
+}
+int bf_get_constant_force(bf_solver* s, float f[3]) {
+    if (!s || !f) return fail(BF_ERR_INVALID_ARGUMENT, "NULL argument");
+    f[0] = s->fconst[0]; f[1] = s->fconst[1]; f[2] = s->fconst[2];
+    return BF_OK;
+}
+int bf_set_constant_force(bf_solver* s, const float f[3]) {
+    if (!s || !f) return fail(BF_ERR_INVALID_ARGUMENT, "NULL argument");
+    // LBM::set_constant_force (LBM.cpp:366-369) only changes the uniform; the
+    // forcing switches were fixed by initialize_fields
+    s->fconst[0] = f[0]; s->fconst[1] = f[1]; s->fconst[2] = f[2];
+    clear_graphs(s);
+    return BF_OK;
+}
+int bf_get_intermolecular_interaction_strength(bf_solver* s, float* g) {
+    if (!s || !g) return fail(BF_ERR_INVALID_ARGUMENT, "NULL argument");
+    *g = s->desc.intermolecular_interaction_strength;
+    return BF_OK;
+}
+int bf_set_intermolecular_interaction_strength(bf_solver* s, float g) {
+    if (!s) return fail(BF_ERR_INVALID_ARGUMENT, "NULL solver");
+    s->desc.intermolecular_interaction_strength = g;
+    clear_graphs(s);
+    return BF_OK;
+}
+int bf_set_velocity_limits(bf_solver* s, float limit, float limit_extreme) {
+    if (!s) return fail(BF_ERR_INVALID_ARGUMENT, "NULL solver");
+    s->desc.velocity_limit = limit;
+    s->desc.velocity_limit_extreme = limit_extreme;
+    clear_graphs(s);
+    return BF_OK;
+}
+int bf_set_thermal_parameters(bf_solver* s, float tau_t, float beta) {
+    if (!s) return fail(BF_ERR_INVALID_ARGUMENT, "NULL solver");
+    if (!(tau_t > 0.5f)) return fail(BF_ERR_INVALID_ARGUMENT, "thermal relaxation time must exceed 0.5");
+    s->desc.thermal_relaxation_time = tau_t;
+    s->desc.thermal_expansion_coefficient = beta;
+    clear_graphs(s);
+    return BF_OK;
+}
+int bf_get_scheme_flags(bf_solver* s, int32_t* flags, int32_t* bits) {
+    if (!s || !flags) return fail(BF_ERR_INVALID_ARGUMENT, "NULL argument");
+    *flags = (s->forcing ? 1 : 0) | (s->constant_force ? 2 : 0) | (s->thermal ? 4 : 0) |
+             (s->desc.multiphase ? 8 : 0) | (s->boundaries ? 16 : 0);
+    if (bits) *bits = s->bits;
+    return BF_OK;
+}
+
+int bf_get_field(bf_solver* s, int32_t kind, bf_field* out) {
+    if (!s || !out) return fail(BF_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (!s->initialized) return fail(BF_ERR_NOT_INITIALIZED, "get_field(): initialize_fields has not run");
+    std::memset(out, 0, sizeof(*out));
+    out->kind = kind;
+    out->resolution[0] = s->desc.resolution[0]; out->resolution[1] = s->desc.resolution[1]; out->resolution[2] = s->desc.resolution[2];
+    switch (kind) {
+    case BF_FIELD_VELOCITY_DENSITY:
+        out->device_ptr = s->vel_den.p; out->components = 4; out->bytes_per_component = 4; out->bytes = (size_t)s->N * 16; break;
+    case BF_FIELD_BOUNDARY:
+        out->device_ptr = s->bnd_tex.p; out->components = 1; out->bytes_per_component = 1; out->bytes = s->N; break;
+    case BF_FIELD_FORCE_TEMPERATURE:
+        out->device_ptr = s->force_temp.p; out->components = 4; out->bytes_per_component = 4; out->bytes = (size_t)s->N * 16; break;
+    case BF_FIELD_POPULATIONS: {
+        const size_t bytes = (size_t)s->N * s->Q * 4;
+        if (s->decode_tmp.bytes < bytes) BF_CUDA(s->decode_tmp.alloc(bytes));
+        cudaError_t e;
+        switch (s->Q) {
+        case 9: e = launch_decode<9>(lat_src(s), s->N, s->N, s->desc.storage, s->decode_tmp.as<float>(), s->stream); break;
+        case 15: e = launch_decode<15>(lat_src(s), s->N, s->N, s->desc.storage, s->decode_tmp.as<float>(), s->stream); break;
+        case 19: e = launch_decode<19>(lat_src(s), s->N, s->N, s->desc.storage, s->decode_tmp.as<float>(), s->stream); break;
+        default: e = launch_decode<27>(lat_src(s), s->N, s->N, s->desc.storage, s->decode_tmp.as<float>(), s->stream); break;
+        }
+        if (e != cudaSuccess) return fail(BF_ERR_CUDA, std::string("decode: ") + cudaGetErrorString(e));
+        out->device_ptr = s->decode_tmp.p; out->components = s->Q; out->bytes_per_component = 4; out->bytes = bytes;
+        break;
+    }
+    case BF_FIELD_THERMAL_POPULATIONS:
+        if (!s->thermal) return fail(BF_ERR_INVALID_ARGUMENT, "get_field(): the flow is not thermal");
+        out->device_ptr = th_src(s); out->components = s->QT; out->bytes_per_component = 4; out->bytes = (size_t)s->N * s->QT * 4; break;
+    default:
+        return fail(BF_ERR_INVALID_ARGUMENT, "get_field(): unknown field kind");
+    }
+    return BF_OK;
+}
+
+int bf_copy_field_to_host(bf_solver* s, int32_t kind, void* dst, size_t bytes) {
+    if (!dst) return fail(BF_ERR_INVALID_ARGUMENT, "copy_field_to_host(): NULL destination");
+    bf_field f;
+    int r = bf_get_field(s, kind, &f);
+    if (r != BF_OK) return r;
+    if (bytes < f.bytes) return fail(BF_ERR_INVALID_ARGUMENT, "copy_field_to_host(): destination too small");
+    BF_CUDA(cudaMemcpyAsync(dst, f.device_ptr, f.bytes, cudaMemcpyDeviceToHost, s->stream));
+    BF_CUDA(cudaStreamSynchronize(s->stream));
+    return BF_OK;
+}
+
+int bf_copy_boundry_bits_to_host(bf_solver* s, uint32_t* dst, size_t cap, size_t* words) {
+    if (!s || !words) return fail(BF_ERR_INVALID_ARGUMENT, "NULL argument");
+    *words = s->bnd_words;
+    if (s->bnd_words == 0) return BF_OK;
+    if (!dst || cap < s->bnd_words) return fail(BF_ERR_INVALID_ARGUMENT, "copy_boundry_bits_to_host(): destination too small");
+    BF_CUDA(cudaStreamSynchronize(s->stream));
+    BF_CUDA(cudaMemcpy(dst, s->bnd.p, s->bnd_words * 4, cudaMemcpyDeviceToHost));
+    return BF_OK;
+}
+
+int bf_reduce(bf_solver* s, double out[5]) {
+    if (!s || !out) return fail(BF_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (!s->initialized) return fail(BF_ERR_NOT_INITIALIZED, "reduce(): initialize_fields has not run");
+    cudaSetDevice(s->device);
+    // moments of the current state, as the next step would read them
+    cudaError_t e = collide(s, true, false, true, true);
+    if (e != cudaSuccess) return fail(BF_ERR_CUDA, std::string("reduce pass: ") + cudaGetErrorString(e));
+    e = launch_reduce_finish(s->partials.as<double>(), s->n_blocks, s->red_out.as<double>(), s->stream);
+    if (e != cudaSuccess) return fail(BF_ERR_CUDA, std::string("reduce finish: ") + cudaGetErrorString(e));
+    BF_CUDA(cudaMemcpyAsync(out, s->red_out.p, 5 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    BF_CUDA(cudaStreamSynchronize(s->stream));
+    return BF_OK;
+}
+
+int bf_benchmark_steps(bf_solver* s, int32_t n_steps, float* ms) {
+    if (!s || !ms) return fail(BF_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (!s->initialized) return fail(BF_ERR_NOT_INITIALIZED, "benchmark_steps(): initialize_fields has not run");
+    if (n_steps <= 0) return fail(BF_ERR_INVALID_ARGUMENT, "benchmark_steps(): n_steps must be positive");
+    cudaSetDevice(s->device);
+    cudaEvent_t a, b;
+    BF_CUDA(cudaEventCreate(&a));
+    BF_CUDA(cudaEventCreate(&b));
+    cudaError_t e = cudaEventRecord(a, s->stream);
+    int r = e == cudaSuccess ? run_steps(s, n_steps, false) : BF_ERR_CUDA;
+    if (r == BF_OK) e = cudaEventRecord(b, s->stream);
+    if (r == BF_OK && e == cudaSuccess) e = cudaEventSynchronize(b);
+    if (r == BF_OK && e == cudaSuccess) e = cudaEventElapsedTime(ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (r != BF_OK) return r;
+    if (e != cudaSuccess) return fail(BF_ERR_CUDA, std::string("benchmark_steps: ") + cudaGetErrorString(e));
+    return BF_OK;
+}
+
+// ---- snapshots ------------------------------------------------------------
+static const char kMagic[8] = {'B', 'F', 'G', 'B', '3', 'S', 'N', '1'};
+
+int bf_save_snapshot(bf_solver* s, const char* path) {
+    if (!s || !path) return fail(BF_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (!s->initialized) return fail(BF_ERR_NOT_INITIALIZED, "save_snapshot(): initialize_fields has not run");
+    BF_CUDA(cudaStreamSynchronize(s->stream));
+    FILE* fp = std::fopen(path, "wb");
+    if (!fp) return fail(BF_ERR_IO, std::string("save_snapshot(): cannot open ") + path);
+    bool ok = true;
+    auto put = [&](const void* p, size_t n) { if (ok && std::fwrite(p, 1, n, fp) != n) ok = false; };
+    put(kMagic, 8);
+    put(&s->desc, sizeof(s->desc));
+    put(&s->ticks, sizeof(s->ticks));
+    int32_t st[3] = {s->lat0_src, s->th0_src, s->psi0_src};
+    put(st, sizeof(st));
+    std::vector<char> h;
+    auto dump = [&](const DeviceBuf& b) {
+        uint64_t n = b.bytes;
+        put(&n, 8);
+        if (!n) return;
+        h.resize(n);
+        if (cudaMemcpy(h.data(), b.p, n, cudaMemcpyDeviceToHost) != cudaSuccess) { ok = false; return; }
+        put(h.data(), n);
+    };
+    dump(s->lat[0]); dump(s->lat[1]); dump(s->th[0]); dump(s->th[1]); dump(s->psi[0]); dump(s->psi[1]);
+    dump(s->vel_den); dump(s->force_temp);
+    if (std::fclose(fp) != 0) ok = false;
+    return ok ? BF_OK : fail(BF_ERR_IO, std::string("save_snapshot(): write failed for ") + path);
+}
+
+int bf_load_snapshot(bf_solver* s, const char* path) {
+    if (!s || !path) return fail(BF_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (!s->initialized) return fail(BF_ERR_NOT_INITIALIZED, "load_snapshot(): initialize_fields with the same configuration must run first");
+    BF_CUDA(cudaStreamSynchronize(s->stream));
+    FILE* fp = std::fopen(path, "rb");
+    if (!fp) return fail(BF_ERR_IO, std::string("load_snapshot(): cannot open ") + path);
+    bool ok = true;
+    auto get = [&](void* p, size_t n) { if (ok && std::fread(p, 1, n, fp) != n) ok = false; };
+    char magic[8];
+    get(magic, 8);
+    bf_init_desc d;
+    get(&d, sizeof(d));
+    int64_t ticks = 0;
+    get(&ticks, sizeof(ticks));
+    int32_t st[3];
+    get(st, sizeof(st));
+    if (!ok || std::memcmp(magic, kMagic, 8) != 0) { std::fclose(fp); return fail(BF_ERR_IO, "load_snapshot(): not a snapshot file"); }
+    if (std::memcmp(d.resolution, s->desc.resolution, sizeof(d.resolution)) != 0 || d.velocity_set != s->desc.velocity_set ||
+        d.storage != s->desc.storage || d.esoteric != s->desc.esoteric || d.multiphase != s->desc.multiphase) {
+        std::fclose(fp);
+        return fail(BF_ERR_INVALID_ARGUMENT, "load_snapshot(): snapshot configuration differs from the solver's");
+    }
+    std::vector<char> h;
+    DeviceBuf* bufs[] = {&s->lat[0], &s->lat[1], &s->th[0], &s->th[1], &s->psi[0], &s->psi[1], &s->vel_den, &s->force_temp};
+    for (DeviceBuf* b : bufs) {
+        uint64_t n = 0;
+        get(&n, 8);
+        if (!ok) break;
+        if (n != b->bytes) { ok = false; break; }
+        if (!n) continue;
+        h.resize(n);
+        get(h.data(), n);
+        if (!ok) break;
+        if (cudaMemcpy(b->p, h.data(), n, cudaMemcpyHostToDevice) != cudaSuccess) ok = false;
+    }
+    std::fclose(fp);
+    if (!ok) return fail(BF_ERR_IO, "load_snapshot(): truncated or mismatched snapshot");
+    s->ticks = ticks;
+    s->lat0_src = st[0]; s->th0_src = st[1]; s->psi0_src = st[2];
+    s->desc.relaxation_time = d.relaxation_time;
+    clear_graphs(s);
+    return BF_OK;
+}
+
+}  // extern "C"

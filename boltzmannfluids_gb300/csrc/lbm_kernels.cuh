@@ -1,0 +1,584 @@
+// lbm_kernels.cuh -- sm_103a kernels of the lattice Boltzmann update.
+//
+// One thread per cell, threads of a block run along x, the DDF is one
+// structure-of-arrays buffer (population plane i at f + i*stride), so every
+// population load/store of a warp touches 32 consecutive elements.
+//
+// step_kernel is the fused stream+collide of the reference's esoteric-pull
+// mode (collide.comp main, :676-794).  The AA pattern follows
+// collide.comp:244-369: on an even step a cell reads population i from
+// (x - c_i, slot i) and writes its post-collision population i to
+// (x + c_i, slot opp(i)); on an odd step it reads (x, slot opp(i)) and
+// writes (x, slot i).  A cell reads and writes the same private set of slots,
+// so the update is race free in place.
+#pragma once
+#include "lbm_common.cuh"
+
+namespace bf {
+
+struct CellSum { float m, px, py, pz, ke; };
+
+template <int Q>
+__device__ __forceinline__ void coords_wrap(int& cx, int& cy, int& cz, int nx, int ny, int nz, bool& open, uint32_t flags) {
+    open = false;
+    if (flags & F_PERIODIC_X) { cx = cx < 0 ? cx + nx : (cx >= nx ? cx - nx : cx); }
+    else open |= (cx < 0 || cx >= nx);
+    if (flags & F_PERIODIC_Y) { cy = cy < 0 ? cy + ny : (cy >= ny ? cy - ny : cy); }
+    else open |= (cy < 0 || cy >= ny);
+    if (flags & F_PERIODIC_Z) { cz = cz < 0 ? cz + nz : (cz >= nz ? cz - nz : cz); }
+    else open |= (cz < 0 || cz >= nz);
+}
+
+__device__ __forceinline__ bool solid_id(const uint8_t* __restrict__ kind, uint32_t id) {
+    return id != 0u && __ldg(kind + id) == 0;
+}
+
+// FP64 block reduction of the five conserved sums; one partial per block.
+__device__ __forceinline__ void block_reduce_store(CellSum cs, double* __restrict__ out) {
+    double v[5] = {(double)cs.m, (double)cs.px, (double)cs.py, (double)cs.pz, (double)cs.ke};
+#pragma unroll
+    for (int k = 0; k < 5; k++)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+    __shared__ double sm[kStepBlock / 32][5];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < 5; k++) sm[warp][k] = v[k];
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+        for (int k = 0; k < 5; k++) {
+            double t = lane < nw ? sm[lane][k] : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+            v[k] = t;
+        }
+        if (lane == 0) {
+            const uint64_t b = blockIdx.x + (uint64_t)gridDim.x * (blockIdx.y + (uint64_t)gridDim.y * blockIdx.z);
+#pragma unroll
+            for (int k = 0; k < 5; k++) out[b * 5 + k] = v[k];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// fused AA stream + collide
+// ---------------------------------------------------------------------------
+template <int Q, int ST, int MODE, bool GENERIC>
+__device__ __forceinline__ CellSum cell_update(const StepParams& p, int x, int y, int z) {
+    using L = Lattice<Q>;
+    using C = Codec<ST>;
+    using T = typename C::T;
+    T* __restrict__ F = static_cast<T*>(p.f);
+    const uint64_t S = p.stride;
+    const int nx = p.nx, ny = p.ny, nz = p.nz;
+    const uint32_t flags = GENERIC ? p.flags : (p.flags & (F_SAVE | F_UPDATE | F_TRT | F_SOURCE | F_FORCE_CONST | F_REDUCE));
+    const uint32_t n = (uint32_t)x + (uint32_t)nx * ((uint32_t)y + (uint32_t)ny * (uint32_t)z);
+    CellSum out = {0.f, 0.f, 0.f, 0.f, 0.f};
+
+    uint32_t bid = 0;
+    if (GENERIC && (flags & F_BOUNDARIES)) {
+        bid = boundary_id(p.bnd, p.bits, n);
+        if (solid_id(p.obj_kind, bid)) {  // collide.comp:696-700
+            if (flags & F_SAVE) {
+                p.vel_den[n] = make_float4(0.f, 0.f, 0.f, 0.f);
+                p.force_temp[n] = make_float4(0.f, 0.f, 0.f, 0.f);
+                p.bnd_tex[n] = (uint8_t)bid;
+            }
+            return out;
+        }
+    }
+    const bool eqb = GENERIC && bid != 0u;  // equilibrium boundary cell (non-solid object)
+
+    // neighbour coordinates (periodic fast path: plain wrap)
+    const int xm = x == 0 ? nx - 1 : x - 1, xp = x == nx - 1 ? 0 : x + 1;
+    const int ym = y == 0 ? ny - 1 : y - 1, yp = y == ny - 1 ? 0 : y + 1;
+    const int zm = z == 0 ? nz - 1 : z - 1, zp = z == nz - 1 ? 0 : z + 1;
+    auto fast_cell = [&](int dx, int dy, int dz) -> uint32_t {
+        const int cx = dx < 0 ? xm : (dx > 0 ? xp : x);
+        const int cy = dy < 0 ? ym : (dy > 0 ? yp : y);
+        const int cz = dz < 0 ? zm : (dz > 0 ? zp : z);
+        return (uint32_t)cx + (uint32_t)nx * ((uint32_t)cy + (uint32_t)ny * (uint32_t)cz);
+    };
+
+    float4 bv = make_float4(1.f, 0.f, 0.f, 0.f);
+    if (eqb && p.bvals) bv = __ldg(p.bvals + n);
+
+    // ---- load (AA read, collide.comp:244-305) ----
+    float f[Q];
+#pragma unroll
+    for (int i = 0; i < Q; i++) {
+        const Dir c = L::c(i);
+        const float w = L::w(i);
+        if (!GENERIC) {
+            if (MODE == AA_EVEN) f[i] = C::dec(F[(uint64_t)i * S + fast_cell(-c.x, -c.y, -c.z)], w);
+            else f[i] = C::dec(F[(uint64_t)opp(i) * S + n], w);
+        } else {
+            int sx = x - c.x, sy = y - c.y, sz = z - c.z;
+            bool sopen;
+            coords_wrap<Q>(sx, sy, sz, nx, ny, nz, sopen, flags);
+            const uint32_t sn = sopen ? 0u : (uint32_t)sx + (uint32_t)nx * ((uint32_t)sy + (uint32_t)ny * (uint32_t)sz);
+            bool done = false;
+            if (MODE != AA_LOCAL && (eqb || (flags & F_BOUNCE_BACK)) && i != 0) {
+                if (eqb && sopen) {
+                    // population entering from outside the domain: f_eq(rho_b, u_b)
+                    const float cu = c.x * bv.y + c.y * bv.z + c.z * bv.w;
+                    const float uu = bv.y * bv.y + bv.z * bv.z + bv.w * bv.w;
+                    f[i] = w * bv.x * (1.f + cu * p.inv_cs2 + cu * cu * p.half_inv_cs4 - uu * p.half_inv_cs2);
+                    done = true;
+                } else if ((flags & F_BOUNCE_BACK) && !sopen && (flags & F_BOUNDARIES)) {
+                    const uint32_t sid = boundary_id(p.bnd, p.bits, sn);
+                    if (solid_id(p.obj_kind, sid)) {
+                        // halfway bounce-back: the cell's own outgoing opposite
+                        // population sits in the other AA slot
+                        const float4 uw = __ldg(p.objects + 3u * sid);
+                        const Dir co = L::c(opp(i));
+                        const float wall = __fmul_rn(__fmul_rn(-2.f * w, co.x * uw.x + co.y * uw.y + co.z * uw.z), 3.f);
+                        const float v = (MODE == AA_EVEN) ? C::dec(F[(uint64_t)opp(i) * S + n], w)
+                                                          : C::dec(F[(uint64_t)i * S + sn], w);
+                        f[i] = __fadd_rn(v, wall);
+                        done = true;
+                    }
+                }
+            }
+            if (!done) {
+                if (MODE == AA_EVEN) f[i] = sopen ? 0.01f : C::dec(F[(uint64_t)i * S + sn], w);
+                else if (MODE == AA_ODD) f[i] = C::dec(F[(uint64_t)opp(i) * S + n], w);
+                else f[i] = C::dec(F[(uint64_t)i * S + n], w);
+            }
+        }
+    }
+
+    // ---- moments ----
+    float rho = 0.f;
+#pragma unroll
+    for (int i = 0; i < Q; i++) rho += f[i];
+    if (GENERIC && !(rho == rho)) atomicOr(p.err, 1u);
+    rho = rho < 0.01f ? 0.01f : rho;  // max(density, 0.01), NaN kept
+    float jx = 0.f, jy = 0.f, jz = 0.f;
+#pragma unroll
+    for (int i = 0; i < Q; i++) {
+        const Dir c = L::c(i);
+        if (c.x) jx += c.x > 0 ? f[i] : -f[i];
+        if (c.y) jy += c.y > 0 ? f[i] : -f[i];
+        if (c.z) jz += c.z > 0 ? f[i] : -f[i];
+    }
+
+    // ---- forces (collide.comp:707-720) ----
+    float Fx = 0.f, Fy = 0.f, Fz = 0.f;
+    if (flags & F_FORCE_CONST) { Fx = p.fconst[0]; Fy = p.fconst[1]; Fz = p.fconst[2]; }
+    float temperature = 0.f;
+    if (GENERIC) {
+        if (flags & F_FORCE_FIELD) { const float4 fv = __ldg(p.force + n); Fx = fv.x; Fy = fv.y; Fz = fv.z; }
+        if (flags & F_THERMAL) {
+            constexpr int QT = L::D == 2 ? 5 : 7;
+#pragma unroll
+            for (int i = 0; i < QT; i++) temperature += __ldg(p.th_src + (uint64_t)i * S + n);
+            const float k = __fmul_rn(-p.beta, __fsub_rn(temperature, 1.0f));
+            Fx = __fadd_rn(Fx, __fmul_rn(k, Fx)); Fy = __fadd_rn(Fy, __fmul_rn(k, Fy)); Fz = __fadd_rn(Fz, __fmul_rn(k, Fz));
+        }
+        if (flags & F_MULTIPHASE) {
+            const float self_psi = 1.0f - expf(-rho);
+            float sx = 0.f, sy = 0.f, sz = 0.f;
+#pragma unroll
+            for (int i = 1; i < Q; i++) {
+                const Dir c = L::c(i);
+                int ax = x + c.x, ay = y + c.y, az = z + c.z;
+                bool aopen;
+                coords_wrap<Q>(ax, ay, az, nx, ny, nz, aopen, flags);
+                const float ps = aopen ? self_psi
+                                       : __ldg(p.psi_src + (uint32_t)ax + (uint32_t)nx * ((uint32_t)ay + (uint32_t)ny * (uint32_t)az));
+                const float wp = __fmul_rn(L::w(i), ps);
+                if (c.x) sx = __fadd_rn(sx, c.x > 0 ? wp : -wp);
+                if (c.y) sy = __fadd_rn(sy, c.y > 0 ? wp : -wp);
+                if (c.z) sz = __fadd_rn(sz, c.z > 0 ? wp : -wp);
+            }
+            const float k = __fmul_rn(-self_psi, p.G);
+            Fx = __fadd_rn(Fx, __fmul_rn(sx, k)); Fy = __fadd_rn(Fy, __fmul_rn(sy, k)); Fz = __fadd_rn(Fz, __fmul_rn(sz, k));
+        }
+    }
+
+    // ---- velocity, limiter (collide.comp:722-725) ----
+    // The moments use the shader's operation order with rounded (uncontracted)
+    // operations, so rho and u agree bit for bit with a literal FP32 restatement
+    // given the same populations; only the collision below is reassociated.
+    float ux = __fdiv_rn(jx, rho), uy = __fdiv_rn(jy, rho), uz = __fdiv_rn(jz, rho);
+    if (flags & (F_FORCE_CONST | F_FORCE_FIELD | F_THERMAL | F_MULTIPHASE)) {
+        const float r2 = __fmul_rn(2.0f, rho);
+        ux = __fadd_rn(ux, __fdiv_rn(Fx, r2));
+        uy = __fadd_rn(uy, __fdiv_rn(Fy, r2));
+        uz = __fadd_rn(uz, __fdiv_rn(Fz, r2));
+    }
+    const float len = sqrtf(__fadd_rn(__fadd_rn(__fmul_rn(ux, ux), __fmul_rn(uy, uy)), __fmul_rn(uz, uz)));
+    const bool out_ext = len > p.vlim_ext;
+    if (len > p.vlim) {
+        ux = __fmul_rn(__fdiv_rn(ux, len), p.vlim);
+        uy = __fmul_rn(__fdiv_rn(uy, len), p.vlim);
+        uz = __fmul_rn(__fdiv_rn(uz, len), p.vlim);
+    }
+    if (eqb) {
+        const int kind = __ldg(p.obj_kind + bid);
+        if (kind == 1) { ux = bv.y; uy = bv.z; uz = bv.w; } else { rho = bv.x; }
+        Fx = Fy = Fz = 0.f;
+    }
+    const float uu = ux * ux + uy * uy + uz * uz;
+
+    // ---- collision + AA store (collide.comp:727-760) ----
+    if (flags & F_UPDATE) {
+        const float fu = Fx * ux + Fy * uy + Fz * uz;
+        const float base = 1.0f - uu * p.half_inv_cs2;
+        float fn[Q];
+        if (!(flags & F_TRT)) {
+#pragma unroll
+            for (int i = 0; i < Q; i++) {
+                const Dir c = L::c(i);
+                const float w = L::w(i);
+                const float cu = c.x * ux + c.y * uy + c.z * uz;
+                const float feq = w * rho * (base + cu * p.inv_cs2 + cu * cu * p.half_inv_cs4);
+                float v = fmaf(feq - f[i], p.inv_tau, f[i]);
+                if (flags & F_SOURCE) {
+                    const float fc = c.x * Fx + c.y * Fy + c.z * Fz;
+                    v += p.src_pref * w * (fc * p.inv_cs2 + fc * cu * p.inv_cs4 - fu * p.inv_cs2);
+                }
+                fn[i] = (out_ext || eqb) ? feq : v;
+            }
+        } else {
+            const float wp = p.inv_tau, wm = p.trt_inv_tau_minus;
+            const float sp_pref = 1.0f - 0.5f * wp, sm_pref = 1.0f - 0.5f * wm;
+            {
+                const float w = L::w(0);
+                const float feq = w * rho * base;
+                float v = f[0] - wp * (f[0] - feq);
+                if (flags & F_SOURCE) v += sp_pref * w * (-fu * p.inv_cs2);
+                fn[0] = (out_ext || eqb) ? feq : v;
+            }
+#pragma unroll
+            for (int i = 1; i < Q; i += 2) {
+                const int j = i + 1;
+                const Dir c = L::c(i);
+                const float w = L::w(i);
+                const float cu = c.x * ux + c.y * uy + c.z * uz;
+                const float ep = w * rho * (base + cu * cu * p.half_inv_cs4);
+                const float em = w * rho * (cu * p.inv_cs2);
+                const float fp = 0.5f * (f[i] + f[j]), fm = 0.5f * (f[i] - f[j]);
+                const float dp = wp * (fp - ep), dm = wm * (fm - em);
+                float vi = f[i] - dp - dm, vj = f[j] - dp + dm;
+                if (flags & F_SOURCE) {
+                    const float fc = c.x * Fx + c.y * Fy + c.z * Fz;
+                    const float Sp = sp_pref * w * (fc * cu * p.inv_cs4 - fu * p.inv_cs2);
+                    const float Sm = sm_pref * w * (fc * p.inv_cs2);
+                    vi += Sp + Sm; vj += Sp - Sm;
+                }
+                fn[i] = (out_ext || eqb) ? ep + em : vi;
+                fn[j] = (out_ext || eqb) ? ep - em : vj;
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < Q; i++) {
+            const Dir c = L::c(i);
+            const float w = L::w(i);
+            if (MODE == AA_EVEN) {
+                if (!GENERIC) {
+                    F[(uint64_t)opp(i) * S + fast_cell(c.x, c.y, c.z)] = C::enc(fn[i], w);
+                } else {
+                    int dx = x + c.x, dy = y + c.y, dz = z + c.z;
+                    bool dopen;
+                    coords_wrap<Q>(dx, dy, dz, nx, ny, nz, dopen, flags);
+                    if (!dopen)
+                        F[(uint64_t)opp(i) * S + (uint32_t)dx + (uint32_t)nx * ((uint32_t)dy + (uint32_t)ny * (uint32_t)dz)] =
+                            C::enc(fn[i], w);
+                }
+            } else {
+                F[(uint64_t)i * S + n] = C::enc(fn[i], w);
+            }
+        }
+    }
+
+    if (GENERIC && (flags & F_MULTIPHASE) && !(flags & F_MEASURE)) {  // collide.comp:763-769, psi of the effective density
+        float eff = rho;
+        if (bid != 0u) eff = __ldg(p.objects + 3u * bid + 2u).w;
+        p.psi_tgt[n] = 1.0f - expf(-eff);
+    }
+    if (GENERIC && (flags & F_THERMAL) && !(flags & F_MEASURE)) {  // collide.comp:771-782
+        constexpr int QT = L::D == 2 ? 5 : 7;
+#pragma unroll
+        for (int i = 0; i < QT; i++) {
+            const Dir c = ThermalLattice<QT>::c(i);
+            const float w = ThermalLattice<QT>::w(i);
+            const float cu = c.x * ux + c.y * uy + c.z * uz;
+            const float geq = w * temperature * (1.0f + cu * p.inv_cs2 + cu * cu * p.half_inv_cs4 - uu * p.half_inv_cs2);
+            const float g = __ldg(p.th_src + (uint64_t)i * S + n);
+            p.th_tgt[(uint64_t)i * S + n] = fmaf(geq - g, p.inv_tau_t, g);
+        }
+    }
+    if (flags & F_SAVE) {  // collide.comp:784-792
+        p.vel_den[n] = make_float4(ux, uy, uz, rho);
+        if (GENERIC) {
+            p.force_temp[n] = make_float4(Fx, Fy, Fz, temperature);
+            if (p.bnd_tex) p.bnd_tex[n] = (uint8_t)bid;
+        } else if (p.force_temp) {
+            p.force_temp[n] = make_float4(Fx, Fy, Fz, 0.f);
+        }
+    }
+    if (flags & F_REDUCE) {
+        out.m = rho; out.px = rho * ux; out.py = rho * uy; out.pz = rho * uz;
+        out.ke = 0.5f * rho * uu;
+    }
+    return out;
+}
+
+template <int Q, int ST, int MODE, bool GENERIC>
+__global__ void __launch_bounds__(kStepBlock) step_kernel(const __grid_constant__ StepParams p) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    CellSum cs = {0.f, 0.f, 0.f, 0.f, 0.f};
+    if (x < p.nx) cs = cell_update<Q, ST, MODE, GENERIC>(p, x, blockIdx.y, blockIdx.z);
+    if (p.flags & F_REDUCE) block_reduce_store(cs, p.red_partials);
+}
+
+// ---------------------------------------------------------------------------
+// two-buffer pull streaming (stream.comp main, :498-584)
+// ---------------------------------------------------------------------------
+template <int Q, int ST>
+__global__ void __launch_bounds__(kStepBlock) stream_kernel(const __grid_constant__ StreamParams p) {
+    using L = Lattice<Q>;
+    using C = Codec<ST>;
+    using T = typename C::T;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
+    if (x >= p.nx) return;
+    const T* __restrict__ src = static_cast<const T*>(p.src);
+    T* __restrict__ dst = static_cast<T*>(p.dst);
+    const uint64_t S = p.stride;
+    const uint32_t n = (uint32_t)x + (uint32_t)p.nx * ((uint32_t)y + (uint32_t)p.ny * (uint32_t)z);
+    if (p.flags & F_BOUNDARIES) {
+        if (solid_id(p.obj_kind, boundary_id(p.bnd, p.bits, n))) return;
+    }
+#pragma unroll
+    for (int i = 0; i < Q; i++) {
+        const Dir c = L::c(i);
+        const float w = L::w(i);
+        int sx = x - c.x, sy = y - c.y, sz = z - c.z;
+        bool open;
+        coords_wrap<Q>(sx, sy, sz, p.nx, p.ny, p.nz, open, p.flags);
+        if (open) { dst[(uint64_t)i * S + n] = C::enc(0.01f, w); continue; }
+        const uint32_t sn = (uint32_t)sx + (uint32_t)p.nx * ((uint32_t)sy + (uint32_t)p.ny * (uint32_t)sz);
+        uint32_t sid = (p.flags & F_BOUNDARIES) ? boundary_id(p.bnd, p.bits, sn) : 0u;
+        if (sid != 0u && solid_id(p.obj_kind, sid)) {
+            const int inv = opp(i);
+            const Dir ci = L::c(inv);
+            const float4 uw = __ldg(p.objects + 3u * sid);
+            const float corr = __fmul_rn(__fmul_rn(-2.f * L::w(inv), ci.x * uw.x + ci.y * uw.y + ci.z * uw.z), 3.f);
+            dst[(uint64_t)i * S + n] = C::enc(__fadd_rn(C::dec(src[(uint64_t)inv * S + n], L::w(inv)), corr), w);
+        } else {
+            dst[(uint64_t)i * S + n] = src[(uint64_t)i * S + sn];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// thermal pull streaming (stream_thermal.comp main, :457-526), SoA layout
+// ---------------------------------------------------------------------------
+template <int QT>
+__global__ void __launch_bounds__(kStepBlock) stream_thermal_kernel(const __grid_constant__ ThermalStreamParams p) {
+    using TL = ThermalLattice<QT>;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
+    if (x >= p.nx) return;
+    const uint64_t S = p.stride;
+    const uint32_t n = (uint32_t)x + (uint32_t)p.nx * ((uint32_t)y + (uint32_t)p.ny * (uint32_t)z);
+    if (p.flags & F_BOUNDARIES) {
+        if (solid_id(p.obj_kind, boundary_id(p.bnd, p.bits, n))) return;
+    }
+#pragma unroll
+    for (int i = 0; i < QT; i++) {
+        const Dir c = TL::c(i);
+        int sx = x - c.x, sy = y - c.y, sz = z - c.z;
+        bool open;
+        coords_wrap<QT>(sx, sy, sz, p.nx, p.ny, p.nz, open, p.flags);
+        if (open) continue;  // no write (stream_thermal.comp:481-503)
+        const uint32_t sn = (uint32_t)sx + (uint32_t)p.nx * ((uint32_t)sy + (uint32_t)p.ny * (uint32_t)sz);
+        uint32_t sid = (p.flags & F_BOUNDARIES) ? boundary_id(p.bnd, p.bits, sn) : 0u;
+        if (sid != 0u && solid_id(p.obj_kind, sid)) {
+            const int inv = (i == 0) ? 0 : ((i & 1) ? i + 1 : i - 1);
+            const float Tw = __ldg(p.objects + 3u * sid).w;
+            p.dst[(uint64_t)i * S + n] = __fadd_rn(-__ldg(p.src + (uint64_t)inv * S + n), __fmul_rn(2.f * TL::w(inv), Tw));
+        } else {
+            p.dst[(uint64_t)i * S + n] = __ldg(p.src + (uint64_t)i * S + sn);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// equilibrium initialisation (set_equilibrium_populations.comp:179-221)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float feq_init_dot(float ax, float ay, float az, float bx, float by, float bz) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(ax, bx), __fmul_rn(ay, by)), __fmul_rn(az, bz));
+}
+__device__ __forceinline__ float feq_init_literal(float w, float r, float cu, float uu) {
+    float a = __fadd_rn(1.0f, __fmul_rn(3.0f, cu));
+    a = __fadd_rn(a, __fdiv_rn(__fmul_rn(9.0f, __fmul_rn(cu, cu)), 2.0f));
+    a = __fsub_rn(a, __fdiv_rn(__fmul_rn(3.0f, uu), 2.0f));
+    return __fmul_rn(__fmul_rn(w, r), a);
+}
+
+template <int Q, int ST>
+__global__ void init_kernel(const __grid_constant__ InitParams p) {
+    using L = Lattice<Q>;
+    using C = Codec<ST>;
+    using T = typename C::T;
+    const uint64_t n = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (n >= p.n_cells) return;
+    T* F = static_cast<T*>(p.f);
+    const float r = p.rho ? p.rho[n] : 1.0f;
+    float ux = 0.f, uy = 0.f, uz = 0.f;
+    const uint32_t id = p.ids ? p.ids[n] : 0u;
+    const bool solid = id != 0u && p.obj_kind[id] == 0;
+    if (p.u && !solid) { ux = p.u[3 * n]; uy = p.u[3 * n + 1]; uz = p.u[3 * n + 2]; }
+    // w*rho*(1 + 3*cu + 9*cu^2/2 - 3*uu/2) with the shader's literal constants
+    // and operation order, rounded operations only (init runs once)
+    const float uu = feq_init_dot(ux, uy, uz, ux, uy, uz);
+#pragma unroll
+    for (int i = 0; i < Q; i++) {
+        const Dir c = L::c(i);
+        const float w = L::w(i);
+        const float cu = feq_init_dot((float)c.x, (float)c.y, (float)c.z, ux, uy, uz);
+        F[i * p.stride + n] = C::enc(feq_init_literal(w, r, cu, uu), w);
+    }
+}
+
+template <int QT>
+__global__ void init_thermal_kernel(const __grid_constant__ InitParams p) {
+    using TL = ThermalLattice<QT>;
+    const uint64_t n = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (n >= p.n_cells) return;
+    const float t = p.T ? p.T[n] : 1.0f;
+    if (t == 0.0f) return;  // set_equilibrium_populations_thermal.comp:171-172
+    float ux = 0.f, uy = 0.f, uz = 0.f;
+    const uint32_t id = p.ids ? p.ids[n] : 0u;
+    const bool solid = id != 0u && p.obj_kind[id] == 0;
+    if (p.u && !solid) { ux = p.u[3 * n]; uy = p.u[3 * n + 1]; uz = p.u[3 * n + 2]; }
+    const float uu = feq_init_dot(ux, uy, uz, ux, uy, uz);
+#pragma unroll
+    for (int i = 0; i < QT; i++) {
+        const Dir c = TL::c(i);
+        const float cu = feq_init_dot((float)c.x, (float)c.y, (float)c.z, ux, uy, uz);
+        p.th[i * p.stride + n] = feq_init_literal(TL::w(i), t, cu, uu);
+    }
+}
+
+// decode / encode the whole DDF (readback, snapshots)
+template <int Q, int ST>
+__global__ void decode_kernel(const void* f, uint64_t stride, uint32_t n_cells, float* out) {
+    using C = Codec<ST>;
+    using T = typename C::T;
+    const uint64_t n = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (n >= n_cells) return;
+    const T* F = static_cast<const T*>(f);
+#pragma unroll
+    for (int i = 0; i < Q; i++) out[(uint64_t)i * n_cells + n] = C::dec(F[(uint64_t)i * stride + n], Lattice<Q>::w(i));
+}
+template <int Q, int ST>
+__global__ void encode_kernel(void* f, uint64_t stride, uint32_t n_cells, const float* in) {
+    using C = Codec<ST>;
+    using T = typename C::T;
+    const uint64_t n = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (n >= n_cells) return;
+    T* F = static_cast<T*>(f);
+#pragma unroll
+    for (int i = 0; i < Q; i++) F[(uint64_t)i * stride + n] = C::enc(in[(uint64_t)i * n_cells + n], Lattice<Q>::w(i));
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+inline dim3 cell_grid(int nx, int ny, int nz, int& block) {
+    block = nx >= kStepBlock ? kStepBlock : ((nx + 31) / 32) * 32;
+    return dim3((unsigned)((nx + block - 1) / block), (unsigned)ny, (unsigned)nz);
+}
+
+template <int Q, int ST>
+cudaError_t launch_step_st(const StepParams& p, int mode, bool generic, cudaStream_t st) {
+    int block;
+    dim3 grid = cell_grid(p.nx, p.ny, p.nz, block);
+    if (!generic) {
+        if (mode == AA_EVEN) step_kernel<Q, ST, AA_EVEN, false><<<grid, block, 0, st>>>(p);
+        else step_kernel<Q, ST, AA_ODD, false><<<grid, block, 0, st>>>(p);
+    } else {
+        if (mode == AA_EVEN) step_kernel<Q, ST, AA_EVEN, true><<<grid, block, 0, st>>>(p);
+        else if (mode == AA_ODD) step_kernel<Q, ST, AA_ODD, true><<<grid, block, 0, st>>>(p);
+        else step_kernel<Q, ST, AA_LOCAL, true><<<grid, block, 0, st>>>(p);
+    }
+    return cudaGetLastError();
+}
+
+template <int Q>
+cudaError_t launch_step(const StepParams& p, int storage, int mode, bool generic, cudaStream_t st) {
+    switch (storage) {
+    case ST_FP32: return launch_step_st<Q, ST_FP32>(p, mode, generic, st);
+    case ST_FP16: return launch_step_st<Q, ST_FP16>(p, mode, generic, st);
+    case ST_FP16S: return launch_step_st<Q, ST_FP16S>(p, mode, generic, st);
+    case ST_FP16C: return launch_step_st<Q, ST_FP16C>(p, mode, generic, st);
+    }
+    return cudaErrorInvalidValue;
+}
+
+template <int Q>
+cudaError_t launch_stream(const StreamParams& p, int storage, cudaStream_t st) {
+    int block;
+    dim3 grid = cell_grid(p.nx, p.ny, p.nz, block);
+    switch (storage) {
+    case ST_FP32: stream_kernel<Q, ST_FP32><<<grid, block, 0, st>>>(p); break;
+    case ST_FP16: stream_kernel<Q, ST_FP16><<<grid, block, 0, st>>>(p); break;
+    case ST_FP16S: stream_kernel<Q, ST_FP16S><<<grid, block, 0, st>>>(p); break;
+    case ST_FP16C: stream_kernel<Q, ST_FP16C><<<grid, block, 0, st>>>(p); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+template <int Q>
+cudaError_t launch_init(const InitParams& p, int storage, cudaStream_t st) {
+    const unsigned blocks = (unsigned)((p.n_cells + 255u) / 256u);
+    switch (storage) {
+    case ST_FP32: init_kernel<Q, ST_FP32><<<blocks, 256, 0, st>>>(p); break;
+    case ST_FP16: init_kernel<Q, ST_FP16><<<blocks, 256, 0, st>>>(p); break;
+    case ST_FP16S: init_kernel<Q, ST_FP16S><<<blocks, 256, 0, st>>>(p); break;
+    case ST_FP16C: init_kernel<Q, ST_FP16C><<<blocks, 256, 0, st>>>(p); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+template <int Q>
+cudaError_t launch_decode(const void* f, uint64_t stride, uint32_t n, int storage, float* out, cudaStream_t st) {
+    const unsigned blocks = (n + 255u) / 256u;
+    switch (storage) {
+    case ST_FP32: decode_kernel<Q, ST_FP32><<<blocks, 256, 0, st>>>(f, stride, n, out); break;
+    case ST_FP16: decode_kernel<Q, ST_FP16><<<blocks, 256, 0, st>>>(f, stride, n, out); break;
+    case ST_FP16S: decode_kernel<Q, ST_FP16S><<<blocks, 256, 0, st>>>(f, stride, n, out); break;
+    case ST_FP16C: decode_kernel<Q, ST_FP16C><<<blocks, 256, 0, st>>>(f, stride, n, out); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+template <int Q>
+cudaError_t launch_encode(void* f, uint64_t stride, uint32_t n, int storage, const float* in, cudaStream_t st) {
+    const unsigned blocks = (n + 255u) / 256u;
+    switch (storage) {
+    case ST_FP32: encode_kernel<Q, ST_FP32><<<blocks, 256, 0, st>>>(f, stride, n, in); break;
+    case ST_FP16: encode_kernel<Q, ST_FP16><<<blocks, 256, 0, st>>>(f, stride, n, in); break;
+    case ST_FP16S: encode_kernel<Q, ST_FP16S><<<blocks, 256, 0, st>>>(f, stride, n, in); break;
+    case ST_FP16C: encode_kernel<Q, ST_FP16C><<<blocks, 256, 0, st>>>(f, stride, n, in); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+#define BF_INSTANTIATE_Q(Q)                                                                                   \
+    template cudaError_t launch_step<Q>(const StepParams&, int, int, bool, cudaStream_t);                    \
+    template cudaError_t launch_stream<Q>(const StreamParams&, int, cudaStream_t);                           \
+    template cudaError_t launch_init<Q>(const InitParams&, int, cudaStream_t);                               \
+    template cudaError_t launch_decode<Q>(const void*, uint64_t, uint32_t, int, float*, cudaStream_t);        \
+    template cudaError_t launch_encode<Q>(void*, uint64_t, uint32_t, int, const float*, cudaStream_t);
+
+}  // namespace bf

@@ -1,0 +1,6 @@
+// Instantiates the D*Q19 step, stream, init and codec kernels (one
+// translation unit per velocity set keeps the build parallel).
+#include "lbm_kernels.cuh"
+namespace bf {
+BF_INSTANTIATE_Q(19)
+}

@@ -1,0 +1,226 @@
+/*
+ * bf_lbm.h -- C ABI of the GB300 lattice Boltzmann solver.
+ *
+ * Drop-in replacement for the GL compute path behind BoltzmannFluids' solver
+ * class `LBM` (BoltzmannFluids/Source/LBM/LBM.h:26-332).  Every entry point
+ * below names the reference member it replaces.  Plain C types only: device
+ * memory is owned by the solver handle; host arrays are caller-owned and are
+ * only read or written during the call.
+ *
+ * Threading: one solver handle belongs to one host thread at a time (the
+ * reference's LBM object is likewise bound to the thread owning its GL
+ * context, BoltzmannFluids_UI/Source/GUIApplication/SimulationController.cpp:17).
+ * Each handle owns one CUDA stream; all calls are ordered on it.
+ *
+ * Errors: every call returns a bf_status (0 = BF_OK, negative = error) and
+ * records a message retrievable with bf_last_error(); the reference printed
+ * "[LBM Error] ..." and asserted (LBM.cpp:429-437, :570-573, :1024-1032).
+ */
+#ifndef BF_LBM_H
+#define BF_LBM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BF_ABI_VERSION 1
+
+typedef enum {
+    BF_OK = 0,
+    BF_ERR_INVALID_ARGUMENT = -1, /* bad size, enum, pointer or order of calls */
+    BF_ERR_CUDA = -2,             /* a CUDA runtime call failed */
+    BF_ERR_OUT_OF_MEMORY = -3,    /* device allocation failed */
+    BF_ERR_NOT_INITIALIZED = -4,  /* bf_initialize_fields has not run */
+    BF_ERR_UNSTABLE = -5,         /* the step kernels saw a NaN density */
+    BF_ERR_TIMEOUT = -6,          /* a bounded host wait gave up */
+    BF_ERR_IO = -7,               /* snapshot file could not be read/written */
+    BF_ERR_NO_DEVICE = -8         /* no CUDA device is visible */
+} bf_status;
+
+/* VelocitySet (BoltzmannFluids/Source/LBMConstants/VelocitySet.h:18-23): same numeric values. */
+typedef enum { BF_D2Q9 = 2, BF_D3Q15 = 3, BF_D3Q19 = 4, BF_D3Q27 = 5 } bf_velocity_set;
+
+/* DDF storage.  BF_STORE_FP16 is the reference's FloatingPointAccuracy::fp16
+ * (an R16F lattice: IEEE half of f itself, LBM.cpp:446-449);
+ * BF_STORE_FP16S stores IEEE half of the shifted population f_i - w_i;
+ * BF_STORE_FP16C stores (f_i - w_i)/w_i in a custom 1-4-11 16-bit float
+ * (exponent range 2^-12..2^2, subnormals to 2^-23, saturating).
+ * Arithmetic is FP32 in every mode. */
+typedef enum { BF_STORE_FP32 = 0, BF_STORE_FP16 = 1, BF_STORE_FP16S = 2, BF_STORE_FP16C = 3 } bf_storage;
+
+/* How a fluid cell next to a solid cell receives populations in the
+ * esoteric (AA, in-place) mode.
+ * BF_BOUNDARY_SKIP: as the reference's collide.comp reads it (:696-700):
+ *   solid cells are skipped and neighbours read whatever their slots hold.
+ * BF_BOUNDARY_BOUNCE_BACK: halfway bounce-back with the moving-wall term of
+ *   stream.comp:487-496/576-580 (rho_wall = 1), folded into the AA step. */
+typedef enum { BF_BOUNDARY_SKIP = 0, BF_BOUNDARY_BOUNCE_BACK = 1 } bf_boundary_mode;
+
+typedef enum { BF_COLLISION_BGK = 0, BF_COLLISION_TRT = 1 } bf_collision;
+
+/* Boundary object kinds.  The reference only has solid objects; the two
+ * equilibrium kinds are extensions: a cell of such an object is updated to
+ * f_eq(rho_local, u_b) (velocity) or f_eq(rho_b, u_local) (density), where
+ * (rho_b, u_b) are the cell's initial density and velocity and populations
+ * that would stream in from outside the domain are taken as f_eq(rho_b, u_b). */
+typedef enum { BF_OBJECT_SOLID = 0, BF_OBJECT_EQ_VELOCITY = 1, BF_OBJECT_EQ_DENSITY = 2 } bf_object_kind;
+
+typedef enum {
+    BF_FIELD_VELOCITY_DENSITY = 0, /* float4 (u.xyz, rho) per cell: get_velocity_density_texture, LBM.h:97 */
+    BF_FIELD_BOUNDARY = 1,         /* uint8 boundary id per cell: get_boundry_texture, LBM.h:98 */
+    BF_FIELD_FORCE_TEMPERATURE = 2,/* float4 (F.xyz, T) per cell: get_force_temperature_texture, LBM.h:99 */
+    BF_FIELD_POPULATIONS = 3,      /* float per (population, cell), SoA i*N+cell, decoded to FP32 */
+    BF_FIELD_THERMAL_POPULATIONS = 4 /* float per (population, cell), SoA */
+} bf_field_kind;
+
+typedef struct bf_solver bf_solver;
+
+/* Arguments of LBM::initialize_fields (LBM.h:48-58) plus the public knobs of
+ * LBM.h:139-145, :242-243, :257 and the extensions. Fill with
+ * bf_init_desc_default() first. */
+typedef struct {
+    int32_t resolution[3];          /* cells; resolution[2] must be 1 for D2Q9 (LBM.cpp:434-437) */
+    float relaxation_time;          /* tau */
+    int32_t periodic[3];            /* periodic_x/y/z */
+    int32_t velocity_set;           /* bf_velocity_set */
+    int32_t storage;                /* bf_storage (fp_accuracy) */
+    int32_t multiphase;             /* is_flow_multiphase: Shan-Chen pseudopotential */
+    int32_t esoteric;               /* is_collide_esoteric: 1 = AA in place, 0 = two buffers */
+    int32_t boundary_mode;          /* bf_boundary_mode (esoteric mode only) */
+    int32_t collision;              /* bf_collision */
+    float trt_magic;                /* TRT magic parameter Lambda (1/4 by default) */
+    float velocity_limit;           /* LBM.h:144 (0.25) */
+    float velocity_limit_extreme;   /* LBM.h:145 (0.30) */
+    float intermolecular_interaction_strength; /* G, LBM.h:257 (-6) */
+    float thermal_relaxation_time;  /* tau_T; initialize_fields sets 2 (LBM.cpp:461) */
+    float thermal_expansion_coefficient; /* beta, LBM.h:243 (0.5) */
+    int32_t thermal_init_equilibrium;/* 0: as the reference reads (thermal lattice left zero), 1: equilibrium */
+    int32_t two_buffer_fixed;       /* esoteric=0 only. 0: reference's swap order (stream reads the
+                                       un-collided buffer, LBM.cpp:1646-1647/1509-1513); 1: collide then stream */
+    int32_t reserved[8];
+} bf_init_desc;
+
+/* Fills the defaults of LBM.h (tau 0.53, periodic, D2Q9, fp32, limits 0.25/0.30,
+ * G -6, tau_T 2, beta 0.5, two-buffer, skip boundaries, BGK, Lambda 1/4). */
+void bf_init_desc_default(bf_init_desc* desc);
+
+/* Object record, the 3 x vec4 layout of LBM.cpp:613-626 plus a kind. */
+typedef struct {
+    float velocity_translational[3];
+    float temperature;
+    float velocity_angular[3];
+    float center_of_mass[3];
+    float effective_density;
+    int32_t kind;                   /* bf_object_kind */
+} bf_object;
+
+/* device view of a field (headless stand-in for the reference's Texture3D) */
+typedef struct {
+    void* device_ptr;
+    int32_t kind;                   /* bf_field_kind */
+    int32_t resolution[3];
+    int32_t components;             /* 4, 1 */
+    int32_t bytes_per_component;    /* 4 or 1 */
+    size_t bytes;
+} bf_field;
+
+/* ---- host-only lattice helpers (no device needed) ----------------------- */
+/* get_velosity_vectors (VelocitySet.cpp:53-142, :180-204): writes count*4
+ * floats (c.x, c.y, c.z, w) of the flow set (BF_D2Q9..BF_D3Q27) or, with
+ * thermal != 0, of its thermal set (D2Q5 for D2Q9, D3Q7 otherwise).
+ * out may be NULL to query *count. */
+int bf_get_velosity_vectors(int32_t velocity_set, int32_t thermal, float* out, int32_t* count);
+/* bits per boundary id for a given object count (LBM.cpp:569): 0, 1, 2, 4 or 8 */
+int bf_bits_per_boundry(int32_t object_count, int32_t* bits);
+/* packs one id per cell into uint32 words, `bits` per id, low bits first,
+ * exactly as LBM.cpp:634-659.  out may be NULL to query *words. */
+int bf_pack_boundries(const uint32_t* ids, size_t cells, int32_t bits, uint32_t* out, size_t capacity_words,
+                      size_t* words);
+
+/* ---- lifetime ---------------------------------------------------------- */
+/* LBM::LBM (implicit constructor).  Selects the current CUDA device. */
+int bf_create(bf_solver** out);
+/* LBM::~LBM: frees every device buffer of the handle. */
+int bf_destroy(bf_solver* s);
+/* message of the last failed call on this thread */
+const char* bf_last_error(void);
+int bf_abi_version(void);
+
+/* ---- boundary objects (LBM.h:60-82) ------------------------------------ */
+/* LBM::set_boundry_properties (all three overloads, LBM.cpp:1015-1065). id in 1..255. */
+int bf_set_boundry_properties(bf_solver* s, uint32_t boundry_id, const bf_object* object);
+/* LBM::clear_boundry_properties (LBM.cpp:1067-1070) */
+int bf_clear_boundry_properties(bf_solver* s);
+
+/* ---- initialisation ---------------------------------------------------- */
+/* LBM::initialize_fields (LBM.cpp:415-506) given the per-cell results of the
+ * initialisation lambda as host arrays of N = rx*ry*rz cells, x fastest:
+ *   density[N]   (NULL: 1)         velocity[3N] (NULL: 0)
+ *   force[3N]    (NULL: 0)         temperature[N] (NULL: 1)
+ *   boundry_id[N] (NULL: all 0)
+ * Derives the forcing/constant-force/thermal switches and the packed boundary
+ * bits exactly as LBM.cpp:523-569, uploads, writes equilibrium populations
+ * and runs the reference's save-only first pass (LBM.cpp:502). */
+int bf_initialize_fields(bf_solver* s, const bf_init_desc* desc,
+                         const float* density, const float* velocity, const float* force,
+                         const float* temperature, const uint32_t* boundry_id);
+
+/* ---- time stepping ----------------------------------------------------- */
+/* LBM::iterate_time (LBM.cpp:220-240) run n_steps times with
+ * target_tick_per_second = 0.  save_fields != 0 writes the macroscopic fields
+ * on the last step (the reference's 60 Hz "collide_save" variant).  Steps are
+ * launched from a captured CUDA graph per batch; the call returns once the
+ * work is queued (use bf_synchronize to wait). */
+int bf_iterate_time(bf_solver* s, int32_t n_steps, int32_t save_fields);
+/* waits for the handle's stream; gives up with BF_ERR_TIMEOUT after timeout_ms
+ * (<= 0: wait without limit), and returns BF_ERR_UNSTABLE if a step saw NaN. */
+int bf_synchronize(bf_solver* s, int32_t timeout_ms);
+
+/* ---- getters / setters (LBM.h:35-38, :105-120) -------------------------- */
+int bf_get_total_ticks_elapsed(bf_solver* s, int64_t* ticks);
+int bf_get_resolution(bf_solver* s, int32_t resolution[3]);
+int bf_get_velocity_set_vector_count(bf_solver* s, int32_t* q);
+int bf_get_relaxation_time(bf_solver* s, float* tau);
+int bf_set_relaxation_time(bf_solver* s, float tau);
+int bf_get_constant_force(bf_solver* s, float force[3]);
+int bf_set_constant_force(bf_solver* s, const float force[3]);
+int bf_get_intermolecular_interaction_strength(bf_solver* s, float* g);
+int bf_set_intermolecular_interaction_strength(bf_solver* s, float g);
+int bf_set_velocity_limits(bf_solver* s, float limit, float limit_extreme);
+int bf_set_thermal_parameters(bf_solver* s, float thermal_relaxation_time, float thermal_expansion_coefficient);
+/* flags: bit0 forcing scheme, bit1 constant force field, bit2 thermal, bit3
+ * multiphase, bit4 boundaries present; bits_per_boundry as LBM.cpp:569 */
+int bf_get_scheme_flags(bf_solver* s, int32_t* flags, int32_t* bits_per_boundry);
+
+/* ---- field readback (LBM.h:97-99, LBM.cpp:1444-1457) -------------------- */
+/* device pointer + shape of a field; valid until the next bf_initialize_fields/bf_destroy */
+int bf_get_field(bf_solver* s, int32_t kind, bf_field* out);
+/* copies a field to host memory (bytes must be at least the field's size) */
+int bf_copy_field_to_host(bf_solver* s, int32_t kind, void* dst, size_t bytes);
+/* packed boundary words as built by LBM.cpp:634-659 (count in *words) */
+int bf_copy_boundry_bits_to_host(bf_solver* s, uint32_t* dst, size_t capacity_words, size_t* words);
+
+/* ---- conservation reductions (FP64) ------------------------------------ */
+/* Sums over non-solid cells of the last saved step: out = {mass, momentum x,
+ * y, z, kinetic energy 0.5*rho*|u|^2}.  Runs one step with field saving and
+ * a fused FP64 block reduction if the last step did not save. No counterpart
+ * in the reference. */
+int bf_reduce(bf_solver* s, double out[5]);
+
+/* ---- timing ------------------------------------------------------------ */
+/* Runs n_steps steps (no field saving) between two CUDA events recorded on
+ * the handle's stream and returns the elapsed device time in milliseconds.
+ * No counterpart in the reference, which only counts ticks (LBM.cpp:242-250). */
+int bf_benchmark_steps(bf_solver* s, int32_t n_steps, float* ms);
+
+/* ---- snapshots (LBM.h:123-126, declared but never defined upstream) ------ */
+int bf_save_snapshot(bf_solver* s, const char* path);
+int bf_load_snapshot(bf_solver* s, const char* path);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,775 @@
+/*
+ * lbm_oracle.c -- CPU restatement of BoltzmannFluids' per-timestep lattice
+ * Boltzmann update.  TEST INFRASTRUCTURE ONLY: the parity tests, the smoke
+ * check and the CPU-baseline leg of bench.py load this library as the
+ * checker; the product (boltzmannfluids_gb300) never links or calls it.
+ *
+ * Parity status: the reference's shaders cannot run here (no graphics stack,
+ * GraphicsCortex not vendored).  This restatement is pinned by
+ *   - golden tables parsed from the reference's own source text
+ *     (tests/golden/, generated by tests/golden/make_golden.py), and
+ *   - oracle/build_ref.py, which compiles the reference's collide/stream
+ *     shader sources as C++ on the host (oracle/_ref/) where that recipe
+ *     succeeds; tests/test_oracle_vs_ref.py compares the two.
+ * Without the second item the restatement is "parity unpinned".
+ *
+ * The file is compiled twice: REAL=float gives the "ref-literal" FP32
+ * stepper (same operation order as the GLSL, no FMA contraction), REAL=double
+ * gives the FP64 accuracy oracle (orc64_* symbols).
+ *
+ * Memory-level restatement: the DDF lives in one buffer with the reference's
+ * SoA address  i*N + cell  (collide.comp:196-200), and every read/write goes
+ * through the same AA index functions as collide.comp:244-369, so the
+ * in-place esoteric-pull semantics (0.01 open-boundary reads, dropped
+ * out-of-range writes, skipped solid cells) fall out exactly.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#ifndef REAL
+#define REAL float
+#endif
+#ifndef ORC
+#define ORC(n) orc32_##n
+#endif
+#define IS_F32 (sizeof(REAL) == 4)
+
+/* ------------------------------------------------------------------------ */
+/* velocity sets: VelocitySet.cpp:53-142 (flow), :180-204 (thermal).         */
+/* enum values follow VelocitySet.h:9-19.                                     */
+/* ------------------------------------------------------------------------ */
+enum { ORC_D2Q9 = 2, ORC_D3Q15 = 3, ORC_D3Q19 = 4, ORC_D3Q27 = 5 };
+enum { ORC_STORE_FP32 = 0, ORC_STORE_FP16 = 1, ORC_STORE_FP16S = 2, ORC_STORE_FP16C = 3 };
+enum { ORC_BOUNDARY_SKIP = 0, ORC_BOUNDARY_BOUNCE_BACK = 1 };
+enum { ORC_BGK = 0, ORC_TRT = 1 };
+enum { ORC_OBJ_SOLID = 0, ORC_OBJ_EQ_VELOCITY = 1, ORC_OBJ_EQ_DENSITY = 2 };
+
+typedef struct { int cx, cy, cz; double w; } orc_dir;
+
+static const orc_dir D2Q9_T[9] = {
+    {0, 0, 0, 4.0 / 9}, {1, 0, 0, 1.0 / 9}, {-1, 0, 0, 1.0 / 9}, {0, 1, 0, 1.0 / 9}, {0, -1, 0, 1.0 / 9},
+    {1, 1, 0, 1.0 / 36}, {-1, -1, 0, 1.0 / 36}, {1, -1, 0, 1.0 / 36}, {-1, 1, 0, 1.0 / 36}};
+static const orc_dir D3Q15_T[15] = {
+    {0, 0, 0, 2.0 / 9}, {1, 0, 0, 1.0 / 9}, {-1, 0, 0, 1.0 / 9}, {0, 1, 0, 1.0 / 9}, {0, -1, 0, 1.0 / 9},
+    {0, 0, 1, 1.0 / 9}, {0, 0, -1, 1.0 / 9}, {1, 1, 1, 1.0 / 72}, {-1, -1, -1, 1.0 / 72}, {1, 1, -1, 1.0 / 72},
+    {-1, -1, 1, 1.0 / 72}, {1, -1, 1, 1.0 / 72}, {-1, 1, -1, 1.0 / 72}, {-1, 1, 1, 1.0 / 72}, {1, -1, -1, 1.0 / 72}};
+static const orc_dir D3Q19_T[19] = {
+    {0, 0, 0, 1.0 / 3}, {1, 0, 0, 1.0 / 18}, {-1, 0, 0, 1.0 / 18}, {0, 1, 0, 1.0 / 18}, {0, -1, 0, 1.0 / 18},
+    {0, 0, 1, 1.0 / 18}, {0, 0, -1, 1.0 / 18}, {1, 1, 0, 1.0 / 36}, {-1, -1, 0, 1.0 / 36}, {1, -1, 0, 1.0 / 36},
+    {-1, 1, 0, 1.0 / 36}, {1, 0, 1, 1.0 / 36}, {-1, 0, -1, 1.0 / 36}, {1, 0, -1, 1.0 / 36}, {-1, 0, 1, 1.0 / 36},
+    {0, 1, 1, 1.0 / 36}, {0, -1, -1, 1.0 / 36}, {0, 1, -1, 1.0 / 36}, {0, -1, 1, 1.0 / 36}};
+static const orc_dir D3Q27_T[27] = {
+    {0, 0, 0, 8.0 / 27}, {1, 0, 0, 2.0 / 27}, {-1, 0, 0, 2.0 / 27}, {0, 1, 0, 2.0 / 27}, {0, -1, 0, 2.0 / 27},
+    {0, 0, 1, 2.0 / 27}, {0, 0, -1, 2.0 / 27}, {1, 1, 0, 1.0 / 54}, {-1, -1, 0, 1.0 / 54}, {1, 0, 1, 1.0 / 54},
+    {-1, 0, -1, 1.0 / 54}, {0, 1, 1, 1.0 / 54}, {0, -1, -1, 1.0 / 54}, {1, -1, 0, 1.0 / 54}, {-1, 1, 0, 1.0 / 54},
+    {1, 0, -1, 1.0 / 54}, {-1, 0, 1, 1.0 / 54}, {0, 1, -1, 1.0 / 54}, {0, -1, 1, 1.0 / 54}, {1, 1, 1, 1.0 / 216},
+    {-1, -1, -1, 1.0 / 216}, {1, 1, -1, 1.0 / 216}, {-1, -1, 1, 1.0 / 216}, {1, -1, 1, 1.0 / 216},
+    {-1, 1, -1, 1.0 / 216}, {-1, 1, 1, 1.0 / 216}, {1, -1, -1, 1.0 / 216}};
+static const orc_dir D2Q5_T[5] = {
+    {0, 0, 0, 1.0 / 3}, {1, 0, 0, 1.0 / 6}, {-1, 0, 0, 1.0 / 6}, {0, 1, 0, 1.0 / 6}, {0, -1, 0, 1.0 / 6}};
+static const orc_dir D3Q7_T[7] = {
+    {0, 0, 0, 1.0 / 4}, {1, 0, 0, 1.0 / 8}, {-1, 0, 0, 1.0 / 8}, {0, 1, 0, 1.0 / 8},
+    {0, -1, 0, 1.0 / 8}, {0, 0, 1, 1.0 / 8}, {0, 0, -1, 1.0 / 8}};
+
+/* ------------------------------------------------------------------------ */
+/* 16-bit storage emulation                                                  */
+/* ------------------------------------------------------------------------ */
+/* IEEE binary32 -> binary16 with round-to-nearest-even (the conversion an
+ * R16F imageStore is assumed to perform), then back to binary32. */
+static uint16_t f32_to_f16_rne(float f) {
+    uint32_t x; memcpy(&x, &f, 4);
+    uint32_t sign = (x >> 16) & 0x8000u;
+    uint32_t mag = x & 0x7fffffffu;
+    if (mag >= 0x7f800000u) return (uint16_t)(sign | (mag > 0x7f800000u ? 0x7e00u : 0x7c00u));
+    if (mag >= 0x477ff000u) return (uint16_t)(sign | 0x7c00u); /* rounds to >= 65520 -> inf */
+    if (mag < 0x38800000u) { /* result is subnormal or zero */
+        if (mag < 0x33000000u) return (uint16_t)sign; /* < 2^-25 rounds to 0 (2^-25 ties to even 0) */
+        uint32_t m = (mag & 0x7fffffu) | 0x800000u;
+        int e = (int)(mag >> 23); /* 102..112 */
+        int shift = 126 - e;      /* value = m * 2^(e-150); half sub unit 2^-24 */
+        uint32_t q = m >> shift, rem = m & ((1u << shift) - 1u), half = 1u << (shift - 1);
+        if (rem > half || (rem == half && (q & 1u))) q++;
+        return (uint16_t)(sign | q);
+    }
+    uint32_t e = (mag >> 23) - 112u;
+    uint32_t m = mag & 0x7fffffu;
+    uint32_t q = (e << 10) | (m >> 13);
+    uint32_t rem = m & 0x1fffu;
+    if (rem > 0x1000u || (rem == 0x1000u && (q & 1u))) q++;
+    return (uint16_t)(sign | q);
+}
+static float f16_to_f32(uint16_t h) {
+    uint32_t sign = (uint32_t)(h & 0x8000u) << 16;
+    uint32_t e = (h >> 10) & 0x1fu, m = h & 0x3ffu, x;
+    if (e == 0) {
+        float v = (float)m * 5.9604644775390625e-08f; /* m * 2^-24, exact */
+        return sign ? -v : v;
+    }
+    if (e == 31) x = sign | 0x7f800000u | (m << 13);
+    else x = sign | ((e + 112u) << 23) | (m << 13);
+    float f; memcpy(&f, &x, 4); return f;
+}
+/* custom 16-bit: 1 sign, 4 exponent, 11 mantissa bits; normal value
+ * 2^(e-13)*(1+m/2048) for e=1..15, subnormal 2^-12*(m/2048); saturates at the
+ * largest finite value (2^2*(2-2^-11)); round to nearest even. */
+static uint16_t f32_to_c16(float f) {
+    uint32_t x; memcpy(&x, &f, 4);
+    uint32_t sign = (x >> 16) & 0x8000u;
+    uint32_t mag = x & 0x7fffffffu;
+    if (mag > 0x7f800000u) return (uint16_t)sign; /* NaN -> 0 */
+    if (mag >= 0x40fff800u) return (uint16_t)(sign | 0x7fffu); /* >= 8 - 2^-10 rounds past the top: saturate */
+    if (mag < 0x39800000u) { /* < 2^-12: subnormal range, unit 2^-23 */
+        if (mag < 0x33800000u) return (uint16_t)sign; /* < 2^-24 */
+        uint32_t m = (mag & 0x7fffffu) | 0x800000u;
+        int e = (int)(mag >> 23); /* 104..114 */
+        int shift = 127 - e; /* value = m*2^(e-150); unit 2^-23 -> q = m*2^(e-127) */
+        uint32_t q = m >> shift, rem = m & ((1u << shift) - 1u), half = 1u << (shift - 1);
+        if (rem > half || (rem == half && (q & 1u))) q++;
+        return (uint16_t)(sign | q);
+    }
+    uint32_t e = (mag >> 23) - 114u; /* 2^-12 -> e=1 */
+    uint32_t m = mag & 0x7fffffu;
+    uint32_t q = (e << 11) | (m >> 12);
+    uint32_t rem = m & 0xfffu;
+    if (rem > 0x800u || (rem == 0x800u && (q & 1u))) q++;
+    return (uint16_t)(sign | q);
+}
+static float c16_to_f32(uint16_t h) {
+    uint32_t sign = (uint32_t)(h & 0x8000u) << 16;
+    uint32_t e = (h >> 11) & 0xfu, m = h & 0x7ffu, x;
+    if (e == 0) {
+        float v = (float)m * 1.1920928955078125e-07f; /* m * 2^-23 */
+        return sign ? -v : v;
+    }
+    x = sign | ((e + 114u) << 23) | (m << 12);
+    float f; memcpy(&f, &x, 4); return f;
+}
+
+/* ------------------------------------------------------------------------ */
+/* solver state                                                              */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+    int nx, ny, nz, velocity_set, storage, multiphase, esoteric;
+    int periodic[3];
+    float tau;
+    int boundary_mode, collision;
+    float trt_magic, velocity_limit, velocity_limit_extreme;
+    float G, tau_t, beta;
+    int thermal_init_equilibrium;  /* 0: as read (lattice left at zero), 1: equilibrium */
+    int two_buffer_fixed;          /* 0: as read (double swap), 1: collide -> stream */
+} orc_desc;
+
+typedef struct {
+    orc_desc d;
+    int Q, Qt, dims;
+    size_t N;
+    const orc_dir* V;
+    const orc_dir* Vt;
+    REAL cs;
+    REAL* lat[2];
+    int lat0_src;
+    uint32_t* boundries;
+    int bits, nobj;
+    float* objects;   /* 12 floats per id: (u,T) (omega,0) (com,rho_eff) as LBM.cpp:613-626 */
+    int* obj_kind;
+    int forcing, constant_force, thermal;
+    REAL fconst[3];
+    float* forces;    /* N*4 */
+    REAL* th[2];
+    int th0_src;
+    REAL* mp[2];
+    int mp0_src;
+    float* bvals;     /* N*4 (rho_b, u_b) for equilibrium boundary cells */
+    REAL* vel_den;    /* N*4 */
+    REAL* force_temp; /* N*4 */
+    float* bnd_tex;   /* N */
+    long ticks;
+} orc_t;
+
+typedef struct { REAL x, y, z; } v3;
+static v3 mk3(REAL x, REAL y, REAL z) { v3 r = {x, y, z}; return r; }
+static REAL dot3(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
+static REAL store_round(const orc_t* s, REAL v, int i) {
+    if (!IS_F32) return v;
+    switch (s->d.storage) {
+    case ORC_STORE_FP16: return (REAL)f16_to_f32(f32_to_f16_rne((float)v));
+    case ORC_STORE_FP16S: {
+        float w = (float)s->V[i].w;
+        return (REAL)(f16_to_f32(f32_to_f16_rne((float)v - w)) + w);
+    }
+    case ORC_STORE_FP16C: {
+        float w = (float)s->V[i].w;
+        float winv = 1.0f / w;
+        return (REAL)fmaf(c16_to_f32(f32_to_c16(((float)v - w) * winv)), w, w);
+    }
+    default: return v;
+    }
+}
+
+static int opp(int i) { /* collide.comp:219-222 */
+    int r = (i % 2 == 1) ? i + 1 : i - 1;
+    return r < 0 ? 0 : r;
+}
+static int opp_t(int i, int Qt) { /* stream_thermal.comp:249-255 */
+    if (i == 0 || i >= Qt) return 0;
+    return (i % 2 == 1) ? i + 1 : i - 1;
+}
+static int pmod(int i, int n) { int r = i % n; return r < 0 ? r + n : r; }
+
+static size_t cid(const orc_t* s, int x, int y, int z) { return ((size_t)z * s->d.ny + y) * s->d.nx + x; }
+
+static uint32_t get_boundry(const orc_t* s, size_t cell) { /* collide.comp:401-418 */
+    if (s->nobj <= 1) return 0;
+    uint64_t bits_begin = (uint64_t)cell * (uint64_t)s->bits;
+    uint64_t dw = bits_begin / 32;
+    uint32_t sub = (uint32_t)(bits_begin % 32);
+    uint32_t mask = (1u << s->bits) - 1u;
+    return (s->boundries[dw] & (mask << sub)) >> sub;
+}
+static int is_solid(const orc_t* s, uint32_t id) {
+    return id != 0 && s->obj_kind[id] == ORC_OBJ_SOLID;
+}
+
+/* wrap / open-boundary test shared by all neighbour lookups (collide.comp:278-295) */
+static int wrap(const orc_t* s, int* x, int* y, int* z) {
+    int open = 0;
+    if (s->d.periodic[0]) *x = pmod(*x, s->d.nx); else open |= (*x < 0 || *x >= s->d.nx);
+    if (s->d.periodic[1]) *y = pmod(*y, s->d.ny); else open |= (*y < 0 || *y >= s->d.ny);
+    if (s->d.periodic[2]) *z = pmod(*z, s->d.nz); else open |= (*z < 0 || *z >= s->d.nz);
+    return open;
+}
+
+static REAL* LSRC(orc_t* s) { return s->lat[s->lat0_src ? 0 : 1]; }
+static REAL* LTGT(orc_t* s) { return s->lat[s->lat0_src ? 1 : 0]; }
+static REAL* TSRC(orc_t* s) { return s->th[s->th0_src ? 0 : 1]; }
+static REAL* TTGT(orc_t* s) { return s->th[s->th0_src ? 1 : 0]; }
+static REAL* MSRC(orc_t* s) { return s->mp[s->mp0_src ? 0 : 1]; }
+static REAL* MTGT(orc_t* s) { return s->mp[s->mp0_src ? 1 : 0]; }
+
+/* AA read address (collide.comp:244-305): returns 0 and fills (cell,slot),
+ * or returns 1 for an open-boundary read. */
+static int aa_read_addr(orc_t* s, int x, int y, int z, int i, int odd, size_t* cell, int* slot) {
+    int rx = x, ry = y, rz = z, ri = i;
+    if (s->d.esoteric) {
+        if (!odd) { rx = x - s->V[i].cx; ry = y - s->V[i].cy; rz = z - s->V[i].cz; ri = i; }
+        else { ri = opp(i); }
+    }
+    if (wrap(s, &rx, &ry, &rz)) return 1;
+    *cell = cid(s, rx, ry, rz); *slot = ri;
+    return 0;
+}
+/* AA write address (collide.comp:307-369) */
+static int aa_write_addr(orc_t* s, int x, int y, int z, int i, int odd, size_t* cell, int* slot) {
+    int wx = x, wy = y, wz = z, wi = i;
+    if (s->d.esoteric) {
+        if (!odd) { wi = opp(i); wx = x - s->V[wi].cx; wy = y - s->V[wi].cy; wz = z - s->V[wi].cz; }
+        else { wi = i; }
+    }
+    if (wrap(s, &wx, &wy, &wz)) return 1;
+    *cell = cid(s, wx, wy, wz); *slot = wi;
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* physics (collide.comp:512-629, :634-673)                                  */
+/* ------------------------------------------------------------------------ */
+static REAL feq_ref(const orc_t* s, REAL rho, v3 u, int i) { /* collide.comp:589-606 */
+    REAL w = (REAL)s->V[i].w;
+    v3 c = mk3((REAL)s->V[i].cx, (REAL)s->V[i].cy, (REAL)s->V[i].cz);
+    REAL cs = s->cs;
+    REAL cu = dot3(c, u);
+    REAL cu2 = cu * cu;         /* pow(ci_dot_u, 2) taken as x*x (GLSL pow(x<0,y) is undefined) */
+    REAL uu = dot3(u, u);
+    REAL cs2 = cs * cs;         /* pow(cs, 2) */
+    REAL cs4 = cs2 * cs2;       /* pow(cs, 4) */
+    return w * rho * ((REAL)1 + cu / cs2 + cu2 / (REAL)2 / cs4 - uu / (REAL)2 / cs2);
+}
+static REAL feq_t_ref(const orc_t* s, REAL T, v3 u, int i) { /* collide.comp:634-651 */
+    REAL w = (REAL)s->Vt[i].w;
+    v3 c = mk3((REAL)s->Vt[i].cx, (REAL)s->Vt[i].cy, (REAL)s->Vt[i].cz);
+    REAL cs = s->cs;
+    REAL cu = dot3(c, u);
+    REAL cu2 = cu * cu;
+    REAL uu = dot3(u, u);
+    REAL cs2 = cs * cs;
+    REAL cs4 = cs2 * cs2;
+    return w * T * ((REAL)1 + cu / cs2 + cu2 / (REAL)2.0 / cs4 - uu / (REAL)2.0 / cs2);
+}
+static REAL feq_init(const orc_t* s, REAL rho, v3 u, int i) { /* set_equilibrium_populations.comp:179-196 */
+    REAL w = (REAL)s->V[i].w;
+    v3 c = mk3((REAL)s->V[i].cx, (REAL)s->V[i].cy, (REAL)s->V[i].cz);
+    REAL cu = dot3(c, u);
+    REAL cu2 = cu * cu;
+    REAL uu = dot3(u, u);
+    return w * rho * ((REAL)1 + (REAL)3 * cu + (REAL)9 * cu2 / (REAL)2 - (REAL)3 * uu / (REAL)2);
+}
+static REAL feq_t_init(const orc_t* s, REAL T, v3 u, int i) { /* set_equilibrium_populations_thermal.comp:139-156 */
+    REAL w = (REAL)s->Vt[i].w;
+    v3 c = mk3((REAL)s->Vt[i].cx, (REAL)s->Vt[i].cy, (REAL)s->Vt[i].cz);
+    REAL cu = dot3(c, u);
+    REAL cu2 = cu * cu;
+    REAL uu = dot3(u, u);
+    return w * T * ((REAL)1 + (REAL)3 * cu + (REAL)9 * cu2 / (REAL)2 - (REAL)3 * uu / (REAL)2);
+}
+/* Guo source term, split as (1-dt/2tau) * w * (F.c/cs2 + (F.c)(u.c)/cs4 - F.u/cs2) (collide.comp:608-625) */
+static REAL source_ref(const orc_t* s, int i, v3 F, v3 u) {
+    REAL tau = (REAL)s->d.tau;
+    REAL w = (REAL)s->V[i].w;
+    v3 c = mk3((REAL)s->V[i].cx, (REAL)s->V[i].cy, (REAL)s->V[i].cz);
+    REAL cs = s->cs, cs2 = cs * cs, cs4 = cs2 * cs2;
+    return ((REAL)1 - (REAL)1 / ((REAL)2 * tau)) * w * (dot3(F, c) / cs2 + (dot3(F, c) * dot3(u, c) / cs4 - dot3(F, u) / cs2));
+}
+static REAL psi(REAL rho) { /* collide.comp:512-516 */
+    REAL rho0 = 1;
+    return rho0 * ((REAL)1 - (IS_F32 ? (REAL)expf((float)(-rho / rho0)) : (REAL)exp((double)(-rho / rho0))));
+}
+
+/* Shan-Chen interaction force (collide.comp:534-584) */
+static v3 sc_force(orc_t* s, int x, int y, int z, REAL self_density) {
+    REAL self_psi = psi(self_density);
+    REAL G = (REAL)s->d.G;
+    v3 f = mk3(0, 0, 0);
+    REAL* src = MSRC(s);
+    for (int i = 1; i < s->Q; i++) {
+        int nx = x + s->V[i].cx, ny = y + s->V[i].cy, nz = z + s->V[i].cz;
+        int open = wrap(s, &nx, &ny, &nz);
+        REAL nd = open ? self_density : src[cid(s, nx, ny, nz)];
+        REAL p = psi(nd);
+        REAL w = (REAL)s->V[i].w;
+        f.x += w * p * (REAL)s->V[i].cx;
+        f.y += w * p * (REAL)s->V[i].cy;
+        f.z += w * p * (REAL)s->V[i].cz;
+    }
+    REAL k = -self_psi * G;
+    f.x *= k; f.y *= k; f.z *= k;
+    return f;
+}
+
+static v3 get_force(orc_t* s, size_t cell) { /* collide.comp:451-463 */
+    if (!s->forcing) return mk3(0, 0, 0);
+    if (s->constant_force) return mk3(s->fconst[0], s->fconst[1], s->fconst[2]);
+    return mk3((REAL)s->forces[cell * 4 + 0], (REAL)s->forces[cell * 4 + 1], (REAL)s->forces[cell * 4 + 2]);
+}
+
+/* ------------------------------------------------------------------------ */
+/* collide.comp main (:676-794) over every cell                               */
+/* ------------------------------------------------------------------------ */
+#define QMAX 27
+static void collide(orc_t* s, int save, int update) {
+    const int Q = s->Q;
+    const int odd = (int)(s->ticks % 2 == 1);
+    REAL* L = LSRC(s);
+    const size_t N = s->N;
+    const int bb = s->d.esoteric && s->d.boundary_mode == ORC_BOUNDARY_BOUNCE_BACK;
+    /* cells are independent within one dispatch: the AA step reads and
+     * writes the same private set of slots per cell, so the loop is safe to
+     * run in parallel exactly as the GPU dispatch is. */
+    #pragma omp parallel for collapse(2) schedule(static)
+    for (int z = 0; z < s->d.nz; z++)
+    for (int y = 0; y < s->d.ny; y++)
+    for (int x = 0; x < s->d.nx; x++) {
+        size_t cell = cid(s, x, y, z);
+        uint32_t bid = get_boundry(s, cell);
+        if (is_solid(s, bid)) continue; /* collide.comp:696-700 */
+        int eqb = bid != 0; /* equilibrium boundary cell (extension) */
+        REAL f[QMAX];
+        for (int i = 0; i < Q; i++) {
+            size_t rc; int rs;
+            int open = aa_read_addr(s, x, y, z, i, odd, &rc, &rs);
+            if ((bb || eqb) && s->d.esoteric) {
+                /* halfway bounce-back folded into AA (extension): when the
+                 * streaming source x-c_i is solid, take the cell's own
+                 * outgoing opposite population instead (stored in the other
+                 * AA slot) plus the moving-wall term of stream.comp:487-496. */
+                int sx = x - s->V[i].cx, sy = y - s->V[i].cy, sz = z - s->V[i].cz;
+                int sopen = wrap(s, &sx, &sy, &sz);
+                uint32_t sid = sopen ? 0 : get_boundry(s, cid(s, sx, sy, sz));
+                if (eqb && sopen) {
+                    REAL rb = (REAL)s->bvals[cell * 4 + 0];
+                    v3 ub = mk3((REAL)s->bvals[cell * 4 + 1], (REAL)s->bvals[cell * 4 + 2], (REAL)s->bvals[cell * 4 + 3]);
+                    f[i] = feq_ref(s, rb, ub, i);
+                    continue;
+                }
+                if (bb && !sopen && is_solid(s, sid)) {
+                    int oi = opp(i);
+                    size_t oc; int os;
+                    if (!odd) { oc = cell; os = oi; }
+                    else { oc = cid(s, sx, sy, sz); os = i; }
+                    const float* ob = &s->objects[sid * 12];
+                    v3 uw = mk3((REAL)ob[0], (REAL)ob[1], (REAL)ob[2]);
+                    v3 co = mk3((REAL)s->V[oi].cx, (REAL)s->V[oi].cy, (REAL)s->V[oi].cz);
+                    f[i] = L[(size_t)os * N + oc] + (REAL)(-2) * (REAL)s->V[oi].w * (REAL)1.0 * dot3(co, uw) * (REAL)3;
+                    continue;
+                }
+            }
+            f[i] = open ? (REAL)0.01 : L[(size_t)rs * N + rc];
+        }
+        REAL density = 0;
+        for (int i = 0; i < Q; i++) density += f[i];
+        if (density < (REAL)0.01) density = (REAL)0.01; /* max(density, 0.01) */
+        v3 force = get_force(s, cell);
+        REAL temperature = 0;
+        if (s->thermal) {
+            REAL* TS = TSRC(s);
+            for (int i = 0; i < s->Qt; i++) temperature += TS[cell * s->Qt + i];
+            REAL k = -(REAL)s->d.beta * (temperature - (REAL)1);
+            v3 b = mk3(k * force.x, k * force.y, k * force.z);
+            force.x += b.x; force.y += b.y; force.z += b.z;
+        }
+        if (s->d.multiphase) {
+            v3 sc = sc_force(s, x, y, z, density);
+            force.x += sc.x; force.y += sc.y; force.z += sc.z;
+        }
+        v3 vel = mk3(0, 0, 0);
+        for (int i = 0; i < Q; i++) {
+            vel.x += f[i] * (REAL)s->V[i].cx;
+            vel.y += f[i] * (REAL)s->V[i].cy;
+            vel.z += f[i] * (REAL)s->V[i].cz;
+        }
+        vel.x /= density; vel.y /= density; vel.z /= density;
+        vel.x += force.x / ((REAL)2 * density);
+        vel.y += force.y / ((REAL)2 * density);
+        vel.z += force.z / ((REAL)2 * density);
+        REAL len = (REAL)sqrt((double)dot3(vel, vel));
+        if (IS_F32) len = (REAL)sqrtf((float)dot3(vel, vel));
+        int out_lim = len > (REAL)s->d.velocity_limit;
+        int out_ext = len > (REAL)s->d.velocity_limit_extreme;
+        if (out_lim) {
+            REAL lim = (REAL)s->d.velocity_limit;
+            vel.x = vel.x / len * lim; vel.y = vel.y / len * lim; vel.z = vel.z / len * lim;
+        }
+        if (eqb) {
+            /* equilibrium boundary cell (extension): velocity kind keeps the
+             * prescribed u with the received density, density kind keeps the
+             * prescribed rho with the received velocity. */
+            int kind = s->obj_kind[bid];
+            REAL rb = (REAL)s->bvals[cell * 4 + 0];
+            v3 ub = mk3((REAL)s->bvals[cell * 4 + 1], (REAL)s->bvals[cell * 4 + 2], (REAL)s->bvals[cell * 4 + 3]);
+            if (kind == ORC_OBJ_EQ_VELOCITY) vel = ub; else density = rb;
+            force = mk3(0, 0, 0);
+        }
+        if (update) {
+            REAL fn[QMAX];
+            for (int i = 0; i < Q; i++) {
+                REAL fe = feq_ref(s, density, vel, i);
+                REAL upd;
+                if (eqb) upd = fe;
+                else if (s->d.collision == ORC_TRT) {
+                    int oi = opp(i);
+                    REAL fo = f[oi];
+                    REAL feo = feq_ref(s, density, vel, oi);
+                    REAL tau = (REAL)s->d.tau;
+                    REAL wp = (REAL)1 / tau;
+                    REAL taum = (REAL)s->d.trt_magic / (tau - (REAL)0.5) + (REAL)0.5;
+                    REAL wm = (REAL)1 / taum;
+                    REAL fp = (f[i] + fo) * (REAL)0.5, fm = (f[i] - fo) * (REAL)0.5;
+                    REAL ep = (fe + feo) * (REAL)0.5, em = (fe - feo) * (REAL)0.5;
+                    /* Guo term split into its odd (F.c) and even parts */
+                    REAL w = (REAL)s->V[i].w;
+                    v3 c = mk3((REAL)s->V[i].cx, (REAL)s->V[i].cy, (REAL)s->V[i].cz);
+                    REAL cs = s->cs, cs2 = cs * cs, cs4 = cs2 * cs2;
+                    REAL Sm = w * (dot3(force, c) / cs2);
+                    REAL Sp = w * (dot3(force, c) * dot3(vel, c) / cs4 - dot3(force, vel) / cs2);
+                    upd = f[i] - wp * (fp - ep) - wm * (fm - em) + ((REAL)1 - wp * (REAL)0.5) * Sp + ((REAL)1 - wm * (REAL)0.5) * Sm;
+                } else {
+                    upd = f[i] + (-(f[i] - fe) / (REAL)s->d.tau) + source_ref(s, i, force, vel);
+                }
+                fn[i] = (!out_ext || eqb) ? upd : fe;
+            }
+            for (int i = 0; i < Q; i++) {
+                size_t wc; int ws;
+                if (aa_write_addr(s, x, y, z, i, odd, &wc, &ws)) continue;
+                L[(size_t)ws * N + wc] = store_round(s, fn[i], ws);
+            }
+        }
+        if (s->d.multiphase) {
+            REAL eff = density;
+            if (s->nobj > 1 && bid != 0) eff = (REAL)s->objects[bid * 12 + 11];
+            MTGT(s)[cell] = eff;
+        }
+        if (s->thermal) {
+            REAL* TS = TSRC(s); REAL* TT = TTGT(s);
+            for (int i = 0; i < s->Qt; i++) {
+                REAL ge = feq_t_ref(s, temperature, vel, i);
+                REAL g = TS[cell * s->Qt + i];
+                TT[cell * s->Qt + i] = g + (-(g - ge) / (REAL)s->d.tau_t);
+            }
+        }
+        if (save) {
+            s->vel_den[cell * 4 + 0] = vel.x; s->vel_den[cell * 4 + 1] = vel.y;
+            s->vel_den[cell * 4 + 2] = vel.z; s->vel_den[cell * 4 + 3] = density;
+            s->bnd_tex[cell] = (float)bid;
+            s->force_temp[cell * 4 + 0] = force.x; s->force_temp[cell * 4 + 1] = force.y;
+            s->force_temp[cell * 4 + 2] = force.z; s->force_temp[cell * 4 + 3] = temperature;
+        }
+    }
+    /* LBM.cpp:1646-1652 */
+    if (!s->d.esoteric && update && !s->d.two_buffer_fixed) s->lat0_src = !s->lat0_src;
+    if (s->d.multiphase) s->mp0_src = !s->mp0_src;
+    s->th0_src = !s->th0_src;
+}
+
+/* stream.comp main (:498-584), two-buffer mode */
+static void stream(orc_t* s) {
+    const int Q = s->Q;
+    const size_t N = s->N;
+    REAL* S = LSRC(s); REAL* T = LTGT(s);
+    #pragma omp parallel for collapse(2) schedule(static)
+    for (int i = 0; i < Q; i++)
+    for (int z = 0; z < s->d.nz; z++)
+    for (int y = 0; y < s->d.ny; y++)
+    for (int x = 0; x < s->d.nx; x++) {
+        size_t cell = cid(s, x, y, z);
+        int inv = (i == 0 || i >= Q) ? 0 : ((i % 2 == 1) ? i + 1 : i - 1);
+        if (is_solid(s, get_boundry(s, cell))) continue;
+        int sx = x - s->V[i].cx, sy = y - s->V[i].cy, sz = z - s->V[i].cz;
+        if (wrap(s, &sx, &sy, &sz)) { T[(size_t)i * N + cell] = store_round(s, (REAL)0.01, i); continue; }
+        size_t sc = cid(s, sx, sy, sz);
+        uint32_t sid = get_boundry(s, sc);
+        if (is_solid(s, sid)) {
+            const float* ob = &s->objects[sid * 12];
+            v3 uw = mk3((REAL)ob[0], (REAL)ob[1], (REAL)ob[2]);
+            v3 c = mk3((REAL)s->V[inv].cx, (REAL)s->V[inv].cy, (REAL)s->V[inv].cz);
+            REAL corr = (REAL)(-2) * (REAL)s->V[inv].w * (REAL)1.0 * dot3(c, uw) * (REAL)3;
+            T[(size_t)i * N + cell] = store_round(s, S[(size_t)inv * N + cell] + corr, i);
+        } else {
+            T[(size_t)i * N + cell] = S[(size_t)i * N + sc];
+        }
+    }
+    s->lat0_src = !s->lat0_src; /* LBM.cpp:1553-1554 */
+}
+
+/* stream_thermal.comp main (:457-526) */
+static void stream_thermal(orc_t* s) {
+    const int Qt = s->Qt;
+    REAL* S = TSRC(s); REAL* T = TTGT(s);
+    #pragma omp parallel for collapse(2) schedule(static)
+    for (int z = 0; z < s->d.nz; z++)
+    for (int y = 0; y < s->d.ny; y++)
+    for (int x = 0; x < s->d.nx; x++)
+    for (int i = 0; i < Qt; i++) {
+        size_t cell = cid(s, x, y, z);
+        int inv = opp_t(i, Qt);
+        if (is_solid(s, get_boundry(s, cell))) continue;
+        int sx = x - s->Vt[i].cx, sy = y - s->Vt[i].cy, sz = z - s->Vt[i].cz;
+        if (wrap(s, &sx, &sy, &sz)) continue;
+        size_t sc = cid(s, sx, sy, sz);
+        uint32_t sid = get_boundry(s, sc);
+        if (is_solid(s, sid)) {
+            REAL Tw = (REAL)s->objects[sid * 12 + 3];
+            T[cell * Qt + i] = -S[cell * Qt + inv] + (REAL)2 * (REAL)s->Vt[inv].w * Tw;
+        } else {
+            T[cell * Qt + i] = S[sc * Qt + i];
+        }
+    }
+    s->th0_src = !s->th0_src;
+}
+
+/* LBM.cpp:1484-1493 */
+static void iterate(orc_t* s, int save, int update) {
+    collide(s, save, update);
+    if (!s->d.esoteric) stream(s);
+    if (s->thermal) stream_thermal(s);
+}
+
+/* ------------------------------------------------------------------------ */
+/* public API                                                                 */
+/* ------------------------------------------------------------------------ */
+/* bits per boundary id, LBM.cpp:569 / :606 (float log2 as the reference) */
+int ORC(bits_per_boundry)(int object_count) {
+    if (object_count <= 1) return 0;
+    return (int)exp2(ceil(log2f(ceilf(log2f((float)object_count)))));
+}
+
+/* boundary bit packing, LBM.cpp:634-659; returns number of uint32 words */
+size_t ORC(pack_boundries)(const uint32_t* ids, size_t n, int bits, uint32_t* out, size_t out_words) {
+    size_t words = (n * (size_t)bits + 31) / 32;
+    if (!out) return words;
+    memset(out, 0, out_words * 4);
+    for (size_t v = 0; v < n; v++) {
+        size_t b = v * (size_t)bits;
+        out[b / 32] |= (ids[v] << (b % 32));
+    }
+    return words;
+}
+
+void ORC(destroy)(orc_t* s) {
+    if (!s) return;
+    free(s->lat[0]); free(s->lat[1]); free(s->boundries); free(s->objects); free(s->obj_kind);
+    free(s->forces); free(s->th[0]); free(s->th[1]); free(s->mp[0]); free(s->mp[1]); free(s->bvals);
+    free(s->vel_den); free(s->force_temp); free(s->bnd_tex);
+    free(s);
+}
+
+/*
+ * Mirrors LBM::initialize_fields (LBM.cpp:415-506) given the per-cell
+ * results of the initialisation lambda as arrays:
+ *   rho[N], u[N*3], force[N*3], T[N], ids[N]; objects: nobj*12 floats laid
+ *   out as (u,T)(omega,0)(com,rho_eff); obj_kind: nobj ints (0 = solid).
+ * Flag derivation follows LBM.cpp:523-556.
+ */
+orc_t* ORC(create)(const orc_desc* d, const float* rho, const float* u, const float* force,
+                   const float* T, const uint32_t* ids, int nobj_in, const float* objects, const int* obj_kind) {
+    orc_t* s = (orc_t*)calloc(1, sizeof(orc_t));
+    s->d = *d;
+    switch (d->velocity_set) {
+    case ORC_D2Q9: s->Q = 9; s->V = D2Q9_T; s->dims = 2; s->Qt = 5; s->Vt = D2Q5_T; break;
+    case ORC_D3Q15: s->Q = 15; s->V = D3Q15_T; s->dims = 3; s->Qt = 7; s->Vt = D3Q7_T; break;
+    case ORC_D3Q19: s->Q = 19; s->V = D3Q19_T; s->dims = 3; s->Qt = 7; s->Vt = D3Q7_T; break;
+    case ORC_D3Q27: s->Q = 27; s->V = D3Q27_T; s->dims = 3; s->Qt = 7; s->Vt = D3Q7_T; break;
+    default: free(s); return NULL;
+    }
+    s->cs = (REAL)(1.0 / sqrt(3.0));
+    s->N = (size_t)d->nx * d->ny * d->nz;
+    const size_t N = s->N;
+    s->lat0_src = 1; s->th0_src = 1; s->mp0_src = 1;
+    s->lat[0] = (REAL*)calloc(N * s->Q, sizeof(REAL));
+    if (!d->esoteric) s->lat[1] = (REAL*)calloc(N * s->Q, sizeof(REAL));
+
+    /* objects: slot 0 is fluid with default temperature/density (LBM.cpp:439-441) */
+    uint32_t maxid = 0;
+    for (size_t c = 0; c < N; c++) if (ids && ids[c] > maxid) maxid = ids[c];
+    int nobj = nobj_in > 1 ? nobj_in : 1;
+    if ((int)maxid + 1 > nobj) nobj = (int)maxid + 1;
+    s->nobj = nobj;
+    s->objects = (float*)calloc((size_t)nobj * 12, sizeof(float));
+    s->obj_kind = (int*)calloc((size_t)nobj, sizeof(int));
+    for (int k = 0; k < nobj; k++) { s->objects[k * 12 + 3] = 1.0f; s->objects[k * 12 + 11] = 1.0f; }
+    if (objects) for (int k = 1; k < nobj_in; k++) memcpy(&s->objects[k * 12], &objects[k * 12], 12 * sizeof(float));
+    if (obj_kind) for (int k = 1; k < nobj_in; k++) s->obj_kind[k] = obj_kind[k];
+
+    /* LBM.cpp:523-556: constant-force and thermal detection relative to cell (0,0,0) */
+    s->constant_force = 1;
+    float f0[3] = {0, 0, 0};
+    if (force) { f0[0] = force[0]; f0[1] = force[1]; f0[2] = force[2]; }
+    s->fconst[0] = f0[0]; s->fconst[1] = f0[1]; s->fconst[2] = f0[2];
+    s->thermal = 0;
+    float T0 = T ? T[0] : 1.0f;
+    for (size_t c = 0; c < N; c++) {
+        if (force && (force[c * 3] != f0[0] || force[c * 3 + 1] != f0[1] || force[c * 3 + 2] != f0[2])) s->constant_force = 0;
+        if (T && T[c] != T0) s->thermal = 1;
+        uint32_t id = ids ? ids[c] : 0;
+        if (id != 0 && s->objects[id * 12 + 3] != T0) s->thermal = 1;
+    }
+    s->forcing = !(s->constant_force && f0[0] == 0 && f0[1] == 0 && f0[2] == 0);
+    if (s->forcing && !s->constant_force) {
+        s->forces = (float*)calloc(N * 4, sizeof(float));
+        for (size_t c = 0; c < N; c++) for (int k = 0; k < 3; k++) s->forces[c * 4 + k] = force[c * 3 + k];
+    }
+
+    s->bits = ORC(bits_per_boundry)(nobj);
+    if (nobj > 1) {
+        size_t words = ORC(pack_boundries)(NULL, N, s->bits, NULL, 0);
+        s->boundries = (uint32_t*)calloc(words + 1, 4);
+        uint32_t* tmp = (uint32_t*)calloc(N, 4);
+        if (ids) memcpy(tmp, ids, N * 4);
+        ORC(pack_boundries)(tmp, N, s->bits, s->boundries, words + 1);
+        free(tmp);
+    }
+    /* equilibrium boundary values: the cell's initial (rho, u) */
+    s->bvals = (float*)calloc(N * 4, sizeof(float));
+    for (size_t c = 0; c < N; c++) {
+        s->bvals[c * 4 + 0] = rho ? rho[c] : 1.0f;
+        for (int k = 0; k < 3; k++) s->bvals[c * 4 + 1 + k] = u ? u[c * 3 + k] : 0.0f;
+    }
+
+    if (d->multiphase) {
+        s->mp[0] = (REAL*)calloc(N, sizeof(REAL));
+        s->mp[1] = (REAL*)calloc(N, sizeof(REAL));
+    }
+    s->vel_den = (REAL*)calloc(N * 4, sizeof(REAL));
+    s->force_temp = (REAL*)calloc(N * 4, sizeof(REAL));
+    s->bnd_tex = (float*)calloc(N, sizeof(float));
+
+    /* host side of LBM.cpp:537-538: solid cells get zero velocity */
+    /* set_equilibrium_populations.comp main (:198-221) */
+    REAL* L = s->lat[0];
+    for (size_t c = 0; c < N; c++) {
+        uint32_t id = ids ? ids[c] : 0;
+        v3 uc = mk3(0, 0, 0);
+        if (u && !is_solid(s, id)) uc = mk3((REAL)u[c * 3], (REAL)u[c * 3 + 1], (REAL)u[c * 3 + 2]);
+        REAL r = rho ? (REAL)rho[c] : (REAL)1;
+        for (int i = 0; i < s->Q; i++) L[(size_t)i * N + c] = store_round(s, feq_init(s, r, uc, i), i);
+    }
+    if (s->thermal) {
+        s->th[0] = (REAL*)calloc(N * s->Qt, sizeof(REAL));
+        s->th[1] = (REAL*)calloc(N * s->Qt, sizeof(REAL));
+        if (d->thermal_init_equilibrium) {
+            for (size_t c = 0; c < N; c++) {
+                REAL t = T ? (REAL)T[c] : (REAL)1;
+                if (t == 0) continue; /* set_equilibrium_populations_thermal.comp:171-172 */
+                uint32_t id = ids ? ids[c] : 0;
+                v3 uc = mk3(0, 0, 0);
+                if (u && !is_solid(s, id)) uc = mk3((REAL)u[c * 3], (REAL)u[c * 3 + 1], (REAL)u[c * 3 + 2]);
+                for (int i = 0; i < s->Qt; i++) s->th[0][c * s->Qt + i] = feq_t_init(s, t, uc, i);
+            }
+        }
+        /* as read, set_equilibrium_populations_thermal.comp:101-107 writes
+         * index Qt*N+cell for every population, past the end of the buffer:
+         * the thermal lattice keeps its initial (zero) contents. */
+    }
+    s->ticks = 0;
+    iterate(s, 1, 0); /* LBM.cpp:502: _iterate_time(true, false) */
+    return s;
+}
+
+/* LBM::iterate_time with target_tick_per_second = 0 (LBM.cpp:220-240) */
+void ORC(iterate)(orc_t* s, int n, int save_last) {
+    for (int k = 0; k < n; k++) {
+        iterate(s, save_last && k == n - 1, 1);
+        s->ticks++;
+    }
+}
+
+long ORC(ticks)(orc_t* s) { return s->ticks; }
+int ORC(thermal)(orc_t* s) { return s->thermal; }
+int ORC(forcing)(orc_t* s) { return s->forcing; }
+int ORC(constant_force)(orc_t* s) { return s->constant_force; }
+int ORC(bits)(orc_t* s) { return s->bits; }
+size_t ORC(cells)(orc_t* s) { return s->N; }
+int ORC(q)(orc_t* s) { return s->Q; }
+
+/* copies out the macroscopic textures: vel_den N*4, force_temp N*4, bnd N */
+void ORC(get_fields)(orc_t* s, double* vel_den, double* force_temp, float* bnd) {
+    for (size_t k = 0; k < s->N * 4; k++) {
+        if (vel_den) vel_den[k] = (double)s->vel_den[k];
+        if (force_temp) force_temp[k] = (double)s->force_temp[k];
+    }
+    if (bnd) memcpy(bnd, s->bnd_tex, s->N * sizeof(float));
+}
+/* copies the raw DDF buffer (source lattice, SoA i*N+cell) */
+void ORC(get_lattice)(orc_t* s, double* out) {
+    REAL* L = LSRC(s);
+    for (size_t k = 0; k < s->N * (size_t)s->Q; k++) out[k] = (double)L[k];
+}
+void ORC(set_lattice)(orc_t* s, const double* in) {
+    REAL* L = LSRC(s);
+    for (size_t k = 0; k < s->N * (size_t)s->Q; k++) L[k] = (REAL)in[k];
+}
+void ORC(get_thermal)(orc_t* s, double* out) {
+    if (!s->thermal) return;
+    REAL* L = TSRC(s);
+    for (size_t k = 0; k < s->N * (size_t)s->Qt; k++) out[k] = (double)L[k];
+}
+void ORC(get_boundries)(orc_t* s, uint32_t* out, size_t words) {
+    if (s->boundries) memcpy(out, s->boundries, words * 4);
+}
+/* FP64 sums over non-solid cells of the last saved fields: mass, momentum xyz, kinetic energy */
+void ORC(reduce)(orc_t* s, double out[5]) {
+    double m = 0, px = 0, py = 0, pz = 0, ke = 0;
+    for (size_t c = 0; c < s->N; c++) {
+        uint32_t id = get_boundry(s, c);
+        if (is_solid(s, id)) continue;
+        double r = (double)s->vel_den[c * 4 + 3];
+        double ux = (double)s->vel_den[c * 4 + 0], uy = (double)s->vel_den[c * 4 + 1], uz = (double)s->vel_den[c * 4 + 2];
+        m += r; px += r * ux; py += r * uy; pz += r * uz; ke += 0.5 * r * (ux * ux + uy * uy + uz * uz);
+    }
+    out[0] = m; out[1] = px; out[2] = py; out[3] = pz; out[4] = ke;
+}
+uint16_t ORC(f32_to_f16)(float f) { return f32_to_f16_rne(f); }
+float ORC(f16_to_f32)(uint16_t h) { return f16_to_f32(h); }
+uint16_t ORC(f32_to_c16)(float f) { return f32_to_c16(f); }
+float ORC(c16_to_f32)(uint16_t h) { return c16_to_f32(h); }

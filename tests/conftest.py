@@ -1,0 +1,28 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (runs the sm_103a kernels)")
+
+
+@pytest.fixture(scope="session")
+def product_lib():
+    """Builds (if needed) and loads libbfgb300.so."""
+    from boltzmannfluids_gb300 import build as b
+    b.build()
+    import boltzmannfluids_gb300 as bf
+    return bf.load_library()
+
+
+@pytest.fixture(scope="session")
+def oracle_mod():
+    from oracle import oracle as o
+    o.load()
+    return o

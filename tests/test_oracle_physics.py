@@ -1,0 +1,149 @@
+"""CPU checks of the oracle's physics and of the semantics it restates."""
+import numpy as np
+import pytest
+
+from oracle.oracle import Oracle
+
+
+def shear_wave(nx, ny, amp=0.05):
+    y = np.arange(ny)
+    u = np.zeros((ny, nx, 3), np.float32)
+    u[..., 0] = amp * np.sin(2 * np.pi * y / ny)[:, None]
+    return u.reshape(-1, 3)
+
+
+@pytest.mark.parametrize("precision,tol", [(64, 1e-14), (32, 1e-6)])
+@pytest.mark.parametrize("vs", [2, 3, 4, 5])
+def test_equilibrium_at_rest_is_a_fixed_point(vs, precision, tol):
+    # FP32 sums of the FP32 weights are not exactly 1, so FP32 drifts by ulps
+    res = (12, 10, 1) if vs == 2 else (8, 6, 5)
+    o = Oracle(res, 0.7, velocity_set=vs, esoteric=True, precision=precision)
+    o.iterate(7)
+    vd, _ = o.fields()
+    assert np.abs(vd[:, 3] - 1.0).max() < tol and np.all(vd[:, :3] == 0.0)
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+@pytest.mark.parametrize("esoteric", [True, False])
+def test_shear_wave_decay_matches_viscosity(precision, esoteric):
+    nx, ny, tau = 16, 32, 0.8
+    o = Oracle((nx, ny, 1), tau, velocity=shear_wave(nx, ny), velocity_set=2, esoteric=esoteric,
+               two_buffer_fixed=True, precision=precision)
+    o.iterate(200)
+    vd, _ = o.fields()
+    nu = (tau - 0.5) / 3
+    k = 2 * np.pi / ny
+    # fields are saved at the collide of the last step: 200 decays after init
+    expect = 0.05 * np.exp(-nu * k * k * 200)
+    assert abs(np.abs(vd[:, 0]).max() / expect - 1) < 5e-3
+
+
+@pytest.mark.parametrize("vs", [2, 4])
+def test_mass_conserved_periodic(vs):
+    rng = np.random.default_rng(3)
+    res = (20, 16, 1) if vs == 2 else (10, 8, 6)
+    n = res[0] * res[1] * res[2]
+    rho = 1 + 0.01 * rng.uniform(-1, 1, n)
+    u = 0.03 * rng.uniform(-1, 1, (n, 3))
+    if vs == 2:
+        u[:, 2] = 0
+    o = Oracle(res, 0.6, density=rho, velocity=u, velocity_set=vs, esoteric=True, precision=64)
+    m0 = o.lattice().sum()
+    o.iterate(25)
+    assert abs(o.lattice().sum() - m0) < 1e-10 * m0
+
+
+def cavity(nx, ny):
+    ids = np.zeros((ny, nx), np.uint32)
+    ids[0, :] = 1
+    ids[:, 0] = 1
+    ids[:, -1] = 1
+    ids[-1, :] = 2
+    return ids, {1: dict(velocity=(0, 0, 0)), 2: dict(velocity=(0.1, 0, 0))}
+
+
+def test_aa_bounce_back_equals_two_buffer_stream_bounce_back():
+    """Halfway bounce-back folded into the AA step reproduces the two-buffer
+    collide -> stream.comp bounce-back (moving wall) bit for bit."""
+    nx, ny = 24, 20
+    ids, objs = cavity(nx, ny)
+    kw = dict(boundry_id=ids, periodic=(False, False, True), velocity_set=2, objects=objs)
+    a = Oracle((nx, ny, 1), 0.6, esoteric=True, boundary_mode=1, **kw)
+    b = Oracle((nx, ny, 1), 0.6, esoteric=False, two_buffer_fixed=True, **kw)
+    for n in (1, 1, 5, 60):
+        a.iterate(n)
+        b.iterate(n)
+        va, fa = a.fields()
+        vb, fb = b.fields()
+        assert np.array_equal(va, vb)
+    assert np.abs(va[:, 0]).max() > 0.01  # the lid drives a flow
+
+
+def test_two_buffer_as_read_restreams_the_initial_buffer():
+    """As read, LBM.cpp swaps after collide (:1646-1647) and _stream then
+    pulls from the other buffer (:1509-1513), which after initialisation is
+    never written again: every step re-streams the initial equilibrium, so
+    the fields freeze while the fixed order lets the lid drive a flow."""
+    nx, ny = 16, 12
+    ids, objs = cavity(nx, ny)
+    kw = dict(boundry_id=ids, periodic=(False, False, True), velocity_set=2, objects=objs, esoteric=False)
+    o = Oracle((nx, ny, 1), 0.6, two_buffer_fixed=False, **kw)
+    f = Oracle((nx, ny, 1), 0.6, two_buffer_fixed=True, **kw)
+    o.iterate(2)
+    f.iterate(2)
+    v2, _ = o.fields()
+    w2, _ = f.fields()
+    o.iterate(10)
+    f.iterate(10)
+    v12, _ = o.fields()
+    w12, _ = f.fields()
+    assert np.array_equal(v2, v12)
+    assert not np.array_equal(w2, w12)
+
+
+def test_thermal_init_as_read_leaves_zero_temperature():
+    nx, ny = 12, 10
+    ids = np.zeros((ny, nx), np.uint32)
+    ids[0, :] = 1
+    ids[-1, :] = 2
+    objs = {1: dict(temperature=1.5), 2: dict(temperature=0.5)}
+    o = Oracle((nx, ny, 1), 0.6, boundry_id=ids, periodic=(True, False, True), velocity_set=2, objects=objs,
+               esoteric=True)
+    assert o.thermal
+    _, ft = o.fields()
+    fluid = ids.reshape(-1) == 0
+    assert np.all(ft[fluid, 3] == 0.0)  # T = sum of a zero thermal lattice
+    o.iterate(20)
+    _, ft = o.fields()
+    assert ft[fluid, 3].max() > 0  # heat enters from the Dirichlet walls
+    o2 = Oracle((nx, ny, 1), 0.6, boundry_id=ids, periodic=(True, False, True), velocity_set=2, objects=objs,
+                esoteric=True, thermal_init_equilibrium=True)
+    _, ft2 = o2.fields()
+    assert np.allclose(ft2[fluid, 3], 1.0)
+
+
+def test_fp32_oracle_tracks_fp64_oracle():
+    nx, ny = 24, 24
+    rng = np.random.default_rng(5)
+    u = 0.02 * rng.uniform(-1, 1, (nx * ny, 3))
+    u[:, 2] = 0
+    a = Oracle((nx, ny, 1), 0.6, velocity=u, velocity_set=2, esoteric=True, precision=32)
+    b = Oracle((nx, ny, 1), 0.6, velocity=u, velocity_set=2, esoteric=True, precision=64)
+    a.iterate(100)
+    b.iterate(100)
+    va, _ = a.fields()
+    vb, _ = b.fields()
+    assert np.abs(va[:, 3] - vb[:, 3]).max() < 1e-5
+    assert np.abs(va[:, :3] - vb[:, :3]).max() < 1e-5 * max(np.abs(vb[:, :3]).max(), 1e-3) * 10
+
+
+def test_shan_chen_conserves_mass_and_separates():
+    nx = ny = 32
+    rng = np.random.default_rng(4)
+    rho = 0.69 + 0.01 * rng.uniform(-1, 1, nx * ny)
+    o = Oracle((nx, ny, 1), 1.0, density=rho, velocity_set=2, esoteric=True, multiphase=True, G=-5.0, precision=64)
+    m0 = o.lattice().sum()
+    o.iterate(400)
+    vd, _ = o.fields()
+    assert abs(o.lattice().sum() - m0) < 1e-9 * m0
+    assert vd[:, 3].max() - vd[:, 3].min() > 0.1  # spinodal decomposition started

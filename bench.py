@@ -172,9 +172,48 @@ def run_reference(args):
     return 0
 
 
-def run_gpu(args):
+def run_e2e(bf, res, vel, steps, world):
+    """Public-API run from host memory: bf_initialize_fields from pinned host
+    arrays, `steps` calls of one time step, read-back of the u/rho field."""
+    import ctypes as C
     import numpy as np
+    n = res[0] * res[1] * res[2]
+    lib = bf.load_library()
+    host_u = vel
+    host_out = np.empty(n * 4, np.float32)
+    try:
+        import torch
+        pin_u = torch.from_numpy(vel.reshape(-1)).pin_memory()
+        pin_out = torch.empty(n * 4, dtype=torch.float32).pin_memory()
+        host_u = pin_u.numpy().reshape(-1, 3)
+        host_out = pin_out.numpy()
+    except Exception:
+        pass
+    t0 = time.perf_counter()
+    s = bf.LBM()
+    s.is_collide_esoteric = True
+    s.collision = bf.Collision.trt
+    s.initialize_fields_from_arrays(res, TAU, velocity=host_u, periodic=(True, True, True),
+                                    velocity_set=bf.VelocitySet.D3Q19)
+    for _ in range(steps - 1):
+        s.iterate_time(steps=1, save=False)
+    s.iterate_time(steps=1, save=True)
+    rc = lib.bf_copy_field_to_host(s._h, 0, host_out.ctypes.data_as(C.c_void_p), host_out.nbytes)
+    if rc != 0:
+        raise RuntimeError(lib.bf_last_error().decode())
+    dt = time.perf_counter() - t0
+    del s
+    return {"value": round(world * n * steps / dt / 1e6, 1), "unit": "MLUPs",
+            "h2d_bytes_per_step": int(n * 3 * 4 / steps), "d2h_bytes_per_step": int(n * 4 * 4 / steps),
+            "note": "timed: upload of the initial fields, the steps, read-back of the u/rho field; bytes amortised per step"}
+
+
+def run_gpu(args):
     rank, world, local = dist_env()
+    if world > 1:
+        # one process per GPU: the solver library uses the process's first
+        # visible device, so each rank sees only its own
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
     import boltzmannfluids_gb300 as bf
     from boltzmannfluids_gb300 import build as _b
     _b.build()
@@ -182,19 +221,16 @@ def run_gpu(args):
     if world > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
+        torch.cuda.set_device(0)
         dist.init_process_group("nccl")
-    else:
-        import ctypes
-        # the C library picks the current device; one process drives one GPU
-    if world > 1:
-        pass
-    res = RES
+    res = (args.size, args.size, args.size)
     n = res[0] * res[1] * res[2]
     vel = seeded_velocity(n)
+    main_st = {"fp32": bf.FloatingPointAccuracy.fp32, "fp16s": bf.FloatingPointAccuracy.fp16s,
+               "fp16c": bf.FloatingPointAccuracy.fp16c}[args.storage]
 
     # ---- device-resident throughput (value) ----
-    s = make_solver(bf.FloatingPointAccuracy.fp32, velocity=vel)
+    s = make_solver(main_st, res=res, velocity=vel)
     s.iterate_time(steps=max(args.warmup, 3), save=False)
     s.synchronize()
     if dist:
@@ -212,15 +248,16 @@ def run_gpu(args):
         t_step = float(t.item())
     mlups = world * n / (t_step * 1e-3) / 1e6
     peak, peak_kind = measured_peak()
-    achieved = BYTES_PER_CELL[0] * n / (t_step * 1e-3) / 1e9
+    achieved = BYTES_PER_CELL[int(main_st)] * n / (t_step * 1e-3) / 1e9
     # KE / mass after the timed run (FP64 reductions)
     red = s.reduce()
     del s
 
     # ---- 16-bit storage modes (same workload) ----
     sweep = {}
-    for name, st in (("fp16s", bf.FloatingPointAccuracy.fp16s), ("fp16c", bf.FloatingPointAccuracy.fp16c)):
-        s2 = make_solver(st, velocity=vel)
+    for name, st in (() if args.no_sweep else (("fp16s", bf.FloatingPointAccuracy.fp16s),
+                                                ("fp16c", bf.FloatingPointAccuracy.fp16c))):
+        s2 = make_solver(st, res=res, velocity=vel)
         s2.iterate_time(steps=3, save=False)
         s2.synchronize()
         k = max(4, args.steps // 2)
@@ -232,38 +269,9 @@ def run_gpu(args):
         del s2
 
     # ---- end to end through the C ABI with host buffers (e2e) ----
-    import ctypes as C
-    lib = bf.load_library()
-    cudart = None
-    host_u = vel
-    host_out = np.empty(n * 4, np.float32)
-    try:
-        import torch
-        pin_u = torch.from_numpy(vel.reshape(-1)).pin_memory()
-        pin_out = torch.empty(n * 4, dtype=torch.float32).pin_memory()
-        host_u = pin_u.numpy().reshape(-1, 3)
-        host_out = pin_out.numpy()
-    except Exception:
-        pass
-    e2e_steps = args.steps
-    t0 = time.perf_counter()
-    s3 = bf.LBM()
-    s3.is_collide_esoteric = True
-    s3.collision = bf.Collision.trt
-    s3.initialize_fields_from_arrays(res, TAU, velocity=host_u, periodic=(True, True, True),
-                                     velocity_set=bf.VelocitySet.D3Q19)
-    for _ in range(e2e_steps - 1):
-        s3.iterate_time(steps=1, save=False)
-    s3.iterate_time(steps=1, save=True)
-    rc = lib.bf_copy_field_to_host(s3._h, 0, host_out.ctypes.data_as(C.c_void_p), host_out.nbytes)
-    if rc != 0:
-        raise RuntimeError(lib.bf_last_error().decode())
-    e2e_dt = time.perf_counter() - t0
-    e2e_mlups = world * n * e2e_steps / e2e_dt / 1e6
-    h2d = (n * 3 * 4) / e2e_steps
-    d2h = (n * 4 * 4) / e2e_steps
-    del s3
-
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(bf, res, vel, args.steps, world)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         mlups_cpu, threads, sample = cpu_baseline_sample()
@@ -273,19 +281,19 @@ def run_gpu(args):
         line = {
             "metric": METRIC, "value": round(mlups, 1), "unit": "MLUPs", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(t_step, 4), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "D3Q19 TRT (magic 1/4, tau 0.55) esoteric-pull, 512^3 periodic box, FP32 DDF",
-                       "cells": n, "velocity_set": "D3Q19", "collision": "TRT", "storage": "fp32",
-                       "l2": "inputs larger than L2 (10.2 GB DDF vs 129 MB L2), no flush",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded equilibrium start, u noise 1e-4)",
+            "config": {"workload": f"D3Q19 TRT (magic 1/4, tau 0.55) esoteric-pull, {args.size}^3 periodic box, "
+                                   f"{args.storage} DDF",
+                       "cells": n, "velocity_set": "D3Q19", "collision": "TRT", "storage": args.storage,
+                       "l2": f"inputs larger than L2 ({n * 19 * (4 if args.storage == 'fp32' else 2) / 1e9:.2f} GB "
+                             f"DDF vs 129 MB L2), no flush",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": None,
-                         "peak_kind": peak_kind, "bytes_per_cell": BYTES_PER_CELL[0]},
+                         "peak_kind": peak_kind, "bytes_per_cell": BYTES_PER_CELL[int(main_st)]},
             "storage_sweep": sweep,
             "conservation_fp64": {"mass": red[0], "momentum": list(red[1:4]), "kinetic_energy": red[4]},
-            "e2e": {"value": round(e2e_mlups, 1), "unit": "MLUPs", "h2d_bytes_per_step": int(h2d),
-                    "d2h_bytes_per_step": int(d2h),
-                    "note": "initial fields uploaded once and the u/rho field read back once per run; bytes amortised per step"},
+            "e2e": e2e,
             "gpu_launches": args.steps,
             "clocks": clock_info,
         }
@@ -305,6 +313,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--size", type=int, default=512, help="cube edge of the periodic box (512 = the workload)")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
+    ap.add_argument("--no-sweep", action="store_true", help="skip the 16-bit storage legs (profiling runs)")
+    ap.add_argument("--storage", default="fp32", choices=["fp32", "fp16s", "fp16c"], help="storage of the main leg")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -37,7 +37,10 @@ def build(verbose=False, force=False):
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _deps():
         return LIB
     os.makedirs(BUILD, exist_ok=True)
-    flags = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-v" if verbose else "-O3",
+    # -ffp-contract=off for the host side: the launch constants must be the
+    # same roundings as the oracle's on x86 and on Arm (where GCC would fuse)
+    flags = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+             "-Xptxas", "-v" if verbose else "-O3",
              "--expt-relaxed-constexpr", *ARCH]
 
     def compile_one(src):

@@ -159,18 +159,18 @@ void fill_constants(bf_solver* s, StepParams& p) {
     const float cs = (float)(1.0 / std::sqrt(3.0));
     const float cs2 = cs * cs, cs4 = cs2 * cs2;
     const float tau = s->desc.relaxation_time;
-    p.inv_tau = 1.0f / tau;
-    p.src_pref = 1.0f - 1.0f / (2.0f * tau);
-    p.inv_cs2 = 1.0f / cs2;
-    p.half_inv_cs4 = 1.0f / (2.0f * cs4);
-    p.half_inv_cs2 = 1.0f / (2.0f * cs2);
-    p.inv_cs4 = 1.0f / cs4;
+    p.R2 = 1.0f / cs2;
+    p.R4 = 1.0f / cs4;
+    p.Rtau = 1.0f / tau;
+    p.P = 1.0f - 1.0f / (2.0f * tau);
     const float tau_minus = s->desc.trt_magic / (tau - 0.5f) + 0.5f;
-    p.trt_inv_tau_minus = 1.0f / tau_minus;
+    p.Wm = 1.0f / tau_minus;
+    p.Pp = 1.0f - p.Rtau * 0.5f;
+    p.Pm = 1.0f - p.Wm * 0.5f;
     p.vlim = s->desc.velocity_limit;
     p.vlim_ext = s->desc.velocity_limit_extreme;
     p.fconst[0] = s->fconst[0]; p.fconst[1] = s->fconst[1]; p.fconst[2] = s->fconst[2];
-    p.inv_tau_t = 1.0f / s->desc.thermal_relaxation_time;
+    p.Rtau_t = 1.0f / s->desc.thermal_relaxation_time;
     p.beta = s->desc.thermal_expansion_coefficient;
     p.G = s->desc.intermolecular_interaction_strength;
 }

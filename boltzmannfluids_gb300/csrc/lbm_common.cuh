@@ -90,35 +90,20 @@ __host__ __device__ constexpr int opp(int i) { return i == 0 ? 0 : ((i & 1) ? i 
 // ---------------------------------------------------------------------------
 enum Storage { ST_FP32 = 0, ST_FP16 = 1, ST_FP16S = 2, ST_FP16C = 3 };
 
-// custom 1-4-11 float: normal 2^(e-13)*(1+m/2048), e=1..15; subnormal
-// 2^-12*m/2048; saturating; round to nearest even.  Integer-only code.
+// custom 16-bit "c16": 1 sign, 4 exponent, 11 mantissa bits = the top 15
+// bits of an FP32 scaled by 2^-114 (normal 2^(e-13)*(1+m/2048), subnormal
+// 2^-12*m/2048).  Encode: scale |f| by 2^-114, round the bit pattern to
+// nearest even at bit 12, saturate at the largest code (also for NaN/inf).
 __device__ __forceinline__ uint16_t encode_c16(float f) {
-    uint32_t x = __float_as_uint(f);
-    uint32_t sign = (x >> 16) & 0x8000u;
-    uint32_t mag = x & 0x7fffffffu;
-    if (mag > 0x7f800000u) return (uint16_t)sign;
-    if (mag >= 0x40fff800u) return (uint16_t)(sign | 0x7fffu);
-    if (mag < 0x39800000u) {
-        if (mag < 0x33800000u) return (uint16_t)sign;
-        uint32_t m = (mag & 0x7fffffu) | 0x800000u;
-        uint32_t shift = 127u - (mag >> 23);
-        uint32_t q = m >> shift, rem = m & ((1u << shift) - 1u), half = 1u << (shift - 1u);
-        q += (rem > half || (rem == half && (q & 1u))) ? 1u : 0u;
-        return (uint16_t)(sign | q);
-    }
-    uint32_t q = (((mag >> 23) - 114u) << 11) | ((mag & 0x7fffffu) >> 12);
-    uint32_t rem = mag & 0xfffu;
-    q += (rem > 0x800u || (rem == 0x800u && (q & 1u))) ? 1u : 0u;
+    const uint32_t sign = (__float_as_uint(f) >> 16) & 0x8000u;
+    uint32_t b = __float_as_uint(__fmul_rn(fabsf(f), 0x1p-114f));
+    b = b + 0x7ffu + ((b >> 12) & 1u);
+    const uint32_t q = min(b >> 12, 0x7fffu);
     return (uint16_t)(sign | q);
 }
 __device__ __forceinline__ float decode_c16(uint16_t h) {
-    uint32_t sign = (uint32_t)(h & 0x8000u) << 16;
-    uint32_t e = (h >> 11) & 0xfu, m = h & 0x7ffu;
-    if (e == 0) {
-        float v = (float)m * 1.1920928955078125e-07f;
-        return __uint_as_float(__float_as_uint(v) | sign);
-    }
-    return __uint_as_float(sign | ((e + 114u) << 23) | (m << 12));
+    const float a = __uint_as_float((uint32_t)(h & 0x7fffu) << 12);
+    return __uint_as_float(__float_as_uint(__fmul_rn(a, 0x1p114f)) | ((uint32_t)(h & 0x8000u) << 16));
 }
 
 template <int ST> struct Codec;
@@ -134,13 +119,13 @@ template <> struct Codec<ST_FP16> {  // R16F: IEEE half of f
 };
 template <> struct Codec<ST_FP16S> {  // IEEE half of f - w
     using T = __half;
-    __device__ __forceinline__ static float dec(T v, float w) { return __half2float(v) + w; }
-    __device__ __forceinline__ static T enc(float v, float w) { return __float2half_rn(v - w); }
+    __device__ __forceinline__ static float dec(T v, float w) { return __fadd_rn(__half2float(v), w); }
+    __device__ __forceinline__ static T enc(float v, float w) { return __float2half_rn(__fsub_rn(v, w)); }
 };
 template <> struct Codec<ST_FP16C> {  // custom 16-bit of (f - w)/w
     using T = uint16_t;
     __device__ __forceinline__ static float dec(T v, float w) { return fmaf(decode_c16(v), w, w); }
-    __device__ __forceinline__ static T enc(float v, float w) { return encode_c16((v - w) * (1.0f / w)); }
+    __device__ __forceinline__ static T enc(float v, float w) { return encode_c16(__fmul_rn(__fsub_rn(v, w), 1.0f / w)); }
 };
 
 // ---------------------------------------------------------------------------
@@ -175,14 +160,14 @@ struct alignas(16) StepParams {
     uint32_t flags;
     uint32_t n_cells;
     int bits;                 // bits per boundary id (0, 1, 2, 4, 8)
-    // collision constants (host-computed from the reference's FP32 values)
-    float inv_tau;            // 1/tau
-    float src_pref;           // 1 - 1/(2 tau)
-    float inv_cs2;            // 1/cs^2 with cs = float(1/sqrt(3))
-    float half_inv_cs4;       // 1/(2 cs^4)
-    float half_inv_cs2;       // 1/(2 cs^2)
-    float inv_cs4;            // 1/cs^4
-    float trt_inv_tau_minus;  // TRT omega-
+    // launch constants, FP32, computed on the host exactly as the oracle
+    // does: cs = float(1/sqrt(3)), cs2 = cs*cs, cs4 = cs2*cs2
+    float R2;                 // 1/cs2
+    float R4;                 // 1/cs4
+    float Rtau;               // 1/tau (= TRT omega+)
+    float P;                  // 1 - 1/(2 tau), Guo prefactor
+    float Wm;                 // TRT omega- = 1/(Lambda/(tau-1/2) + 1/2)
+    float Pp, Pm;             // TRT Guo prefactors 1 - omega+/2, 1 - omega-/2
     float vlim, vlim_ext;
     float fconst[3];
     const float4* force;      // per-cell force field (reference vec4 layout)
@@ -193,7 +178,7 @@ struct alignas(16) StepParams {
     // thermal lattice (SoA, FP32)
     const float* th_src;
     float* th_tgt;
-    float inv_tau_t, beta;
+    float Rtau_t, beta;       // 1/tau_T, thermal expansion coefficient
     // Shan-Chen: psi of the effective density, ping-pong
     const float* psi_src;
     float* psi_tgt;

@@ -18,6 +18,61 @@ namespace bf {
 
 struct CellSum { float m, px, py, pz, ke; };
 
+// Rounded, never-contracted FP32 operations: the kernels evaluate the same
+// expression tree as the oracle's canonical FP32 restatement (the shader's
+// operation order, divisions by launch uniforms as multiplications by their
+// once-rounded reciprocals), so FP32 results agree bit for bit.
+#define FMUL __fmul_rn
+#define FADD __fadd_rn
+#define FSUB __fsub_rn
+
+// exp for the pseudopotential psi = 1 - exp(-rho), the same operations as the
+// oracle's exp_f32: Cody-Waite reduction x = k ln2 + r (ln2 split in a 15-bit
+// head and a tail), degree-7 Taylor polynomial of exp(r) in Horner form
+// (|r| <= ln2/2, truncation < 6e-9 relative), exact scaling by 2^k.
+// Valid for x in [-87, 88].
+__device__ __forceinline__ float exp_f32(float x) {
+    const float L2E = 0x1.715476p+0f, LN2_HI = 0x1.62e4p-1f, LN2_LO = 0x1.7f7d1cp-20f;
+    const float kf = rintf(FMUL(x, L2E));
+    const float r = FSUB(FSUB(x, FMUL(kf, LN2_HI)), FMUL(kf, LN2_LO));
+    float q = 0x1.a01a02p-13f;
+    q = FADD(FMUL(q, r), 0x1.6c16c2p-10f);
+    q = FADD(FMUL(q, r), 0x1.111112p-7f);
+    q = FADD(FMUL(q, r), 0x1.555556p-5f);
+    q = FADD(FMUL(q, r), 0x1.555556p-3f);
+    q = FADD(FMUL(q, r), 0x1p-1f);
+    q = FADD(FMUL(q, r), 1.0f);
+    q = FADD(FMUL(q, r), 1.0f);
+    return FMUL(q, __uint_as_float((uint32_t)((int)kf + 127) << 23));
+}
+
+// c . v for a lattice direction with components in {-1, 0, 1}: the dot
+// product's x, y, z sum with the zero terms dropped (they add +-0 only)
+template <int CX, int CY, int CZ>
+__device__ __forceinline__ float cdot(float vx, float vy, float vz) {
+    float acc = 0.0f;
+    bool first = true;
+    if (CX != 0) { acc = CX > 0 ? vx : -vx; first = false; }
+    if (CY != 0) { const float t = CY > 0 ? vy : -vy; acc = first ? t : FADD(acc, t); first = false; }
+    if (CZ != 0) { const float t = CZ > 0 ? vz : -vz; acc = first ? t : FADD(acc, t); first = false; }
+    return acc;
+}
+__device__ __forceinline__ float cdot_rt(const Dir c, float vx, float vy, float vz) {
+    float acc = 0.0f;
+    bool first = true;
+    if (c.x != 0) { acc = c.x > 0 ? vx : -vx; first = false; }
+    if (c.y != 0) { const float t = c.y > 0 ? vy : -vy; acc = first ? t : FADD(acc, t); first = false; }
+    if (c.z != 0) { const float t = c.z > 0 ? vz : -vz; acc = first ? t : FADD(acc, t); first = false; }
+    return acc;
+}
+__device__ __forceinline__ float dot3r(float ax, float ay, float az, float bx, float by, float bz) {
+    return FADD(FADD(FMUL(ax, bx), FMUL(ay, by)), FMUL(az, bz));
+}
+// (1 + cu/cs2 + cu^2/2/cs4 - uu/2/cs2) with uuh = (uu*0.5)/cs2 precomputed
+__device__ __forceinline__ float eq_bracket(float cu, float uuh, float R2, float R4) {
+    return FSUB(FADD(FADD(1.0f, FMUL(cu, R2)), FMUL(FMUL(FMUL(cu, cu), 0.5f), R4)), uuh);
+}
+
 template <int Q>
 __device__ __forceinline__ void coords_wrap(int& cx, int& cy, int& cz, int nx, int ny, int nz, bool& open, uint32_t flags) {
     open = false;
@@ -85,7 +140,7 @@ __device__ __forceinline__ CellSum cell_update(const StepParams& p, int x, int y
             if (flags & F_SAVE) {
                 p.vel_den[n] = make_float4(0.f, 0.f, 0.f, 0.f);
                 p.force_temp[n] = make_float4(0.f, 0.f, 0.f, 0.f);
-                p.bnd_tex[n] = (uint8_t)bid;
+                if (p.bnd_tex) p.bnd_tex[n] = (uint8_t)bid;
             }
             return out;
         }
@@ -124,9 +179,9 @@ __device__ __forceinline__ CellSum cell_update(const StepParams& p, int x, int y
             if (MODE != AA_LOCAL && (eqb || (flags & F_BOUNCE_BACK)) && i != 0) {
                 if (eqb && sopen) {
                     // population entering from outside the domain: f_eq(rho_b, u_b)
-                    const float cu = c.x * bv.y + c.y * bv.z + c.z * bv.w;
-                    const float uu = bv.y * bv.y + bv.z * bv.z + bv.w * bv.w;
-                    f[i] = w * bv.x * (1.f + cu * p.inv_cs2 + cu * cu * p.half_inv_cs4 - uu * p.half_inv_cs2);
+                    const float cu = cdot_rt(c, bv.y, bv.z, bv.w);
+                    const float uuh = FMUL(FMUL(dot3r(bv.y, bv.z, bv.w, bv.y, bv.z, bv.w), 0.5f), p.R2);
+                    f[i] = FMUL(FMUL(w, bv.x), eq_bracket(cu, uuh, p.R2, p.R4));
                     done = true;
                 } else if ((flags & F_BOUNCE_BACK) && !sopen && (flags & F_BOUNDARIES)) {
                     const uint32_t sid = boundary_id(p.bnd, p.bits, sn);
@@ -152,18 +207,18 @@ __device__ __forceinline__ CellSum cell_update(const StepParams& p, int x, int y
     }
 
     // ---- moments ----
-    float rho = 0.f;
+    float rho = f[0];
 #pragma unroll
-    for (int i = 0; i < Q; i++) rho += f[i];
+    for (int i = 1; i < Q; i++) rho = FADD(rho, f[i]);
     if (GENERIC && !(rho == rho)) atomicOr(p.err, 1u);
     rho = rho < 0.01f ? 0.01f : rho;  // max(density, 0.01), NaN kept
     float jx = 0.f, jy = 0.f, jz = 0.f;
 #pragma unroll
     for (int i = 0; i < Q; i++) {
         const Dir c = L::c(i);
-        if (c.x) jx += c.x > 0 ? f[i] : -f[i];
-        if (c.y) jy += c.y > 0 ? f[i] : -f[i];
-        if (c.z) jz += c.z > 0 ? f[i] : -f[i];
+        if (c.x) jx = FADD(jx, c.x > 0 ? f[i] : -f[i]);
+        if (c.y) jy = FADD(jy, c.y > 0 ? f[i] : -f[i]);
+        if (c.z) jz = FADD(jz, c.z > 0 ? f[i] : -f[i]);
     }
 
     // ---- forces (collide.comp:707-720) ----
@@ -175,12 +230,12 @@ __device__ __forceinline__ CellSum cell_update(const StepParams& p, int x, int y
         if (flags & F_THERMAL) {
             constexpr int QT = L::D == 2 ? 5 : 7;
 #pragma unroll
-            for (int i = 0; i < QT; i++) temperature += __ldg(p.th_src + (uint64_t)i * S + n);
+            for (int i = 0; i < QT; i++) temperature = FADD(temperature, __ldg(p.th_src + (uint64_t)i * S + n));
             const float k = __fmul_rn(-p.beta, __fsub_rn(temperature, 1.0f));
             Fx = __fadd_rn(Fx, __fmul_rn(k, Fx)); Fy = __fadd_rn(Fy, __fmul_rn(k, Fy)); Fz = __fadd_rn(Fz, __fmul_rn(k, Fz));
         }
         if (flags & F_MULTIPHASE) {
-            const float self_psi = 1.0f - expf(-rho);
+            const float self_psi = FSUB(1.0f, exp_f32(-rho));
             float sx = 0.f, sy = 0.f, sz = 0.f;
 #pragma unroll
             for (int i = 1; i < Q; i++) {
@@ -223,56 +278,64 @@ __device__ __forceinline__ CellSum cell_update(const StepParams& p, int x, int y
         if (kind == 1) { ux = bv.y; uy = bv.z; uz = bv.w; } else { rho = bv.x; }
         Fx = Fy = Fz = 0.f;
     }
-    const float uu = ux * ux + uy * uy + uz * uz;
+    const float uu = dot3r(ux, uy, uz, ux, uy, uz);
+    const float uuh = FMUL(FMUL(uu, 0.5f), p.R2);
 
     // ---- collision + AA store (collide.comp:727-760) ----
     if (flags & F_UPDATE) {
-        const float fu = Fx * ux + Fy * uy + Fz * uz;
-        const float base = 1.0f - uu * p.half_inv_cs2;
+        const float fu = dot3r(Fx, Fy, Fz, ux, uy, uz);
+        const float fuR2 = FMUL(fu, p.R2);
+        const bool src = (flags & F_SOURCE) != 0;
+        auto feq = [&](int i) -> float {
+            return FMUL(FMUL(L::w(i), rho), eq_bracket(cdot_rt(L::c(i), ux, uy, uz), uuh, p.R2, p.R4));
+        };
         float fn[Q];
-        if (!(flags & F_TRT)) {
+        if (eqb) {
+#pragma unroll
+            for (int i = 0; i < Q; i++) fn[i] = feq(i);
+        } else if (!(flags & F_TRT)) {
 #pragma unroll
             for (int i = 0; i < Q; i++) {
                 const Dir c = L::c(i);
                 const float w = L::w(i);
-                const float cu = c.x * ux + c.y * uy + c.z * uz;
-                const float feq = w * rho * (base + cu * p.inv_cs2 + cu * cu * p.half_inv_cs4);
-                float v = fmaf(feq - f[i], p.inv_tau, f[i]);
-                if (flags & F_SOURCE) {
-                    const float fc = c.x * Fx + c.y * Fy + c.z * Fz;
-                    v += p.src_pref * w * (fc * p.inv_cs2 + fc * cu * p.inv_cs4 - fu * p.inv_cs2);
+                const float fe = feq(i);
+                float v = FADD(f[i], FMUL(FSUB(fe, f[i]), p.Rtau));  // old + (-(old - feq)/tau)
+                if (src) {
+                    const float cu = cdot_rt(c, ux, uy, uz);
+                    const float fc = cdot_rt(c, Fx, Fy, Fz);
+                    // (1-1/(2tau)) w (F.c/cs2 + ((F.c)(u.c)/cs4 - F.u/cs2))
+                    v = FADD(v, FMUL(FMUL(p.P, w), FADD(FMUL(fc, p.R2), FSUB(FMUL(FMUL(fc, cu), p.R4), fuR2))));
                 }
-                fn[i] = (out_ext || eqb) ? feq : v;
+                fn[i] = out_ext ? fe : v;
             }
         } else {
-            const float wp = p.inv_tau, wm = p.trt_inv_tau_minus;
-            const float sp_pref = 1.0f - 0.5f * wp, sm_pref = 1.0f - 0.5f * wm;
             {
-                const float w = L::w(0);
-                const float feq = w * rho * base;
-                float v = f[0] - wp * (f[0] - feq);
-                if (flags & F_SOURCE) v += sp_pref * w * (-fu * p.inv_cs2);
-                fn[0] = (out_ext || eqb) ? feq : v;
+                const float fe0 = feq(0);
+                const float dp = FMUL(FSUB(f[0], fe0), p.Rtau);
+                float v = FSUB(f[0], dp);
+                if (src) v = FADD(v, FMUL(FMUL(p.Pp, L::w(0)), FSUB(0.0f, fuR2)));
+                fn[0] = out_ext ? fe0 : v;
             }
 #pragma unroll
             for (int i = 1; i < Q; i += 2) {
                 const int j = i + 1;
                 const Dir c = L::c(i);
                 const float w = L::w(i);
-                const float cu = c.x * ux + c.y * uy + c.z * uz;
-                const float ep = w * rho * (base + cu * cu * p.half_inv_cs4);
-                const float em = w * rho * (cu * p.inv_cs2);
-                const float fp = 0.5f * (f[i] + f[j]), fm = 0.5f * (f[i] - f[j]);
-                const float dp = wp * (fp - ep), dm = wm * (fm - em);
-                float vi = f[i] - dp - dm, vj = f[j] - dp + dm;
-                if (flags & F_SOURCE) {
-                    const float fc = c.x * Fx + c.y * Fy + c.z * Fz;
-                    const float Sp = sp_pref * w * (fc * cu * p.inv_cs4 - fu * p.inv_cs2);
-                    const float Sm = sm_pref * w * (fc * p.inv_cs2);
-                    vi += Sp + Sm; vj += Sp - Sm;
+                const float fei = feq(i), fej = feq(j);
+                const float fp = FMUL(FADD(f[i], f[j]), 0.5f), fm = FMUL(FSUB(f[i], f[j]), 0.5f);
+                const float ep = FMUL(FADD(fei, fej), 0.5f), em = FMUL(FSUB(fei, fej), 0.5f);
+                const float dp = FMUL(FSUB(fp, ep), p.Rtau), dm = FMUL(FSUB(fm, em), p.Wm);
+                float vi = FSUB(FSUB(f[i], dp), dm), vj = FADD(FSUB(f[j], dp), dm);
+                if (src) {
+                    const float cu = cdot_rt(c, ux, uy, uz);
+                    const float fc = cdot_rt(c, Fx, Fy, Fz);
+                    const float Sp = FMUL(FMUL(p.Pp, w), FSUB(FMUL(FMUL(fc, cu), p.R4), fuR2));
+                    const float Sm = FMUL(FMUL(p.Pm, w), FMUL(fc, p.R2));
+                    vi = FADD(vi, FADD(Sp, Sm));
+                    vj = FADD(vj, FSUB(Sp, Sm));
                 }
-                fn[i] = (out_ext || eqb) ? ep + em : vi;
-                fn[j] = (out_ext || eqb) ? ep - em : vj;
+                fn[i] = out_ext ? fei : vi;
+                fn[j] = out_ext ? fej : vj;
             }
         }
 #pragma unroll
@@ -299,7 +362,7 @@ __device__ __forceinline__ CellSum cell_update(const StepParams& p, int x, int y
     if (GENERIC && (flags & F_MULTIPHASE) && !(flags & F_MEASURE)) {  // collide.comp:763-769, psi of the effective density
         float eff = rho;
         if (bid != 0u) eff = __ldg(p.objects + 3u * bid + 2u).w;
-        p.psi_tgt[n] = 1.0f - expf(-eff);
+        p.psi_tgt[n] = FSUB(1.0f, exp_f32(-eff));
     }
     if (GENERIC && (flags & F_THERMAL) && !(flags & F_MEASURE)) {  // collide.comp:771-782
         constexpr int QT = L::D == 2 ? 5 : 7;
@@ -307,10 +370,10 @@ __device__ __forceinline__ CellSum cell_update(const StepParams& p, int x, int y
         for (int i = 0; i < QT; i++) {
             const Dir c = ThermalLattice<QT>::c(i);
             const float w = ThermalLattice<QT>::w(i);
-            const float cu = c.x * ux + c.y * uy + c.z * uz;
-            const float geq = w * temperature * (1.0f + cu * p.inv_cs2 + cu * cu * p.half_inv_cs4 - uu * p.half_inv_cs2);
+            const float cu = cdot_rt(c, ux, uy, uz);
+            const float geq = FMUL(FMUL(w, temperature), eq_bracket(cu, uuh, p.R2, p.R4));
             const float g = __ldg(p.th_src + (uint64_t)i * S + n);
-            p.th_tgt[(uint64_t)i * S + n] = fmaf(geq - g, p.inv_tau_t, g);
+            p.th_tgt[(uint64_t)i * S + n] = FADD(g, FMUL(FSUB(geq, g), p.Rtau_t));  // g + (-(g - geq)/tau_T)
         }
     }
     if (flags & F_SAVE) {  // collide.comp:784-792

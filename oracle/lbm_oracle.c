@@ -111,40 +111,30 @@ static float f16_to_f32(uint16_t h) {
     else x = sign | ((e + 112u) << 23) | (m << 13);
     float f; memcpy(&f, &x, 4); return f;
 }
-/* custom 16-bit: 1 sign, 4 exponent, 11 mantissa bits; normal value
- * 2^(e-13)*(1+m/2048) for e=1..15, subnormal 2^-12*(m/2048); saturates at the
- * largest finite value (2^2*(2-2^-11)); round to nearest even. */
+/* custom 16-bit "c16": 1 sign, 4 exponent, 11 mantissa bits; magnitude
+ * 2^(e-13)*(1+m/2048) for e=1..15 and 2^-12*(m/2048) for e=0, i.e. the top
+ * 15 bits of an FP32 scaled by 2^-114.  Encoding: scale |f| by 2^-114 in
+ * FP32 (exact for |f| >= 2^-12, rounded into FP32 subnormals below), round
+ * the bit pattern to nearest even at bit 12, saturate at the largest code
+ * (2^2*(2-2^-11)); NaN saturates too.  Decoding scales back by 2^114 (exact). */
 static uint16_t f32_to_c16(float f) {
     uint32_t x; memcpy(&x, &f, 4);
     uint32_t sign = (x >> 16) & 0x8000u;
-    uint32_t mag = x & 0x7fffffffu;
-    if (mag > 0x7f800000u) return (uint16_t)sign; /* NaN -> 0 */
-    if (mag >= 0x40fff800u) return (uint16_t)(sign | 0x7fffu); /* >= 8 - 2^-10 rounds past the top: saturate */
-    if (mag < 0x39800000u) { /* < 2^-12: subnormal range, unit 2^-23 */
-        if (mag < 0x33800000u) return (uint16_t)sign; /* < 2^-24 */
-        uint32_t m = (mag & 0x7fffffu) | 0x800000u;
-        int e = (int)(mag >> 23); /* 104..114 */
-        int shift = 127 - e; /* value = m*2^(e-150); unit 2^-23 -> q = m*2^(e-127) */
-        uint32_t q = m >> shift, rem = m & ((1u << shift) - 1u), half = 1u << (shift - 1);
-        if (rem > half || (rem == half && (q & 1u))) q++;
-        return (uint16_t)(sign | q);
-    }
-    uint32_t e = (mag >> 23) - 114u; /* 2^-12 -> e=1 */
-    uint32_t m = mag & 0x7fffffu;
-    uint32_t q = (e << 11) | (m >> 12);
-    uint32_t rem = m & 0xfffu;
-    if (rem > 0x800u || (rem == 0x800u && (q & 1u))) q++;
+    float a = fabsf(f) * 0x1p-114f;
+    uint32_t b; memcpy(&b, &a, 4);
+    b = b + 0x7ffu + ((b >> 12) & 1u);
+    uint32_t q = b >> 12;
+    if (q > 0x7fffu) q = 0x7fffu;
     return (uint16_t)(sign | q);
 }
 static float c16_to_f32(uint16_t h) {
-    uint32_t sign = (uint32_t)(h & 0x8000u) << 16;
-    uint32_t e = (h >> 11) & 0xfu, m = h & 0x7ffu, x;
-    if (e == 0) {
-        float v = (float)m * 1.1920928955078125e-07f; /* m * 2^-23 */
-        return sign ? -v : v;
-    }
-    x = sign | ((e + 114u) << 23) | (m << 12);
-    float f; memcpy(&f, &x, 4); return f;
+    uint32_t b = (uint32_t)(h & 0x7fffu) << 12;
+    float a; memcpy(&a, &b, 4);
+    float v = a * 0x1p114f;
+    uint32_t vb; memcpy(&vb, &v, 4);
+    vb |= (uint32_t)(h & 0x8000u) << 16;
+    memcpy(&v, &vb, 4);
+    return v;
 }
 
 /* ------------------------------------------------------------------------ */
@@ -168,13 +158,17 @@ typedef struct {
     const orc_dir* V;
     const orc_dir* Vt;
     REAL cs;
+    /* launch constants, computed once per launch as the host does:
+     * divisions by these uniforms are evaluated as multiplications by their
+     * correctly rounded reciprocals (see the canonical-order note below). */
+    REAL R2, R4, Rtau, P, Rtau_t, Wm, Pp, Pm;
     REAL* lat[2];
     int lat0_src;
     uint32_t* boundries;
     int bits, nobj;
     float* objects;   /* 12 floats per id: (u,T) (omega,0) (com,rho_eff) as LBM.cpp:613-626 */
     int* obj_kind;
-    int forcing, constant_force, thermal;
+    int forcing, constant_force, thermal, src_on;
     REAL fconst[3];
     float* forces;    /* N*4 */
     REAL* th[2];
@@ -276,27 +270,38 @@ static int aa_write_addr(orc_t* s, int x, int y, int z, int i, int odd, size_t* 
 /* ------------------------------------------------------------------------ */
 /* physics (collide.comp:512-629, :634-673)                                  */
 /* ------------------------------------------------------------------------ */
-static REAL feq_ref(const orc_t* s, REAL rho, v3 u, int i) { /* collide.comp:589-606 */
+/*
+ * Canonical FP32 evaluation.  The shader's divisions by launch uniforms
+ * (x/cs^2, x/cs^4, x/tau) are taken as x * (1/uniform) with the reciprocal
+ * rounded once per launch -- what a GL driver does with a division by a
+ * uniform -- and every other operation is rounded separately in the order
+ * the GLSL source writes it (no FMA contraction; /2 is the exact *0.5).
+ * Divisions by per-cell values (rho, |u|) stay IEEE divisions.  The CUDA
+ * kernels evaluate the same expression tree, so FP32 results agree bit for
+ * bit given the same inputs.
+ */
+static REAL eq_bracket(const orc_t* s, REAL cu, REAL uuh) { /* (1 + cu/cs2 + cu^2/2/cs4 - uu/2/cs2) */
+    REAL cu2 = cu * cu;                 /* pow(ci_dot_u, 2) taken as x*x (GLSL pow(x<0,y) is undefined) */
+    return (((REAL)1 + cu * s->R2) + (cu2 * (REAL)0.5) * s->R4) - uuh;
+}
+static REAL uu_half(const orc_t* s, v3 u) { return (dot3(u, u) * (REAL)0.5) * s->R2; }
+static REAL feq_ref(const orc_t* s, REAL rho, v3 u, REAL uuh, int i) { /* collide.comp:589-606 */
     REAL w = (REAL)s->V[i].w;
     v3 c = mk3((REAL)s->V[i].cx, (REAL)s->V[i].cy, (REAL)s->V[i].cz);
-    REAL cs = s->cs;
-    REAL cu = dot3(c, u);
-    REAL cu2 = cu * cu;         /* pow(ci_dot_u, 2) taken as x*x (GLSL pow(x<0,y) is undefined) */
-    REAL uu = dot3(u, u);
-    REAL cs2 = cs * cs;         /* pow(cs, 2) */
-    REAL cs4 = cs2 * cs2;       /* pow(cs, 4) */
-    return w * rho * ((REAL)1 + cu / cs2 + cu2 / (REAL)2 / cs4 - uu / (REAL)2 / cs2);
+    return (w * rho) * eq_bracket(s, dot3(c, u), uuh);
 }
-static REAL feq_t_ref(const orc_t* s, REAL T, v3 u, int i) { /* collide.comp:634-651 */
+static REAL feq_t_ref(const orc_t* s, REAL T, v3 u, REAL uuh, int i) { /* collide.comp:634-651 */
     REAL w = (REAL)s->Vt[i].w;
     v3 c = mk3((REAL)s->Vt[i].cx, (REAL)s->Vt[i].cy, (REAL)s->Vt[i].cz);
-    REAL cs = s->cs;
-    REAL cu = dot3(c, u);
-    REAL cu2 = cu * cu;
-    REAL uu = dot3(u, u);
-    REAL cs2 = cs * cs;
-    REAL cs4 = cs2 * cs2;
-    return w * T * ((REAL)1 + cu / cs2 + cu2 / (REAL)2.0 / cs4 - uu / (REAL)2.0 / cs2);
+    return (w * T) * eq_bracket(s, dot3(c, u), uuh);
+}
+/* Guo source term (collide.comp:608-625):
+ * (1-dt/(2tau)) * w * (F.c/cs2 + ((F.c)(u.c)/cs4 - F.u/cs2)) */
+static REAL source_ref(const orc_t* s, int i, v3 F, v3 u) {
+    REAL w = (REAL)s->V[i].w;
+    v3 c = mk3((REAL)s->V[i].cx, (REAL)s->V[i].cy, (REAL)s->V[i].cz);
+    REAL fc = dot3(F, c);
+    return (s->P * w) * (fc * s->R2 + ((fc * dot3(u, c)) * s->R4 - dot3(F, u) * s->R2));
 }
 static REAL feq_init(const orc_t* s, REAL rho, v3 u, int i) { /* set_equilibrium_populations.comp:179-196 */
     REAL w = (REAL)s->V[i].w;
@@ -314,17 +319,30 @@ static REAL feq_t_init(const orc_t* s, REAL T, v3 u, int i) { /* set_equilibrium
     REAL uu = dot3(u, u);
     return w * T * ((REAL)1 + (REAL)3 * cu + (REAL)9 * cu2 / (REAL)2 - (REAL)3 * uu / (REAL)2);
 }
-/* Guo source term, split as (1-dt/2tau) * w * (F.c/cs2 + (F.c)(u.c)/cs4 - F.u/cs2) (collide.comp:608-625) */
-static REAL source_ref(const orc_t* s, int i, v3 F, v3 u) {
-    REAL tau = (REAL)s->d.tau;
-    REAL w = (REAL)s->V[i].w;
-    v3 c = mk3((REAL)s->V[i].cx, (REAL)s->V[i].cy, (REAL)s->V[i].cz);
-    REAL cs = s->cs, cs2 = cs * cs, cs4 = cs2 * cs2;
-    return ((REAL)1 - (REAL)1 / ((REAL)2 * tau)) * w * (dot3(F, c) / cs2 + (dot3(F, c) * dot3(u, c) / cs4 - dot3(F, u) / cs2));
+/* exp for the FP32 pseudopotential, identical to the CUDA kernels' copy:
+ * Cody-Waite reduction x = k ln2 + r with ln2 split in a 15-bit head (exact
+ * products for |k| < 2^9) and a tail, exp(r) by the degree-7 Taylor
+ * polynomial in Horner form (|r| <= ln2/2, truncation < 6e-9 relative),
+ * then an exact scaling by 2^k.  Valid for x in [-87, 88]. */
+static float exp_f32(float x) {
+    const float L2E = 0x1.715476p+0f, LN2_HI = 0x1.62e4p-1f, LN2_LO = 0x1.7f7d1cp-20f;
+    float kf = rintf(x * L2E);
+    float r = (x - kf * LN2_HI) - kf * LN2_LO;
+    float q = 0x1.a01a02p-13f;                 /* 1/5040 */
+    q = q * r + 0x1.6c16c2p-10f;               /* 1/720 */
+    q = q * r + 0x1.111112p-7f;                /* 1/120 */
+    q = q * r + 0x1.555556p-5f;                /* 1/24 */
+    q = q * r + 0x1.555556p-3f;                /* 1/6 */
+    q = q * r + 0x1p-1f;
+    q = q * r + 1.0f;
+    q = q * r + 1.0f;
+    uint32_t sb = (uint32_t)((int)kf + 127) << 23;
+    float sc; memcpy(&sc, &sb, 4);
+    return q * sc;
 }
-static REAL psi(REAL rho) { /* collide.comp:512-516 */
+static REAL psi(REAL rho) { /* collide.comp:512-516, rho0 = 1 */
     REAL rho0 = 1;
-    return rho0 * ((REAL)1 - (IS_F32 ? (REAL)expf((float)(-rho / rho0)) : (REAL)exp((double)(-rho / rho0))));
+    return rho0 * ((REAL)1 - (IS_F32 ? (REAL)exp_f32((float)(-rho / rho0)) : (REAL)exp((double)(-rho / rho0))));
 }
 
 /* Shan-Chen interaction force (collide.comp:534-584) */
@@ -390,7 +408,7 @@ static void collide(orc_t* s, int save, int update) {
                 if (eqb && sopen) {
                     REAL rb = (REAL)s->bvals[cell * 4 + 0];
                     v3 ub = mk3((REAL)s->bvals[cell * 4 + 1], (REAL)s->bvals[cell * 4 + 2], (REAL)s->bvals[cell * 4 + 3]);
-                    f[i] = feq_ref(s, rb, ub, i);
+                    f[i] = feq_ref(s, rb, ub, uu_half(s, ub), i);
                     continue;
                 }
                 if (bb && !sopen && is_solid(s, sid)) {
@@ -452,32 +470,48 @@ static void collide(orc_t* s, int save, int update) {
             force = mk3(0, 0, 0);
         }
         if (update) {
-            REAL fn[QMAX];
-            for (int i = 0; i < Q; i++) {
-                REAL fe = feq_ref(s, density, vel, i);
-                REAL upd;
-                if (eqb) upd = fe;
-                else if (s->d.collision == ORC_TRT) {
-                    int oi = opp(i);
-                    REAL fo = f[oi];
-                    REAL feo = feq_ref(s, density, vel, oi);
-                    REAL tau = (REAL)s->d.tau;
-                    REAL wp = (REAL)1 / tau;
-                    REAL taum = (REAL)s->d.trt_magic / (tau - (REAL)0.5) + (REAL)0.5;
-                    REAL wm = (REAL)1 / taum;
-                    REAL fp = (f[i] + fo) * (REAL)0.5, fm = (f[i] - fo) * (REAL)0.5;
-                    REAL ep = (fe + feo) * (REAL)0.5, em = (fe - feo) * (REAL)0.5;
-                    /* Guo term split into its odd (F.c) and even parts */
-                    REAL w = (REAL)s->V[i].w;
-                    v3 c = mk3((REAL)s->V[i].cx, (REAL)s->V[i].cy, (REAL)s->V[i].cz);
-                    REAL cs = s->cs, cs2 = cs * cs, cs4 = cs2 * cs2;
-                    REAL Sm = w * (dot3(force, c) / cs2);
-                    REAL Sp = w * (dot3(force, c) * dot3(vel, c) / cs4 - dot3(force, vel) / cs2);
-                    upd = f[i] - wp * (fp - ep) - wm * (fm - em) + ((REAL)1 - wp * (REAL)0.5) * Sp + ((REAL)1 - wm * (REAL)0.5) * Sm;
-                } else {
-                    upd = f[i] + (-(f[i] - fe) / (REAL)s->d.tau) + source_ref(s, i, force, vel);
+            REAL fn[QMAX], fe[QMAX];
+            const REAL uuh = uu_half(s, vel);
+            for (int i = 0; i < Q; i++) fe[i] = feq_ref(s, density, vel, uuh, i);
+            if (eqb) {
+                for (int i = 0; i < Q; i++) fn[i] = fe[i];
+            } else if (s->d.collision == ORC_TRT) {
+                /* TRT (extension), pairwise over (i, opp i):
+                 * f+- = (f_i +- f_opp)/2, relaxed with omega+ = 1/tau and
+                 * omega- = 1/(Lambda/(tau-1/2) + 1/2); the Guo term's even part
+                 * (F.c)(u.c)/cs4 - F.u/cs2 gets (1-omega+/2), its odd part
+                 * F.c/cs2 gets (1-omega-/2). */
+                const REAL fu = dot3(force, vel);
+                {
+                    REAL dp = (f[0] - fe[0]) * s->Rtau;
+                    REAL v = f[0] - dp;
+                    if (s->src_on) v = v + (s->Pp * (REAL)s->V[0].w) * ((REAL)0 - fu * s->R2);
+                    fn[0] = out_ext ? fe[0] : v;
                 }
-                fn[i] = (!out_ext || eqb) ? upd : fe;
+                for (int i = 1; i < Q; i += 2) {
+                    const int j = i + 1;
+                    REAL fp = (f[i] + f[j]) * (REAL)0.5, fm = (f[i] - f[j]) * (REAL)0.5;
+                    REAL ep = (fe[i] + fe[j]) * (REAL)0.5, em = (fe[i] - fe[j]) * (REAL)0.5;
+                    REAL dp = (fp - ep) * s->Rtau, dm = (fm - em) * s->Wm;
+                    REAL vi = (f[i] - dp) - dm, vj = (f[j] - dp) + dm;
+                    if (s->src_on) {
+                        REAL w = (REAL)s->V[i].w;
+                        v3 c = mk3((REAL)s->V[i].cx, (REAL)s->V[i].cy, (REAL)s->V[i].cz);
+                        REAL fc = dot3(force, c);
+                        REAL Sp = (s->Pp * w) * ((fc * dot3(vel, c)) * s->R4 - fu * s->R2);
+                        REAL Sm = (s->Pm * w) * (fc * s->R2);
+                        vi = vi + (Sp + Sm);
+                        vj = vj + (Sp - Sm);
+                    }
+                    fn[i] = out_ext ? fe[i] : vi;
+                    fn[j] = out_ext ? fe[j] : vj;
+                }
+            } else {
+                for (int i = 0; i < Q; i++) {
+                    REAL upd = f[i] + (fe[i] - f[i]) * s->Rtau; /* old + (-(old - feq)/tau) */
+                    if (s->src_on) upd = upd + source_ref(s, i, force, vel);
+                    fn[i] = out_ext ? fe[i] : upd;
+                }
             }
             for (int i = 0; i < Q; i++) {
                 size_t wc; int ws;
@@ -492,10 +526,11 @@ static void collide(orc_t* s, int save, int update) {
         }
         if (s->thermal) {
             REAL* TS = TSRC(s); REAL* TT = TTGT(s);
+            const REAL uuh = uu_half(s, vel);
             for (int i = 0; i < s->Qt; i++) {
-                REAL ge = feq_t_ref(s, temperature, vel, i);
+                REAL ge = feq_t_ref(s, temperature, vel, uuh, i);
                 REAL g = TS[cell * s->Qt + i];
-                TT[cell * s->Qt + i] = g + (-(g - ge) / (REAL)s->d.tau_t);
+                TT[cell * s->Qt + i] = g + (ge - g) * s->Rtau_t; /* g + (-(g - geq)/tau_T) */
             }
         }
         if (save) {
@@ -623,6 +658,19 @@ orc_t* ORC(create)(const orc_desc* d, const float* rho, const float* u, const fl
     default: free(s); return NULL;
     }
     s->cs = (REAL)(1.0 / sqrt(3.0));
+    {
+        REAL cs2 = s->cs * s->cs, cs4 = cs2 * cs2;
+        REAL tau = (REAL)d->tau;
+        s->R2 = (REAL)1 / cs2;
+        s->R4 = (REAL)1 / cs4;
+        s->Rtau = (REAL)1 / tau;
+        s->P = (REAL)1 - (REAL)1 / ((REAL)2 * tau);
+        s->Rtau_t = (REAL)1 / (REAL)d->tau_t;
+        REAL taum = (REAL)d->trt_magic / (tau - (REAL)0.5) + (REAL)0.5;
+        s->Wm = (REAL)1 / taum;
+        s->Pp = (REAL)1 - s->Rtau * (REAL)0.5;
+        s->Pm = (REAL)1 - s->Wm * (REAL)0.5;
+    }
     s->N = (size_t)d->nx * d->ny * d->nz;
     const size_t N = s->N;
     s->lat0_src = 1; s->th0_src = 1; s->mp0_src = 1;
@@ -655,6 +703,8 @@ orc_t* ORC(create)(const orc_desc* d, const float* rho, const float* u, const fl
         if (id != 0 && s->objects[id * 12 + 3] != T0) s->thermal = 1;
     }
     s->forcing = !(s->constant_force && f0[0] == 0 && f0[1] == 0 && f0[2] == 0);
+    /* collide.comp:609: the source term exists with forcing, multiphase or thermal flow */
+    s->src_on = s->forcing || d->multiphase || s->thermal;
     if (s->forcing && !s->constant_force) {
         s->forces = (float*)calloc(N * 4, sizeof(float));
         for (size_t c = 0; c < N; c++) for (int k = 0; k < 3; k++) s->forces[c * 4 + k] = force[c * 3 + k];

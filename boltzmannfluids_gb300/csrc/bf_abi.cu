@@ -178,7 +178,11 @@ void fill_constants(bf_solver* s, StepParams& p) {
 // LBM::_collide (LBM.cpp:1557-1653): one launch of the fused AA step, then the swaps
 cudaError_t collide(bf_solver* s, bool save, bool update, bool reduce, bool measure) {
     StepParams p{};
-    p.f = lat_src(s);
+    {
+        char* base = static_cast<char*>(lat_src(s));
+        const size_t plane_bytes = (size_t)s->N * storage_bytes(s->desc.storage);
+        for (int i = 0; i < s->Q; i++) p.plane[i] = base + (size_t)i * plane_bytes;
+    }
     p.stride = s->N;
     p.nx = s->desc.resolution[0]; p.ny = s->desc.resolution[1]; p.nz = s->desc.resolution[2];
     p.n_cells = s->N;

@@ -154,8 +154,8 @@ enum : uint32_t {
 enum AAMode { AA_EVEN = 0, AA_ODD = 1, AA_LOCAL = 2 };
 
 struct alignas(16) StepParams {
-    void* f;                  // DDF, SoA: population i of cell n at f[i*stride + n]
-    uint64_t stride;          // elements per population plane
+    void* plane[27];          // DDF planes: population slot i of cell n at plane[i][n]
+    uint64_t stride;          // elements per population plane (thermal lattice uses the same)
     int nx, ny, nz;
     uint32_t flags;
     uint32_t n_cells;

@@ -119,22 +119,200 @@ __device__ __forceinline__ void block_reduce_store(CellSum cs, double* __restric
 }
 
 // ---------------------------------------------------------------------------
-// fused AA stream + collide
+// moments, limiter and collision shared by the fast and the generic kernels
 // ---------------------------------------------------------------------------
-template <int Q, int ST, int MODE, bool GENERIC>
+struct Moments {
+    float rho, ux, uy, uz, Fx, Fy, Fz;
+    bool out_ext;
+};
+
+// rho = sum f (clamped >= 0.01), u = j/rho (+ F/(2 rho)), velocity limiter
+// (collide.comp:702-725).  Rounded operations in the shader's order.
+template <int Q>
+__device__ __forceinline__ void velocity_and_limit(const float (&f)[Q], Moments& m, bool forced, float vlim,
+                                                   float vlim_ext) {
+    using L = Lattice<Q>;
+    float jx = 0.f, jy = 0.f, jz = 0.f;
+#pragma unroll
+    for (int i = 0; i < Q; i++) {
+        const Dir c = L::c(i);
+        if (c.x) jx = FADD(jx, c.x > 0 ? f[i] : -f[i]);
+        if (c.y) jy = FADD(jy, c.y > 0 ? f[i] : -f[i]);
+        if (c.z) jz = FADD(jz, c.z > 0 ? f[i] : -f[i]);
+    }
+    m.ux = __fdiv_rn(jx, m.rho);
+    m.uy = __fdiv_rn(jy, m.rho);
+    m.uz = __fdiv_rn(jz, m.rho);
+    if (forced) {
+        const float r2 = FMUL(2.0f, m.rho);
+        m.ux = FADD(m.ux, __fdiv_rn(m.Fx, r2));
+        m.uy = FADD(m.uy, __fdiv_rn(m.Fy, r2));
+        m.uz = FADD(m.uz, __fdiv_rn(m.Fz, r2));
+    }
+    const float len = sqrtf(dot3r(m.ux, m.uy, m.uz, m.ux, m.uy, m.uz));
+    m.out_ext = len > vlim_ext;
+    if (len > vlim) {
+        m.ux = FMUL(__fdiv_rn(m.ux, len), vlim);
+        m.uy = FMUL(__fdiv_rn(m.uy, len), vlim);
+        m.uz = FMUL(__fdiv_rn(m.uz, len), vlim);
+    }
+}
+
+template <int Q>
+__device__ __forceinline__ float density_of(const float (&f)[Q]) {
+    float rho = f[0];
+#pragma unroll
+    for (int i = 1; i < Q; i++) rho = FADD(rho, f[i]);
+    return rho;
+}
+
+// Post-collision populations, handed to emit(i, value) as soon as each is
+// known.  BGK follows collide.comp:589-629/727-745; TRT is an extension,
+// evaluated pairwise over (i, opp i) with the symmetric and antisymmetric
+// parts of the equilibrium written out directly:
+//   e+ = w rho ((1 - uu/2/cs2) + cu^2/2/cs4),  e- = w rho cu/cs2,
+//   f_i <- f_i - omega+ (f+ - e+) -+ omega- (f- - e-),
+// Guo term split into even part (1-omega+/2) w ((F.c)(u.c)/cs4 - F.u/cs2)
+// and odd part (1-omega-/2) w F.c/cs2.  With |u| above the extreme limit the
+// populations become the equilibrium (BGK: feq, TRT: e+ +- e-).
+template <int Q, class Emit>
+__device__ __forceinline__ void collide_emit(const float (&f)[Q], const Moments& m, const StepParams& p, bool trt,
+                                             bool src, bool to_equilibrium, Emit emit) {
+    using L = Lattice<Q>;
+    const float uuh = FMUL(FMUL(dot3r(m.ux, m.uy, m.uz, m.ux, m.uy, m.uz), 0.5f), p.R2);
+    const float fuR2 = FMUL(dot3r(m.Fx, m.Fy, m.Fz, m.ux, m.uy, m.uz), p.R2);
+    if (to_equilibrium || !trt) {
+#pragma unroll
+        for (int i = 0; i < Q; i++) {
+            const Dir c = L::c(i);
+            const float w = L::w(i);
+            const float cu = cdot_rt(c, m.ux, m.uy, m.uz);
+            const float fe = FMUL(FMUL(w, m.rho), eq_bracket(cu, uuh, p.R2, p.R4));
+            float v = FADD(f[i], FMUL(FSUB(fe, f[i]), p.Rtau));  // old + (-(old - feq)/tau)
+            if (src) {
+                const float fc = cdot_rt(c, m.Fx, m.Fy, m.Fz);
+                // (1-1/(2tau)) w (F.c/cs2 + ((F.c)(u.c)/cs4 - F.u/cs2))
+                v = FADD(v, FMUL(FMUL(p.P, w), FADD(FMUL(fc, p.R2), FSUB(FMUL(FMUL(fc, cu), p.R4), fuR2))));
+            }
+            emit(i, (to_equilibrium || m.out_ext) ? fe : v);
+        }
+        return;
+    }
+    const float one_m = FSUB(1.0f, uuh);
+    {
+        const float fe0 = FMUL(FMUL(L::w(0), m.rho), one_m);
+        float v = FSUB(f[0], FMUL(FSUB(f[0], fe0), p.Rtau));
+        if (src) v = FADD(v, FMUL(FMUL(p.Pp, L::w(0)), FSUB(0.0f, fuR2)));
+        emit(0, m.out_ext ? fe0 : v);
+    }
+#pragma unroll
+    for (int i = 1; i < Q; i += 2) {
+        const int j = i + 1;
+        const Dir c = L::c(i);
+        const float w = L::w(i);
+        const float cu = cdot_rt(c, m.ux, m.uy, m.uz);
+        const float wr = FMUL(w, m.rho);
+        const float ep = FMUL(wr, FADD(one_m, FMUL(FMUL(FMUL(cu, cu), 0.5f), p.R4)));
+        const float em = FMUL(wr, FMUL(cu, p.R2));
+        const float fp = FMUL(FADD(f[i], f[j]), 0.5f), fm = FMUL(FSUB(f[i], f[j]), 0.5f);
+        const float dp = FMUL(FSUB(fp, ep), p.Rtau), dm = FMUL(FSUB(fm, em), p.Wm);
+        float vi = FSUB(FSUB(f[i], dp), dm), vj = FADD(FSUB(f[j], dp), dm);
+        if (src) {
+            const float fc = cdot_rt(c, m.Fx, m.Fy, m.Fz);
+            const float Sp = FMUL(FMUL(p.Pp, w), FSUB(FMUL(FMUL(fc, cu), p.R4), fuR2));
+            const float Sm = FMUL(FMUL(p.Pm, w), FMUL(fc, p.R2));
+            vi = FADD(vi, FADD(Sp, Sm));
+            vj = FADD(vj, FSUB(Sp, Sm));
+        }
+        emit(i, m.out_ext ? FADD(ep, em) : vi);
+        emit(j, m.out_ext ? FSUB(ep, em) : vj);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// fast AA step: fully periodic box, no objects, no thermal / Shan-Chen /
+// force field (constant force allowed).  Population planes are addressed
+// through per-plane pointers and 32-bit wrap offsets.
+// ---------------------------------------------------------------------------
+constexpr int kFastMinBlocks = 4;  // 256 threads x 4 blocks: at most 64 registers
+
+template <int Q, int ST, int MODE>
+__global__ void __launch_bounds__(kStepBlock, kFastMinBlocks) fast_step_kernel(const __grid_constant__ StepParams p) {
+    using L = Lattice<Q>;
+    using C = Codec<ST>;
+    using T = typename C::T;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    CellSum cs = {0.f, 0.f, 0.f, 0.f, 0.f};
+    if (x < p.nx) {
+        const int y = blockIdx.y, z = blockIdx.z;
+        const int nx = p.nx, ny = p.ny, nz = p.nz, nxy = nx * ny;
+        const uint32_t n = (uint32_t)x + (uint32_t)nx * ((uint32_t)y + (uint32_t)ny * (uint32_t)z);
+        // element offsets to the neighbour at -1 / +1 along each axis, periodic
+        const int oxm = x == 0 ? nx - 1 : -1, oxp = x == nx - 1 ? 1 - nx : 1;
+        const int oym = y == 0 ? (ny - 1) * nx : -nx, oyp = y == ny - 1 ? (1 - ny) * nx : nx;
+        const int ozm = z == 0 ? (nz - 1) * nxy : -nxy, ozp = z == nz - 1 ? (1 - nz) * nxy : nxy;
+        auto at = [&](int dx, int dy, int dz) -> uint32_t {
+            const int o = (dx < 0 ? oxm : (dx > 0 ? oxp : 0)) + (dy < 0 ? oym : (dy > 0 ? oyp : 0)) +
+                          (dz < 0 ? ozm : (dz > 0 ? ozp : 0));
+            return n + (uint32_t)o;  // modular: the true index lies in [0, N)
+        };
+        float f[Q];
+#pragma unroll
+        for (int i = 0; i < Q; i++) {
+            const Dir c = L::c(i);
+            if (MODE == AA_EVEN) f[i] = C::dec(static_cast<const T*>(p.plane[i])[at(-c.x, -c.y, -c.z)], L::w(i));
+            else f[i] = C::dec(static_cast<const T*>(p.plane[opp(i)])[n], L::w(i));
+        }
+        Moments m;
+        m.rho = density_of<Q>(f);
+        if (!(m.rho == m.rho)) atomicOr(p.err, 1u);
+        m.rho = m.rho < 0.01f ? 0.01f : m.rho;
+        const bool forced = (p.flags & F_FORCE_CONST) != 0;
+        m.Fx = forced ? p.fconst[0] : 0.f;
+        m.Fy = forced ? p.fconst[1] : 0.f;
+        m.Fz = forced ? p.fconst[2] : 0.f;
+        velocity_and_limit<Q>(f, m, forced, p.vlim, p.vlim_ext);
+        if (p.flags & F_UPDATE) {
+            collide_emit<Q>(f, m, p, (p.flags & F_TRT) != 0, (p.flags & F_SOURCE) != 0, false,
+                            [&](int i, float v) {
+                                const Dir c = L::c(i);
+                                if (MODE == AA_EVEN)
+                                    static_cast<T*>(p.plane[opp(i)])[at(c.x, c.y, c.z)] = C::enc(v, L::w(i));
+                                else
+                                    static_cast<T*>(p.plane[i])[n] = C::enc(v, L::w(i));
+                            });
+        }
+        if (p.flags & F_SAVE) {
+            p.vel_den[n] = make_float4(m.ux, m.uy, m.uz, m.rho);
+            if (p.force_temp) p.force_temp[n] = make_float4(m.Fx, m.Fy, m.Fz, 0.f);
+        }
+        if (p.flags & F_REDUCE) {
+            const float uu = dot3r(m.ux, m.uy, m.uz, m.ux, m.uy, m.uz);
+            cs.m = m.rho; cs.px = m.rho * m.ux; cs.py = m.rho * m.uy; cs.pz = m.rho * m.uz;
+            cs.ke = 0.5f * m.rho * uu;
+        }
+    }
+    if (p.flags & F_REDUCE) block_reduce_store(cs, p.red_partials);
+}
+
+// ---------------------------------------------------------------------------
+// generic AA / two-buffer step: open boundaries, packed boundary ids, solid
+// skipping or bounce-back, equilibrium boundary cells, force fields, thermal
+// lattice, Shan-Chen pseudopotential, field saving and reductions
+// ---------------------------------------------------------------------------
+template <int Q, int ST, int MODE>
 __device__ __forceinline__ CellSum cell_update(const StepParams& p, int x, int y, int z) {
     using L = Lattice<Q>;
     using C = Codec<ST>;
     using T = typename C::T;
-    T* __restrict__ F = static_cast<T*>(p.f);
-    const uint64_t S = p.stride;
     const int nx = p.nx, ny = p.ny, nz = p.nz;
-    const uint32_t flags = GENERIC ? p.flags : (p.flags & (F_SAVE | F_UPDATE | F_TRT | F_SOURCE | F_FORCE_CONST | F_REDUCE));
+    const uint32_t flags = p.flags;
     const uint32_t n = (uint32_t)x + (uint32_t)nx * ((uint32_t)y + (uint32_t)ny * (uint32_t)z);
+    auto plane = [&](int i) -> T* { return static_cast<T*>(p.plane[i]); };
     CellSum out = {0.f, 0.f, 0.f, 0.f, 0.f};
 
     uint32_t bid = 0;
-    if (GENERIC && (flags & F_BOUNDARIES)) {
+    if (flags & F_BOUNDARIES) {
         bid = boundary_id(p.bnd, p.bits, n);
         if (solid_id(p.obj_kind, bid)) {  // collide.comp:696-700
             if (flags & F_SAVE) {
@@ -145,19 +323,7 @@ __device__ __forceinline__ CellSum cell_update(const StepParams& p, int x, int y
             return out;
         }
     }
-    const bool eqb = GENERIC && bid != 0u;  // equilibrium boundary cell (non-solid object)
-
-    // neighbour coordinates (periodic fast path: plain wrap)
-    const int xm = x == 0 ? nx - 1 : x - 1, xp = x == nx - 1 ? 0 : x + 1;
-    const int ym = y == 0 ? ny - 1 : y - 1, yp = y == ny - 1 ? 0 : y + 1;
-    const int zm = z == 0 ? nz - 1 : z - 1, zp = z == nz - 1 ? 0 : z + 1;
-    auto fast_cell = [&](int dx, int dy, int dz) -> uint32_t {
-        const int cx = dx < 0 ? xm : (dx > 0 ? xp : x);
-        const int cy = dy < 0 ? ym : (dy > 0 ? yp : y);
-        const int cz = dz < 0 ? zm : (dz > 0 ? zp : z);
-        return (uint32_t)cx + (uint32_t)nx * ((uint32_t)cy + (uint32_t)ny * (uint32_t)cz);
-    };
-
+    const bool eqb = bid != 0u;  // equilibrium boundary cell (non-solid object)
     float4 bv = make_float4(1.f, 0.f, 0.f, 0.f);
     if (eqb && p.bvals) bv = __ldg(p.bvals + n);
 
@@ -167,236 +333,135 @@ __device__ __forceinline__ CellSum cell_update(const StepParams& p, int x, int y
     for (int i = 0; i < Q; i++) {
         const Dir c = L::c(i);
         const float w = L::w(i);
-        if (!GENERIC) {
-            if (MODE == AA_EVEN) f[i] = C::dec(F[(uint64_t)i * S + fast_cell(-c.x, -c.y, -c.z)], w);
-            else f[i] = C::dec(F[(uint64_t)opp(i) * S + n], w);
-        } else {
-            int sx = x - c.x, sy = y - c.y, sz = z - c.z;
-            bool sopen;
-            coords_wrap<Q>(sx, sy, sz, nx, ny, nz, sopen, flags);
-            const uint32_t sn = sopen ? 0u : (uint32_t)sx + (uint32_t)nx * ((uint32_t)sy + (uint32_t)ny * (uint32_t)sz);
-            bool done = false;
-            if (MODE != AA_LOCAL && (eqb || (flags & F_BOUNCE_BACK)) && i != 0) {
-                if (eqb && sopen) {
-                    // population entering from outside the domain: f_eq(rho_b, u_b)
-                    const float cu = cdot_rt(c, bv.y, bv.z, bv.w);
-                    const float uuh = FMUL(FMUL(dot3r(bv.y, bv.z, bv.w, bv.y, bv.z, bv.w), 0.5f), p.R2);
-                    f[i] = FMUL(FMUL(w, bv.x), eq_bracket(cu, uuh, p.R2, p.R4));
+        int sx = x - c.x, sy = y - c.y, sz = z - c.z;
+        bool sopen;
+        coords_wrap<Q>(sx, sy, sz, nx, ny, nz, sopen, flags);
+        const uint32_t sn = sopen ? 0u : (uint32_t)sx + (uint32_t)nx * ((uint32_t)sy + (uint32_t)ny * (uint32_t)sz);
+        bool done = false;
+        if (MODE != AA_LOCAL && (eqb || (flags & F_BOUNCE_BACK)) && i != 0) {
+            if (eqb && sopen) {
+                // population entering from outside the domain: f_eq(rho_b, u_b)
+                const float cu = cdot_rt(c, bv.y, bv.z, bv.w);
+                const float uuh = FMUL(FMUL(dot3r(bv.y, bv.z, bv.w, bv.y, bv.z, bv.w), 0.5f), p.R2);
+                f[i] = FMUL(FMUL(w, bv.x), eq_bracket(cu, uuh, p.R2, p.R4));
+                done = true;
+            } else if ((flags & F_BOUNCE_BACK) && !sopen && (flags & F_BOUNDARIES)) {
+                const uint32_t sid = boundary_id(p.bnd, p.bits, sn);
+                if (solid_id(p.obj_kind, sid)) {
+                    // halfway bounce-back: the cell's own outgoing opposite
+                    // population sits in the other AA slot; moving-wall term of
+                    // stream.comp:487-496 with rho_wall = 1
+                    const float4 uw = __ldg(p.objects + 3u * sid);
+                    const Dir co = L::c(opp(i));
+                    const float wall = FMUL(FMUL(-2.f * w, co.x * uw.x + co.y * uw.y + co.z * uw.z), 3.f);
+                    const float v = (MODE == AA_EVEN) ? C::dec(plane(opp(i))[n], w) : C::dec(plane(i)[sn], w);
+                    f[i] = FADD(v, wall);
                     done = true;
-                } else if ((flags & F_BOUNCE_BACK) && !sopen && (flags & F_BOUNDARIES)) {
-                    const uint32_t sid = boundary_id(p.bnd, p.bits, sn);
-                    if (solid_id(p.obj_kind, sid)) {
-                        // halfway bounce-back: the cell's own outgoing opposite
-                        // population sits in the other AA slot
-                        const float4 uw = __ldg(p.objects + 3u * sid);
-                        const Dir co = L::c(opp(i));
-                        const float wall = __fmul_rn(__fmul_rn(-2.f * w, co.x * uw.x + co.y * uw.y + co.z * uw.z), 3.f);
-                        const float v = (MODE == AA_EVEN) ? C::dec(F[(uint64_t)opp(i) * S + n], w)
-                                                          : C::dec(F[(uint64_t)i * S + sn], w);
-                        f[i] = __fadd_rn(v, wall);
-                        done = true;
-                    }
                 }
             }
-            if (!done) {
-                if (MODE == AA_EVEN) f[i] = sopen ? 0.01f : C::dec(F[(uint64_t)i * S + sn], w);
-                else if (MODE == AA_ODD) f[i] = C::dec(F[(uint64_t)opp(i) * S + n], w);
-                else f[i] = C::dec(F[(uint64_t)i * S + n], w);
-            }
+        }
+        if (!done) {
+            if (MODE == AA_EVEN) f[i] = sopen ? 0.01f : C::dec(plane(i)[sn], w);
+            else if (MODE == AA_ODD) f[i] = C::dec(plane(opp(i))[n], w);
+            else f[i] = C::dec(plane(i)[n], w);
         }
     }
 
-    // ---- moments ----
-    float rho = f[0];
-#pragma unroll
-    for (int i = 1; i < Q; i++) rho = FADD(rho, f[i]);
-    if (GENERIC && !(rho == rho)) atomicOr(p.err, 1u);
-    rho = rho < 0.01f ? 0.01f : rho;  // max(density, 0.01), NaN kept
-    float jx = 0.f, jy = 0.f, jz = 0.f;
-#pragma unroll
-    for (int i = 0; i < Q; i++) {
-        const Dir c = L::c(i);
-        if (c.x) jx = FADD(jx, c.x > 0 ? f[i] : -f[i]);
-        if (c.y) jy = FADD(jy, c.y > 0 ? f[i] : -f[i]);
-        if (c.z) jz = FADD(jz, c.z > 0 ? f[i] : -f[i]);
-    }
-
-    // ---- forces (collide.comp:707-720) ----
-    float Fx = 0.f, Fy = 0.f, Fz = 0.f;
-    if (flags & F_FORCE_CONST) { Fx = p.fconst[0]; Fy = p.fconst[1]; Fz = p.fconst[2]; }
+    // ---- moments and forces (collide.comp:702-725) ----
+    Moments m;
+    m.rho = density_of<Q>(f);
+    if (!(m.rho == m.rho)) atomicOr(p.err, 1u);
+    m.rho = m.rho < 0.01f ? 0.01f : m.rho;  // max(density, 0.01), NaN kept
+    m.Fx = m.Fy = m.Fz = 0.f;
+    if (flags & F_FORCE_CONST) { m.Fx = p.fconst[0]; m.Fy = p.fconst[1]; m.Fz = p.fconst[2]; }
+    if (flags & F_FORCE_FIELD) { const float4 fv = __ldg(p.force + n); m.Fx = fv.x; m.Fy = fv.y; m.Fz = fv.z; }
     float temperature = 0.f;
-    if (GENERIC) {
-        if (flags & F_FORCE_FIELD) { const float4 fv = __ldg(p.force + n); Fx = fv.x; Fy = fv.y; Fz = fv.z; }
-        if (flags & F_THERMAL) {
-            constexpr int QT = L::D == 2 ? 5 : 7;
+    constexpr int QT = L::D == 2 ? 5 : 7;
+    if (flags & F_THERMAL) {
 #pragma unroll
-            for (int i = 0; i < QT; i++) temperature = FADD(temperature, __ldg(p.th_src + (uint64_t)i * S + n));
-            const float k = __fmul_rn(-p.beta, __fsub_rn(temperature, 1.0f));
-            Fx = __fadd_rn(Fx, __fmul_rn(k, Fx)); Fy = __fadd_rn(Fy, __fmul_rn(k, Fy)); Fz = __fadd_rn(Fz, __fmul_rn(k, Fz));
-        }
-        if (flags & F_MULTIPHASE) {
-            const float self_psi = FSUB(1.0f, exp_f32(-rho));
-            float sx = 0.f, sy = 0.f, sz = 0.f;
+        for (int i = 0; i < QT; i++) temperature = FADD(temperature, __ldg(p.th_src + (uint64_t)i * p.stride + n));
+        const float k = FMUL(-p.beta, FSUB(temperature, 1.0f));
+        m.Fx = FADD(m.Fx, FMUL(k, m.Fx)); m.Fy = FADD(m.Fy, FMUL(k, m.Fy)); m.Fz = FADD(m.Fz, FMUL(k, m.Fz));
+    }
+    if (flags & F_MULTIPHASE) {  // collide.comp:534-584
+        const float self_psi = FSUB(1.0f, exp_f32(-m.rho));
+        float sx = 0.f, sy = 0.f, sz = 0.f;
 #pragma unroll
-            for (int i = 1; i < Q; i++) {
-                const Dir c = L::c(i);
-                int ax = x + c.x, ay = y + c.y, az = z + c.z;
-                bool aopen;
-                coords_wrap<Q>(ax, ay, az, nx, ny, nz, aopen, flags);
-                const float ps = aopen ? self_psi
-                                       : __ldg(p.psi_src + (uint32_t)ax + (uint32_t)nx * ((uint32_t)ay + (uint32_t)ny * (uint32_t)az));
-                const float wp = __fmul_rn(L::w(i), ps);
-                if (c.x) sx = __fadd_rn(sx, c.x > 0 ? wp : -wp);
-                if (c.y) sy = __fadd_rn(sy, c.y > 0 ? wp : -wp);
-                if (c.z) sz = __fadd_rn(sz, c.z > 0 ? wp : -wp);
-            }
-            const float k = __fmul_rn(-self_psi, p.G);
-            Fx = __fadd_rn(Fx, __fmul_rn(sx, k)); Fy = __fadd_rn(Fy, __fmul_rn(sy, k)); Fz = __fadd_rn(Fz, __fmul_rn(sz, k));
+        for (int i = 1; i < Q; i++) {
+            const Dir c = L::c(i);
+            int ax = x + c.x, ay = y + c.y, az = z + c.z;
+            bool aopen;
+            coords_wrap<Q>(ax, ay, az, nx, ny, nz, aopen, flags);
+            const float ps = aopen ? self_psi
+                                   : __ldg(p.psi_src + (uint32_t)ax + (uint32_t)nx * ((uint32_t)ay + (uint32_t)ny * (uint32_t)az));
+            const float wp = FMUL(L::w(i), ps);
+            if (c.x) sx = FADD(sx, c.x > 0 ? wp : -wp);
+            if (c.y) sy = FADD(sy, c.y > 0 ? wp : -wp);
+            if (c.z) sz = FADD(sz, c.z > 0 ? wp : -wp);
         }
+        const float k = FMUL(-self_psi, p.G);
+        m.Fx = FADD(m.Fx, FMUL(sx, k)); m.Fy = FADD(m.Fy, FMUL(sy, k)); m.Fz = FADD(m.Fz, FMUL(sz, k));
     }
-
-    // ---- velocity, limiter (collide.comp:722-725) ----
-    // The moments use the shader's operation order with rounded (uncontracted)
-    // operations, so rho and u agree bit for bit with a literal FP32 restatement
-    // given the same populations; only the collision below is reassociated.
-    float ux = __fdiv_rn(jx, rho), uy = __fdiv_rn(jy, rho), uz = __fdiv_rn(jz, rho);
-    if (flags & (F_FORCE_CONST | F_FORCE_FIELD | F_THERMAL | F_MULTIPHASE)) {
-        const float r2 = __fmul_rn(2.0f, rho);
-        ux = __fadd_rn(ux, __fdiv_rn(Fx, r2));
-        uy = __fadd_rn(uy, __fdiv_rn(Fy, r2));
-        uz = __fadd_rn(uz, __fdiv_rn(Fz, r2));
-    }
-    const float len = sqrtf(__fadd_rn(__fadd_rn(__fmul_rn(ux, ux), __fmul_rn(uy, uy)), __fmul_rn(uz, uz)));
-    const bool out_ext = len > p.vlim_ext;
-    if (len > p.vlim) {
-        ux = __fmul_rn(__fdiv_rn(ux, len), p.vlim);
-        uy = __fmul_rn(__fdiv_rn(uy, len), p.vlim);
-        uz = __fmul_rn(__fdiv_rn(uz, len), p.vlim);
-    }
+    velocity_and_limit<Q>(f, m, (flags & (F_FORCE_CONST | F_FORCE_FIELD | F_THERMAL | F_MULTIPHASE)) != 0, p.vlim,
+                          p.vlim_ext);
     if (eqb) {
         const int kind = __ldg(p.obj_kind + bid);
-        if (kind == 1) { ux = bv.y; uy = bv.z; uz = bv.w; } else { rho = bv.x; }
-        Fx = Fy = Fz = 0.f;
+        if (kind == 1) { m.ux = bv.y; m.uy = bv.z; m.uz = bv.w; } else { m.rho = bv.x; }
+        m.Fx = m.Fy = m.Fz = 0.f;
     }
-    const float uu = dot3r(ux, uy, uz, ux, uy, uz);
-    const float uuh = FMUL(FMUL(uu, 0.5f), p.R2);
 
     // ---- collision + AA store (collide.comp:727-760) ----
     if (flags & F_UPDATE) {
-        const float fu = dot3r(Fx, Fy, Fz, ux, uy, uz);
-        const float fuR2 = FMUL(fu, p.R2);
-        const bool src = (flags & F_SOURCE) != 0;
-        auto feq = [&](int i) -> float {
-            return FMUL(FMUL(L::w(i), rho), eq_bracket(cdot_rt(L::c(i), ux, uy, uz), uuh, p.R2, p.R4));
-        };
-        float fn[Q];
-        if (eqb) {
-#pragma unroll
-            for (int i = 0; i < Q; i++) fn[i] = feq(i);
-        } else if (!(flags & F_TRT)) {
-#pragma unroll
-            for (int i = 0; i < Q; i++) {
-                const Dir c = L::c(i);
-                const float w = L::w(i);
-                const float fe = feq(i);
-                float v = FADD(f[i], FMUL(FSUB(fe, f[i]), p.Rtau));  // old + (-(old - feq)/tau)
-                if (src) {
-                    const float cu = cdot_rt(c, ux, uy, uz);
-                    const float fc = cdot_rt(c, Fx, Fy, Fz);
-                    // (1-1/(2tau)) w (F.c/cs2 + ((F.c)(u.c)/cs4 - F.u/cs2))
-                    v = FADD(v, FMUL(FMUL(p.P, w), FADD(FMUL(fc, p.R2), FSUB(FMUL(FMUL(fc, cu), p.R4), fuR2))));
-                }
-                fn[i] = out_ext ? fe : v;
-            }
-        } else {
-            {
-                const float fe0 = feq(0);
-                const float dp = FMUL(FSUB(f[0], fe0), p.Rtau);
-                float v = FSUB(f[0], dp);
-                if (src) v = FADD(v, FMUL(FMUL(p.Pp, L::w(0)), FSUB(0.0f, fuR2)));
-                fn[0] = out_ext ? fe0 : v;
-            }
-#pragma unroll
-            for (int i = 1; i < Q; i += 2) {
-                const int j = i + 1;
-                const Dir c = L::c(i);
-                const float w = L::w(i);
-                const float fei = feq(i), fej = feq(j);
-                const float fp = FMUL(FADD(f[i], f[j]), 0.5f), fm = FMUL(FSUB(f[i], f[j]), 0.5f);
-                const float ep = FMUL(FADD(fei, fej), 0.5f), em = FMUL(FSUB(fei, fej), 0.5f);
-                const float dp = FMUL(FSUB(fp, ep), p.Rtau), dm = FMUL(FSUB(fm, em), p.Wm);
-                float vi = FSUB(FSUB(f[i], dp), dm), vj = FADD(FSUB(f[j], dp), dm);
-                if (src) {
-                    const float cu = cdot_rt(c, ux, uy, uz);
-                    const float fc = cdot_rt(c, Fx, Fy, Fz);
-                    const float Sp = FMUL(FMUL(p.Pp, w), FSUB(FMUL(FMUL(fc, cu), p.R4), fuR2));
-                    const float Sm = FMUL(FMUL(p.Pm, w), FMUL(fc, p.R2));
-                    vi = FADD(vi, FADD(Sp, Sm));
-                    vj = FADD(vj, FSUB(Sp, Sm));
-                }
-                fn[i] = out_ext ? fei : vi;
-                fn[j] = out_ext ? fej : vj;
-            }
-        }
-#pragma unroll
-        for (int i = 0; i < Q; i++) {
+        collide_emit<Q>(f, m, p, (flags & F_TRT) != 0, (flags & F_SOURCE) != 0, eqb, [&](int i, float v) {
             const Dir c = L::c(i);
             const float w = L::w(i);
             if (MODE == AA_EVEN) {
-                if (!GENERIC) {
-                    F[(uint64_t)opp(i) * S + fast_cell(c.x, c.y, c.z)] = C::enc(fn[i], w);
-                } else {
-                    int dx = x + c.x, dy = y + c.y, dz = z + c.z;
-                    bool dopen;
-                    coords_wrap<Q>(dx, dy, dz, nx, ny, nz, dopen, flags);
-                    if (!dopen)
-                        F[(uint64_t)opp(i) * S + (uint32_t)dx + (uint32_t)nx * ((uint32_t)dy + (uint32_t)ny * (uint32_t)dz)] =
-                            C::enc(fn[i], w);
-                }
+                int dx = x + c.x, dy = y + c.y, dz = z + c.z;
+                bool dopen;
+                coords_wrap<Q>(dx, dy, dz, nx, ny, nz, dopen, flags);
+                if (!dopen)
+                    plane(opp(i))[(uint32_t)dx + (uint32_t)nx * ((uint32_t)dy + (uint32_t)ny * (uint32_t)dz)] = C::enc(v, w);
             } else {
-                F[(uint64_t)i * S + n] = C::enc(fn[i], w);
+                plane(i)[n] = C::enc(v, w);
             }
-        }
+        });
     }
 
-    if (GENERIC && (flags & F_MULTIPHASE) && !(flags & F_MEASURE)) {  // collide.comp:763-769, psi of the effective density
-        float eff = rho;
+    if ((flags & F_MULTIPHASE) && !(flags & F_MEASURE)) {  // collide.comp:763-769, psi of the effective density
+        float eff = m.rho;
         if (bid != 0u) eff = __ldg(p.objects + 3u * bid + 2u).w;
         p.psi_tgt[n] = FSUB(1.0f, exp_f32(-eff));
     }
-    if (GENERIC && (flags & F_THERMAL) && !(flags & F_MEASURE)) {  // collide.comp:771-782
-        constexpr int QT = L::D == 2 ? 5 : 7;
+    if ((flags & F_THERMAL) && !(flags & F_MEASURE)) {  // collide.comp:771-782
+        const float uuh = FMUL(FMUL(dot3r(m.ux, m.uy, m.uz, m.ux, m.uy, m.uz), 0.5f), p.R2);
 #pragma unroll
         for (int i = 0; i < QT; i++) {
             const Dir c = ThermalLattice<QT>::c(i);
             const float w = ThermalLattice<QT>::w(i);
-            const float cu = cdot_rt(c, ux, uy, uz);
+            const float cu = cdot_rt(c, m.ux, m.uy, m.uz);
             const float geq = FMUL(FMUL(w, temperature), eq_bracket(cu, uuh, p.R2, p.R4));
-            const float g = __ldg(p.th_src + (uint64_t)i * S + n);
-            p.th_tgt[(uint64_t)i * S + n] = FADD(g, FMUL(FSUB(geq, g), p.Rtau_t));  // g + (-(g - geq)/tau_T)
+            const float g = __ldg(p.th_src + (uint64_t)i * p.stride + n);
+            p.th_tgt[(uint64_t)i * p.stride + n] = FADD(g, FMUL(FSUB(geq, g), p.Rtau_t));  // g + (-(g - geq)/tau_T)
         }
     }
     if (flags & F_SAVE) {  // collide.comp:784-792
-        p.vel_den[n] = make_float4(ux, uy, uz, rho);
-        if (GENERIC) {
-            p.force_temp[n] = make_float4(Fx, Fy, Fz, temperature);
-            if (p.bnd_tex) p.bnd_tex[n] = (uint8_t)bid;
-        } else if (p.force_temp) {
-            p.force_temp[n] = make_float4(Fx, Fy, Fz, 0.f);
-        }
+        p.vel_den[n] = make_float4(m.ux, m.uy, m.uz, m.rho);
+        p.force_temp[n] = make_float4(m.Fx, m.Fy, m.Fz, temperature);
+        if (p.bnd_tex) p.bnd_tex[n] = (uint8_t)bid;
     }
     if (flags & F_REDUCE) {
-        out.m = rho; out.px = rho * ux; out.py = rho * uy; out.pz = rho * uz;
-        out.ke = 0.5f * rho * uu;
+        const float uu = dot3r(m.ux, m.uy, m.uz, m.ux, m.uy, m.uz);
+        out.m = m.rho; out.px = m.rho * m.ux; out.py = m.rho * m.uy; out.pz = m.rho * m.uz;
+        out.ke = 0.5f * m.rho * uu;
     }
     return out;
 }
 
-template <int Q, int ST, int MODE, bool GENERIC>
+template <int Q, int ST, int MODE>
 __global__ void __launch_bounds__(kStepBlock) step_kernel(const __grid_constant__ StepParams p) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     CellSum cs = {0.f, 0.f, 0.f, 0.f, 0.f};
-    if (x < p.nx) cs = cell_update<Q, ST, MODE, GENERIC>(p, x, blockIdx.y, blockIdx.z);
+    if (x < p.nx) cs = cell_update<Q, ST, MODE>(p, x, blockIdx.y, blockIdx.z);
     if (p.flags & F_REDUCE) block_reduce_store(cs, p.red_partials);
 }
 
@@ -564,12 +629,12 @@ cudaError_t launch_step_st(const StepParams& p, int mode, bool generic, cudaStre
     int block;
     dim3 grid = cell_grid(p.nx, p.ny, p.nz, block);
     if (!generic) {
-        if (mode == AA_EVEN) step_kernel<Q, ST, AA_EVEN, false><<<grid, block, 0, st>>>(p);
-        else step_kernel<Q, ST, AA_ODD, false><<<grid, block, 0, st>>>(p);
+        if (mode == AA_EVEN) fast_step_kernel<Q, ST, AA_EVEN><<<grid, block, 0, st>>>(p);
+        else fast_step_kernel<Q, ST, AA_ODD><<<grid, block, 0, st>>>(p);
     } else {
-        if (mode == AA_EVEN) step_kernel<Q, ST, AA_EVEN, true><<<grid, block, 0, st>>>(p);
-        else if (mode == AA_ODD) step_kernel<Q, ST, AA_ODD, true><<<grid, block, 0, st>>>(p);
-        else step_kernel<Q, ST, AA_LOCAL, true><<<grid, block, 0, st>>>(p);
+        if (mode == AA_EVEN) step_kernel<Q, ST, AA_EVEN><<<grid, block, 0, st>>>(p);
+        else if (mode == AA_ODD) step_kernel<Q, ST, AA_ODD><<<grid, block, 0, st>>>(p);
+        else step_kernel<Q, ST, AA_LOCAL><<<grid, block, 0, st>>>(p);
     }
     return cudaGetLastError();
 }

@@ -476,35 +476,42 @@ static void collide(orc_t* s, int save, int update) {
             if (eqb) {
                 for (int i = 0; i < Q; i++) fn[i] = fe[i];
             } else if (s->d.collision == ORC_TRT) {
-                /* TRT (extension), pairwise over (i, opp i):
-                 * f+- = (f_i +- f_opp)/2, relaxed with omega+ = 1/tau and
-                 * omega- = 1/(Lambda/(tau-1/2) + 1/2); the Guo term's even part
-                 * (F.c)(u.c)/cs4 - F.u/cs2 gets (1-omega+/2), its odd part
-                 * F.c/cs2 gets (1-omega-/2). */
+                /* TRT (extension), pairwise over (i, opp i) with the symmetric
+                 * and antisymmetric equilibrium parts written out:
+                 *   e+ = w rho ((1 - uu/2/cs2) + cu^2/2/cs4),  e- = w rho cu/cs2
+                 *   f_i <- f_i - omega+ (f+ - e+) -+ omega- (f- - e-)
+                 * omega+ = 1/tau, omega- = 1/(Lambda/(tau-1/2) + 1/2); the Guo
+                 * term's even part (F.c)(u.c)/cs4 - F.u/cs2 gets (1-omega+/2),
+                 * its odd part F.c/cs2 gets (1-omega-/2).  Above the extreme
+                 * velocity limit the populations become e+ +- e-. */
                 const REAL fu = dot3(force, vel);
+                const REAL one_m = (REAL)1 - uuh;
                 {
-                    REAL dp = (f[0] - fe[0]) * s->Rtau;
-                    REAL v = f[0] - dp;
+                    REAL fe0 = ((REAL)s->V[0].w * density) * one_m;
+                    REAL v = f[0] - (f[0] - fe0) * s->Rtau;
                     if (s->src_on) v = v + (s->Pp * (REAL)s->V[0].w) * ((REAL)0 - fu * s->R2);
-                    fn[0] = out_ext ? fe[0] : v;
+                    fn[0] = out_ext ? fe0 : v;
                 }
                 for (int i = 1; i < Q; i += 2) {
                     const int j = i + 1;
+                    REAL w = (REAL)s->V[i].w;
+                    v3 c = mk3((REAL)s->V[i].cx, (REAL)s->V[i].cy, (REAL)s->V[i].cz);
+                    REAL cu = dot3(c, vel);
+                    REAL wr = w * density;
+                    REAL ep = wr * (one_m + ((cu * cu) * (REAL)0.5) * s->R4);
+                    REAL em = wr * (cu * s->R2);
                     REAL fp = (f[i] + f[j]) * (REAL)0.5, fm = (f[i] - f[j]) * (REAL)0.5;
-                    REAL ep = (fe[i] + fe[j]) * (REAL)0.5, em = (fe[i] - fe[j]) * (REAL)0.5;
                     REAL dp = (fp - ep) * s->Rtau, dm = (fm - em) * s->Wm;
                     REAL vi = (f[i] - dp) - dm, vj = (f[j] - dp) + dm;
                     if (s->src_on) {
-                        REAL w = (REAL)s->V[i].w;
-                        v3 c = mk3((REAL)s->V[i].cx, (REAL)s->V[i].cy, (REAL)s->V[i].cz);
                         REAL fc = dot3(force, c);
-                        REAL Sp = (s->Pp * w) * ((fc * dot3(vel, c)) * s->R4 - fu * s->R2);
+                        REAL Sp = (s->Pp * w) * ((fc * cu) * s->R4 - fu * s->R2);
                         REAL Sm = (s->Pm * w) * (fc * s->R2);
                         vi = vi + (Sp + Sm);
                         vj = vj + (Sp - Sm);
                     }
-                    fn[i] = out_ext ? fe[i] : vi;
-                    fn[j] = out_ext ? fe[j] : vj;
+                    fn[i] = out_ext ? ep + em : vi;
+                    fn[j] = out_ext ? ep - em : vj;
                 }
             } else {
                 for (int i = 0; i < Q; i++) {

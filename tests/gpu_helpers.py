@@ -73,8 +73,12 @@ def rel_errors(vd, vr, mask=None):
     return e_rho, e_u
 
 
-def step_and_compare(s, o, checkpoints, rtol=RTOL, mask=None, check_temperature=False):
-    """Steps both to each checkpoint (saving fields there) and compares."""
+def step_and_compare(s, o, checkpoints, rtol=RTOL, mask=None, check_temperature=False, exact=True):
+    """Steps both to each checkpoint (saving fields there) and compares.
+
+    The bar is RTOL; with exact=True the fields must also agree bit for bit:
+    the kernels and the FP32 oracle evaluate the same canonical expression
+    tree with individually rounded operations."""
     done = 0
     worst = (0.0, 0.0)
     for k in checkpoints:
@@ -87,10 +91,15 @@ def step_and_compare(s, o, checkpoints, rtol=RTOL, mask=None, check_temperature=
         worst = (max(worst[0], e_rho), max(worst[1], e_u))
         assert e_rho <= rtol, f"step {k}: rho rel err {e_rho:.3e}"
         assert e_u <= rtol, f"step {k}: u rel err {e_u:.3e}"
+        if exact:
+            m = slice(None) if mask is None else mask
+            assert np.array_equal(vd[m], vr[m]), f"step {k}: fields within {max(e_rho, e_u):.2e} but not bit-exact"
         if check_temperature:
             m = slice(None) if mask is None else mask
             t_scale = max(float(np.abs(fr[m, 3]).max()), 1e-3)
             e_t = float(np.abs(ft[m, 3] - fr[m, 3]).max() / t_scale)
             assert e_t <= rtol, f"step {k}: T rel err {e_t:.3e}"
+            if exact:
+                assert np.array_equal(ft[m], fr[m]), f"step {k}: force/temperature not bit-exact"
     s.synchronize()
     return worst

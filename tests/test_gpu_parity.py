@@ -34,12 +34,12 @@ def test_aa_raw_lattice_after_one_and_two_steps(q):
     res = grid(q)
     rho, u = seeded_fields(res, seed=7, dims=2 if q == 9 else 3)
     s, o = make_pair(res, 0.7, VS[q], density=rho, velocity=u)
-    for k in (1, 1):
+    for k in (1, 1, 5):
         s.iterate_time(steps=k)
         o.iterate(k)
         a = s.get_populations().astype(np.float64)
         b = o.lattice()
-        assert np.abs(a - b).max() <= 2e-6 * np.abs(b).max()
+        assert np.array_equal(a, b)
 
 
 @pytest.mark.parametrize("q", [9, 19])
@@ -182,29 +182,25 @@ def test_shan_chen(q):
     n = res[0] * res[1] * res[2]
     rho = (0.69 + 0.01 * rng.uniform(-1, 1, n)).astype(np.float32)
     s, o = make_pair(res, 1.0, VS[q], density=rho, multiphase=True, G=-5.0)
-    # psi = 1 - exp(-rho) uses the platforms' expf (ulp-level differences)
-    step_and_compare(s, o, [1, 2, 20])
+    # psi = 1 - exp(-rho) uses the same hand-written exp on both sides
+    step_and_compare(s, o, [1, 2, 20, 60])
 
 
 @pytest.mark.parametrize("storage", [1, 2, 3])
-def test_16bit_storage_one_step_matches_emulation(storage):
-    """One step with 16-bit storage: the oracle emulates the same codec
-    (IEEE half RNE, or the custom 1-4-11 format); a one-ulp FP32 difference
-    may move a value across a 16-bit rounding boundary, so the bar is a few
-    16-bit units on the decoded populations."""
+def test_16bit_storage_matches_emulation(storage):
+    """16-bit storage: the oracle emulates the same codecs (IEEE half RNE of
+    f or of f - w, and the custom c16 format of (f - w)/w); with FP32
+    arithmetic identical on both sides the stored lattices agree bit for bit."""
     res = (20, 14, 12)
     rho, u = seeded_fields(res, seed=31)
     s, o = make_pair(res, 0.6, 4, density=rho, velocity=u, storage=storage)
     a0 = s.get_populations().astype(np.float64)
     b0 = o.lattice()
-    assert np.array_equal(a0.astype(np.float32), b0.astype(np.float32))  # identical encoding of the init
-    s.iterate_time(steps=1)
-    o.iterate(1)
-    a = s.get_populations().astype(np.float64)
-    b = o.lattice()
-    unit = 2.0 ** -11 * np.maximum(np.abs(b - (0 if storage == 1 else 0)), 1e-4)
-    assert np.mean(a == b) > 0.99
-    assert np.all(np.abs(a - b) <= 2 * unit)
+    assert np.array_equal(a0, b0)  # identical encoding of the initial state
+    for k in (1, 1, 10):
+        s.iterate_time(steps=k)
+        o.iterate(k)
+        assert np.array_equal(s.get_populations().astype(np.float64), o.lattice())
 
 
 def test_equilibrium_boundaries_inlet_outlet():

@@ -154,6 +154,17 @@ uint32_t base_flags(bf_solver* s) {
     return fl;
 }
 
+// Largest float y with sqrtf(y) <= lim (IEEE sqrt is monotone), so that
+// "uu > y" decides exactly as "sqrtf(uu) > lim" (collide.comp:723-724).
+float sqrt_threshold(float lim) {
+    if (!(lim >= 0.0f)) return -1.0f;  // negative or NaN limit: every cell is limited
+    if (std::isinf(lim)) return INFINITY;
+    float y = lim * lim;
+    while (std::sqrt(y) <= lim && std::isfinite(y)) y = std::nextafter(y, INFINITY);
+    while (std::sqrt(y) > lim) y = std::nextafter(y, -INFINITY);
+    return y;
+}
+
 void fill_constants(bf_solver* s, StepParams& p) {
     // the reference's FP32 constants: cs = float(1/sqrt(3)) (LBM.cpp:1587)
     const float cs = (float)(1.0 / std::sqrt(3.0));
@@ -161,6 +172,8 @@ void fill_constants(bf_solver* s, StepParams& p) {
     const float tau = s->desc.relaxation_time;
     p.R2 = 1.0f / cs2;
     p.R4 = 1.0f / cs4;
+    p.R2h = p.R2 * 0.5f;
+    p.R4h = p.R4 * 0.5f;
     p.Rtau = 1.0f / tau;
     p.P = 1.0f - 1.0f / (2.0f * tau);
     const float tau_minus = s->desc.trt_magic / (tau - 0.5f) + 0.5f;
@@ -169,6 +182,8 @@ void fill_constants(bf_solver* s, StepParams& p) {
     p.Pm = 1.0f - p.Wm * 0.5f;
     p.vlim = s->desc.velocity_limit;
     p.vlim_ext = s->desc.velocity_limit_extreme;
+    p.t_lim = sqrt_threshold(p.vlim);
+    p.t_ext = sqrt_threshold(p.vlim_ext);
     p.fconst[0] = s->fconst[0]; p.fconst[1] = s->fconst[1]; p.fconst[2] = s->fconst[2];
     p.Rtau_t = 1.0f / s->desc.thermal_relaxation_time;
     p.beta = s->desc.thermal_expansion_coefficient;

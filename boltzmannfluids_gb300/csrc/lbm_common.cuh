@@ -164,11 +164,13 @@ struct alignas(16) StepParams {
     // does: cs = float(1/sqrt(3)), cs2 = cs*cs, cs4 = cs2*cs2
     float R2;                 // 1/cs2
     float R4;                 // 1/cs4
+    float R2h, R4h;           // R2/2, R4/2 (exact halvings)
     float Rtau;               // 1/tau (= TRT omega+)
     float P;                  // 1 - 1/(2 tau), Guo prefactor
     float Wm;                 // TRT omega- = 1/(Lambda/(tau-1/2) + 1/2)
     float Pp, Pm;             // TRT Guo prefactors 1 - omega+/2, 1 - omega-/2
     float vlim, vlim_ext;
+    float t_lim, t_ext;       // largest |u|^2 whose IEEE sqrt does not exceed vlim / vlim_ext
     float fconst[3];
     const float4* force;      // per-cell force field (reference vec4 layout)
     const uint32_t* bnd;      // packed boundary ids

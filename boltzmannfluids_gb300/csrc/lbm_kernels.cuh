@@ -19,9 +19,12 @@ namespace bf {
 struct CellSum { float m, px, py, pz, ke; };
 
 // Rounded, never-contracted FP32 operations: the kernels evaluate the same
-// expression tree as the oracle's canonical FP32 restatement (the shader's
-// operation order, divisions by launch uniforms as multiplications by their
-// once-rounded reciprocals), so FP32 results agree bit for bit.
+// expression tree as the oracle's canonical FP32 restatement, so FP32
+// results agree bit for bit.  That tree: divisions by launch uniforms become
+// multiplications by once-rounded reciprocals (a /2 folds in exactly),
+// u = j * (1/rho) with one IEEE division, opposite populations are summed
+// pairwise (s = f_i + f_opp, d = f_i - f_opp), and the multiply-adds marked
+// FFMA are single-rounding fused operations (C's fmaf on the host side).
 #define FMUL __fmul_rn
 #define FADD __fadd_rn
 #define FSUB __fsub_rn
@@ -65,12 +68,14 @@ __device__ __forceinline__ float cdot_rt(const Dir c, float vx, float vy, float 
     if (c.z != 0) { const float t = c.z > 0 ? vz : -vz; acc = first ? t : FADD(acc, t); first = false; }
     return acc;
 }
-__device__ __forceinline__ float dot3r(float ax, float ay, float az, float bx, float by, float bz) {
-    return FADD(FADD(FMUL(ax, bx), FMUL(ay, by)), FMUL(az, bz));
+#define FFMA __fmaf_rn
+// u.u = fma(uz, uz, fma(uy, uy, ux*ux))
+__device__ __forceinline__ float uu_of(float ux, float uy, float uz) {
+    return FFMA(uz, uz, FFMA(uy, uy, FMUL(ux, ux)));
 }
-// (1 + cu/cs2 + cu^2/2/cs4 - uu/2/cs2) with uuh = (uu*0.5)/cs2 precomputed
-__device__ __forceinline__ float eq_bracket(float cu, float uuh, float R2, float R4) {
-    return FSUB(FADD(FADD(1.0f, FMUL(cu, R2)), FMUL(FMUL(FMUL(cu, cu), 0.5f), R4)), uuh);
+// (1 + cu/cs2 + cu^2/2/cs4 - uu/2/cs2) = fma(cu^2, R4/2, fma(cu, R2, 1 - uu R2/2))
+__device__ __forceinline__ float bracket(float cu, float one_m, float R2, float R4h) {
+    return FFMA(FMUL(cu, cu), R4h, FFMA(cu, R2, one_m));
 }
 
 template <int Q>
@@ -126,83 +131,98 @@ struct Moments {
     bool out_ext;
 };
 
-// rho = sum f (clamped >= 0.01), u = j/rho (+ F/(2 rho)), velocity limiter
-// (collide.comp:702-725).  Rounded operations in the shader's order.
+// s_k = f_i + f_opp, d_k = f_i - f_opp for the pair (i, i+1), i = 2k+1
 template <int Q>
-__device__ __forceinline__ void velocity_and_limit(const float (&f)[Q], Moments& m, bool forced, float vlim,
-                                                   float vlim_ext) {
-    using L = Lattice<Q>;
-    float jx = 0.f, jy = 0.f, jz = 0.f;
-#pragma unroll
-    for (int i = 0; i < Q; i++) {
-        const Dir c = L::c(i);
-        if (c.x) jx = FADD(jx, c.x > 0 ? f[i] : -f[i]);
-        if (c.y) jy = FADD(jy, c.y > 0 ? f[i] : -f[i]);
-        if (c.z) jz = FADD(jz, c.z > 0 ? f[i] : -f[i]);
-    }
-    m.ux = __fdiv_rn(jx, m.rho);
-    m.uy = __fdiv_rn(jy, m.rho);
-    m.uz = __fdiv_rn(jz, m.rho);
-    if (forced) {
-        const float r2 = FMUL(2.0f, m.rho);
-        m.ux = FADD(m.ux, __fdiv_rn(m.Fx, r2));
-        m.uy = FADD(m.uy, __fdiv_rn(m.Fy, r2));
-        m.uz = FADD(m.uz, __fdiv_rn(m.Fz, r2));
-    }
-    const float len = sqrtf(dot3r(m.ux, m.uy, m.uz, m.ux, m.uy, m.uz));
-    m.out_ext = len > vlim_ext;
-    if (len > vlim) {
-        m.ux = FMUL(__fdiv_rn(m.ux, len), vlim);
-        m.uy = FMUL(__fdiv_rn(m.uy, len), vlim);
-        m.uz = FMUL(__fdiv_rn(m.uz, len), vlim);
-    }
-}
+__device__ __forceinline__ float pair_sum(const float (&f)[Q], int i) { return FADD(f[i], f[i + 1]); }
+template <int Q>
+__device__ __forceinline__ float pair_diff(const float (&f)[Q], int i) { return FSUB(f[i], f[i + 1]); }
 
+// rho = f_0 + s_1 + s_2 + ...  (collide.comp:383-388, pairwise order)
 template <int Q>
 __device__ __forceinline__ float density_of(const float (&f)[Q]) {
     float rho = f[0];
 #pragma unroll
-    for (int i = 1; i < Q; i++) rho = FADD(rho, f[i]);
+    for (int i = 1; i < Q; i += 2) rho = FADD(rho, pair_sum<Q>(f, i));
     return rho;
 }
 
+// u = j/rho (+ F/(2 rho)) and the velocity limiter (collide.comp:722-725):
+// j from the pair differences, r = 1/rho once, u = j r, u = fma(F, r/2, u).
+// |u| > limit is tested on |u|^2 against thresholds t = the largest float
+// whose IEEE square root does not exceed the limit, which decides exactly as
+// sqrt(|u|^2) > limit does; the square root is taken only for limited cells.
+template <int Q>
+__device__ __forceinline__ void velocity_and_limit(const float (&f)[Q], Moments& m, bool forced, float vlim,
+                                                   float t_lim, float t_ext) {
+    using L = Lattice<Q>;
+    float jx = 0.f, jy = 0.f, jz = 0.f;
+    bool fx = true, fy = true, fz = true;
+#pragma unroll
+    for (int i = 1; i < Q; i += 2) {
+        const Dir c = L::c(i);
+        const float d = pair_diff<Q>(f, i);
+        if (c.x) { const float t = c.x > 0 ? d : -d; jx = fx ? t : FADD(jx, t); fx = false; }
+        if (c.y) { const float t = c.y > 0 ? d : -d; jy = fy ? t : FADD(jy, t); fy = false; }
+        if (c.z) { const float t = c.z > 0 ? d : -d; jz = fz ? t : FADD(jz, t); fz = false; }
+    }
+    const float r = __fdiv_rn(1.0f, m.rho);
+    m.ux = FMUL(jx, r);
+    m.uy = FMUL(jy, r);
+    m.uz = FMUL(jz, r);
+    if (forced) {
+        const float h = FMUL(r, 0.5f);
+        m.ux = FFMA(m.Fx, h, m.ux);
+        m.uy = FFMA(m.Fy, h, m.uy);
+        m.uz = FFMA(m.Fz, h, m.uz);
+    }
+    const float uu = uu_of(m.ux, m.uy, m.uz);
+    m.out_ext = uu > t_ext;
+    if (uu > t_lim) {  // normalize(u) * limit
+        const float q = __fdiv_rn(vlim, sqrtf(uu));
+        m.ux = FMUL(m.ux, q);
+        m.uy = FMUL(m.uy, q);
+        m.uz = FMUL(m.uz, q);
+    }
+}
+
 // Post-collision populations, handed to emit(i, value) as soon as each is
-// known.  BGK follows collide.comp:589-629/727-745; TRT is an extension,
-// evaluated pairwise over (i, opp i) with the symmetric and antisymmetric
-// parts of the equilibrium written out directly:
-//   e+ = w rho ((1 - uu/2/cs2) + cu^2/2/cs4),  e- = w rho cu/cs2,
-//   f_i <- f_i - omega+ (f+ - e+) -+ omega- (f- - e-),
-// Guo term split into even part (1-omega+/2) w ((F.c)(u.c)/cs4 - F.u/cs2)
-// and odd part (1-omega-/2) w F.c/cs2.  With |u| above the extreme limit the
+// known.  BGK follows collide.comp:589-629/727-745:
+//   feq = (w rho) bracket(cu),  f <- fma(feq - f, 1/tau, f)
+//   + fma(P w, fma(F.c, R2, fma((F.c) cu, R4, -(F.u) R2)), .)   [Guo]
+// TRT is an extension, evaluated over the pair (i, opp i):
+//   e+ = (w rho) fma(cu^2, R4/2, 1 - uu R2/2),  e- = (w rho R2) cu
+//   P = fma(f_i + f_opp, 1/2, -e+),  M = fma(f_i - f_opp, 1/2, -e-)
+//   f_i <- fma(-M, omega-, fma(-P, omega+, f_i)),  f_opp <- fma(M, omega-, fma(-P, omega+, f_opp))
+// with the Guo term split into its even part (1-omega+/2) w ((F.c)(u.c)/cs4 - F.u/cs2)
+// and odd part (1-omega-/2) w F.c/cs2.  Above the extreme velocity limit the
 // populations become the equilibrium (BGK: feq, TRT: e+ +- e-).
 template <int Q, class Emit>
 __device__ __forceinline__ void collide_emit(const float (&f)[Q], const Moments& m, const StepParams& p, bool trt,
                                              bool src, bool to_equilibrium, Emit emit) {
     using L = Lattice<Q>;
-    const float uuh = FMUL(FMUL(dot3r(m.ux, m.uy, m.uz, m.ux, m.uy, m.uz), 0.5f), p.R2);
-    const float fuR2 = FMUL(dot3r(m.Fx, m.Fy, m.Fz, m.ux, m.uy, m.uz), p.R2);
+    const float one_m = FSUB(1.0f, FMUL(uu_of(m.ux, m.uy, m.uz), p.R2h));
+    const float fuR2 = FMUL(FFMA(m.Fz, m.uz, FFMA(m.Fy, m.uy, FMUL(m.Fx, m.ux))), p.R2);
     if (to_equilibrium || !trt) {
 #pragma unroll
         for (int i = 0; i < Q; i++) {
             const Dir c = L::c(i);
             const float w = L::w(i);
             const float cu = cdot_rt(c, m.ux, m.uy, m.uz);
-            const float fe = FMUL(FMUL(w, m.rho), eq_bracket(cu, uuh, p.R2, p.R4));
-            float v = FADD(f[i], FMUL(FSUB(fe, f[i]), p.Rtau));  // old + (-(old - feq)/tau)
+            const float fe = FMUL(FMUL(w, m.rho), bracket(cu, one_m, p.R2, p.R4h));
+            float v = FFMA(FSUB(fe, f[i]), p.Rtau, f[i]);  // old + (-(old - feq)/tau)
             if (src) {
                 const float fc = cdot_rt(c, m.Fx, m.Fy, m.Fz);
-                // (1-1/(2tau)) w (F.c/cs2 + ((F.c)(u.c)/cs4 - F.u/cs2))
-                v = FADD(v, FMUL(FMUL(p.P, w), FADD(FMUL(fc, p.R2), FSUB(FMUL(FMUL(fc, cu), p.R4), fuR2))));
+                v = FFMA(FMUL(p.P, w), FFMA(fc, p.R2, FFMA(FMUL(fc, cu), p.R4, -fuR2)), v);
             }
             emit(i, (to_equilibrium || m.out_ext) ? fe : v);
         }
         return;
     }
-    const float one_m = FSUB(1.0f, uuh);
     {
-        const float fe0 = FMUL(FMUL(L::w(0), m.rho), one_m);
-        float v = FSUB(f[0], FMUL(FSUB(f[0], fe0), p.Rtau));
-        if (src) v = FADD(v, FMUL(FMUL(p.Pp, L::w(0)), FSUB(0.0f, fuR2)));
+        const float w0 = L::w(0);
+        const float fe0 = FMUL(FMUL(w0, m.rho), one_m);
+        float v = FFMA(FSUB(fe0, f[0]), p.Rtau, f[0]);
+        if (src) v = FFMA(FMUL(p.Pp, w0), -fuR2, v);
         emit(0, m.out_ext ? fe0 : v);
     }
 #pragma unroll
@@ -212,14 +232,15 @@ __device__ __forceinline__ void collide_emit(const float (&f)[Q], const Moments&
         const float w = L::w(i);
         const float cu = cdot_rt(c, m.ux, m.uy, m.uz);
         const float wr = FMUL(w, m.rho);
-        const float ep = FMUL(wr, FADD(one_m, FMUL(FMUL(FMUL(cu, cu), 0.5f), p.R4)));
-        const float em = FMUL(wr, FMUL(cu, p.R2));
-        const float fp = FMUL(FADD(f[i], f[j]), 0.5f), fm = FMUL(FSUB(f[i], f[j]), 0.5f);
-        const float dp = FMUL(FSUB(fp, ep), p.Rtau), dm = FMUL(FSUB(fm, em), p.Wm);
-        float vi = FSUB(FSUB(f[i], dp), dm), vj = FADD(FSUB(f[j], dp), dm);
+        const float ep = FMUL(wr, FFMA(FMUL(cu, cu), p.R4h, one_m));
+        const float em = FMUL(FMUL(wr, p.R2), cu);
+        const float Pd = FFMA(pair_sum<Q>(f, i), 0.5f, -ep);
+        const float Md = FFMA(pair_diff<Q>(f, i), 0.5f, -em);
+        float vi = FFMA(-Md, p.Wm, FFMA(-Pd, p.Rtau, f[i]));
+        float vj = FFMA(Md, p.Wm, FFMA(-Pd, p.Rtau, f[j]));
         if (src) {
             const float fc = cdot_rt(c, m.Fx, m.Fy, m.Fz);
-            const float Sp = FMUL(FMUL(p.Pp, w), FSUB(FMUL(FMUL(fc, cu), p.R4), fuR2));
+            const float Sp = FMUL(FMUL(p.Pp, w), FFMA(FMUL(fc, cu), p.R4, -fuR2));
             const float Sm = FMUL(FMUL(p.Pm, w), FMUL(fc, p.R2));
             vi = FADD(vi, FADD(Sp, Sm));
             vj = FADD(vj, FSUB(Sp, Sm));
@@ -271,7 +292,7 @@ __global__ void __launch_bounds__(kStepBlock, kFastMinBlocks) fast_step_kernel(c
         m.Fx = forced ? p.fconst[0] : 0.f;
         m.Fy = forced ? p.fconst[1] : 0.f;
         m.Fz = forced ? p.fconst[2] : 0.f;
-        velocity_and_limit<Q>(f, m, forced, p.vlim, p.vlim_ext);
+        velocity_and_limit<Q>(f, m, forced, p.vlim, p.t_lim, p.t_ext);
         if (p.flags & F_UPDATE) {
             collide_emit<Q>(f, m, p, (p.flags & F_TRT) != 0, (p.flags & F_SOURCE) != 0, false,
                             [&](int i, float v) {
@@ -287,7 +308,7 @@ __global__ void __launch_bounds__(kStepBlock, kFastMinBlocks) fast_step_kernel(c
             if (p.force_temp) p.force_temp[n] = make_float4(m.Fx, m.Fy, m.Fz, 0.f);
         }
         if (p.flags & F_REDUCE) {
-            const float uu = dot3r(m.ux, m.uy, m.uz, m.ux, m.uy, m.uz);
+            const float uu = uu_of(m.ux, m.uy, m.uz);
             cs.m = m.rho; cs.px = m.rho * m.ux; cs.py = m.rho * m.uy; cs.pz = m.rho * m.uz;
             cs.ke = 0.5f * m.rho * uu;
         }
@@ -342,8 +363,8 @@ __device__ __forceinline__ CellSum cell_update(const StepParams& p, int x, int y
             if (eqb && sopen) {
                 // population entering from outside the domain: f_eq(rho_b, u_b)
                 const float cu = cdot_rt(c, bv.y, bv.z, bv.w);
-                const float uuh = FMUL(FMUL(dot3r(bv.y, bv.z, bv.w, bv.y, bv.z, bv.w), 0.5f), p.R2);
-                f[i] = FMUL(FMUL(w, bv.x), eq_bracket(cu, uuh, p.R2, p.R4));
+                const float one_mb = FSUB(1.0f, FMUL(uu_of(bv.y, bv.z, bv.w), p.R2h));
+                f[i] = FMUL(FMUL(w, bv.x), bracket(cu, one_mb, p.R2, p.R4h));
                 done = true;
             } else if ((flags & F_BOUNCE_BACK) && !sopen && (flags & F_BOUNDARIES)) {
                 const uint32_t sid = boundary_id(p.bnd, p.bits, sn);
@@ -381,7 +402,7 @@ __device__ __forceinline__ CellSum cell_update(const StepParams& p, int x, int y
 #pragma unroll
         for (int i = 0; i < QT; i++) temperature = FADD(temperature, __ldg(p.th_src + (uint64_t)i * p.stride + n));
         const float k = FMUL(-p.beta, FSUB(temperature, 1.0f));
-        m.Fx = FADD(m.Fx, FMUL(k, m.Fx)); m.Fy = FADD(m.Fy, FMUL(k, m.Fy)); m.Fz = FADD(m.Fz, FMUL(k, m.Fz));
+        m.Fx = FFMA(k, m.Fx, m.Fx); m.Fy = FFMA(k, m.Fy, m.Fy); m.Fz = FFMA(k, m.Fz, m.Fz);
     }
     if (flags & F_MULTIPHASE) {  // collide.comp:534-584
         const float self_psi = FSUB(1.0f, exp_f32(-m.rho));
@@ -400,10 +421,10 @@ __device__ __forceinline__ CellSum cell_update(const StepParams& p, int x, int y
             if (c.z) sz = FADD(sz, c.z > 0 ? wp : -wp);
         }
         const float k = FMUL(-self_psi, p.G);
-        m.Fx = FADD(m.Fx, FMUL(sx, k)); m.Fy = FADD(m.Fy, FMUL(sy, k)); m.Fz = FADD(m.Fz, FMUL(sz, k));
+        m.Fx = FFMA(sx, k, m.Fx); m.Fy = FFMA(sy, k, m.Fy); m.Fz = FFMA(sz, k, m.Fz);
     }
     velocity_and_limit<Q>(f, m, (flags & (F_FORCE_CONST | F_FORCE_FIELD | F_THERMAL | F_MULTIPHASE)) != 0, p.vlim,
-                          p.vlim_ext);
+                          p.t_lim, p.t_ext);
     if (eqb) {
         const int kind = __ldg(p.obj_kind + bid);
         if (kind == 1) { m.ux = bv.y; m.uy = bv.z; m.uz = bv.w; } else { m.rho = bv.x; }
@@ -433,15 +454,15 @@ __device__ __forceinline__ CellSum cell_update(const StepParams& p, int x, int y
         p.psi_tgt[n] = FSUB(1.0f, exp_f32(-eff));
     }
     if ((flags & F_THERMAL) && !(flags & F_MEASURE)) {  // collide.comp:771-782
-        const float uuh = FMUL(FMUL(dot3r(m.ux, m.uy, m.uz, m.ux, m.uy, m.uz), 0.5f), p.R2);
+        const float one_m = FSUB(1.0f, FMUL(uu_of(m.ux, m.uy, m.uz), p.R2h));
 #pragma unroll
         for (int i = 0; i < QT; i++) {
             const Dir c = ThermalLattice<QT>::c(i);
             const float w = ThermalLattice<QT>::w(i);
             const float cu = cdot_rt(c, m.ux, m.uy, m.uz);
-            const float geq = FMUL(FMUL(w, temperature), eq_bracket(cu, uuh, p.R2, p.R4));
+            const float geq = FMUL(FMUL(w, temperature), bracket(cu, one_m, p.R2, p.R4h));
             const float g = __ldg(p.th_src + (uint64_t)i * p.stride + n);
-            p.th_tgt[(uint64_t)i * p.stride + n] = FADD(g, FMUL(FSUB(geq, g), p.Rtau_t));  // g + (-(g - geq)/tau_T)
+            p.th_tgt[(uint64_t)i * p.stride + n] = FFMA(FSUB(geq, g), p.Rtau_t, g);  // g + (-(g - geq)/tau_T)
         }
     }
     if (flags & F_SAVE) {  // collide.comp:784-792
@@ -450,7 +471,7 @@ __device__ __forceinline__ CellSum cell_update(const StepParams& p, int x, int y
         if (p.bnd_tex) p.bnd_tex[n] = (uint8_t)bid;
     }
     if (flags & F_REDUCE) {
-        const float uu = dot3r(m.ux, m.uy, m.uz, m.ux, m.uy, m.uz);
+        const float uu = uu_of(m.ux, m.uy, m.uz);
         out.m = m.rho; out.px = m.rho * m.ux; out.py = m.rho * m.uy; out.pz = m.rho * m.uz;
         out.ke = 0.5f * m.rho * uu;
     }

@@ -161,7 +161,8 @@ typedef struct {
     /* launch constants, computed once per launch as the host does:
      * divisions by these uniforms are evaluated as multiplications by their
      * correctly rounded reciprocals (see the canonical-order note below). */
-    REAL R2, R4, Rtau, P, Rtau_t, Wm, Pp, Pm;
+    REAL R2, R4, R2h, R4h, Rtau, P, Rtau_t, Wm, Pp, Pm;
+    int forced; /* force term in u: forcing, thermal or multiphase */
     REAL* lat[2];
     int lat0_src;
     uint32_t* boundries;
@@ -271,38 +272,29 @@ static int aa_write_addr(orc_t* s, int x, int y, int z, int i, int odd, size_t* 
 /* physics (collide.comp:512-629, :634-673)                                  */
 /* ------------------------------------------------------------------------ */
 /*
- * Canonical FP32 evaluation.  The shader's divisions by launch uniforms
- * (x/cs^2, x/cs^4, x/tau) are taken as x * (1/uniform) with the reciprocal
- * rounded once per launch -- what a GL driver does with a division by a
- * uniform -- and every other operation is rounded separately in the order
- * the GLSL source writes it (no FMA contraction; /2 is the exact *0.5).
- * Divisions by per-cell values (rho, |u|) stay IEEE divisions.  The CUDA
- * kernels evaluate the same expression tree, so FP32 results agree bit for
- * bit given the same inputs.
+ * Canonical FP32 evaluation, shared bit for bit with the CUDA kernels.
+ * The reference's formulas (collide.comp:589-629, :634-651, :722-745) are
+ * evaluated in one fixed order: divisions by launch uniforms (cs^2, cs^4,
+ * tau) become multiplications by their once-rounded reciprocals (/2 folds
+ * into them exactly), u = j * (1/rho) with one IEEE division, and the sums
+ * marked FMA below are single-rounding fused multiply-adds.  Everything else
+ * is one rounded operation at a time (the file is compiled without FMA
+ * contraction).  GLSL leaves both reassociation and contraction to the
+ * driver, so this is one admissible evaluation of the same expressions.
  */
-static REAL eq_bracket(const orc_t* s, REAL cu, REAL uuh) { /* (1 + cu/cs2 + cu^2/2/cs4 - uu/2/cs2) */
-    REAL cu2 = cu * cu;                 /* pow(ci_dot_u, 2) taken as x*x (GLSL pow(x<0,y) is undefined) */
-    return (((REAL)1 + cu * s->R2) + (cu2 * (REAL)0.5) * s->R4) - uuh;
+#define FMA(a, b, c) (IS_F32 ? (REAL)fmaf((float)(a), (float)(b), (float)(c)) : (REAL)fma((double)(a), (double)(b), (double)(c)))
+/* u.u = fma(uz, uz, fma(uy, uy, ux*ux)) */
+static REAL uu_of(v3 u) { return FMA(u.z, u.z, FMA(u.y, u.y, u.x * u.x)); }
+/* c . v for c in {-1,0,1}^3: the nonzero terms summed in x, y, z order */
+static REAL cdot(int cx, int cy, int cz, v3 v) {
+    REAL acc = 0; int first = 1;
+    if (cx) { acc = cx > 0 ? v.x : -v.x; first = 0; }
+    if (cy) { REAL t = cy > 0 ? v.y : -v.y; acc = first ? t : acc + t; first = 0; }
+    if (cz) { REAL t = cz > 0 ? v.z : -v.z; acc = first ? t : acc + t; first = 0; }
+    return acc;
 }
-static REAL uu_half(const orc_t* s, v3 u) { return (dot3(u, u) * (REAL)0.5) * s->R2; }
-static REAL feq_ref(const orc_t* s, REAL rho, v3 u, REAL uuh, int i) { /* collide.comp:589-606 */
-    REAL w = (REAL)s->V[i].w;
-    v3 c = mk3((REAL)s->V[i].cx, (REAL)s->V[i].cy, (REAL)s->V[i].cz);
-    return (w * rho) * eq_bracket(s, dot3(c, u), uuh);
-}
-static REAL feq_t_ref(const orc_t* s, REAL T, v3 u, REAL uuh, int i) { /* collide.comp:634-651 */
-    REAL w = (REAL)s->Vt[i].w;
-    v3 c = mk3((REAL)s->Vt[i].cx, (REAL)s->Vt[i].cy, (REAL)s->Vt[i].cz);
-    return (w * T) * eq_bracket(s, dot3(c, u), uuh);
-}
-/* Guo source term (collide.comp:608-625):
- * (1-dt/(2tau)) * w * (F.c/cs2 + ((F.c)(u.c)/cs4 - F.u/cs2)) */
-static REAL source_ref(const orc_t* s, int i, v3 F, v3 u) {
-    REAL w = (REAL)s->V[i].w;
-    v3 c = mk3((REAL)s->V[i].cx, (REAL)s->V[i].cy, (REAL)s->V[i].cz);
-    REAL fc = dot3(F, c);
-    return (s->P * w) * (fc * s->R2 + ((fc * dot3(u, c)) * s->R4 - dot3(F, u) * s->R2));
-}
+/* (1 + cu/cs2 + cu^2/2/cs4 - uu/2/cs2) = fma(cu^2, R4/2, fma(cu, R2, 1 - uu R2/2)) */
+static REAL bracket(const orc_t* s, REAL cu, REAL one_m) { return FMA(cu * cu, s->R4h, FMA(cu, s->R2, one_m)); }
 static REAL feq_init(const orc_t* s, REAL rho, v3 u, int i) { /* set_equilibrium_populations.comp:179-196 */
     REAL w = (REAL)s->V[i].w;
     v3 c = mk3((REAL)s->V[i].cx, (REAL)s->V[i].cy, (REAL)s->V[i].cz);
@@ -345,24 +337,22 @@ static REAL psi(REAL rho) { /* collide.comp:512-516, rho0 = 1 */
     return rho0 * ((REAL)1 - (IS_F32 ? (REAL)exp_f32((float)(-rho / rho0)) : (REAL)exp((double)(-rho / rho0))));
 }
 
-/* Shan-Chen interaction force (collide.comp:534-584) */
-static v3 sc_force(orc_t* s, int x, int y, int z, REAL self_density) {
-    REAL self_psi = psi(self_density);
-    REAL G = (REAL)s->d.G;
+/* Shan-Chen interaction force sum (collide.comp:534-584): acc = sum over
+ * i >= 1 of w_i psi(rho(x + c_i)) c_i, the nonzero terms added in order; the
+ * caller multiplies by -psi(rho_self) G.  Out-of-domain neighbours use rho_self. */
+static v3 sc_force_acc(orc_t* s, int x, int y, int z, REAL self_density) {
     v3 f = mk3(0, 0, 0);
+    int fx = 1, fy = 1, fz = 1;
     REAL* src = MSRC(s);
     for (int i = 1; i < s->Q; i++) {
         int nx = x + s->V[i].cx, ny = y + s->V[i].cy, nz = z + s->V[i].cz;
         int open = wrap(s, &nx, &ny, &nz);
-        REAL nd = open ? self_density : src[cid(s, nx, ny, nz)];
-        REAL p = psi(nd);
-        REAL w = (REAL)s->V[i].w;
-        f.x += w * p * (REAL)s->V[i].cx;
-        f.y += w * p * (REAL)s->V[i].cy;
-        f.z += w * p * (REAL)s->V[i].cz;
+        REAL p = open ? psi(self_density) : src[cid(s, nx, ny, nz)];
+        REAL wp = (REAL)s->V[i].w * p;
+        if (s->V[i].cx) { REAL t = s->V[i].cx > 0 ? wp : -wp; f.x = fx ? t : f.x + t; fx = 0; }
+        if (s->V[i].cy) { REAL t = s->V[i].cy > 0 ? wp : -wp; f.y = fy ? t : f.y + t; fy = 0; }
+        if (s->V[i].cz) { REAL t = s->V[i].cz > 0 ? wp : -wp; f.z = fz ? t : f.z + t; fz = 0; }
     }
-    REAL k = -self_psi * G;
-    f.x *= k; f.y *= k; f.z *= k;
     return f;
 }
 
@@ -408,7 +398,8 @@ static void collide(orc_t* s, int save, int update) {
                 if (eqb && sopen) {
                     REAL rb = (REAL)s->bvals[cell * 4 + 0];
                     v3 ub = mk3((REAL)s->bvals[cell * 4 + 1], (REAL)s->bvals[cell * 4 + 2], (REAL)s->bvals[cell * 4 + 3]);
-                    f[i] = feq_ref(s, rb, ub, uu_half(s, ub), i);
+                    f[i] = ((REAL)s->V[i].w * rb) * bracket(s, cdot(s->V[i].cx, s->V[i].cy, s->V[i].cz, ub),
+                                                             (REAL)1 - uu_of(ub) * s->R2h);
                     continue;
                 }
                 if (bb && !sopen && is_solid(s, sid)) {
@@ -425,8 +416,13 @@ static void collide(orc_t* s, int save, int update) {
             }
             f[i] = open ? (REAL)0.01 : L[(size_t)rs * N + rc];
         }
-        REAL density = 0;
-        for (int i = 0; i < Q; i++) density += f[i];
+        /* ---- canonical FP32 evaluation (shared with the CUDA kernels) ----
+         * opposite populations pair as (i, i+1), i odd:  s = f_i + f_i+1,
+         * d = f_i - f_i+1; rho and the momentum are summed pairwise in order. */
+        REAL sp[QMAX / 2 + 1], dp_[QMAX / 2 + 1];
+        for (int i = 1; i < Q; i += 2) { sp[i / 2] = f[i] + f[i + 1]; dp_[i / 2] = f[i] - f[i + 1]; }
+        REAL density = f[0];
+        for (int i = 1; i < Q; i += 2) density = density + sp[i / 2];
         if (density < (REAL)0.01) density = (REAL)0.01; /* max(density, 0.01) */
         v3 force = get_force(s, cell);
         REAL temperature = 0;
@@ -434,30 +430,40 @@ static void collide(orc_t* s, int save, int update) {
             REAL* TS = TSRC(s);
             for (int i = 0; i < s->Qt; i++) temperature += TS[cell * s->Qt + i];
             REAL k = -(REAL)s->d.beta * (temperature - (REAL)1);
-            v3 b = mk3(k * force.x, k * force.y, k * force.z);
-            force.x += b.x; force.y += b.y; force.z += b.z;
+            force.x = FMA(k, force.x, force.x);
+            force.y = FMA(k, force.y, force.y);
+            force.z = FMA(k, force.z, force.z);
         }
         if (s->d.multiphase) {
-            v3 sc = sc_force(s, x, y, z, density);
-            force.x += sc.x; force.y += sc.y; force.z += sc.z;
+            v3 sc = sc_force_acc(s, x, y, z, density);
+            REAL k = -psi(density) * (REAL)s->d.G;
+            force.x = FMA(sc.x, k, force.x);
+            force.y = FMA(sc.y, k, force.y);
+            force.z = FMA(sc.z, k, force.z);
         }
-        v3 vel = mk3(0, 0, 0);
-        for (int i = 0; i < Q; i++) {
-            vel.x += f[i] * (REAL)s->V[i].cx;
-            vel.y += f[i] * (REAL)s->V[i].cy;
-            vel.z += f[i] * (REAL)s->V[i].cz;
+        REAL jx = 0, jy = 0, jz = 0;
+        int fx = 1, fy = 1, fz = 1;
+        for (int i = 1; i < Q; i += 2) {
+            REAL d = dp_[i / 2];
+            if (s->V[i].cx) { REAL t = s->V[i].cx > 0 ? d : -d; jx = fx ? t : jx + t; fx = 0; }
+            if (s->V[i].cy) { REAL t = s->V[i].cy > 0 ? d : -d; jy = fy ? t : jy + t; fy = 0; }
+            if (s->V[i].cz) { REAL t = s->V[i].cz > 0 ? d : -d; jz = fz ? t : jz + t; fz = 0; }
         }
-        vel.x /= density; vel.y /= density; vel.z /= density;
-        vel.x += force.x / ((REAL)2 * density);
-        vel.y += force.y / ((REAL)2 * density);
-        vel.z += force.z / ((REAL)2 * density);
-        REAL len = (REAL)sqrt((double)dot3(vel, vel));
-        if (IS_F32) len = (REAL)sqrtf((float)dot3(vel, vel));
+        REAL r = (REAL)1 / density;
+        v3 vel = mk3(jx * r, jy * r, jz * r);
+        if (s->forced) {
+            REAL h = r * (REAL)0.5;
+            vel.x = FMA(force.x, h, vel.x);
+            vel.y = FMA(force.y, h, vel.y);
+            vel.z = FMA(force.z, h, vel.z);
+        }
+        REAL uu = uu_of(vel);
+        REAL len = IS_F32 ? (REAL)sqrtf((float)uu) : (REAL)sqrt((double)uu);
         int out_lim = len > (REAL)s->d.velocity_limit;
         int out_ext = len > (REAL)s->d.velocity_limit_extreme;
-        if (out_lim) {
-            REAL lim = (REAL)s->d.velocity_limit;
-            vel.x = vel.x / len * lim; vel.y = vel.y / len * lim; vel.z = vel.z / len * lim;
+        if (out_lim) { /* normalize(u) * limit */
+            REAL q = (REAL)s->d.velocity_limit / len;
+            vel.x = vel.x * q; vel.y = vel.y * q; vel.z = vel.z * q;
         }
         if (eqb) {
             /* equilibrium boundary cell (extension): velocity kind keeps the
@@ -469,55 +475,58 @@ static void collide(orc_t* s, int save, int update) {
             if (kind == ORC_OBJ_EQ_VELOCITY) vel = ub; else density = rb;
             force = mk3(0, 0, 0);
         }
+        const REAL one_m = (REAL)1 - uu_of(vel) * s->R2h;
         if (update) {
-            REAL fn[QMAX], fe[QMAX];
-            const REAL uuh = uu_half(s, vel);
-            for (int i = 0; i < Q; i++) fe[i] = feq_ref(s, density, vel, uuh, i);
-            if (eqb) {
-                for (int i = 0; i < Q; i++) fn[i] = fe[i];
-            } else if (s->d.collision == ORC_TRT) {
-                /* TRT (extension), pairwise over (i, opp i) with the symmetric
-                 * and antisymmetric equilibrium parts written out:
+            REAL fn[QMAX];
+            const REAL fuR2 = FMA(force.z, vel.z, FMA(force.y, vel.y, force.x * vel.x)) * s->R2;
+            if (eqb || s->d.collision != ORC_TRT) {
+                for (int i = 0; i < Q; i++) {
+                    REAL w = (REAL)s->V[i].w;
+                    REAL cu = cdot(s->V[i].cx, s->V[i].cy, s->V[i].cz, vel);
+                    REAL fe = (w * density) * bracket(s, cu, one_m);
+                    REAL v = FMA(fe - f[i], s->Rtau, f[i]); /* old + (-(old - feq)/tau) */
+                    if (s->src_on) {
+                        REAL fc = cdot(s->V[i].cx, s->V[i].cy, s->V[i].cz, force);
+                        REAL inner = FMA(fc, s->R2, FMA(fc * cu, s->R4, -fuR2));
+                        v = FMA(s->P * w, inner, v);
+                    }
+                    fn[i] = (eqb || out_ext) ? fe : v;
+                }
+            } else {
+                /* TRT (extension), pairwise over (i, opp i):
                  *   e+ = w rho ((1 - uu/2/cs2) + cu^2/2/cs4),  e- = w rho cu/cs2
                  *   f_i <- f_i - omega+ (f+ - e+) -+ omega- (f- - e-)
                  * omega+ = 1/tau, omega- = 1/(Lambda/(tau-1/2) + 1/2); the Guo
                  * term's even part (F.c)(u.c)/cs4 - F.u/cs2 gets (1-omega+/2),
                  * its odd part F.c/cs2 gets (1-omega-/2).  Above the extreme
                  * velocity limit the populations become e+ +- e-. */
-                const REAL fu = dot3(force, vel);
-                const REAL one_m = (REAL)1 - uuh;
                 {
-                    REAL fe0 = ((REAL)s->V[0].w * density) * one_m;
-                    REAL v = f[0] - (f[0] - fe0) * s->Rtau;
-                    if (s->src_on) v = v + (s->Pp * (REAL)s->V[0].w) * ((REAL)0 - fu * s->R2);
+                    REAL w0 = (REAL)s->V[0].w;
+                    REAL fe0 = (w0 * density) * one_m;
+                    REAL v = FMA(fe0 - f[0], s->Rtau, f[0]);
+                    if (s->src_on) v = FMA(s->Pp * w0, -fuR2, v);
                     fn[0] = out_ext ? fe0 : v;
                 }
                 for (int i = 1; i < Q; i += 2) {
                     const int j = i + 1;
                     REAL w = (REAL)s->V[i].w;
-                    v3 c = mk3((REAL)s->V[i].cx, (REAL)s->V[i].cy, (REAL)s->V[i].cz);
-                    REAL cu = dot3(c, vel);
+                    REAL cu = cdot(s->V[i].cx, s->V[i].cy, s->V[i].cz, vel);
                     REAL wr = w * density;
-                    REAL ep = wr * (one_m + ((cu * cu) * (REAL)0.5) * s->R4);
-                    REAL em = wr * (cu * s->R2);
-                    REAL fp = (f[i] + f[j]) * (REAL)0.5, fm = (f[i] - f[j]) * (REAL)0.5;
-                    REAL dp = (fp - ep) * s->Rtau, dm = (fm - em) * s->Wm;
-                    REAL vi = (f[i] - dp) - dm, vj = (f[j] - dp) + dm;
+                    REAL ep = wr * FMA(cu * cu, s->R4h, one_m);
+                    REAL em = (wr * s->R2) * cu;
+                    REAL Pd = FMA(sp[i / 2], (REAL)0.5, -ep);
+                    REAL Md = FMA(dp_[i / 2], (REAL)0.5, -em);
+                    REAL vi = FMA(-Md, s->Wm, FMA(-Pd, s->Rtau, f[i]));
+                    REAL vj = FMA(Md, s->Wm, FMA(-Pd, s->Rtau, f[j]));
                     if (s->src_on) {
-                        REAL fc = dot3(force, c);
-                        REAL Sp = (s->Pp * w) * ((fc * cu) * s->R4 - fu * s->R2);
+                        REAL fc = cdot(s->V[i].cx, s->V[i].cy, s->V[i].cz, force);
+                        REAL Sp = (s->Pp * w) * FMA(fc * cu, s->R4, -fuR2);
                         REAL Sm = (s->Pm * w) * (fc * s->R2);
                         vi = vi + (Sp + Sm);
                         vj = vj + (Sp - Sm);
                     }
                     fn[i] = out_ext ? ep + em : vi;
                     fn[j] = out_ext ? ep - em : vj;
-                }
-            } else {
-                for (int i = 0; i < Q; i++) {
-                    REAL upd = f[i] + (fe[i] - f[i]) * s->Rtau; /* old + (-(old - feq)/tau) */
-                    if (s->src_on) upd = upd + source_ref(s, i, force, vel);
-                    fn[i] = out_ext ? fe[i] : upd;
                 }
             }
             for (int i = 0; i < Q; i++) {
@@ -527,17 +536,20 @@ static void collide(orc_t* s, int save, int update) {
             }
         }
         if (s->d.multiphase) {
+            /* the ping-pong texture holds psi of the effective density
+             * (the reference stores the density and applies psi on reading;
+             * psi is a pure function of it, so the two are equivalent) */
             REAL eff = density;
             if (s->nobj > 1 && bid != 0) eff = (REAL)s->objects[bid * 12 + 11];
-            MTGT(s)[cell] = eff;
+            MTGT(s)[cell] = psi(eff);
         }
         if (s->thermal) {
             REAL* TS = TSRC(s); REAL* TT = TTGT(s);
-            const REAL uuh = uu_half(s, vel);
             for (int i = 0; i < s->Qt; i++) {
-                REAL ge = feq_t_ref(s, temperature, vel, uuh, i);
+                REAL cu = cdot(s->Vt[i].cx, s->Vt[i].cy, s->Vt[i].cz, vel);
+                REAL ge = ((REAL)s->Vt[i].w * temperature) * bracket(s, cu, one_m);
                 REAL g = TS[cell * s->Qt + i];
-                TT[cell * s->Qt + i] = g + (ge - g) * s->Rtau_t; /* g + (-(g - geq)/tau_T) */
+                TT[cell * s->Qt + i] = FMA(ge - g, s->Rtau_t, g); /* g + (-(g - geq)/tau_T) */
             }
         }
         if (save) {
@@ -670,6 +682,8 @@ orc_t* ORC(create)(const orc_desc* d, const float* rho, const float* u, const fl
         REAL tau = (REAL)d->tau;
         s->R2 = (REAL)1 / cs2;
         s->R4 = (REAL)1 / cs4;
+        s->R2h = s->R2 * (REAL)0.5;
+        s->R4h = s->R4 * (REAL)0.5;
         s->Rtau = (REAL)1 / tau;
         s->P = (REAL)1 - (REAL)1 / ((REAL)2 * tau);
         s->Rtau_t = (REAL)1 / (REAL)d->tau_t;
@@ -712,6 +726,7 @@ orc_t* ORC(create)(const orc_desc* d, const float* rho, const float* u, const fl
     s->forcing = !(s->constant_force && f0[0] == 0 && f0[1] == 0 && f0[2] == 0);
     /* collide.comp:609: the source term exists with forcing, multiphase or thermal flow */
     s->src_on = s->forcing || d->multiphase || s->thermal;
+    s->forced = s->src_on;
     if (s->forcing && !s->constant_force) {
         s->forces = (float*)calloc(N * 4, sizeof(float));
         for (size_t c = 0; c < N; c++) for (int k = 0; k < 3; k++) s->forces[c * 4 + k] = force[c * 3 + k];

@@ -1,0 +1,270 @@
+// LBM.hpp -- C++ facade with the member names, argument meaning and
+// defaults of BoltzmannFluids' solver class (BoltzmannFluids/Source/LBM/LBM.h:26-145),
+// implemented over the C ABI of bf_lbm.h.  Header only: link libbfgb300.so.
+//
+// Differences a caller of the reference sees:
+//  * errors throw bf::LBMError (the reference printed "[LBM Error]" and
+//    asserted, LBM.cpp:429-437);
+//  * the Texture3D getters return bf::Field, a headless device buffer
+//    (pointer + shape) instead of a GL texture; copy_to_host() reads it back;
+//  * render2d_*/render3d_* are not provided (no graphics stack).
+#pragma once
+
+#include <cstdint>
+#include <functional>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../bf_lbm.h"
+
+namespace bf {
+
+struct ivec3 {
+    int32_t x = 0, y = 0, z = 0;
+    ivec3() = default;
+    ivec3(int32_t x_, int32_t y_, int32_t z_) : x(x_), y(y_), z(z_) {}
+    template <class V> ivec3(const V& v) : x((int32_t)v.x), y((int32_t)v.y), z((int32_t)v.z) {}
+};
+struct vec3 {
+    float x = 0, y = 0, z = 0;
+    vec3() = default;
+    vec3(float x_, float y_, float z_) : x(x_), y(y_), z(z_) {}
+    template <class V> vec3(const V& v) : x((float)v.x), y((float)v.y), z((float)v.z) {}
+};
+
+enum VelocitySet { D2Q9 = BF_D2Q9, D3Q15 = BF_D3Q15, D3Q19 = BF_D3Q19, D3Q27 = BF_D3Q27 };
+enum FloatingPointAccuracy { fp16 = BF_STORE_FP16, fp32 = BF_STORE_FP32, fp16s = BF_STORE_FP16S, fp16c = BF_STORE_FP16C };
+
+class LBMError : public std::runtime_error {
+public:
+    LBMError(int code, const std::string& what) : std::runtime_error("[LBM Error] " + what), code(code) {}
+    int code;
+};
+
+inline void check(int code) {
+    if (code != BF_OK) throw LBMError(code, bf_last_error());
+}
+
+// headless stand-in for the reference's shared_ptr<Texture3D>
+struct Field {
+    bf_field desc{};
+    bf_solver* owner = nullptr;
+    void* device_ptr() const { return desc.device_ptr; }
+    size_t bytes() const { return desc.bytes; }
+    template <class T> std::vector<T> copy_to_host() const {
+        std::vector<T> out(desc.bytes / sizeof(T));
+        check(bf_copy_field_to_host(owner, desc.kind, out.data(), out.size() * sizeof(T)));
+        return out;
+    }
+};
+
+class LBM {
+public:
+    static constexpr uint32_t not_a_boundry = 0;
+    static constexpr uint32_t max_boundry_count = 255;
+    static constexpr float referance_temperature = 1.0f;
+    static constexpr float referance_boundry_density = 1.0f;
+
+    // LBM::FluidProperties (LBM.h:41-47)
+    struct FluidProperties {
+        vec3 velocity = vec3(0, 0, 0);
+        vec3 force = vec3(0, 0, 0);
+        float density = 1;
+        float temperature = referance_temperature;
+        uint32_t boundry_id = not_a_boundry;
+    };
+
+    LBM() { check(bf_create(&s_)); }
+    ~LBM() { bf_destroy(s_); }
+    LBM(const LBM&) = delete;
+    LBM& operator=(const LBM&) = delete;
+
+    // ---- simulation controls (LBM.h:34-38) ----
+    // target_tick_per_second is accepted for signature compatibility; every
+    // call advances one tick (the reference's behaviour with tps <= 0)
+    void iterate_time(float target_tick_per_second = 0) {
+        (void)target_tick_per_second;
+        check(bf_iterate_time(s_, 1, 1));
+    }
+    void iterate_time_steps(int32_t steps, bool save_fields = true) { check(bf_iterate_time(s_, steps, save_fields)); }
+    int32_t get_total_ticks_elapsed() {
+        int64_t t = 0;
+        check(bf_get_total_ticks_elapsed(s_, &t));
+        return (int32_t)t;
+    }
+    ivec3 get_resolution() {
+        int32_t r[3];
+        check(bf_get_resolution(s_, r));
+        return ivec3(r[0], r[1], r[2]);
+    }
+    int32_t get_velocity_set_vector_count() {
+        int32_t q = 0;
+        check(bf_get_velocity_set_vector_count(s_, &q));
+        return q;
+    }
+
+    // ---- initialisation (LBM.h:48-58) ----
+    void initialize_fields(std::function<void(ivec3, FluidProperties&)> initialization_lambda, ivec3 resolution,
+                           float relaxation_time, bool periodic_x = true, bool periodic_y = true,
+                           bool periodic_z = true, VelocitySet velocity_set = D2Q9,
+                           FloatingPointAccuracy fp_accuracy = fp32, bool is_flow_multiphase = false) {
+        const size_t n = (size_t)resolution.x * resolution.y * resolution.z;
+        std::vector<float> rho(n), u(3 * n), f(3 * n), T(n);
+        std::vector<uint32_t> ids(n);
+        size_t k = 0;
+        for (int32_t z = 0; z < resolution.z; z++)
+            for (int32_t y = 0; y < resolution.y; y++)
+                for (int32_t x = 0; x < resolution.x; x++, k++) {
+                    FluidProperties p;
+                    initialization_lambda(ivec3(x, y, z), p);
+                    rho[k] = p.density;
+                    u[3 * k] = p.velocity.x; u[3 * k + 1] = p.velocity.y; u[3 * k + 2] = p.velocity.z;
+                    f[3 * k] = p.force.x; f[3 * k + 1] = p.force.y; f[3 * k + 2] = p.force.z;
+                    T[k] = p.temperature;
+                    ids[k] = p.boundry_id;
+                }
+        bf_init_desc d;
+        bf_init_desc_default(&d);
+        d.resolution[0] = resolution.x; d.resolution[1] = resolution.y; d.resolution[2] = resolution.z;
+        d.relaxation_time = relaxation_time;
+        d.periodic[0] = periodic_x; d.periodic[1] = periodic_y; d.periodic[2] = periodic_z;
+        d.velocity_set = velocity_set;
+        d.storage = fp_accuracy;
+        d.multiphase = is_flow_multiphase;
+        d.esoteric = is_collide_esoteric;
+        d.boundary_mode = boundary_mode;
+        d.collision = collision;
+        d.trt_magic = trt_magic;
+        d.velocity_limit = velocity_limit;
+        d.velocity_limit_extreme = velocity_limit_extreme;
+        d.intermolecular_interaction_strength = intermolecular_interaction_strength;
+        d.thermal_relaxation_time = thermal_relaxation_time;
+        d.thermal_expansion_coefficient = thermal_expension_coeficient;
+        d.thermal_init_equilibrium = thermal_init_equilibrium;
+        d.two_buffer_fixed = two_buffer_fixed;
+        check(bf_initialize_fields(s_, &d, rho.data(), u.data(), f.data(), T.data(), ids.data()));
+        velocity_set_ = velocity_set;
+        fp_ = fp_accuracy;
+        periodic_[0] = periodic_x; periodic_[1] = periodic_y; periodic_[2] = periodic_z;
+    }
+
+    // ---- boundary objects (LBM.h:60-82) ----
+    void set_boundry_properties(uint32_t boundry_id, vec3 velocity_translational, vec3 velocity_angular,
+                                vec3 center_of_mass, float temperature = referance_temperature,
+                                float effective_density = referance_boundry_density,
+                                bf_object_kind kind = BF_OBJECT_SOLID) {
+        bf_object o{};
+        o.velocity_translational[0] = velocity_translational.x;
+        o.velocity_translational[1] = velocity_translational.y;
+        o.velocity_translational[2] = velocity_translational.z;
+        o.velocity_angular[0] = velocity_angular.x; o.velocity_angular[1] = velocity_angular.y;
+        o.velocity_angular[2] = velocity_angular.z;
+        o.center_of_mass[0] = center_of_mass.x; o.center_of_mass[1] = center_of_mass.y;
+        o.center_of_mass[2] = center_of_mass.z;
+        o.temperature = temperature;
+        o.effective_density = effective_density;
+        o.kind = kind;
+        check(bf_set_boundry_properties(s_, boundry_id, &o));
+    }
+    void set_boundry_properties(uint32_t boundry_id, vec3 velocity_translational,
+                                float temperature = referance_temperature,
+                                float effective_density = referance_boundry_density) {
+        set_boundry_properties(boundry_id, velocity_translational, vec3(), vec3(), temperature, effective_density);
+    }
+    void set_boundry_properties(uint32_t boundry_id, float temperature,
+                                float effective_density = referance_boundry_density) {
+        set_boundry_properties(boundry_id, vec3(), vec3(), vec3(), temperature, effective_density);
+    }
+    void clear_boundry_properties() { check(bf_clear_boundry_properties(s_)); }
+
+    // ---- readback (LBM.h:97-99) ----
+    Field get_velocity_density_texture() { return field(BF_FIELD_VELOCITY_DENSITY); }
+    Field get_boundry_texture() { return field(BF_FIELD_BOUNDARY); }
+    Field get_force_temperature_texture() { return field(BF_FIELD_FORCE_TEMPERATURE); }
+
+    // ---- low-level getters / setters (LBM.h:105-120) ----
+    float get_relaxation_time() {
+        float t = 0;
+        check(bf_get_relaxation_time(s_, &t));
+        return t;
+    }
+    VelocitySet get_velocity_set() { return velocity_set_; }
+    int32_t get_dimentionality() { return velocity_set_ == D2Q9 ? 2 : 3; }
+    FloatingPointAccuracy get_floating_point_accuracy() { return fp_; }
+    bool get_periodic_boundry_x() { return periodic_[0]; }
+    bool get_periodic_boundry_y() { return periodic_[1]; }
+    bool get_periodic_boundry_z() { return periodic_[2]; }
+    bool get_is_forcing_scheme() { return flags() & 1; }
+    bool get_is_force_field_constant() { return flags() & 2; }
+    bool get_is_flow_multiphase() { return flags() & 8; }
+    vec3 get_constant_force() {
+        float f[3];
+        check(bf_get_constant_force(s_, f));
+        return vec3(f[0], f[1], f[2]);
+    }
+    float get_intermolecular_interaction_strength() {
+        float g = 0;
+        check(bf_get_intermolecular_interaction_strength(s_, &g));
+        return g;
+    }
+    void set_relaxation_time(float relaxation_time) { check(bf_set_relaxation_time(s_, relaxation_time)); }
+    void set_constant_force(vec3 constant_force) {
+        const float f[3] = {constant_force.x, constant_force.y, constant_force.z};
+        check(bf_set_constant_force(s_, f));
+    }
+    void set_intermolecular_interaction_strength(float value) {
+        intermolecular_interaction_strength = value;
+        check(bf_set_intermolecular_interaction_strength(s_, value));
+    }
+
+    // ---- snapshots (LBM.h:123-126, declared but not defined upstream) ----
+    void save_current_tick_mesoscropic(const std::string& path) { check(bf_save_snapshot(s_, path.c_str())); }
+    void load_tick_mesoscropic(const std::string& path, int32_t target_tick = -1) {
+        (void)target_tick;
+        check(bf_load_snapshot(s_, path.c_str()));
+    }
+
+    // FP64 {mass, momentum x, y, z, kinetic energy} of the current state (extension)
+    std::vector<double> reduce() {
+        std::vector<double> out(5);
+        check(bf_reduce(s_, out.data()));
+        return out;
+    }
+    void synchronize(int32_t timeout_ms = 0) { check(bf_synchronize(s_, timeout_ms)); }
+
+    // ---- public knobs (LBM.h:139-145, :242-243, :257) + extensions ----
+    bool is_lattice_texture3d = false;  // storage layout of the GL path: no effect here
+    bool is_collide_esoteric = false;
+    float velocity_limit = 0.25f;
+    float velocity_limit_extreme = 0.30f;
+    float thermal_relaxation_time = 2.0f;       // what initialize_fields sets (LBM.cpp:461)
+    float thermal_expension_coeficient = 0.5f;  // LBM.h:243
+    float intermolecular_interaction_strength = -6.0f;
+    bf_boundary_mode boundary_mode = BF_BOUNDARY_SKIP;
+    bf_collision collision = BF_COLLISION_BGK;
+    float trt_magic = 0.25f;
+    bool thermal_init_equilibrium = false;
+    bool two_buffer_fixed = false;
+
+    bf_solver* handle() { return s_; }
+
+private:
+    Field field(int kind) {
+        Field f;
+        f.owner = s_;
+        check(bf_get_field(s_, kind, &f.desc));
+        return f;
+    }
+    int32_t flags() {
+        int32_t fl = 0, bits = 0;
+        check(bf_get_scheme_flags(s_, &fl, &bits));
+        return fl;
+    }
+    bf_solver* s_ = nullptr;
+    VelocitySet velocity_set_ = D2Q9;
+    FloatingPointAccuracy fp_ = fp32;
+    bool periodic_[3] = {true, true, true};
+};
+
+}  // namespace bf

@@ -75,6 +75,8 @@ int bits_per_boundry(int count) {
 
 }  // namespace
 
+void bf::record_error(const std::string& msg) { g_last_error = msg; }
+
 struct bf_solver {
     int device = 0;
     cudaStream_t stream = nullptr;

@@ -2,6 +2,7 @@
 // shared by the sm_103a lattice Boltzmann kernels.
 #pragma once
 #include <cstdint>
+#include <string>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
@@ -248,6 +249,9 @@ template <int QT> cudaError_t launch_stream_thermal(const ThermalStreamParams& p
 template <int QT> cudaError_t launch_init_thermal(const InitParams& p, cudaStream_t st);
 
 cudaError_t launch_reduce_finish(const double* partials, uint32_t n_blocks, double* out, cudaStream_t st);
+
+// sets the thread's message returned by bf_last_error()
+void record_error(const std::string& msg);
 
 constexpr int kStepBlock = 256;
 

@@ -151,6 +151,7 @@ ABI = {
     "bf_bits_per_boundry": (C.c_int, [C.c_int32, C.POINTER(C.c_int32)]),
     "bf_pack_boundries": (C.c_int, [C.c_void_p, C.c_size_t, C.c_int32, C.c_void_p, C.c_size_t,
                                     C.POINTER(C.c_size_t)]),
+    "bf_reduce_field_noalloc": (C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.POINTER(C.c_double)]),
 }
 
 _lib = None

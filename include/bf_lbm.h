@@ -220,6 +220,25 @@ int bf_benchmark_steps(bf_solver* s, int32_t n_steps, float* ms);
 int bf_save_snapshot(bf_solver* s, const char* path);
 int bf_load_snapshot(bf_solver* s, const char* path);
 
+/* ---- allocation-free reduction ------------------------------------------ */
+/* No counterpart in the reference.  FP64 {mass, momentum x, y, z, kinetic
+ * energy 0.5*rho*|u|^2} of n_cells float4 (u.xyz, rho) cells in device
+ * memory (the layout of BF_FIELD_VELOCITY_DENSITY), written to the host
+ * array out[5].  Meant for callers that must not allocate device memory --
+ * a renderer or UI frame callback working under a fixed memory budget, or
+ * code that must not stall other streams (cudaFree synchronizes the whole
+ * device): it calls no cudaMalloc, cudaFree or allocating library routine.
+ * Its scratch is one fixed 327,744-byte device array that every GPU loading
+ * the library keeps until the process exits; that limits a call to
+ * 134,217,728 cells (512^3), and larger counts return
+ * BF_ERR_INVALID_ARGUMENT.  The work runs on `stream` (NULL: the legacy
+ * default stream) and the call returns once it is done.  The first call on
+ * a device looks up the array's device address (cudaGetSymbolAddress);
+ * make that first call before any stream capture.  All calls share the
+ * array and every call overwrites what it reads, so calls that overlap on
+ * the GPU (different streams or host threads) race: serialise them. */
+int bf_reduce_field_noalloc(const void* vel_den_device, size_t n_cells, void* stream, double out[5]);
+
 #ifdef __cplusplus
 }
 #endif

@@ -208,6 +208,28 @@ def run_e2e(bf, res, vel, steps, world):
             "note": "timed: upload of the initial fields, the steps, read-back of the u/rho field; bytes amortised per step"}
 
 
+def run_adjoint_leg(bf):
+    """Differentiation configuration: D2Q9 BGK channel 512x256, tau 0.6,
+    Poiseuille inlet u_max 0.05, partial-bounce-back obstacle in the central
+    64x64 box, T = 2000 steps, checkpoints every 100 steps; ms per gradient
+    (forward + backward) against the forward solve, device time by CUDA events."""
+    from boltzmannfluids_gb300.adjoint import AdjointChannel, channel_setup
+    res = (512, 256, 1)
+    s, u_in, tgt = channel_setup(res)
+    out = {"workload": "D2Q9 BGK channel 512x256, PSM obstacle, T=2000"}
+    for K, key in ((100, "checkpoint_every_100"), (2000, "all_states_stored")):
+        g = AdjointChannel(res, 0.6, bf.VelocitySet.D2Q9, 2000, K)
+        g.set_parameters(s, u_in)
+        g.set_target(tgt)
+        g.forward()
+        g.backward()
+        f_ms, b_ms = g.time(5)
+        out[key] = {"forward_ms": round(f_ms, 3), "backward_ms": round(b_ms, 3),
+                    "ms_per_gradient": round(f_ms + b_ms, 3), "gradient_over_forward": round((f_ms + b_ms) / f_ms, 3)}
+        del g
+    return out
+
+
 def run_gpu(args):
     rank, world, local = dist_env()
     if world > 1:
@@ -272,6 +294,9 @@ def run_gpu(args):
     e2e = None
     if not args.no_e2e:
         e2e = run_e2e(bf, res, vel, args.steps, world)
+    adj = None
+    if not args.no_adjoint:
+        adj = run_adjoint_leg(bf)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         mlups_cpu, threads, sample = cpu_baseline_sample()
@@ -294,6 +319,7 @@ def run_gpu(args):
             "storage_sweep": sweep,
             "conservation_fp64": {"mass": red[0], "momentum": list(red[1:4]), "kinetic_energy": red[4]},
             "e2e": e2e,
+            "adjoint": adj,
             "gpu_launches": args.steps,
             "clocks": clock_info,
         }
@@ -317,6 +343,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--no-sweep", action="store_true", help="skip the 16-bit storage legs (profiling runs)")
     ap.add_argument("--storage", default="fp32", choices=["fp32", "fp16s", "fp16c"], help="storage of the main leg")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

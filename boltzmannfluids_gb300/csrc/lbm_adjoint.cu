@@ -1,0 +1,586 @@
+// lbm_adjoint.cu -- differentiable channel-flow model and its hand-written
+// discrete adjoint (no counterpart in the reference, which has no adjoint).
+//
+// Model (D2Q9 with nz = 1, or D3Q19; periodic in z).  One step maps the
+// post-collision state f^(t-1) to f^t:
+//   pull   g_i(x) = f_i(x - c_i)                 source inside the domain
+//          g_i(x) = f_opp(i)(x)                  source outside in y: halfway bounce-back wall
+//          g_i(x) = feq_i(1, (u_in(y,z),0,0))    source at x < 0 or x >= nx: equilibrium inlet/outlet
+//   BGK    g^c_i = g_i + (feq_i(rho,u) - g_i)/tau,  feq = w rho (1 + 3 c.u + 4.5 (c.u)^2 - 1.5 u.u)
+//   PSM    f_i = (1 - s) g^c_i + s g_opp(i)      partial bounce-back, solid fraction s in [0,1]
+// f^0 = feq(1, (u_in,0,0)).  The objective reads the pulled populations of step T:
+//   J = wd sum 2 s j_x + wm sum |u - u*|^2.
+//
+// The adjoint step is the transposed pull (a push) of the transposed
+// per-cell Jacobian.  With the equilibrium inlet/outlet every population of
+// f^(t-1) feeds at most one g of step t, so every adjoint slot is written by
+// exactly one thread (plain stores; slots that feed nothing get 0).  The
+// transposed BGK Jacobian costs O(Q) per cell:
+//   mu_i = (1-w)(1-s) L_i + w (A0 + (c_i - u).V) + s L_opp(i),
+//   A0 = sum_k (1-s) L_k w_k B_k,  V = sum_k (1-s) L_k w_k (3 c_k + 9 (c_k.u) c_k - 3 u),
+// with w = 1/tau and B_k = feq_k/(w_k rho).  Parameter gradients accumulate in
+// FP64 (per-cell terms are summed in FP32 first).  The forward trajectory is
+// checkpointed every K steps; the forward leaves the last segment's states in
+// the K-state segment buffer and every earlier segment is recomputed into it
+// from its checkpoint before its adjoint sweep.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/bf_lbm.h"
+#include "lbm_common.cuh"
+
+namespace bf {
+namespace {
+
+constexpr int kAdjBlock = 256;
+
+struct AdjParams {
+    int nx, ny, nz;
+    uint32_t n;
+    float omega, wd, wm;
+    const float* f_prev;    // f^(t-1), SoA planes of n
+    float* f_next;          // forward output f^t
+    const float* s;         // solid fraction, n
+    const float* uin;       // inlet/outlet profile, ny*nz
+    const float* ustar;     // target velocity, 3n
+    const float* lam_in;    // adjoint of f^t
+    float* lam_out;         // adjoint of f^(t-1)
+    double* grad_s;         // n
+    double* grad_in;        // ny*nz, from the x = 0 cells
+    double* grad_out;       // ny*nz, from the x = nx-1 cells
+    double* partials;       // one per block (objective)
+};
+
+template <int Q>
+__device__ __forceinline__ float feq_plain(int i, float rho, float ux, float uy, float uz) {
+    const Dir c = Lattice<Q>::c(i);
+    const float cu = c.x * ux + c.y * uy + c.z * uz;
+    const float uu = ux * ux + uy * uy + uz * uz;
+    return Lattice<Q>::w(i) * rho * (1.0f + 3.0f * cu + 4.5f * cu * cu - 1.5f * uu);
+}
+// d feq_i(1, (u,0,0)) / d u
+template <int Q>
+__device__ __forceinline__ float dfeq_du(int i, float u) {
+    const Dir c = Lattice<Q>::c(i);
+    return Lattice<Q>::w(i) * (3.0f * c.x + 9.0f * (float)(c.x * c.x) * u - 3.0f * u);
+}
+
+__device__ __forceinline__ uint32_t adj_cell(const AdjParams& p, int x, int y, int z) {
+    return (uint32_t)x + (uint32_t)p.nx * ((uint32_t)y + (uint32_t)p.ny * (uint32_t)z);
+}
+// 0 interior (X, Y, Z set), 1 wall, 2 equilibrium inlet/outlet
+template <int Q>
+__device__ __forceinline__ int adj_source(const AdjParams& p, int x, int y, int z, int i, int& X, int& Y, int& Z) {
+    const Dir c = Lattice<Q>::c(i);
+    X = x - c.x; Y = y - c.y; Z = z - c.z;
+    if (Y < 0 || Y >= p.ny) return 1;
+    if (X < 0 || X >= p.nx) return 2;
+    Z = Z < 0 ? Z + p.nz : (Z >= p.nz ? Z - p.nz : Z);
+    return 0;
+}
+
+template <int Q>
+__device__ __forceinline__ void adj_pull(const AdjParams& p, int x, int y, int z, uint32_t n, float (&g)[Q]) {
+    const float ui = p.uin[(uint32_t)z * p.ny + y];
+#pragma unroll
+    for (int i = 0; i < Q; i++) {
+        int X, Y, Z;
+        const int kind = adj_source<Q>(p, x, y, z, i, X, Y, Z);
+        if (kind == 0) g[i] = p.f_prev[(uint64_t)i * p.n + adj_cell(p, X, Y, Z)];
+        else if (kind == 1) g[i] = p.f_prev[(uint64_t)opp(i) * p.n + n];
+        else g[i] = feq_plain<Q>(i, 1.0f, ui, 0.f, 0.f);
+    }
+}
+
+__device__ __forceinline__ void block_sum_store(double v, double* out) {
+    __shared__ double sm[kAdjBlock / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) sm[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        double t = lane < nw ? sm[lane] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+        if (lane == 0) out[blockIdx.x + (uint64_t)gridDim.x * (blockIdx.y + (uint64_t)gridDim.y * blockIdx.z)] = t;
+    }
+}
+
+template <int Q>
+__global__ void __launch_bounds__(kAdjBlock) adj_init_kernel(AdjParams p) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
+    if (x >= p.nx) return;
+    const uint32_t n = adj_cell(p, x, y, z);
+    const float ui = p.uin[(uint32_t)z * p.ny + y];
+#pragma unroll
+    for (int i = 0; i < Q; i++) p.f_next[(uint64_t)i * p.n + n] = feq_plain<Q>(i, 1.0f, ui, 0.f, 0.f);
+}
+
+template <int Q, bool FINAL>
+__global__ void __launch_bounds__(kAdjBlock) adj_forward_kernel(AdjParams p) {
+    using L = Lattice<Q>;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
+    double contrib = 0.0;
+    if (x < p.nx) {
+        const uint32_t n = adj_cell(p, x, y, z);
+        float g[Q];
+        adj_pull<Q>(p, x, y, z, n, g);
+        float rho = 0.f, jx = 0.f, jy = 0.f, jz = 0.f;
+#pragma unroll
+        for (int i = 0; i < Q; i++) {
+            const Dir c = L::c(i);
+            rho += g[i]; jx += c.x * g[i]; jy += c.y * g[i]; jz += c.z * g[i];
+        }
+        const float rr = 1.0f / rho;
+        const float ux = jx * rr, uy = jy * rr, uz = jz * rr;
+        const float s = p.s[n];
+        if (FINAL) {
+            const float dx = ux - p.ustar[3 * (uint64_t)n], dy = uy - p.ustar[3 * (uint64_t)n + 1],
+                        dz = uz - p.ustar[3 * (uint64_t)n + 2];
+            contrib = (double)p.wd * 2.0 * (double)s * (double)jx +
+                      (double)p.wm * ((double)dx * dx + (double)dy * dy + (double)dz * dz);
+        } else {
+#pragma unroll
+            for (int i = 0; i < Q; i++) {
+                const float gc = g[i] + (feq_plain<Q>(i, rho, ux, uy, uz) - g[i]) * p.omega;
+                const float gco = g[opp(i)];
+                p.f_next[(uint64_t)i * p.n + n] = (1.0f - s) * gc + s * gco;
+            }
+        }
+    }
+    if (FINAL) block_sum_store(contrib, p.partials);
+}
+
+template <int Q, bool FINAL>
+__global__ void __launch_bounds__(kAdjBlock) adj_backward_kernel(AdjParams p) {
+    using L = Lattice<Q>;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
+    if (x >= p.nx) return;
+    const uint32_t n = adj_cell(p, x, y, z);
+    float g[Q];
+    adj_pull<Q>(p, x, y, z, n, g);
+    float rho = 0.f, jx = 0.f, jy = 0.f, jz = 0.f;
+#pragma unroll
+    for (int i = 0; i < Q; i++) {
+        const Dir c = L::c(i);
+        rho += g[i]; jx += c.x * g[i]; jy += c.y * g[i]; jz += c.z * g[i];
+    }
+    const float rr = 1.0f / rho;
+    const float ux = jx * rr, uy = jy * rr, uz = jz * rr;
+    const float s = p.s[n];
+    float mu[Q];
+    double gs;
+    if (FINAL) {
+        // dJ/dg_i = wd 2 s c_ix + wm sum_a 2 (u_a - u*_a)(c_ia - u_a)/rho,  dJ/ds = wd 2 j_x
+        const float dx = 2.0f * p.wm * (ux - p.ustar[3 * (uint64_t)n]) * rr;
+        const float dy = 2.0f * p.wm * (uy - p.ustar[3 * (uint64_t)n + 1]) * rr;
+        const float dz = 2.0f * p.wm * (uz - p.ustar[3 * (uint64_t)n + 2]) * rr;
+#pragma unroll
+        for (int i = 0; i < Q; i++) {
+            const Dir c = L::c(i);
+            mu[i] = 2.0f * p.wd * s * c.x + dx * (c.x - ux) + dy * (c.y - uy) + dz * (c.z - uz);
+        }
+        gs = (double)p.wd * 2.0 * (double)jx;
+    } else {
+        const float om = p.omega, oms = 1.0f - s;
+        const float uu = ux * ux + uy * uy + uz * uz;
+        float A0 = 0.f, Vx = 0.f, Vy = 0.f, Vz = 0.f, lam[Q], gsf = 0.f;
+#pragma unroll
+        for (int k = 0; k < Q; k++) {
+            const Dir c = L::c(k);
+            const float w = L::w(k);
+            lam[k] = p.lam_in[(uint64_t)k * p.n + n];
+            const float cu = c.x * ux + c.y * uy + c.z * uz;
+            const float Lk = oms * lam[k] * w;
+            A0 += Lk * (1.0f + 3.0f * cu + 4.5f * cu * cu - 1.5f * uu);
+            const float t9 = 9.0f * cu;
+            Vx += Lk * (3.0f * c.x + t9 * c.x - 3.0f * ux);
+            Vy += Lk * (3.0f * c.y + t9 * c.y - 3.0f * uy);
+            Vz += Lk * (3.0f * c.z + t9 * c.z - 3.0f * uz);
+            const float gck = g[k] + (feq_plain<Q>(k, rho, ux, uy, uz) - g[k]) * om;
+            gsf += lam[k] * (g[opp(k)] - gck);
+        }
+        gs = (double)gsf;  // per-cell sum in FP32, accumulated over steps in FP64
+#pragma unroll
+        for (int i = 0; i < Q; i++) {
+            const Dir c = L::c(i);
+            const float dot = (c.x - ux) * Vx + (c.y - uy) * Vy + (c.z - uz) * Vz;
+            mu[i] = (1.0f - om) * oms * lam[i] + om * (A0 + dot) + s * lam[opp(i)];
+        }
+    }
+    p.grad_s[n] += gs;
+    // transpose of the pull
+    const float ui = p.uin[(uint32_t)z * p.ny + y];
+    float guf = 0.f;
+    bool eq_source = false;
+#pragma unroll
+    for (int i = 0; i < Q; i++) {
+        int X, Y, Z;
+        const int kind = adj_source<Q>(p, x, y, z, i, X, Y, Z);
+        if (kind == 0) p.lam_out[(uint64_t)i * p.n + adj_cell(p, X, Y, Z)] = mu[i];
+        else if (kind == 1) p.lam_out[(uint64_t)opp(i) * p.n + n] = mu[i];
+        else { guf += mu[i] * dfeq_du<Q>(i, ui); eq_source = true; }
+    }
+    // populations of f^(t-1) that leave through the inlet or outlet feed nothing
+#pragma unroll
+    for (int j = 0; j < Q; j++) {
+        const Dir c = L::c(j);
+        const int X = x + c.x, Y = y + c.y;
+        if (Y >= 0 && Y < p.ny && (X < 0 || X >= p.nx)) p.lam_out[(uint64_t)j * p.n + n] = 0.0f;
+    }
+    if (eq_source) {
+        const uint32_t row = (uint32_t)z * p.ny + y;
+        if (x == 0) p.grad_in[row] += (double)guf;
+        else p.grad_out[row] += (double)guf;
+    }
+}
+
+// d f^0 / d u_in: grad[row] += sum_x sum_i lam^0_i(x) dfeq_i/du, one block per (y, z) row
+template <int Q>
+__global__ void __launch_bounds__(kAdjBlock) adj_init_grad_kernel(AdjParams p) {
+    const int y = blockIdx.x, z = blockIdx.y;
+    const uint32_t row = (uint32_t)z * p.ny + y;
+    const float ui = p.uin[row];
+    double acc = 0.0;
+    for (int x = threadIdx.x; x < p.nx; x += blockDim.x) {
+        const uint32_t n = adj_cell(p, x, y, z);
+#pragma unroll
+        for (int i = 0; i < Q; i++) acc += (double)(p.lam_in[(uint64_t)i * p.n + n] * dfeq_du<Q>(i, ui));
+    }
+    __shared__ double sm[kAdjBlock];
+    sm[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = kAdjBlock / 2; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s) sm[threadIdx.x] += sm[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) p.grad_in[row] += sm[0];
+}
+
+__global__ void sum_partials_kernel(const double* partials, uint32_t nb, double* out) {
+    __shared__ double sm[256];
+    double acc = 0.0;
+    for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x) acc += partials[b];
+    sm[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s) sm[threadIdx.x] += sm[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = sm[0];
+}
+
+}  // namespace
+}  // namespace bf
+
+using namespace bf;
+
+struct bf_adjoint {
+    bf_adjoint_desc d{};
+    int Q = 0;
+    uint32_t n = 0, rows = 0, nblocks = 0;
+    int nseg = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<void*> allocs;
+    float *s = nullptr, *uin = nullptr, *ustar = nullptr;
+    std::vector<float*> ckpt, seg;
+    float *pp[2] = {nullptr, nullptr}, *lam[2] = {nullptr, nullptr};
+    double *grad_s = nullptr, *grad_in = nullptr, *grad_out = nullptr, *partials = nullptr, *J = nullptr;
+    cudaGraphExec_t fwd_graph = nullptr, bwd_graph = nullptr;
+    bool forward_done = false;
+};
+
+namespace {
+
+int afail(int code, const std::string& msg) {
+    bf::record_error(msg);
+    return code;
+}
+#define ACUDA(call)                                                                                       \
+    do {                                                                                                  \
+        cudaError_t e_ = (call);                                                                          \
+        if (e_ != cudaSuccess)                                                                            \
+            return afail(e_ == cudaErrorMemoryAllocation ? BF_ERR_OUT_OF_MEMORY : BF_ERR_CUDA,            \
+                         std::string(#call " failed: ") + cudaGetErrorString(e_));                        \
+    } while (0)
+
+AdjParams base_params(bf_adjoint* a) {
+    AdjParams p{};
+    p.nx = a->d.resolution[0]; p.ny = a->d.resolution[1]; p.nz = a->d.resolution[2];
+    p.n = a->n;
+    p.omega = 1.0f / a->d.relaxation_time;
+    p.wd = a->d.drag_weight;
+    p.wm = a->d.mismatch_weight;
+    p.s = a->s; p.uin = a->uin; p.ustar = a->ustar;
+    p.grad_s = a->grad_s; p.grad_in = a->grad_in; p.grad_out = a->grad_out; p.partials = a->partials;
+    return p;
+}
+
+dim3 adj_grid(const bf_adjoint* a, int& block) {
+    const int nx = a->d.resolution[0];
+    block = nx >= kAdjBlock ? kAdjBlock : ((nx + 31) / 32) * 32;
+    return dim3((unsigned)((nx + block - 1) / block), (unsigned)a->d.resolution[1], (unsigned)a->d.resolution[2]);
+}
+
+template <int Q>
+cudaError_t enqueue_forward(bf_adjoint* a) {
+    int block;
+    const dim3 grid = adj_grid(a, block);
+    const int T = a->d.steps, K = a->d.checkpoint_interval;
+    AdjParams p = base_params(a);
+    p.f_next = a->ckpt[0];
+    adj_init_kernel<Q><<<grid, block, 0, a->stream>>>(p);
+    const float* cur = a->ckpt[0];
+    // states of the last segment go straight to the segment buffer, where the
+    // backward sweep starts, so that segment needs no recomputation
+    const int t_last = (a->nseg - 1) * K;
+    for (int t = 1; t < T; t++) {
+        float* dst = (t % K == 0) ? a->ckpt[t / K] : (t > t_last ? a->seg[t - t_last] : a->pp[t & 1]);
+        p.f_prev = cur;
+        p.f_next = dst;
+        adj_forward_kernel<Q, false><<<grid, block, 0, a->stream>>>(p);
+        cur = dst;
+    }
+    p.f_prev = cur;
+    p.f_next = nullptr;
+    adj_forward_kernel<Q, true><<<grid, block, 0, a->stream>>>(p);
+    sum_partials_kernel<<<1, 256, 0, a->stream>>>(a->partials, a->nblocks, a->J);
+    return cudaGetLastError();
+}
+
+template <int Q>
+cudaError_t enqueue_backward(bf_adjoint* a) {
+    int block;
+    const dim3 grid = adj_grid(a, block);
+    const int T = a->d.steps, K = a->d.checkpoint_interval;
+    AdjParams p = base_params(a);
+    cudaMemsetAsync(a->grad_s, 0, (size_t)a->n * sizeof(double), a->stream);
+    cudaMemsetAsync(a->grad_in, 0, (size_t)a->rows * sizeof(double), a->stream);
+    cudaMemsetAsync(a->grad_out, 0, (size_t)a->rows * sizeof(double), a->stream);
+    int cur_lam = -1;  // index of the buffer holding the adjoint of f^t
+    for (int k = a->nseg - 1; k >= 0; k--) {
+        const int t0 = k * K, t1 = std::min(t0 + K, T);
+        // recompute f^(t0+1) .. f^(t1-1) into seg[1..] (the forward left the
+        // last segment there already)
+        const float* prev = a->ckpt[k];
+        for (int j = 1; j <= t1 - 1 - t0 && k != a->nseg - 1; j++) {
+            p.f_prev = prev;
+            p.f_next = a->seg[j];
+            adj_forward_kernel<Q, false><<<grid, block, 0, a->stream>>>(p);
+            prev = a->seg[j];
+        }
+        for (int t = t1; t >= t0 + 1; t--) {
+            p.f_prev = (t - 1 == t0) ? a->ckpt[k] : a->seg[t - 1 - t0];
+            const int out = cur_lam == 0 ? 1 : 0;
+            p.lam_out = a->lam[out];
+            if (t == T) {
+                p.lam_in = nullptr;
+                adj_backward_kernel<Q, true><<<grid, block, 0, a->stream>>>(p);
+            } else {
+                p.lam_in = a->lam[cur_lam];
+                adj_backward_kernel<Q, false><<<grid, block, 0, a->stream>>>(p);
+            }
+            cur_lam = out;
+        }
+    }
+    p.lam_in = a->lam[cur_lam];
+    adj_init_grad_kernel<Q><<<dim3((unsigned)a->d.resolution[1], (unsigned)a->d.resolution[2]), kAdjBlock, 0, a->stream>>>(p);
+    return cudaGetLastError();
+}
+
+int run_graph(bf_adjoint* a, cudaGraphExec_t* exec, bool forward) {
+    if (!*exec) {
+        ACUDA(cudaStreamBeginCapture(a->stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e;
+        if (a->Q == 9) e = forward ? enqueue_forward<9>(a) : enqueue_backward<9>(a);
+        else e = forward ? enqueue_forward<19>(a) : enqueue_backward<19>(a);
+        cudaGraph_t g = nullptr;
+        cudaError_t e2 = cudaStreamEndCapture(a->stream, &g);
+        if (e != cudaSuccess || e2 != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return afail(BF_ERR_CUDA, std::string("adjoint capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2));
+        }
+        cudaError_t e3 = cudaGraphInstantiate(exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e3 != cudaSuccess) return afail(BF_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e3));
+    }
+    ACUDA(cudaGraphLaunch(*exec, a->stream));
+    return BF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void bf_adjoint_desc_default(bf_adjoint_desc* d) {
+    if (!d) return;
+    std::memset(d, 0, sizeof(*d));
+    d->resolution[0] = 512; d->resolution[1] = 256; d->resolution[2] = 1;
+    d->relaxation_time = 0.6f;
+    d->velocity_set = BF_D2Q9;
+    d->steps = 2000;
+    d->checkpoint_interval = 100;
+    d->drag_weight = 1.0f;
+    d->mismatch_weight = 1.0f;
+}
+
+int bf_adjoint_destroy(bf_adjoint* a) {
+    if (!a) return BF_OK;
+    if (a->stream) cudaStreamSynchronize(a->stream);
+    if (a->fwd_graph) cudaGraphExecDestroy(a->fwd_graph);
+    if (a->bwd_graph) cudaGraphExecDestroy(a->bwd_graph);
+    for (void* p : a->allocs) cudaFree(p);
+    if (a->stream) cudaStreamDestroy(a->stream);
+    delete a;
+    return BF_OK;
+}
+
+int bf_adjoint_create(bf_adjoint** out, const bf_adjoint_desc* d) {
+    if (!out || !d) return afail(BF_ERR_INVALID_ARGUMENT, "bf_adjoint_create: NULL argument");
+    *out = nullptr;
+    const int Q = d->velocity_set == BF_D2Q9 ? 9 : (d->velocity_set == BF_D3Q19 ? 19 : 0);
+    if (!Q) return afail(BF_ERR_INVALID_ARGUMENT, "bf_adjoint_create: velocity set must be D2Q9 or D3Q19");
+    const int nx = d->resolution[0], ny = d->resolution[1], nz = d->resolution[2];
+    if (nx <= 0 || ny <= 0 || nz <= 0 || (Q == 9 && nz != 1) || ny > 65535 || nz > 65535)
+        return afail(BF_ERR_INVALID_ARGUMENT, "bf_adjoint_create: bad resolution");
+    if (d->steps < 1 || d->checkpoint_interval < 1) return afail(BF_ERR_INVALID_ARGUMENT, "bf_adjoint_create: steps and checkpoint_interval must be positive");
+    if (!(d->relaxation_time > 0.5f)) return afail(BF_ERR_INVALID_ARGUMENT, "bf_adjoint_create: relaxation_time must exceed 0.5");
+    const uint64_t n64 = (uint64_t)nx * ny * nz;
+    if (n64 * Q >= (1ull << 40)) return afail(BF_ERR_INVALID_ARGUMENT, "bf_adjoint_create: domain too large");
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return afail(BF_ERR_NO_DEVICE, "bf_adjoint_create: no CUDA device visible");
+    }
+    bf_adjoint* a = new bf_adjoint();
+    a->d = *d;
+    a->Q = Q;
+    a->n = (uint32_t)n64;
+    a->rows = (uint32_t)ny * nz;
+    a->nseg = (d->steps + d->checkpoint_interval - 1) / d->checkpoint_interval;
+    {
+        const int block = nx >= kAdjBlock ? kAdjBlock : ((nx + 31) / 32) * 32;
+        a->nblocks = (uint32_t)((nx + block - 1) / block) * (uint32_t)ny * (uint32_t)nz;
+    }
+    auto alloc = [&](size_t bytes, void** p) -> cudaError_t {
+        cudaError_t e = cudaMalloc(p, bytes);
+        if (e == cudaSuccess) a->allocs.push_back(*p);
+        return e;
+    };
+    const size_t state = (size_t)Q * a->n * sizeof(float);
+    cudaError_t e = cudaStreamCreateWithFlags(&a->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = alloc((size_t)a->n * 4, (void**)&a->s);
+    if (e == cudaSuccess) e = alloc((size_t)a->rows * 4, (void**)&a->uin);
+    if (e == cudaSuccess) e = alloc((size_t)a->n * 12, (void**)&a->ustar);
+    a->ckpt.assign(a->nseg, nullptr);
+    for (int k = 0; k < a->nseg && e == cudaSuccess; k++) e = alloc(state, (void**)&a->ckpt[k]);
+    a->seg.assign(d->checkpoint_interval, nullptr);
+    for (int j = 1; j < d->checkpoint_interval && e == cudaSuccess; j++) e = alloc(state, (void**)&a->seg[j]);
+    for (int k = 0; k < 2 && e == cudaSuccess; k++) e = alloc(state, (void**)&a->pp[k]);
+    for (int k = 0; k < 2 && e == cudaSuccess; k++) e = alloc(state, (void**)&a->lam[k]);
+    if (e == cudaSuccess) e = alloc((size_t)a->n * 8, (void**)&a->grad_s);
+    if (e == cudaSuccess) e = alloc((size_t)a->rows * 8, (void**)&a->grad_in);
+    if (e == cudaSuccess) e = alloc((size_t)a->rows * 8, (void**)&a->grad_out);
+    if (e == cudaSuccess) e = alloc((size_t)a->nblocks * 8, (void**)&a->partials);
+    if (e == cudaSuccess) e = alloc(8, (void**)&a->J);
+    if (e == cudaSuccess) e = cudaMemset(a->s, 0, (size_t)a->n * 4);
+    if (e == cudaSuccess) e = cudaMemset(a->uin, 0, (size_t)a->rows * 4);
+    if (e == cudaSuccess) e = cudaMemset(a->ustar, 0, (size_t)a->n * 12);
+    if (e != cudaSuccess) {
+        const int code = e == cudaErrorMemoryAllocation ? BF_ERR_OUT_OF_MEMORY : BF_ERR_CUDA;
+        std::string msg = std::string("bf_adjoint_create: ") + cudaGetErrorString(e);
+        cudaGetLastError();
+        bf_adjoint_destroy(a);
+        return afail(code, msg);
+    }
+    *out = a;
+    return BF_OK;
+}
+
+int bf_adjoint_set_parameters(bf_adjoint* a, const float* solid_fraction, const float* inlet_velocity) {
+    if (!a) return afail(BF_ERR_INVALID_ARGUMENT, "NULL adjoint");
+    ACUDA(cudaStreamSynchronize(a->stream));
+    if (solid_fraction) ACUDA(cudaMemcpy(a->s, solid_fraction, (size_t)a->n * 4, cudaMemcpyHostToDevice));
+    if (inlet_velocity) ACUDA(cudaMemcpy(a->uin, inlet_velocity, (size_t)a->rows * 4, cudaMemcpyHostToDevice));
+    a->forward_done = false;
+    return BF_OK;
+}
+
+int bf_adjoint_set_target(bf_adjoint* a, const float* u_target) {
+    if (!a || !u_target) return afail(BF_ERR_INVALID_ARGUMENT, "NULL argument");
+    ACUDA(cudaStreamSynchronize(a->stream));
+    ACUDA(cudaMemcpy(a->ustar, u_target, (size_t)a->n * 12, cudaMemcpyHostToDevice));
+    a->forward_done = false;
+    return BF_OK;
+}
+
+int bf_adjoint_forward(bf_adjoint* a, double* objective) {
+    if (!a) return afail(BF_ERR_INVALID_ARGUMENT, "NULL adjoint");
+    int r = run_graph(a, &a->fwd_graph, true);
+    if (r != BF_OK) return r;
+    a->forward_done = true;
+    if (objective) {
+        ACUDA(cudaMemcpyAsync(objective, a->J, sizeof(double), cudaMemcpyDeviceToHost, a->stream));
+        ACUDA(cudaStreamSynchronize(a->stream));
+    }
+    return BF_OK;
+}
+
+int bf_adjoint_backward(bf_adjoint* a, double* grad_solid_fraction, double* grad_inlet_velocity) {
+    if (!a) return afail(BF_ERR_INVALID_ARGUMENT, "NULL adjoint");
+    if (!a->forward_done) return afail(BF_ERR_INVALID_ARGUMENT, "bf_adjoint_backward: run bf_adjoint_forward with the current parameters first");
+    int r = run_graph(a, &a->bwd_graph, false);
+    if (r != BF_OK) return r;
+    if (grad_solid_fraction)
+        ACUDA(cudaMemcpyAsync(grad_solid_fraction, a->grad_s, (size_t)a->n * 8, cudaMemcpyDeviceToHost, a->stream));
+    if (grad_inlet_velocity) {
+        std::vector<double> gin(a->rows), gout(a->rows);
+        ACUDA(cudaMemcpyAsync(gin.data(), a->grad_in, (size_t)a->rows * 8, cudaMemcpyDeviceToHost, a->stream));
+        ACUDA(cudaMemcpyAsync(gout.data(), a->grad_out, (size_t)a->rows * 8, cudaMemcpyDeviceToHost, a->stream));
+        ACUDA(cudaStreamSynchronize(a->stream));
+        for (uint32_t k = 0; k < a->rows; k++) grad_inlet_velocity[k] = gin[k] + gout[k];
+    }
+    ACUDA(cudaStreamSynchronize(a->stream));
+    return BF_OK;
+}
+
+int bf_adjoint_time(bf_adjoint* a, int32_t repeats, float* forward_ms, float* backward_ms) {
+    if (!a || repeats <= 0) return afail(BF_ERR_INVALID_ARGUMENT, "bf_adjoint_time: bad argument");
+    cudaEvent_t e0, e1, e2;
+    ACUDA(cudaEventCreate(&e0));
+    ACUDA(cudaEventCreate(&e1));
+    ACUDA(cudaEventCreate(&e2));
+    float fsum = 0.f, bsum = 0.f;
+    int r = BF_OK;
+    for (int k = 0; k < repeats && r == BF_OK; k++) {
+        cudaEventRecord(e0, a->stream);
+        r = run_graph(a, &a->fwd_graph, true);
+        if (r != BF_OK) break;
+        a->forward_done = true;
+        cudaEventRecord(e1, a->stream);
+        r = run_graph(a, &a->bwd_graph, false);
+        if (r != BF_OK) break;
+        cudaEventRecord(e2, a->stream);
+        cudaEventSynchronize(e2);
+        float f = 0.f, b = 0.f;
+        cudaEventElapsedTime(&f, e0, e1);
+        cudaEventElapsedTime(&b, e1, e2);
+        fsum += f;
+        bsum += b;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaEventDestroy(e2);
+    if (r != BF_OK) return r;
+    if (forward_ms) *forward_ms = fsum / repeats;
+    if (backward_ms) *backward_ms = bsum / repeats;
+    return BF_OK;
+}
+
+}  // extern "C"

@@ -152,6 +152,14 @@ ABI = {
     "bf_pack_boundries": (C.c_int, [C.c_void_p, C.c_size_t, C.c_int32, C.c_void_p, C.c_size_t,
                                     C.POINTER(C.c_size_t)]),
     "bf_reduce_field_noalloc": (C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.POINTER(C.c_double)]),
+    "bf_adjoint_desc_default": (None, [C.c_void_p]),
+    "bf_adjoint_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_void_p]),
+    "bf_adjoint_destroy": (C.c_int, [C.c_void_p]),
+    "bf_adjoint_set_parameters": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "bf_adjoint_set_target": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "bf_adjoint_forward": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "bf_adjoint_backward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "bf_adjoint_time": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
 }
 
 _lib = None

@@ -220,6 +220,45 @@ int bf_benchmark_steps(bf_solver* s, int32_t n_steps, float* ms);
 int bf_save_snapshot(bf_solver* s, const char* path);
 int bf_load_snapshot(bf_solver* s, const char* path);
 
+/* ---- differentiable channel flow and its discrete adjoint ---------------- */
+/* No counterpart in the reference (it has no adjoint).  A forward/backward
+ * pair over the model
+ *   pull   g_i(x) = f_i(x - c_i); halfway bounce-back walls where the source
+ *          is outside in y; g_i = feq_i(1, (u_in(y,z),0,0)) where it is outside
+ *          in x (equilibrium inlet and outlet); periodic in z
+ *   BGK    g^c = g + (feq(rho,u) - g)/tau,   PSM  f_i = (1-s) g^c_i + s g_opp(i)
+ *   f^0 = feq(1, (u_in,0,0)),  J = wd sum 2 s j_x + wm sum |u - u*|^2 at step T,
+ * D2Q9 (resolution[2] = 1) or D3Q19.  bf_adjoint_forward runs T steps and
+ * stores a checkpoint every checkpoint_interval steps; bf_adjoint_backward
+ * recomputes each segment from its checkpoint and runs the hand-written
+ * adjoint (transposed pull and transposed BGK/PSM Jacobian), accumulating
+ * dJ/ds (per cell) and dJ/du_in (per (y,z) row) in FP64. */
+typedef struct bf_adjoint bf_adjoint;
+typedef struct {
+    int32_t resolution[3];
+    float relaxation_time;
+    int32_t velocity_set;          /* BF_D2Q9 or BF_D3Q19 */
+    int32_t steps;                 /* T */
+    int32_t checkpoint_interval;   /* K */
+    float drag_weight;             /* wd */
+    float mismatch_weight;         /* wm */
+    int32_t reserved[8];
+} bf_adjoint_desc;
+/* 512 x 256 x 1 D2Q9, tau 0.6, T 2000, K 100, wd = wm = 1 */
+void bf_adjoint_desc_default(bf_adjoint_desc* desc);
+int bf_adjoint_create(bf_adjoint** out, const bf_adjoint_desc* desc);
+int bf_adjoint_destroy(bf_adjoint* a);
+/* host arrays: solid fraction s[N] (x fastest), inlet profile u_in[ny*nz]; either may be NULL to keep it */
+int bf_adjoint_set_parameters(bf_adjoint* a, const float* solid_fraction, const float* inlet_velocity);
+/* host array u*[3N] */
+int bf_adjoint_set_target(bf_adjoint* a, const float* u_target);
+/* forward solve; *objective = J (FP64 sum) */
+int bf_adjoint_forward(bf_adjoint* a, double* objective);
+/* gradients of the last forward's J: grad_solid_fraction[N], grad_inlet_velocity[ny*nz] (host, FP64) */
+int bf_adjoint_backward(bf_adjoint* a, double* grad_solid_fraction, double* grad_inlet_velocity);
+/* mean device milliseconds of `repeats` forward and backward passes (CUDA events) */
+int bf_adjoint_time(bf_adjoint* a, int32_t repeats, float* forward_ms, float* backward_ms);
+
 /* ---- allocation-free reduction ------------------------------------------ */
 /* No counterpart in the reference.  FP64 {mass, momentum x, y, z, kinetic
  * energy 0.5*rho*|u|^2} of n_cells float4 (u.xyz, rho) cells in device

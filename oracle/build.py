@@ -15,8 +15,9 @@ OUT = os.path.join(HERE, "_build")
 def build(verbose=False):
     os.makedirs(OUT, exist_ok=True)
     src = os.path.join(HERE, "lbm_oracle.c")
+    adj = os.path.join(HERE, "adjoint_oracle.c")
     so = os.path.join(OUT, "liboracle.so")
-    if os.path.exists(so) and os.path.getmtime(so) > os.path.getmtime(src):
+    if os.path.exists(so) and os.path.getmtime(so) > max(os.path.getmtime(src), os.path.getmtime(adj)):
         return so
     flags = ["-O2", "-std=c11", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-fopenmp"]
     objs = []
@@ -27,6 +28,9 @@ def build(verbose=False):
             print(" ".join(cmd))
         subprocess.check_call(cmd)
         objs.append(obj)
+    obj = os.path.join(OUT, "adjoint64.o")
+    subprocess.check_call(["gcc", *flags, "-c", adj, "-o", obj])
+    objs.append(obj)
     tmp = so + ".tmp"
     subprocess.check_call(["gcc", "-shared", "-fopenmp", "-o", tmp, *objs, "-lm"])
     os.replace(tmp, so)

@@ -55,6 +55,14 @@ def load():
         getattr(lib, p + "bits_per_boundry").restype = C.c_int
         getattr(lib, p + "pack_boundries").argtypes = [C.c_void_p, C.c_size_t, C.c_int, C.c_void_p, C.c_size_t]
         getattr(lib, p + "pack_boundries").restype = C.c_size_t
+    lib.adj_create.restype = C.c_void_p
+    lib.adj_create.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_void_p, C.c_void_p,
+                               C.c_void_p, C.c_double, C.c_double]
+    lib.adj_destroy.argtypes = [C.c_void_p]
+    lib.adj_set_params.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.adj_forward.argtypes = [C.c_void_p]
+    lib.adj_forward.restype = C.c_double
+    lib.adj_backward.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
     lib.orc32_f32_to_f16.argtypes = [C.c_float]
     lib.orc32_f32_to_f16.restype = C.c_uint16
     lib.orc32_f16_to_f32.argtypes = [C.c_uint16]
@@ -217,3 +225,39 @@ def pack_boundries(ids, bits):
     lib.orc32_pack_boundries(ids.ctypes.data_as(C.c_void_p), ids.size, int(bits), out.ctypes.data_as(C.c_void_p),
                              words + 1)
     return out[:words]
+
+
+class AdjointOracle:
+    """FP64 reference of the differentiable channel model and its adjoint
+    (oracle/adjoint_oracle.c).  Arrays: s (N,), u_in (ny*nz,), u_target (N, 3)."""
+
+    def __init__(self, resolution, tau, steps, q, s, u_in, u_target, drag_weight=1.0, mismatch_weight=1.0):
+        self.lib = load()
+        nx, ny, nz = (int(v) for v in resolution)
+        self.res = (nx, ny, nz)
+        self.n = nx * ny * nz
+        self._s = np.ascontiguousarray(np.asarray(s, np.float64).reshape(-1))
+        self._u = np.ascontiguousarray(np.asarray(u_in, np.float64).reshape(-1))
+        self._t = np.ascontiguousarray(np.asarray(u_target, np.float64).reshape(-1))
+        self.h = self.lib.adj_create(nx, ny, nz, int(q), float(tau), int(steps), self._s.ctypes.data_as(C.c_void_p),
+                                     self._u.ctypes.data_as(C.c_void_p), self._t.ctypes.data_as(C.c_void_p),
+                                     float(drag_weight), float(mismatch_weight))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.adj_destroy(self.h)
+            self.h = None
+
+    def set_params(self, s, u_in):
+        self._s = np.ascontiguousarray(np.asarray(s, np.float64).reshape(-1))
+        self._u = np.ascontiguousarray(np.asarray(u_in, np.float64).reshape(-1))
+        self.lib.adj_set_params(self.h, self._s.ctypes.data_as(C.c_void_p), self._u.ctypes.data_as(C.c_void_p))
+
+    def forward(self):
+        return self.lib.adj_forward(self.h)
+
+    def backward(self):
+        gs = np.zeros(self.n, np.float64)
+        gu = np.zeros(self.res[1] * self.res[2], np.float64)
+        self.lib.adj_backward(self.h, gs.ctypes.data_as(C.c_void_p), gu.ctypes.data_as(C.c_void_p))
+        return gs, gu

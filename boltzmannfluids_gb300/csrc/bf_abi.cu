@@ -7,6 +7,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <string>
@@ -65,7 +66,7 @@ int q_of(int vs) {
     }
     return 0;
 }
-size_t storage_bytes(int st) { return st == BF_STORE_FP32 ? 4 : 2; }
+size_t storage_bytes(int st) { return st == BF_STORE_FP64 ? 8 : (st == BF_STORE_FP32 ? 4 : 2); }
 
 // LBM.cpp:569 / :606: bits per id = exp2(ceil(log2(ceil(log2(count))))), 0 for one object
 int bits_per_boundry(int count) {
@@ -103,6 +104,7 @@ struct bf_solver {
     // graphs keyed by the state that repeats every two steps
     std::map<int, cudaGraphExec_t> graphs;
     bool graphs_enabled = true;
+    uint32_t pf_blocks = 0;  // L2 prefetch distance of the fast kernel, in blocks (0 = off)
 };
 
 namespace {
@@ -190,6 +192,31 @@ void fill_constants(bf_solver* s, StepParams& p) {
     p.Rtau_t = 1.0f / s->desc.thermal_relaxation_time;
     p.beta = s->desc.thermal_expansion_coefficient;
     p.G = s->desc.intermolecular_interaction_strength;
+    // FP64 reference stepper: the same constants in double from the same inputs
+    const double cs_d = 1.0 / std::sqrt(3.0);
+    const double cs2_d = cs_d * cs_d, cs4_d = cs2_d * cs2_d;
+    const double tau_d = (double)tau;
+    p.k64.R2 = 1.0 / cs2_d;
+    p.k64.R4 = 1.0 / cs4_d;
+    p.k64.R2h = p.k64.R2 * 0.5;
+    p.k64.R4h = p.k64.R4 * 0.5;
+    p.k64.Rtau = 1.0 / tau_d;
+    p.k64.P = 1.0 - 1.0 / (2.0 * tau_d);
+    p.k64.Wm = 1.0 / ((double)s->desc.trt_magic / (tau_d - 0.5) + 0.5);
+    p.k64.Pp = 1.0 - p.k64.Rtau * 0.5;
+    p.k64.Pm = 1.0 - p.k64.Wm * 0.5;
+    p.k64.vlim = (double)s->desc.velocity_limit;
+    p.k64.vlim_ext = (double)s->desc.velocity_limit_extreme;
+    for (int k = 0; k < 3; k++) p.k64.fconst[k] = (double)s->fconst[k];
+}
+
+template <int Q>
+void fill_uoff(StepParams& p) {
+    const uint32_t nx = (uint32_t)p.nx, nxy = (uint32_t)p.nx * (uint32_t)p.ny;
+    for (int i = 0; i < Q; i++) {
+        const Dir c = Lattice<Q>::c(i);
+        p.uoff[i] = (uint32_t)i * (uint32_t)p.stride - ((uint32_t)c.y * nx + (uint32_t)c.z * nxy);
+    }
 }
 
 // LBM::_collide (LBM.cpp:1557-1653): one launch of the fused AA step, then the swaps
@@ -227,7 +254,20 @@ cudaError_t collide(bf_solver* s, bool save, bool update, bool reduce, bool meas
     const uint32_t heavy = F_BOUNDARIES | F_FORCE_FIELD | F_THERMAL | F_MULTIPHASE | F_EQ_BOUNDARIES;
     const bool all_periodic = (p.flags & (F_PERIODIC_X | F_PERIODIC_Y | F_PERIODIC_Z)) ==
                               (F_PERIODIC_X | F_PERIODIC_Y | F_PERIODIC_Z);
-    const bool generic = mode == AA_LOCAL || (p.flags & heavy) || !all_periodic;
+    // the fast kernel indexes every slot with 32 bits off the first plane
+    const bool idx32 = (uint64_t)s->N * (uint64_t)s->Q < (1ull << 32);
+    const bool generic = mode == AA_LOCAL || (p.flags & heavy) || !all_periodic || !idx32;
+    // the prefetch rounds each row range out to 16 bytes, which stays inside
+    // the plane only when every plane starts and ends on a 16-byte boundary
+    const size_t plane_bytes = (size_t)s->N * storage_bytes(s->desc.storage);
+    if (!generic && plane_bytes % 16 == 0 && reinterpret_cast<uintptr_t>(lat_src(s)) % 16 == 0)
+        p.pf_blocks = s->pf_blocks;
+    switch (s->Q) {
+    case 9: fill_uoff<9>(p); break;
+    case 15: fill_uoff<15>(p); break;
+    case 19: fill_uoff<19>(p); break;
+    default: fill_uoff<27>(p); break;
+    }
     cudaError_t e = dispatch_step(s, p, mode, generic);
     if (e != cudaSuccess) return e;
     if (measure) return cudaSuccess;
@@ -435,6 +475,13 @@ int bf_create(bf_solver** out) {
     fluid.effective_density = 1.0f;
     s->objects.push_back(fluid);
     bf_init_desc_default(&s->desc);
+    // fast-kernel L2 prefetch distance: one wave of resident blocks (4 blocks
+    // of 256 threads per SM; longer distances measured slower for FP32 at
+    // 512^3); BF_PREFETCH_BLOCKS overrides (0 = off)
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
+    s->pf_blocks = (uint32_t)std::max(sms, 1) * 4u;
+    if (const char* env = std::getenv("BF_PREFETCH_BLOCKS")) s->pf_blocks = (uint32_t)std::strtoul(env, nullptr, 10);
     *out = s;
     return BF_OK;
 }
@@ -484,7 +531,11 @@ int bf_initialize_fields(bf_solver* s, const bf_init_desc* d, const float* densi
     const uint64_t N64 = (uint64_t)rx * ry * rz;
     if (N64 >= (1ull << 32) || ry > 65535 || rz > 65535)
         return fail(BF_ERR_INVALID_ARGUMENT, "initialize_fields(): at most 2^32-1 cells and 65535 cells along y and z");
-    if (d->storage < BF_STORE_FP32 || d->storage > BF_STORE_FP16C) return fail(BF_ERR_INVALID_ARGUMENT, "initialize_fields(): unknown storage");
+    if (d->storage < BF_STORE_FP32 || d->storage > BF_STORE_FP64) return fail(BF_ERR_INVALID_ARGUMENT, "initialize_fields(): unknown storage");
+    if (d->storage == BF_STORE_FP64 &&
+        (!d->esoteric || !d->periodic[0] || !d->periodic[1] || !d->periodic[2] || d->multiphase ||
+         N64 * (uint64_t)Q >= (1ull << 32)))
+        return fail(BF_ERR_INVALID_ARGUMENT, "initialize_fields(): FP64 storage (the accuracy reference stepper) covers fully periodic esoteric-pull boxes only");
     if (!(d->relaxation_time > 0.5f)) return fail(BF_ERR_INVALID_ARGUMENT, "initialize_fields(): relaxation_time must exceed 0.5");
     if (d->collision == BF_COLLISION_TRT && !(d->trt_magic > 0.f)) return fail(BF_ERR_INVALID_ARGUMENT, "initialize_fields(): TRT magic parameter must be positive");
 
@@ -527,6 +578,8 @@ int bf_initialize_fields(bf_solver* s, const bf_init_desc* d, const float* densi
     if (s->bits > 8) return fail(BF_ERR_INVALID_ARGUMENT, "too many objects are defined, maximum of 255 bits are possible but number of objets were: " + std::to_string(nobj));
     s->has_eq_objects = false;
     for (int k = 1; k < nobj; k++) if (s->objects[k].kind != BF_OBJECT_SOLID) s->has_eq_objects = true;
+    if (d->storage == BF_STORE_FP64 && (s->boundaries || s->thermal || !s->constant_force))
+        return fail(BF_ERR_INVALID_ARGUMENT, "initialize_fields(): FP64 storage (the accuracy reference stepper) takes no boundary objects, temperature field or force field");
 
     const size_t sb = storage_bytes(d->storage);
     const size_t lat_bytes = (size_t)N * Q * sb;
@@ -567,7 +620,7 @@ int bf_initialize_fields(bf_solver* s, const bf_init_desc* d, const float* densi
     BF_CUDA(cudaMemcpy(s->bnd_tex.p, tex_h.data(), N, cudaMemcpyHostToDevice));
 
     // host staging of the lambda results
-    DeviceBuf d_rho, d_u, d_ids, d_T;
+    DeviceBuf d_rho, d_u, d_ids;
     BF_CUDA(d_rho.alloc((size_t)N * 4));
     BF_CUDA(d_u.alloc((size_t)N * 12));
     {

@@ -21,8 +21,11 @@
 // with w = 1/tau and B_k = feq_k/(w_k rho).  Parameter gradients accumulate in
 // FP64 (per-cell terms are summed in FP32 first).  The forward trajectory is
 // checkpointed every K steps; the forward leaves the last segment's states in
-// the K-state segment buffer and every earlier segment is recomputed into it
-// from its checkpoint before its adjoint sweep.
+// a segment buffer and every earlier segment is recomputed from its
+// checkpoint.  Two segment buffers alternate: the recomputation of segment
+// k-1 runs on a second stream while the adjoint sweep of segment k runs on
+// the first (both are captured into one graph with event edges), so the
+// recomputation is hidden behind the sweep as far as the GPU has room.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -286,10 +289,11 @@ struct bf_adjoint {
     int Q = 0;
     uint32_t n = 0, rows = 0, nblocks = 0;
     int nseg = 0;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr, side = nullptr;
+    std::vector<cudaEvent_t> events;  // fork, join, then per segment: recomputed, swept
     std::vector<void*> allocs;
     float *s = nullptr, *uin = nullptr, *ustar = nullptr;
-    std::vector<float*> ckpt, seg;
+    std::vector<float*> ckpt, seg[2];
     float *pp[2] = {nullptr, nullptr}, *lam[2] = {nullptr, nullptr};
     double *grad_s = nullptr, *grad_in = nullptr, *grad_out = nullptr, *partials = nullptr, *J = nullptr;
     cudaGraphExec_t fwd_graph = nullptr, bwd_graph = nullptr;
@@ -341,7 +345,7 @@ cudaError_t enqueue_forward(bf_adjoint* a) {
     // backward sweep starts, so that segment needs no recomputation
     const int t_last = (a->nseg - 1) * K;
     for (int t = 1; t < T; t++) {
-        float* dst = (t % K == 0) ? a->ckpt[t / K] : (t > t_last ? a->seg[t - t_last] : a->pp[t & 1]);
+        float* dst = (t % K == 0) ? a->ckpt[t / K] : (t > t_last ? a->seg[(a->nseg - 1) & 1][t - t_last] : a->pp[t & 1]);
         p.f_prev = cur;
         p.f_next = dst;
         adj_forward_kernel<Q, false><<<grid, block, 0, a->stream>>>(p);
@@ -358,25 +362,36 @@ template <int Q>
 cudaError_t enqueue_backward(bf_adjoint* a) {
     int block;
     const dim3 grid = adj_grid(a, block);
-    const int T = a->d.steps, K = a->d.checkpoint_interval;
+    const int T = a->d.steps, K = a->d.checkpoint_interval, nseg = a->nseg;
     AdjParams p = base_params(a);
     cudaMemsetAsync(a->grad_s, 0, (size_t)a->n * sizeof(double), a->stream);
     cudaMemsetAsync(a->grad_in, 0, (size_t)a->rows * sizeof(double), a->stream);
     cudaMemsetAsync(a->grad_out, 0, (size_t)a->rows * sizeof(double), a->stream);
-    int cur_lam = -1;  // index of the buffer holding the adjoint of f^t
-    for (int k = a->nseg - 1; k >= 0; k--) {
+    cudaEvent_t ev_fork = a->events[0], ev_join = a->events[1];
+    auto ev_recomputed = [&](int k) { return a->events[2 + 2 * k]; };
+    auto ev_swept = [&](int k) { return a->events[3 + 2 * k]; };
+    // recompute f^(t0+1) .. f^(t1-1) of segment k into its buffer, on the side stream
+    auto recompute = [&](int k) {
         const int t0 = k * K, t1 = std::min(t0 + K, T);
-        // recompute f^(t0+1) .. f^(t1-1) into seg[1..] (the forward left the
-        // last segment there already)
+        AdjParams q = p;
         const float* prev = a->ckpt[k];
-        for (int j = 1; j <= t1 - 1 - t0 && k != a->nseg - 1; j++) {
-            p.f_prev = prev;
-            p.f_next = a->seg[j];
-            adj_forward_kernel<Q, false><<<grid, block, 0, a->stream>>>(p);
-            prev = a->seg[j];
+        for (int j = 1; j <= t1 - 1 - t0; j++) {
+            q.f_prev = prev;
+            q.f_next = a->seg[k & 1][j];
+            adj_forward_kernel<Q, false><<<grid, block, 0, a->side>>>(q);
+            prev = q.f_next;
         }
+        cudaEventRecord(ev_recomputed(k), a->side);
+    };
+    cudaEventRecord(ev_fork, a->stream);
+    cudaStreamWaitEvent(a->side, ev_fork, 0);
+    if (nseg >= 2) recompute(nseg - 2);  // the forward left segment nseg-1 in place
+    int cur_lam = -1;  // index of the buffer holding the adjoint of f^t
+    for (int k = nseg - 1; k >= 0; k--) {
+        const int t0 = k * K, t1 = std::min(t0 + K, T);
+        if (k != nseg - 1) cudaStreamWaitEvent(a->stream, ev_recomputed(k), 0);
         for (int t = t1; t >= t0 + 1; t--) {
-            p.f_prev = (t - 1 == t0) ? a->ckpt[k] : a->seg[t - 1 - t0];
+            p.f_prev = (t - 1 == t0) ? a->ckpt[k] : a->seg[k & 1][t - 1 - t0];
             const int out = cur_lam == 0 ? 1 : 0;
             p.lam_out = a->lam[out];
             if (t == T) {
@@ -388,7 +403,15 @@ cudaError_t enqueue_backward(bf_adjoint* a) {
             }
             cur_lam = out;
         }
+        cudaEventRecord(ev_swept(k), a->stream);
+        // segment k-2 reuses this segment's buffer once its sweep is done
+        if (k - 2 >= 0) {
+            cudaStreamWaitEvent(a->side, ev_swept(k), 0);
+            recompute(k - 2);
+        }
     }
+    cudaEventRecord(ev_join, a->side);
+    cudaStreamWaitEvent(a->stream, ev_join, 0);
     p.lam_in = a->lam[cur_lam];
     adj_init_grad_kernel<Q><<<dim3((unsigned)a->d.resolution[1], (unsigned)a->d.resolution[2]), kAdjBlock, 0, a->stream>>>(p);
     return cudaGetLastError();
@@ -436,6 +459,8 @@ int bf_adjoint_destroy(bf_adjoint* a) {
     if (a->fwd_graph) cudaGraphExecDestroy(a->fwd_graph);
     if (a->bwd_graph) cudaGraphExecDestroy(a->bwd_graph);
     for (void* p : a->allocs) cudaFree(p);
+    for (cudaEvent_t ev : a->events) if (ev) cudaEventDestroy(ev);
+    if (a->side) cudaStreamDestroy(a->side);
     if (a->stream) cudaStreamDestroy(a->stream);
     delete a;
     return BF_OK;
@@ -480,8 +505,14 @@ int bf_adjoint_create(bf_adjoint** out, const bf_adjoint_desc* d) {
     if (e == cudaSuccess) e = alloc((size_t)a->n * 12, (void**)&a->ustar);
     a->ckpt.assign(a->nseg, nullptr);
     for (int k = 0; k < a->nseg && e == cudaSuccess; k++) e = alloc(state, (void**)&a->ckpt[k]);
-    a->seg.assign(d->checkpoint_interval, nullptr);
-    for (int j = 1; j < d->checkpoint_interval && e == cudaSuccess; j++) e = alloc(state, (void**)&a->seg[j]);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&a->side, cudaStreamNonBlocking);
+    for (int b = 0; b < (a->nseg >= 2 ? 2 : 1); b++) {
+        a->seg[b].assign(d->checkpoint_interval, nullptr);
+        for (int j = 1; j < d->checkpoint_interval && e == cudaSuccess; j++) e = alloc(state, (void**)&a->seg[b][j]);
+    }
+    a->events.assign(2 + 2 * (size_t)a->nseg, nullptr);
+    for (size_t k = 0; k < a->events.size() && e == cudaSuccess; k++)
+        e = cudaEventCreateWithFlags(&a->events[k], cudaEventDisableTiming);
     for (int k = 0; k < 2 && e == cudaSuccess; k++) e = alloc(state, (void**)&a->pp[k]);
     for (int k = 0; k < 2 && e == cudaSuccess; k++) e = alloc(state, (void**)&a->lam[k]);
     if (e == cudaSuccess) e = alloc((size_t)a->n * 8, (void**)&a->grad_s);

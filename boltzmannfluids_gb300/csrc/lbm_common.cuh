@@ -26,6 +26,9 @@ template <> struct Lattice<9> {
     __host__ __device__ static constexpr float w(int i) {
         return i == 0 ? float(4.0 / 9) : (i < 5 ? float(1.0 / 9) : float(1.0 / 36));
     }
+    __host__ __device__ static constexpr double wd(int i) {
+        return i == 0 ? 4.0 / 9 : (i < 5 ? 1.0 / 9 : 1.0 / 36);
+    }
 };
 template <> struct Lattice<15> {
     static constexpr int D = 3;
@@ -37,6 +40,9 @@ template <> struct Lattice<15> {
     }
     __host__ __device__ static constexpr float w(int i) {
         return i == 0 ? float(2.0 / 9) : (i < 7 ? float(1.0 / 9) : float(1.0 / 72));
+    }
+    __host__ __device__ static constexpr double wd(int i) {
+        return i == 0 ? 2.0 / 9 : (i < 7 ? 1.0 / 9 : 1.0 / 72);
     }
 };
 template <> struct Lattice<19> {
@@ -51,6 +57,9 @@ template <> struct Lattice<19> {
     __host__ __device__ static constexpr float w(int i) {
         return i == 0 ? float(1.0 / 3) : (i < 7 ? float(1.0 / 18) : float(1.0 / 36));
     }
+    __host__ __device__ static constexpr double wd(int i) {
+        return i == 0 ? 1.0 / 3 : (i < 7 ? 1.0 / 18 : 1.0 / 36);
+    }
 };
 template <> struct Lattice<27> {
     static constexpr int D = 3;
@@ -64,6 +73,9 @@ template <> struct Lattice<27> {
     }
     __host__ __device__ static constexpr float w(int i) {
         return i == 0 ? float(8.0 / 27) : (i < 7 ? float(2.0 / 27) : (i < 19 ? float(1.0 / 54) : float(1.0 / 216)));
+    }
+    __host__ __device__ static constexpr double wd(int i) {
+        return i == 0 ? 8.0 / 27 : (i < 7 ? 2.0 / 27 : (i < 19 ? 1.0 / 54 : 1.0 / 216));
     }
 };
 // thermal sets D2Q5 / D3Q7
@@ -83,13 +95,23 @@ template <> struct ThermalLattice<7> {
     __host__ __device__ static constexpr float w(int i) { return i == 0 ? float(1.0 / 4) : float(1.0 / 8); }
 };
 
+// weight of direction i in the arithmetic type R (float: the reference's
+// FP32 constants; double: the FP64 reference stepper)
+template <int Q, class R> struct LatticeW;
+template <int Q> struct LatticeW<Q, float> {
+    __host__ __device__ static constexpr float w(int i) { return Lattice<Q>::w(i); }
+};
+template <int Q> struct LatticeW<Q, double> {
+    __host__ __device__ static constexpr double w(int i) { return Lattice<Q>::wd(i); }
+};
+
 // collide.comp:219-222: opp(i) = i odd ? i+1 : i-1, opp(0) = 0
 __host__ __device__ constexpr int opp(int i) { return i == 0 ? 0 : ((i & 1) ? i + 1 : i - 1); }
 
 // ---------------------------------------------------------------------------
 // storage codecs: encode an FP32 population of direction i for the DDF
 // ---------------------------------------------------------------------------
-enum Storage { ST_FP32 = 0, ST_FP16 = 1, ST_FP16S = 2, ST_FP16C = 3 };
+enum Storage { ST_FP32 = 0, ST_FP16 = 1, ST_FP16S = 2, ST_FP16C = 3, ST_FP64 = 4 };
 
 // custom 16-bit "c16": 1 sign, 4 exponent, 11 mantissa bits = the top 15
 // bits of an FP32 scaled by 2^-114 (normal 2^(e-13)*(1+m/2048), subnormal
@@ -108,25 +130,36 @@ __device__ __forceinline__ float decode_c16(uint16_t h) {
 }
 
 template <int ST> struct Codec;
+// T: the stored element type; R: the arithmetic type of the update
 template <> struct Codec<ST_FP32> {
     using T = float;
+    using R = float;
     __device__ __forceinline__ static float dec(T v, float) { return v; }
     __device__ __forceinline__ static T enc(float v, float) { return v; }
 };
 template <> struct Codec<ST_FP16> {  // R16F: IEEE half of f
     using T = __half;
+    using R = float;
     __device__ __forceinline__ static float dec(T v, float) { return __half2float(v); }
     __device__ __forceinline__ static T enc(float v, float) { return __float2half_rn(v); }
 };
 template <> struct Codec<ST_FP16S> {  // IEEE half of f - w
     using T = __half;
+    using R = float;
     __device__ __forceinline__ static float dec(T v, float w) { return __fadd_rn(__half2float(v), w); }
     __device__ __forceinline__ static T enc(float v, float w) { return __float2half_rn(__fsub_rn(v, w)); }
 };
 template <> struct Codec<ST_FP16C> {  // custom 16-bit of (f - w)/w
     using T = uint16_t;
+    using R = float;
     __device__ __forceinline__ static float dec(T v, float w) { return fmaf(decode_c16(v), w, w); }
     __device__ __forceinline__ static T enc(float v, float w) { return encode_c16(__fmul_rn(__fsub_rn(v, w), 1.0f / w)); }
+};
+template <> struct Codec<ST_FP64> {  // FP64 reference stepper: populations and arithmetic in double
+    using T = double;
+    using R = double;
+    __device__ __forceinline__ static double dec(T v, double) { return v; }
+    __device__ __forceinline__ static T enc(double v, double) { return v; }
 };
 
 // ---------------------------------------------------------------------------
@@ -161,6 +194,19 @@ struct alignas(16) StepParams {
     uint32_t flags;
     uint32_t n_cells;
     int bits;                 // bits per boundary id (0, 1, 2, 4, 8)
+    // fast kernel: blocks ahead (in launch order) whose population rows a
+    // block prefetches into L2 with bulk copies; 0 = off.  Only set when every
+    // population plane starts and ends on a 16-byte boundary.
+    uint32_t pf_blocks;
+    // fast kernel, even step, rows off the y/z faces: element offset of the
+    // slot read for direction i relative to the cell, without its x part:
+    // i * stride - (c_y nx + c_z nx ny), modulo 2^32
+    uint32_t uoff[27];
+    // FP64 reference stepper: the launch constants in double, computed as the
+    // FP64 oracle does (cs = 1/sqrt(3), tau and the limits from the FP32 inputs)
+    struct {
+        double R2, R4, R2h, R4h, Rtau, P, Wm, Pp, Pm, vlim, vlim_ext, fconst[3];
+    } k64;
     // launch constants, FP32, computed on the host exactly as the oracle
     // does: cs = float(1/sqrt(3)), cs2 = cs*cs, cs4 = cs2*cs2
     float R2;                 // 1/cs2

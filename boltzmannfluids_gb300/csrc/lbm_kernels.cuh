@@ -16,7 +16,8 @@
 
 namespace bf {
 
-struct CellSum { float m, px, py, pz, ke; };
+template <class R> struct CellSumT { R m, px, py, pz, ke; };
+using CellSum = CellSumT<float>;
 
 // Rounded, never-contracted FP32 operations: the kernels evaluate the same
 // expression tree as the oracle's canonical FP32 restatement, so FP32
@@ -25,9 +26,20 @@ struct CellSum { float m, px, py, pz, ke; };
 // u = j * (1/rho) with one IEEE division, opposite populations are summed
 // pairwise (s = f_i + f_opp, d = f_i - f_opp), and the multiply-adds marked
 // FFMA are single-rounding fused operations (C's fmaf on the host side).
-#define FMUL __fmul_rn
-#define FADD __fadd_rn
-#define FSUB __fsub_rn
+// The same operations in double drive the FP64 reference stepper.
+__device__ __forceinline__ float r_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float r_add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float r_sub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float r_fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ float r_div(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double r_mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double r_add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double r_sub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double r_fma(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ double r_div(double a, double b) { return __ddiv_rn(a, b); }
+#define FMUL r_mul
+#define FADD r_add
+#define FSUB r_sub
 
 // exp for the pseudopotential psi = 1 - exp(-rho), the same operations as the
 // oracle's exp_f32: Cody-Waite reduction x = k ln2 + r (ln2 split in a 15-bit
@@ -60,21 +72,24 @@ __device__ __forceinline__ float cdot(float vx, float vy, float vz) {
     if (CZ != 0) { const float t = CZ > 0 ? vz : -vz; acc = first ? t : FADD(acc, t); first = false; }
     return acc;
 }
-__device__ __forceinline__ float cdot_rt(const Dir c, float vx, float vy, float vz) {
-    float acc = 0.0f;
+template <class R>
+__device__ __forceinline__ R cdot_rt(const Dir c, R vx, R vy, R vz) {
+    R acc = R(0);
     bool first = true;
     if (c.x != 0) { acc = c.x > 0 ? vx : -vx; first = false; }
-    if (c.y != 0) { const float t = c.y > 0 ? vy : -vy; acc = first ? t : FADD(acc, t); first = false; }
-    if (c.z != 0) { const float t = c.z > 0 ? vz : -vz; acc = first ? t : FADD(acc, t); first = false; }
+    if (c.y != 0) { const R t = c.y > 0 ? vy : -vy; acc = first ? t : FADD(acc, t); first = false; }
+    if (c.z != 0) { const R t = c.z > 0 ? vz : -vz; acc = first ? t : FADD(acc, t); first = false; }
     return acc;
 }
-#define FFMA __fmaf_rn
+#define FFMA r_fma
 // u.u = fma(uz, uz, fma(uy, uy, ux*ux))
-__device__ __forceinline__ float uu_of(float ux, float uy, float uz) {
+template <class R>
+__device__ __forceinline__ R uu_of(R ux, R uy, R uz) {
     return FFMA(uz, uz, FFMA(uy, uy, FMUL(ux, ux)));
 }
 // (1 + cu/cs2 + cu^2/2/cs4 - uu/2/cs2) = fma(cu^2, R4/2, fma(cu, R2, 1 - uu R2/2))
-__device__ __forceinline__ float bracket(float cu, float one_m, float R2, float R4h) {
+template <class R>
+__device__ __forceinline__ R bracket(R cu, R one_m, R R2, R R4h) {
     return FFMA(FMUL(cu, cu), R4h, FFMA(cu, R2, one_m));
 }
 
@@ -94,7 +109,8 @@ __device__ __forceinline__ bool solid_id(const uint8_t* __restrict__ kind, uint3
 }
 
 // FP64 block reduction of the five conserved sums; one partial per block.
-__device__ __forceinline__ void block_reduce_store(CellSum cs, double* __restrict__ out) {
+template <class R>
+__device__ __forceinline__ void block_reduce_store(CellSumT<R> cs, double* __restrict__ out) {
     double v[5] = {(double)cs.m, (double)cs.px, (double)cs.py, (double)cs.pz, (double)cs.ke};
 #pragma unroll
     for (int k = 0; k < 5; k++)
@@ -126,21 +142,22 @@ __device__ __forceinline__ void block_reduce_store(CellSum cs, double* __restric
 // ---------------------------------------------------------------------------
 // moments, limiter and collision shared by the fast and the generic kernels
 // ---------------------------------------------------------------------------
-struct Moments {
-    float rho, ux, uy, uz, Fx, Fy, Fz;
+template <class R> struct MomentsT {
+    R rho, ux, uy, uz, Fx, Fy, Fz;
     bool out_ext;
 };
+using Moments = MomentsT<float>;
 
 // s_k = f_i + f_opp, d_k = f_i - f_opp for the pair (i, i+1), i = 2k+1
-template <int Q>
-__device__ __forceinline__ float pair_sum(const float (&f)[Q], int i) { return FADD(f[i], f[i + 1]); }
-template <int Q>
-__device__ __forceinline__ float pair_diff(const float (&f)[Q], int i) { return FSUB(f[i], f[i + 1]); }
+template <int Q, class R>
+__device__ __forceinline__ R pair_sum(const R (&f)[Q], int i) { return FADD(f[i], f[i + 1]); }
+template <int Q, class R>
+__device__ __forceinline__ R pair_diff(const R (&f)[Q], int i) { return FSUB(f[i], f[i + 1]); }
 
 // rho = f_0 + s_1 + s_2 + ...  (collide.comp:383-388, pairwise order)
-template <int Q>
-__device__ __forceinline__ float density_of(const float (&f)[Q]) {
-    float rho = f[0];
+template <int Q, class R>
+__device__ __forceinline__ R density_of(const R (&f)[Q]) {
+    R rho = f[0];
 #pragma unroll
     for (int i = 1; i < Q; i += 2) rho = FADD(rho, pair_sum<Q>(f, i));
     return rho;
@@ -179,6 +196,42 @@ __device__ __forceinline__ void velocity_and_limit(const float (&f)[Q], Moments&
     m.out_ext = uu > t_ext;
     if (uu > t_lim) {  // normalize(u) * limit
         const float q = __fdiv_rn(vlim, sqrtf(uu));
+        m.ux = FMUL(m.ux, q);
+        m.uy = FMUL(m.uy, q);
+        m.uz = FMUL(m.uz, q);
+    }
+}
+
+// FP64 reference stepper: the same moments in double; the limiter compares
+// sqrt(|u|^2) with the limits directly, as the FP64 oracle does.
+template <int Q>
+__device__ __forceinline__ void velocity_and_limit(const double (&f)[Q], MomentsT<double>& m, bool forced,
+                                                   double vlim, double vlim_ext) {
+    using L = Lattice<Q>;
+    double jx = 0.0, jy = 0.0, jz = 0.0;
+    bool fx = true, fy = true, fz = true;
+#pragma unroll
+    for (int i = 1; i < Q; i += 2) {
+        const Dir c = L::c(i);
+        const double d = pair_diff<Q>(f, i);
+        if (c.x) { const double t = c.x > 0 ? d : -d; jx = fx ? t : FADD(jx, t); fx = false; }
+        if (c.y) { const double t = c.y > 0 ? d : -d; jy = fy ? t : FADD(jy, t); fy = false; }
+        if (c.z) { const double t = c.z > 0 ? d : -d; jz = fz ? t : FADD(jz, t); fz = false; }
+    }
+    const double r = __ddiv_rn(1.0, m.rho);
+    m.ux = FMUL(jx, r);
+    m.uy = FMUL(jy, r);
+    m.uz = FMUL(jz, r);
+    if (forced) {
+        const double h = FMUL(r, 0.5);
+        m.ux = FFMA(m.Fx, h, m.ux);
+        m.uy = FFMA(m.Fy, h, m.uy);
+        m.uz = FFMA(m.Fz, h, m.uz);
+    }
+    const double len = __dsqrt_rn(uu_of(m.ux, m.uy, m.uz));
+    m.out_ext = len > vlim_ext;
+    if (len > vlim) {
+        const double q = __ddiv_rn(vlim, len);
         m.ux = FMUL(m.ux, q);
         m.uy = FMUL(m.uy, q);
         m.uz = FMUL(m.uz, q);
@@ -250,68 +303,223 @@ __device__ __forceinline__ void collide_emit(const float (&f)[Q], const Moments&
     }
 }
 
-// ---------------------------------------------------------------------------
-// fast AA step: fully periodic box, no objects, no thermal / Shan-Chen /
-// force field (constant force allowed).  Population planes are addressed
-// through per-plane pointers and 32-bit wrap offsets.
-// ---------------------------------------------------------------------------
-constexpr int kFastMinBlocks = 4;  // 256 threads x 4 blocks: at most 64 registers
+// launch constants of the collision in the arithmetic type
+template <class R> struct Coef { R R2, R4, R2h, R4h, Rtau, P, Wm, Pp, Pm; };
+__device__ __forceinline__ Coef<float> coef_of(const StepParams& p, float) {
+    return Coef<float>{p.R2, p.R4, p.R2h, p.R4h, p.Rtau, p.P, p.Wm, p.Pp, p.Pm};
+}
+__device__ __forceinline__ Coef<double> coef_of(const StepParams& p, double) {
+    return Coef<double>{p.k64.R2, p.k64.R4, p.k64.R2h, p.k64.R4h, p.k64.Rtau, p.k64.P, p.k64.Wm, p.k64.Pp, p.k64.Pm};
+}
 
-template <int Q, int ST, int MODE>
-__global__ void __launch_bounds__(kStepBlock, kFastMinBlocks) fast_step_kernel(const __grid_constant__ StepParams p) {
+// The same arithmetic as collide_emit with the collision model, the source
+// term and the extreme-velocity case fixed at compile time (the fast kernel
+// branches once per cell on the rare extreme case instead of selecting per
+// population); R = float is the canonical FP32 evaluation, R = double the
+// FP64 reference stepper.
+template <int Q, bool TRT, bool SRC, bool EXT, class R, class Emit>
+__device__ __forceinline__ void collide_fixed(const R (&f)[Q], const MomentsT<R>& m, const Coef<R>& k, Emit emit) {
     using L = Lattice<Q>;
-    using C = Codec<ST>;
-    using T = typename C::T;
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    CellSum cs = {0.f, 0.f, 0.f, 0.f, 0.f};
-    if (x < p.nx) {
-        const int y = blockIdx.y, z = blockIdx.z;
-        const int nx = p.nx, ny = p.ny, nz = p.nz, nxy = nx * ny;
-        const uint32_t n = (uint32_t)x + (uint32_t)nx * ((uint32_t)y + (uint32_t)ny * (uint32_t)z);
-        // element offsets to the neighbour at -1 / +1 along each axis, periodic
-        const int oxm = x == 0 ? nx - 1 : -1, oxp = x == nx - 1 ? 1 - nx : 1;
-        const int oym = y == 0 ? (ny - 1) * nx : -nx, oyp = y == ny - 1 ? (1 - ny) * nx : nx;
-        const int ozm = z == 0 ? (nz - 1) * nxy : -nxy, ozp = z == nz - 1 ? (1 - nz) * nxy : nxy;
-        auto at = [&](int dx, int dy, int dz) -> uint32_t {
-            const int o = (dx < 0 ? oxm : (dx > 0 ? oxp : 0)) + (dy < 0 ? oym : (dy > 0 ? oyp : 0)) +
-                          (dz < 0 ? ozm : (dz > 0 ? ozp : 0));
-            return n + (uint32_t)o;  // modular: the true index lies in [0, N)
-        };
-        float f[Q];
+    using W = LatticeW<Q, R>;
+    const R one_m = FSUB(R(1), FMUL(uu_of(m.ux, m.uy, m.uz), k.R2h));
+    const R fuR2 = SRC ? FMUL(FFMA(m.Fz, m.uz, FFMA(m.Fy, m.uy, FMUL(m.Fx, m.ux))), k.R2) : R(0);
+    if (!TRT) {
 #pragma unroll
         for (int i = 0; i < Q; i++) {
             const Dir c = L::c(i);
-            if (MODE == AA_EVEN) f[i] = C::dec(static_cast<const T*>(p.plane[i])[at(-c.x, -c.y, -c.z)], L::w(i));
-            else f[i] = C::dec(static_cast<const T*>(p.plane[opp(i)])[n], L::w(i));
+            const R w = W::w(i);
+            const R cu = cdot_rt(c, m.ux, m.uy, m.uz);
+            const R fe = FMUL(FMUL(w, m.rho), bracket(cu, one_m, k.R2, k.R4h));
+            if (EXT) { emit(i, fe); continue; }
+            R v = FFMA(FSUB(fe, f[i]), k.Rtau, f[i]);
+            if (SRC) {
+                const R fc = cdot_rt(c, m.Fx, m.Fy, m.Fz);
+                v = FFMA(FMUL(k.P, w), FFMA(fc, k.R2, FFMA(FMUL(fc, cu), k.R4, -fuR2)), v);
+            }
+            emit(i, v);
         }
-        Moments m;
-        m.rho = density_of<Q>(f);
-        if (!(m.rho == m.rho)) atomicOr(p.err, 1u);
-        m.rho = m.rho < 0.01f ? 0.01f : m.rho;
-        const bool forced = (p.flags & F_FORCE_CONST) != 0;
-        m.Fx = forced ? p.fconst[0] : 0.f;
-        m.Fy = forced ? p.fconst[1] : 0.f;
-        m.Fz = forced ? p.fconst[2] : 0.f;
-        velocity_and_limit<Q>(f, m, forced, p.vlim, p.t_lim, p.t_ext);
-        if (p.flags & F_UPDATE) {
-            collide_emit<Q>(f, m, p, (p.flags & F_TRT) != 0, (p.flags & F_SOURCE) != 0, false,
-                            [&](int i, float v) {
-                                const Dir c = L::c(i);
-                                if (MODE == AA_EVEN)
-                                    static_cast<T*>(p.plane[opp(i)])[at(c.x, c.y, c.z)] = C::enc(v, L::w(i));
-                                else
-                                    static_cast<T*>(p.plane[i])[n] = C::enc(v, L::w(i));
-                            });
+        return;
+    }
+    {
+        const R w0 = W::w(0);
+        const R fe0 = FMUL(FMUL(w0, m.rho), one_m);
+        if (EXT) {
+            emit(0, fe0);
+        } else {
+            R v = FFMA(FSUB(fe0, f[0]), k.Rtau, f[0]);
+            if (SRC) v = FFMA(FMUL(k.Pp, w0), -fuR2, v);
+            emit(0, v);
         }
-        if (p.flags & F_SAVE) {
-            p.vel_den[n] = make_float4(m.ux, m.uy, m.uz, m.rho);
-            if (p.force_temp) p.force_temp[n] = make_float4(m.Fx, m.Fy, m.Fz, 0.f);
+    }
+#pragma unroll
+    for (int i = 1; i < Q; i += 2) {
+        const int j = i + 1;
+        const Dir c = L::c(i);
+        const R w = W::w(i);
+        const R cu = cdot_rt(c, m.ux, m.uy, m.uz);
+        const R wr = FMUL(w, m.rho);
+        const R ep = FMUL(wr, FFMA(FMUL(cu, cu), k.R4h, one_m));
+        const R em = FMUL(FMUL(wr, k.R2), cu);
+        if (EXT) {
+            emit(i, FADD(ep, em));
+            emit(j, FSUB(ep, em));
+            continue;
         }
-        if (p.flags & F_REDUCE) {
-            const float uu = uu_of(m.ux, m.uy, m.uz);
-            cs.m = m.rho; cs.px = m.rho * m.ux; cs.py = m.rho * m.uy; cs.pz = m.rho * m.uz;
-            cs.ke = 0.5f * m.rho * uu;
+        const R Pd = FFMA(pair_sum<Q>(f, i), R(0.5), -ep);
+        const R Md = FFMA(pair_diff<Q>(f, i), R(0.5), -em);
+        R vi = FFMA(-Md, k.Wm, FFMA(-Pd, k.Rtau, f[i]));
+        R vj = FFMA(Md, k.Wm, FFMA(-Pd, k.Rtau, f[j]));
+        if (SRC) {
+            const R fc = cdot_rt(c, m.Fx, m.Fy, m.Fz);
+            const R Sp = FMUL(FMUL(k.Pp, w), FFMA(FMUL(fc, cu), k.R4, -fuR2));
+            const R Sm = FMUL(FMUL(k.Pm, w), FMUL(fc, k.R2));
+            vi = FADD(vi, FADD(Sp, Sm));
+            vj = FADD(vj, FSUB(Sp, Sm));
         }
+        emit(i, vi);
+        emit(j, vj);
+    }
+}
+
+// L2 prefetch of a byte range with the bulk-copy engine (no registers held,
+// no completion to wait for).  The range must be 16-byte aligned and sized.
+__device__ __forceinline__ void l2_prefetch_bulk(const void* ptr, uint32_t bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(ptr), "r"(bytes) : "memory");
+}
+
+// Prefetch into L2 the population rows that block `b` (linear launch order,
+// x fastest) reads: on an even step row (y - c_y, z - c_z) of plane i over
+// the block's x range widened by 8 cells each side (the c_x shift), on an odd
+// step row (y, z) of every plane.  Ranges are clipped to the row and rounded
+// out to 16 bytes; that stays inside the plane because planes start and end
+// on 16-byte boundaries whenever pf_blocks is set.
+template <int Q, int ST, int MODE>
+__device__ __forceinline__ void prefetch_block_rows(const StepParams& p, uint32_t b) {
+    using L = Lattice<Q>;
+    using T = typename Codec<ST>::T;
+    const uint32_t gx = gridDim.x, gy = gridDim.y;
+    const uint32_t bx = b % gx, yz = b / gx;
+    const int y = (int)(yz % gy), z = (int)(yz / gy);
+    const int nx = p.nx, ny = p.ny, nz = p.nz;
+    const int x0 = (int)(bx * blockDim.x);
+    const int xlo = MODE == AA_EVEN ? max(x0 - 8, 0) : x0;
+    const int xhi = min(x0 + (int)blockDim.x + (MODE == AA_EVEN ? 8 : 0), nx);
+    const uintptr_t plane_bytes = (uintptr_t)p.n_cells * sizeof(T);
+#pragma unroll
+    for (int i = 0; i < Q; i++) {
+        const Dir c = L::c(i);
+        int ys = y, zs = z;
+        if (MODE == AA_EVEN) {
+            ys -= c.y; ys = ys < 0 ? ys + ny : (ys >= ny ? ys - ny : ys);
+            zs -= c.z; zs = zs < 0 ? zs + nz : (zs >= nz ? zs - nz : zs);
+        }
+        const int slot = MODE == AA_EVEN ? i : opp(i);
+        const uintptr_t base = reinterpret_cast<uintptr_t>(p.plane[slot]);
+        const uintptr_t row = (uintptr_t)nx * ((uintptr_t)ys + (uintptr_t)ny * (uintptr_t)zs);
+        const uintptr_t lo = (base + (row + (uintptr_t)xlo) * sizeof(T)) & ~(uintptr_t)15;
+        uintptr_t hi = (base + (row + (uintptr_t)xhi) * sizeof(T) + 15) & ~(uintptr_t)15;
+        hi = min(hi, base + plane_bytes);
+        if (hi > lo) l2_prefetch_bulk(reinterpret_cast<const void*>(lo), (uint32_t)(hi - lo));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// fast AA step: fully periodic box, no objects, no thermal / Shan-Chen /
+// force field (constant force allowed; TRT and forcing fixed per launch).
+// Slots are addressed by 32-bit element indices off the first plane.  Thread 0 of each block prefetches into L2 the rows of the block
+// pf_blocks ahead in launch order, so that the block's own loads mostly hit
+// L2 and 16-bit storage needs fewer loads in flight to saturate HBM.
+// ---------------------------------------------------------------------------
+constexpr int kFastMinBlocks = 4;  // 256 threads x 4 blocks: at most 64 registers (FP64: 2 blocks, 128)
+
+// One cell of the fast step.  EDGE: the block's row lies on a y or z face of
+// the box, so the y/z neighbour offsets wrap and are computed in the block;
+// otherwise they are the launch constants p.uoff (plane offset minus
+// c_y nx + c_z nx ny), one constant-bank operand per index.
+template <int Q, int ST, int MODE, bool TRT, bool FORCED, bool EDGE>
+__device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepParams& p, int x, int y, int z) {
+    using L = Lattice<Q>;
+    using C = Codec<ST>;
+    using T = typename C::T;
+    using R = typename C::R;
+    using W = LatticeW<Q, R>;
+    CellSumT<R> cs = {R(0), R(0), R(0), R(0), R(0)};
+    const int nx = p.nx, ny = p.ny, nz = p.nz, nxy = nx * ny;
+    const uint32_t n = (uint32_t)x + (uint32_t)nx * ((uint32_t)y + (uint32_t)ny * (uint32_t)z);
+    // The planes are contiguous (plane k at element k * stride of plane 0)
+    // and Q * stride < 2^32, so every slot has a 32-bit element index off
+    // one base: n + (plane offset + y/z neighbour offset, uniform over the
+    // block) + x neighbour offset (per thread, periodic).
+    T* const base = static_cast<T*>(p.plane[0]);
+    const uint32_t S = (uint32_t)p.stride;
+    const int oxm = x == 0 ? nx - 1 : -1, oxp = x == nx - 1 ? 1 - nx : 1;
+    const int oym = y == 0 ? (ny - 1) * nx : -nx, oyp = y == ny - 1 ? (1 - ny) * nx : nx;
+    const int ozm = z == 0 ? (nz - 1) * nxy : -nxy, ozp = z == nz - 1 ? (1 - nz) * nxy : nxy;
+    // slot read for direction i; population i is written to the slot read
+    // for opp(i): even (x + c_i, plane opp i), odd (x, plane i)
+    auto slot = [&](int i, uint32_t nn, int xm, int xp) -> uint32_t {
+        if (MODE == AA_EVEN) {
+            const Dir c = L::c(i);
+            const uint32_t u = EDGE ? (uint32_t)i * S + (uint32_t)((c.y > 0 ? oym : (c.y < 0 ? oyp : 0)) +
+                                                                   (c.z > 0 ? ozm : (c.z < 0 ? ozp : 0)))
+                                    : p.uoff[i];
+            return nn + u + (uint32_t)(c.x > 0 ? xm : (c.x < 0 ? xp : 0));
+        }
+        return nn + (uint32_t)opp(i) * S;
+    };
+    R f[Q];
+#pragma unroll
+    for (int i = 0; i < Q; i++) f[i] = C::dec(base[slot(i, n, oxm, oxp)], W::w(i));
+    // the store phase recomputes its indices (one add each) from opaque
+    // copies of the per-thread terms instead of keeping Q indices live
+    uint32_t n_st = n;
+    int oxm_st = oxm, oxp_st = oxp;
+    asm volatile("" : "+r"(n_st), "+r"(oxm_st), "+r"(oxp_st));
+    MomentsT<R> m;
+    m.rho = density_of<Q>(f);
+    if (!(m.rho == m.rho)) atomicOr(p.err, 1u);
+    m.rho = m.rho < R(0.01) ? R(0.01) : m.rho;
+    constexpr bool F64 = sizeof(R) == 8;
+    m.Fx = FORCED ? (F64 ? R(p.k64.fconst[0]) : R(p.fconst[0])) : R(0);
+    m.Fy = FORCED ? (F64 ? R(p.k64.fconst[1]) : R(p.fconst[1])) : R(0);
+    m.Fz = FORCED ? (F64 ? R(p.k64.fconst[2]) : R(p.fconst[2])) : R(0);
+    if constexpr (F64) velocity_and_limit<Q>(f, m, FORCED, p.k64.vlim, p.k64.vlim_ext);
+    else velocity_and_limit<Q>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
+    if (p.flags & F_UPDATE) {
+        const Coef<R> k = coef_of(p, R(0));
+        auto emit = [&](int i, R v) { base[slot(opp(i), n_st, oxm_st, oxp_st)] = C::enc(v, W::w(i)); };
+        if (m.out_ext) collide_fixed<Q, TRT, FORCED, true>(f, m, k, emit);
+        else collide_fixed<Q, TRT, FORCED, false>(f, m, k, emit);
+    }
+    if (p.flags & F_SAVE) {
+        p.vel_den[n] = make_float4((float)m.ux, (float)m.uy, (float)m.uz, (float)m.rho);
+        if (p.force_temp) p.force_temp[n] = make_float4((float)m.Fx, (float)m.Fy, (float)m.Fz, 0.f);
+    }
+    if (p.flags & F_REDUCE) {
+        const R uu = uu_of(m.ux, m.uy, m.uz);
+        cs.m = m.rho; cs.px = m.rho * m.ux; cs.py = m.rho * m.uy; cs.pz = m.rho * m.uz;
+        cs.ke = R(0.5f) * m.rho * uu;
+    }
+    return cs;
+}
+
+template <int Q, int ST, int MODE, bool TRT, bool FORCED>
+__global__ void __launch_bounds__(kStepBlock, ST == ST_FP64 ? 2 : kFastMinBlocks)
+    fast_step_kernel(const __grid_constant__ StepParams p) {
+    if (p.pf_blocks != 0u && threadIdx.x == 0) {
+        const uint32_t b = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z) + p.pf_blocks;
+        if (b < gridDim.x * gridDim.y * gridDim.z) prefetch_block_rows<Q, ST, MODE>(p, b);
+    }
+    using R = typename Codec<ST>::R;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    CellSumT<R> cs = {R(0), R(0), R(0), R(0), R(0)};
+    if (x < p.nx) {
+        // block-uniform choice: rows on a y or z face wrap their neighbour offsets
+        const bool edge = MODE == AA_EVEN &&
+                          (y == 0 || y == p.ny - 1 || (Lattice<Q>::D == 3 && (z == 0 || z == p.nz - 1)));
+        if (edge) cs = fast_cell<Q, ST, MODE, TRT, FORCED, true>(p, x, y, z);
+        else cs = fast_cell<Q, ST, MODE, TRT, FORCED, false>(p, x, y, z);
     }
     if (p.flags & F_REDUCE) block_reduce_store(cs, p.red_partials);
 }
@@ -560,14 +768,16 @@ __global__ void __launch_bounds__(kStepBlock) stream_thermal_kernel(const __grid
 // ---------------------------------------------------------------------------
 // equilibrium initialisation (set_equilibrium_populations.comp:179-221)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ float feq_init_dot(float ax, float ay, float az, float bx, float by, float bz) {
-    return __fadd_rn(__fadd_rn(__fmul_rn(ax, bx), __fmul_rn(ay, by)), __fmul_rn(az, bz));
+template <class R>
+__device__ __forceinline__ R feq_init_dot(R ax, R ay, R az, R bx, R by, R bz) {
+    return r_add(r_add(r_mul(ax, bx), r_mul(ay, by)), r_mul(az, bz));
 }
-__device__ __forceinline__ float feq_init_literal(float w, float r, float cu, float uu) {
-    float a = __fadd_rn(1.0f, __fmul_rn(3.0f, cu));
-    a = __fadd_rn(a, __fdiv_rn(__fmul_rn(9.0f, __fmul_rn(cu, cu)), 2.0f));
-    a = __fsub_rn(a, __fdiv_rn(__fmul_rn(3.0f, uu), 2.0f));
-    return __fmul_rn(__fmul_rn(w, r), a);
+template <class R>
+__device__ __forceinline__ R feq_init_literal(R w, R r, R cu, R uu) {
+    R a = r_add(R(1), r_mul(R(3), cu));
+    a = r_add(a, r_div(r_mul(R(9), r_mul(cu, cu)), R(2)));
+    a = r_sub(a, r_div(r_mul(R(3), uu), R(2)));
+    return r_mul(r_mul(w, r), a);
 }
 
 template <int Q, int ST>
@@ -575,22 +785,23 @@ __global__ void init_kernel(const __grid_constant__ InitParams p) {
     using L = Lattice<Q>;
     using C = Codec<ST>;
     using T = typename C::T;
+    using R = typename C::R;
     const uint64_t n = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (n >= p.n_cells) return;
     T* F = static_cast<T*>(p.f);
-    const float r = p.rho ? p.rho[n] : 1.0f;
-    float ux = 0.f, uy = 0.f, uz = 0.f;
+    const R r = p.rho ? R(p.rho[n]) : R(1);
+    R ux = R(0), uy = R(0), uz = R(0);
     const uint32_t id = p.ids ? p.ids[n] : 0u;
     const bool solid = id != 0u && p.obj_kind[id] == 0;
     if (p.u && !solid) { ux = p.u[3 * n]; uy = p.u[3 * n + 1]; uz = p.u[3 * n + 2]; }
     // w*rho*(1 + 3*cu + 9*cu^2/2 - 3*uu/2) with the shader's literal constants
     // and operation order, rounded operations only (init runs once)
-    const float uu = feq_init_dot(ux, uy, uz, ux, uy, uz);
+    const R uu = feq_init_dot(ux, uy, uz, ux, uy, uz);
 #pragma unroll
     for (int i = 0; i < Q; i++) {
         const Dir c = L::c(i);
-        const float w = L::w(i);
-        const float cu = feq_init_dot((float)c.x, (float)c.y, (float)c.z, ux, uy, uz);
+        const R w = LatticeW<Q, R>::w(i);
+        const R cu = feq_init_dot(R(c.x), R(c.y), R(c.z), ux, uy, uz);
         F[i * p.stride + n] = C::enc(feq_init_literal(w, r, cu, uu), w);
     }
 }
@@ -624,7 +835,8 @@ __global__ void decode_kernel(const void* f, uint64_t stride, uint32_t n_cells, 
     if (n >= n_cells) return;
     const T* F = static_cast<const T*>(f);
 #pragma unroll
-    for (int i = 0; i < Q; i++) out[(uint64_t)i * n_cells + n] = C::dec(F[(uint64_t)i * stride + n], Lattice<Q>::w(i));
+    for (int i = 0; i < Q; i++)
+        out[(uint64_t)i * n_cells + n] = (float)C::dec(F[(uint64_t)i * stride + n], LatticeW<Q, typename C::R>::w(i));
 }
 template <int Q, int ST>
 __global__ void encode_kernel(void* f, uint64_t stride, uint32_t n_cells, const float* in) {
@@ -634,7 +846,8 @@ __global__ void encode_kernel(void* f, uint64_t stride, uint32_t n_cells, const 
     if (n >= n_cells) return;
     T* F = static_cast<T*>(f);
 #pragma unroll
-    for (int i = 0; i < Q; i++) F[(uint64_t)i * stride + n] = C::enc(in[(uint64_t)i * n_cells + n], Lattice<Q>::w(i));
+    for (int i = 0; i < Q; i++)
+        F[(uint64_t)i * stride + n] = C::enc(in[(uint64_t)i * n_cells + n], LatticeW<Q, typename C::R>::w(i));
 }
 
 // ---------------------------------------------------------------------------
@@ -650,10 +863,28 @@ cudaError_t launch_step_st(const StepParams& p, int mode, bool generic, cudaStre
     int block;
     dim3 grid = cell_grid(p.nx, p.ny, p.nz, block);
     if (!generic) {
-        if (mode == AA_EVEN) fast_step_kernel<Q, ST, AA_EVEN><<<grid, block, 0, st>>>(p);
-        else fast_step_kernel<Q, ST, AA_ODD><<<grid, block, 0, st>>>(p);
+        const bool trt = (p.flags & F_TRT) != 0, forced = (p.flags & F_FORCE_CONST) != 0;
+        if (mode == AA_EVEN) {
+            if (trt) {
+                if (forced) fast_step_kernel<Q, ST, AA_EVEN, true, true><<<grid, block, 0, st>>>(p);
+                else fast_step_kernel<Q, ST, AA_EVEN, true, false><<<grid, block, 0, st>>>(p);
+            } else {
+                if (forced) fast_step_kernel<Q, ST, AA_EVEN, false, true><<<grid, block, 0, st>>>(p);
+                else fast_step_kernel<Q, ST, AA_EVEN, false, false><<<grid, block, 0, st>>>(p);
+            }
+        } else {
+            if (trt) {
+                if (forced) fast_step_kernel<Q, ST, AA_ODD, true, true><<<grid, block, 0, st>>>(p);
+                else fast_step_kernel<Q, ST, AA_ODD, true, false><<<grid, block, 0, st>>>(p);
+            } else {
+                if (forced) fast_step_kernel<Q, ST, AA_ODD, false, true><<<grid, block, 0, st>>>(p);
+                else fast_step_kernel<Q, ST, AA_ODD, false, false><<<grid, block, 0, st>>>(p);
+            }
+        }
     } else {
-        if (mode == AA_EVEN) step_kernel<Q, ST, AA_EVEN><<<grid, block, 0, st>>>(p);
+        // the FP64 reference stepper covers the fast path only
+        if constexpr (ST == ST_FP64) return cudaErrorInvalidValue;
+        else if (mode == AA_EVEN) step_kernel<Q, ST, AA_EVEN><<<grid, block, 0, st>>>(p);
         else if (mode == AA_ODD) step_kernel<Q, ST, AA_ODD><<<grid, block, 0, st>>>(p);
         else step_kernel<Q, ST, AA_LOCAL><<<grid, block, 0, st>>>(p);
     }
@@ -667,6 +898,7 @@ cudaError_t launch_step(const StepParams& p, int storage, int mode, bool generic
     case ST_FP16: return launch_step_st<Q, ST_FP16>(p, mode, generic, st);
     case ST_FP16S: return launch_step_st<Q, ST_FP16S>(p, mode, generic, st);
     case ST_FP16C: return launch_step_st<Q, ST_FP16C>(p, mode, generic, st);
+    case ST_FP64: return launch_step_st<Q, ST_FP64>(p, mode, generic, st);
     }
     return cudaErrorInvalidValue;
 }
@@ -693,6 +925,7 @@ cudaError_t launch_init(const InitParams& p, int storage, cudaStream_t st) {
     case ST_FP16: init_kernel<Q, ST_FP16><<<blocks, 256, 0, st>>>(p); break;
     case ST_FP16S: init_kernel<Q, ST_FP16S><<<blocks, 256, 0, st>>>(p); break;
     case ST_FP16C: init_kernel<Q, ST_FP16C><<<blocks, 256, 0, st>>>(p); break;
+    case ST_FP64: init_kernel<Q, ST_FP64><<<blocks, 256, 0, st>>>(p); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
@@ -706,6 +939,7 @@ cudaError_t launch_decode(const void* f, uint64_t stride, uint32_t n, int storag
     case ST_FP16: decode_kernel<Q, ST_FP16><<<blocks, 256, 0, st>>>(f, stride, n, out); break;
     case ST_FP16S: decode_kernel<Q, ST_FP16S><<<blocks, 256, 0, st>>>(f, stride, n, out); break;
     case ST_FP16C: decode_kernel<Q, ST_FP16C><<<blocks, 256, 0, st>>>(f, stride, n, out); break;
+    case ST_FP64: decode_kernel<Q, ST_FP64><<<blocks, 256, 0, st>>>(f, stride, n, out); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
@@ -718,6 +952,7 @@ cudaError_t launch_encode(void* f, uint64_t stride, uint32_t n, int storage, con
     case ST_FP16: encode_kernel<Q, ST_FP16><<<blocks, 256, 0, st>>>(f, stride, n, in); break;
     case ST_FP16S: encode_kernel<Q, ST_FP16S><<<blocks, 256, 0, st>>>(f, stride, n, in); break;
     case ST_FP16C: encode_kernel<Q, ST_FP16C><<<blocks, 256, 0, st>>>(f, stride, n, in); break;
+    case ST_FP64: encode_kernel<Q, ST_FP64><<<blocks, 256, 0, st>>>(f, stride, n, in); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

@@ -34,7 +34,13 @@ struct vec3 {
 };
 
 enum VelocitySet { D2Q9 = BF_D2Q9, D3Q15 = BF_D3Q15, D3Q19 = BF_D3Q19, D3Q27 = BF_D3Q27 };
-enum FloatingPointAccuracy { fp16 = BF_STORE_FP16, fp32 = BF_STORE_FP32, fp16s = BF_STORE_FP16S, fp16c = BF_STORE_FP16C };
+enum FloatingPointAccuracy {
+    fp16 = BF_STORE_FP16,
+    fp32 = BF_STORE_FP32,
+    fp16s = BF_STORE_FP16S,
+    fp16c = BF_STORE_FP16C,
+    fp64 = BF_STORE_FP64
+};
 
 class LBMError : public std::runtime_error {
 public:

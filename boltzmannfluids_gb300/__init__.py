@@ -5,9 +5,9 @@ ABI in include/bf_lbm.h; `LBM` in this package mirrors the reference's C++
 class over that ABI.
 """
 from .lbm import (LBM, BoundaryMode, Collision, Field, FloatingPointAccuracy, FluidProperties, LBMError,
-                  ObjectKind, VelocitySet, bits_per_boundry, get_velosity_vectors, load_library, pack_boundries,
-                  LIB_PATH)
+                  ObjectKind, RenderMode, VelocitySet, bits_per_boundry, get_velosity_vectors, load_library,
+                  pack_boundries, render3d, LIB_PATH)
 
 __all__ = ["LBM", "BoundaryMode", "Collision", "Field", "FloatingPointAccuracy", "FluidProperties", "LBMError",
-           "ObjectKind", "VelocitySet", "bits_per_boundry", "get_velosity_vectors", "load_library",
-           "pack_boundries", "LIB_PATH"]
+           "ObjectKind", "RenderMode", "VelocitySet", "bits_per_boundry", "get_velosity_vectors", "load_library",
+           "pack_boundries", "render3d", "LIB_PATH"]

@@ -16,7 +16,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libbfgb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["lbm_q9.cu", "lbm_q15.cu", "lbm_q19.cu", "lbm_q27.cu", "lbm_aux.cu", "bf_abi.cu", "bf_noalloc.cu", "lbm_adjoint.cu"]
+SOURCES = ["lbm_q9.cu", "lbm_q15.cu", "lbm_q19.cu", "lbm_q27.cu", "lbm_aux.cu", "bf_abi.cu", "bf_noalloc.cu", "lbm_adjoint.cu",
+           "marching_cubes.cu", "voxelize.cu", "render3d.cu"]
 
 
 def nvcc():

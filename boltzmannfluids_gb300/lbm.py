@@ -31,11 +31,13 @@ class VelocitySet(enum.IntEnum):
 class FloatingPointAccuracy(enum.IntEnum):
     """DDF storage.  fp32/fp16 are the reference's FloatingPointAccuracy
     (FloatingPointAccuracy.h:6-9, fp16 = R16F lattice); fp16s (shifted IEEE
-    half) and fp16c (custom 1-4-11 format of (f-w)/w) are extensions."""
+    half) and fp16c (custom 1-4-11 format of (f-w)/w) are extensions; fp64 is
+    the FP64 accuracy reference stepper (periodic boxes, no objects)."""
     fp32 = 0
     fp16 = 1
     fp16s = 2
     fp16c = 3
+    fp64 = 4
 
 
 class BoundaryMode(enum.IntEnum):
@@ -160,6 +162,16 @@ ABI = {
     "bf_adjoint_forward": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "bf_adjoint_backward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "bf_adjoint_time": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "bf_mc_create": (C.c_int, [C.POINTER(C.c_void_p)]),
+    "bf_mc_destroy": (C.c_int, [C.c_void_p]),
+    "bf_mc_compute": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_int32), C.c_float,
+                                C.POINTER(C.c_float), C.c_void_p, C.POINTER(C.c_uint64)]),
+    "bf_mc_get_vertices": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_uint64)]),
+    "bf_mc_copy_vertices_to_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]),
+    "bf_mc_case_table": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "bf_voxelize_mesh": (C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p, C.POINTER(C.c_int32), C.c_int32, C.c_void_p]),
+    "bf_render3d": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32,
+                              C.c_void_p, C.c_void_p]),
 }
 
 _lib = None
@@ -517,3 +529,26 @@ class LBM:
         ms = C.c_float()
         _check(self._lib.bf_benchmark_steps(self._h, int(steps), C.byref(ms)))
         return ms.value
+
+
+class RenderMode(enum.IntEnum):
+    """bf_render_mode: the five LBM::render3d_* views (LBM.cpp:1207-1376)."""
+    density = 0
+    velocity = 1
+    boundries = 2
+    forces = 3
+    temperature = 4
+
+
+def render3d(lbm: "LBM", mode: RenderMode, view, projection, width: int, height: int, sample_count: int = 64):
+    """Headless LBM::render3d_<mode>(camera, sample_count): view/projection are
+    column-major 4x4 matrices (glm layout); -> float32 (height, width, 4)
+    straight RGBA, row 0 at the bottom (bf_render3d)."""
+    import torch  # device buffer for the image
+    lib = load_library()
+    v = np.ascontiguousarray(np.asarray(view, np.float32).reshape(16))
+    p = np.ascontiguousarray(np.asarray(projection, np.float32).reshape(16))
+    img = torch.empty((int(height), int(width), 4), dtype=torch.float32, device="cuda")
+    _check(lib.bf_render3d(lbm._h, int(mode), v.ctypes.data_as(C.c_void_p), p.ctypes.data_as(C.c_void_p), int(width),
+                           int(height), int(sample_count), C.c_void_p(img.data_ptr()), None))
+    return img.cpu().numpy()

@@ -48,8 +48,19 @@ typedef enum { BF_D2Q9 = 2, BF_D3Q15 = 3, BF_D3Q19 = 4, BF_D3Q27 = 5 } bf_veloci
  * BF_STORE_FP16S stores IEEE half of the shifted population f_i - w_i;
  * BF_STORE_FP16C stores (f_i - w_i)/w_i in a custom 1-4-11 16-bit float
  * (exponent range 2^-12..2^2, subnormals to 2^-23, saturating).
- * Arithmetic is FP32 in every mode. */
-typedef enum { BF_STORE_FP32 = 0, BF_STORE_FP16 = 1, BF_STORE_FP16S = 2, BF_STORE_FP16C = 3 } bf_storage;
+ * Arithmetic is FP32 in these four modes.
+ * BF_STORE_FP64 (no counterpart in the reference) is the accuracy reference
+ * stepper: FP64 populations and FP64 arithmetic in the same operation order
+ * as the FP32 path, for fully periodic esoteric-pull boxes without boundary
+ * objects, temperature or force fields, or multiphase flow (other
+ * configurations fail with BF_ERR_INVALID_ARGUMENT); fields read back as FP32. */
+typedef enum {
+    BF_STORE_FP32 = 0,
+    BF_STORE_FP16 = 1,
+    BF_STORE_FP16S = 2,
+    BF_STORE_FP16C = 3,
+    BF_STORE_FP64 = 4
+} bf_storage;
 
 /* How a fluid cell next to a solid cell receives populations in the
  * esoteric (AA, in-place) mode.
@@ -258,6 +269,77 @@ int bf_adjoint_forward(bf_adjoint* a, double* objective);
 int bf_adjoint_backward(bf_adjoint* a, double* grad_solid_fraction, double* grad_inlet_velocity);
 /* mean device milliseconds of `repeats` forward and backward passes (CUDA events) */
 int bf_adjoint_time(bf_adjoint* a, int32_t repeats, float* forward_ms, float* backward_ms);
+
+/* ---- marching cubes ------------------------------------------------------ */
+/* Replaces MarchingCubes::compute (BoltzmannFluids/Source/MarchingCubes/
+ * MarchingCubes.cpp:3-47, GLSL/MarchingCubes/marching_cubes.comp:41-97), which
+ * binds its buffers but never dispatches.  The mesh it sets out to build is
+ * computed on the GPU: voxels between lattice nodes are classified by which
+ * corner values are >= threshold, triangle counts are prefix-summed, and each
+ * voxel writes its triangles (3 vertices x 3 floats, interpolated on the cut
+ * edges) at its offset, in voxel order (x fastest).  Vertex coordinates map
+ * node i to -0.5 + i / resolution per axis (marching_cubes.comp:52), times
+ * mesh_scale (NULL: 1).  Triangles are oriented with normals pointing from
+ * the >= threshold side outward.  The case table is derived, not copied;
+ * bf_mc_case_table returns it (host only, no GPU needed). */
+typedef struct bf_marching_cubes bf_marching_cubes;
+int bf_mc_create(bf_marching_cubes** out);
+int bf_mc_destroy(bf_marching_cubes* m);
+/* field: device array of resolution[0]*resolution[1]*resolution[2] cells with
+ * `components` floats each; the value used is float `component` of each cell
+ * (the density of BF_FIELD_VELOCITY_DENSITY is components 4, component 3).
+ * Runs on `stream` (NULL: the legacy default stream) and returns once the
+ * mesh is complete; at most 2^32/5 voxels. */
+int bf_mc_compute(bf_marching_cubes* m, const float* field, int32_t components, int32_t component,
+                  const int32_t resolution[3], float threshold, const float mesh_scale[3], void* stream,
+                  uint64_t* triangle_count);
+/* device pointer to the last mesh: triangle_count * 9 floats, owned by m */
+int bf_mc_get_vertices(bf_marching_cubes* m, const float** vertices_device, uint64_t* triangle_count);
+int bf_mc_copy_vertices_to_host(bf_marching_cubes* m, float* out, uint64_t max_triangles, uint64_t* written);
+/* triangles[256*15]: edge numbers (-1 padded), counts[256]; corner k sits at
+ * (k&1, k>>1&1, k>>2&1), edge 4d+j joins the j-th corner with bit d clear to
+ * its neighbour along axis d */
+int bf_mc_case_table(int8_t* triangles, uint8_t* counts);
+
+/* ---- mesh voxeliser ----------------------------------------------------- */
+/* Replaces MeshRasterizer3D::rasterize(mesh, target_texture, model_matrix)
+ * (BoltzmannFluids/Source/MeshRasterizer3D/MeshRasterizer3D.cpp:7-113), which
+ * renders the mesh in 64 depth slabs per voxel layer and toggles a per-pixel
+ * inside/outside parity (raster_unifier.comp:18-35).  Here one ray per voxel
+ * column (i, j) through its centre finds the mesh crossings on the GPU; the
+ * sorted crossing depths bound the inside intervals (an odd count leaves the
+ * rest of the column inside), and voxel (i, j, k) is solid (mask 1) when one
+ * of its `samples_per_voxel` depth samples lies inside.  vertices: host array
+ * of triangle_count * 9 floats; model: column-major 4x4 (NULL: identity)
+ * mapping the mesh into the cube [-1, 1]^3 that spans the volume; column i
+ * is centred at x = -1 + (2i+1)/nx (likewise y), depth samples at
+ * z = -1 + 2(k + (s+1/2)/samples)/nz.  mask: host array of nx*ny*nz bytes
+ * (x fastest).  Layer k grows with z (the reference's camera looks down -z,
+ * so its layer 0 is the top). */
+int bf_voxelize_mesh(const float* vertices, uint64_t triangle_count, const float model[16],
+                     const int32_t resolution[3], int32_t samples_per_voxel, uint8_t* mask);
+
+/* ---- headless volume rendering ------------------------------------------ */
+/* Replaces LBM::render3d_density / _velocity / _boundries / _forces /
+ * _temperature (BoltzmannFluids/Source/LBM/LBM.cpp:1207-1376 with the
+ * fragment shaders GLSL/Renderer3D/*_volumetric.frag), which draw into the
+ * current GL framebuffer.  A CUDA kernel marches one ray per pixel through
+ * the unit cube [-0.5, 0.5]^3 holding the fields of the last saved step and
+ * writes straight (not premultiplied) RGBA floats, row 0 at the bottom, into
+ * rgba_device (width*height*4 floats; compose over a background with
+ * src_alpha / one_minus_src_alpha as the reference's blending does).  view
+ * and projection are column-major 4x4 camera matrices (glm layout).  Pixels
+ * whose ray misses the cube are (0, 0, 0, 0).  Runs on `stream` after the
+ * solver's queued work and returns when the image is complete. */
+typedef enum {
+    BF_RENDER_DENSITY = 0,
+    BF_RENDER_VELOCITY = 1,
+    BF_RENDER_BOUNDRIES = 2,
+    BF_RENDER_FORCES = 3,
+    BF_RENDER_TEMPERATURE = 4
+} bf_render_mode;
+int bf_render3d(bf_solver* s, int32_t mode, const float view[16], const float projection[16], int32_t width,
+                int32_t height, int32_t sample_count, float* rgba_device, void* stream);
 
 /* ---- allocation-free reduction ------------------------------------------ */
 /* No counterpart in the reference.  FP64 {mass, momentum x, y, z, kinetic

@@ -166,8 +166,17 @@ __global__ void __launch_bounds__(kAdjBlock) adj_backward_kernel(AdjParams p) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
     if (x >= p.nx) return;
     const uint32_t n = adj_cell(p, x, y, z);
-    float g[Q];
+    // every load of the step is issued before any arithmetic, so the step
+    // waits on memory once: the pulled state, the incoming adjoint, the
+    // solid fraction and the running parameter gradient
+    float g[Q], lam[Q];
     adj_pull<Q>(p, x, y, z, n, g);
+    if (!FINAL) {
+#pragma unroll
+        for (int k = 0; k < Q; k++) lam[k] = p.lam_in[(uint64_t)k * p.n + n];
+    }
+    const float s = p.s[n];
+    const double gs_prev = p.grad_s[n];
     float rho = 0.f, jx = 0.f, jy = 0.f, jz = 0.f;
 #pragma unroll
     for (int i = 0; i < Q; i++) {
@@ -176,7 +185,6 @@ __global__ void __launch_bounds__(kAdjBlock) adj_backward_kernel(AdjParams p) {
     }
     const float rr = 1.0f / rho;
     const float ux = jx * rr, uy = jy * rr, uz = jz * rr;
-    const float s = p.s[n];
     float mu[Q];
     double gs;
     if (FINAL) {
@@ -193,12 +201,11 @@ __global__ void __launch_bounds__(kAdjBlock) adj_backward_kernel(AdjParams p) {
     } else {
         const float om = p.omega, oms = 1.0f - s;
         const float uu = ux * ux + uy * uy + uz * uz;
-        float A0 = 0.f, Vx = 0.f, Vy = 0.f, Vz = 0.f, lam[Q], gsf = 0.f;
+        float A0 = 0.f, Vx = 0.f, Vy = 0.f, Vz = 0.f, gsf = 0.f;
 #pragma unroll
         for (int k = 0; k < Q; k++) {
             const Dir c = L::c(k);
             const float w = L::w(k);
-            lam[k] = p.lam_in[(uint64_t)k * p.n + n];
             const float cu = c.x * ux + c.y * uy + c.z * uz;
             const float Lk = oms * lam[k] * w;
             A0 += Lk * (1.0f + 3.0f * cu + 4.5f * cu * cu - 1.5f * uu);
@@ -217,7 +224,7 @@ __global__ void __launch_bounds__(kAdjBlock) adj_backward_kernel(AdjParams p) {
             mu[i] = (1.0f - om) * oms * lam[i] + om * (A0 + dot) + s * lam[opp(i)];
         }
     }
-    p.grad_s[n] += gs;
+    p.grad_s[n] = gs_prev + gs;
     // transpose of the pull
     const float ui = p.uin[(uint32_t)z * p.ny + y];
     float guf = 0.f;
@@ -499,13 +506,17 @@ int bf_adjoint_create(bf_adjoint** out, const bf_adjoint_desc* d) {
         return e;
     };
     const size_t state = (size_t)Q * a->n * sizeof(float);
-    cudaError_t e = cudaStreamCreateWithFlags(&a->stream, cudaStreamNonBlocking);
+    // the adjoint sweep (critical path) runs at the highest stream priority,
+    // the overlapped recomputation at the lowest
+    int prio_low = 0, prio_high = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
+    cudaError_t e = cudaStreamCreateWithPriority(&a->stream, cudaStreamNonBlocking, prio_high);
     if (e == cudaSuccess) e = alloc((size_t)a->n * 4, (void**)&a->s);
     if (e == cudaSuccess) e = alloc((size_t)a->rows * 4, (void**)&a->uin);
     if (e == cudaSuccess) e = alloc((size_t)a->n * 12, (void**)&a->ustar);
     a->ckpt.assign(a->nseg, nullptr);
     for (int k = 0; k < a->nseg && e == cudaSuccess; k++) e = alloc(state, (void**)&a->ckpt[k]);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&a->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&a->side, cudaStreamNonBlocking, prio_low);
     for (int b = 0; b < (a->nseg >= 2 ? 2 : 1); b++) {
         a->seg[b].assign(d->checkpoint_interval, nullptr);
         for (int j = 1; j < d->checkpoint_interval && e == cudaSuccess; j++) e = alloc(state, (void**)&a->seg[b][j]);

@@ -230,6 +230,97 @@ def run_adjoint_leg(bf):
     return out
 
 
+def run_precision_leg(bf, size, steps, every=100):
+    """Precision configuration: D3Q19 BGK Taylor-Green vortex, u0 0.05,
+    tau 0.52, periodic size^3, `steps` steps, in FP32, FP16S and FP16C
+    storage against the FP64 reference stepper on the GPU.  Reports the
+    kinetic-energy error curve (FP64 sums, every `every` steps), the final u
+    field error and each storage's MLUPs on this workload (device time)."""
+    import numpy as np
+    from boltzmannfluids_gb300.workloads import taylor_green_3d
+    res = (size, size, size)
+    n = size ** 3
+    rho, u = taylor_green_3d(res, 0.05)
+    runs = {}
+    for name in ("fp64", "fp32", "fp16s", "fp16c"):
+        s = bf.LBM()
+        s.is_collide_esoteric = True
+        s.initialize_fields_from_arrays(res, 0.52, density=rho, velocity=u, velocity_set=bf.VelocitySet.D3Q19,
+                                        fp_accuracy=getattr(bf.FloatingPointAccuracy, name))
+        ke = [s.reduce()[4]]
+        ms = 0.0
+        for _ in range(steps // every):
+            ms += s.benchmark_steps(every)
+            ke.append(s.reduce()[4])
+        s.reduce()  # also saves the fields of the current state
+        vd = s.get_velocity_density_texture().reshape(-1, 4)[:, :3].astype(np.float64)
+        runs[name] = (np.array(ke), vd, ms)
+        del s
+    ke64, u64, ms64 = runs["fp64"]
+    scale = float(np.abs(u64).max())
+    out = {"workload": f"D3Q19 BGK Taylor-Green vortex u0 0.05 tau 0.52, {size}^3 periodic, {steps} steps",
+           "reference": "FP64 stepper on the GPU (storage fp64, bit-exact with the FP64 oracle)",
+           "ke_fp64": [float(v) for v in ke64[:: max(1, len(ke64) // 4)]],
+           "fp64_mlups": round(n * steps / (ms64 * 1e-3) / 1e6, 1)}
+    for name in ("fp32", "fp16s", "fp16c"):
+        ke, uu, ms = runs[name]
+        err = np.abs(ke - ke64) / ke64
+        du = uu - u64
+        out[name] = {"ke_rel_err_max": float(err.max()), "ke_rel_err_final": float(err[-1]),
+                     "ke_rel_err_curve": [float(v) for v in err[:: max(1, len(err) // 4)]],
+                     "u_err_max_over_umax": float(np.abs(du).max() / scale),
+                     "u_err_rms_over_urms": float(np.sqrt((du ** 2).mean() / (u64 ** 2).mean())),
+                     "mlups": round(n * steps / (ms * 1e-3) / 1e6, 1)}
+    return out
+
+
+def run_multiphysics_leg(bf, full=False):
+    """Multiphysics configuration: Shan-Chen spinodal decomposition (D3Q19,
+    psi = 1 - exp(-rho), G = -5, rho = 0.69 + 0.01 U(-1,1) seeded) in FP32,
+    FP16S and FP16C storage with the FP64 mass drift; Rayleigh-Benard
+    convection (D3Q19 flow + D3Q7 temperature, hot bottom / cold top walls,
+    Ra 1e5, Pr 0.71, T noise 1e-3 seeded) with its Nusselt number and mass
+    drift.  Reduced sizes by default (128^3 x 2000 steps, 64x64x34 x 20000);
+    full=True runs the configuration's 256^3 x 20000 and 256x256x130 x 50000."""
+    import numpy as np
+    from boltzmannfluids_gb300.workloads import nusselt, rayleigh_benard, spinodal
+    out = {}
+    res, steps = ((256, 256, 256), 20000) if full else ((128, 128, 128), 2000)
+    n = res[0] * res[1] * res[2]
+    sc = {"workload": f"Shan-Chen spinodal decomposition D3Q19, G -5, {res[0]}^3 periodic, {steps} steps"}
+    rho = spinodal(res, 0.69, 0.01, 4)
+    for name in ("fp32", "fp16s", "fp16c"):
+        s = bf.LBM()
+        s.is_collide_esoteric = True
+        s.intermolecular_interaction_strength = -5.0
+        s.initialize_fields_from_arrays(res, 1.0, density=rho, velocity_set=bf.VelocitySet.D3Q19,
+                                        fp_accuracy=getattr(bf.FloatingPointAccuracy, name), is_flow_multiphase=True)
+        m0 = s.reduce()[0]
+        ms = s.benchmark_steps(steps)
+        m1 = s.reduce()[0]
+        d = s.get_velocity_density_texture().reshape(-1, 4)[:, 3]
+        sc[name] = {"mass_rel_drift": float((m1 - m0) / m0), "rho_min": float(d.min()), "rho_max": float(d.max()),
+                    "mlups": round(n * steps / (ms * 1e-3) / 1e6, 1)}
+        del s
+    sc["note"] = "FP64 arithmetic conserves this flow's mass to 1e-13 (the FP64 oracle on a 32^3 case)"
+    out["shan_chen"] = sc
+    rres, rsteps = ((256, 256, 130), 50000) if full else ((64, 64, 34), 20000)
+    s, kappa, h = rayleigh_benard(rres, kappa=0.02 if full else 0.008)
+    m0 = s.reduce()[0]
+    ms = s.benchmark_steps(rsteps)
+    s.reduce()
+    nu_num = nusselt(s, kappa, h)
+    m1 = s.reduce()[0]
+    rn = rres[0] * rres[1] * rres[2]
+    out["rayleigh_benard"] = {
+        "workload": f"Rayleigh-Benard D3Q19+D3Q7 TRT, {rres[0]}x{rres[1]}x{rres[2]} (walls at z = 0, {rres[2] - 1}), "
+                    f"Ra 1e5, Pr 0.71, {rsteps} steps, FP32",
+        "nusselt": float(nu_num), "mass_rel_drift": float((m1 - m0) / m0),
+        "mlups": round(rn * rsteps / (ms * 1e-3) / 1e6, 1)}
+    del s
+    return out
+
+
 def run_gpu(args):
     rank, world, local = dist_env()
     if world > 1:
@@ -297,6 +388,12 @@ def run_gpu(args):
     adj = None
     if not args.no_adjoint:
         adj = run_adjoint_leg(bf)
+    prec = None
+    if not args.no_precision:
+        prec = run_precision_leg(bf, args.precision_size, args.precision_steps)
+    multi = None
+    if not args.no_multiphysics:
+        multi = run_multiphysics_leg(bf, args.multiphysics_full)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         mlups_cpu, threads, sample = cpu_baseline_sample()
@@ -320,6 +417,8 @@ def run_gpu(args):
             "conservation_fp64": {"mass": red[0], "momentum": list(red[1:4]), "kinetic_energy": red[4]},
             "e2e": e2e,
             "adjoint": adj,
+            "precision": prec,
+            "multiphysics": multi,
             "gpu_launches": args.steps,
             "clocks": clock_info,
         }
@@ -344,6 +443,11 @@ def main():
     ap.add_argument("--no-sweep", action="store_true", help="skip the 16-bit storage legs (profiling runs)")
     ap.add_argument("--storage", default="fp32", choices=["fp32", "fp16s", "fp16c"], help="storage of the main leg")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg")
+    ap.add_argument("--no-precision", action="store_true", help="skip the Taylor-Green precision leg")
+    ap.add_argument("--precision-size", type=int, default=128, help="cube edge of the Taylor-Green precision leg")
+    ap.add_argument("--precision-steps", type=int, default=2000)
+    ap.add_argument("--no-multiphysics", action="store_true", help="skip the Shan-Chen / Rayleigh-Benard leg")
+    ap.add_argument("--multiphysics-full", action="store_true", help="run the multiphysics configurations at full size")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -43,6 +43,8 @@ def build(verbose=False, force=False):
     flags = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
              "-Xptxas", "-v" if verbose else "-O3",
              "--expt-relaxed-constexpr", *ARCH]
+    # tuning: extra -D definitions (e.g. BF_STEP_BLOCK, BF_FAST_MIN_BLOCKS)
+    flags += [f for f in os.environ.get("BF_NVCC_DEFINES", "").split() if f.startswith("-D")]
 
     def compile_one(src):
         obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")

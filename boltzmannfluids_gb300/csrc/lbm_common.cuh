@@ -130,36 +130,55 @@ __device__ __forceinline__ float decode_c16(uint16_t h) {
 }
 
 template <int ST> struct Codec;
-// T: the stored element type; R: the arithmetic type of the update
+// T: the stored element type; R: the arithmetic type of the update.
+// SHIFTED codecs store the shifted population g = f - w_i and the update
+// works on g directly (dec/enc), which drops the two +-w per population and
+// keeps the arithmetic on the small deviations; dec_f/enc_f convert from and
+// to f itself (initialisation, read-back, snapshots).
 template <> struct Codec<ST_FP32> {
     using T = float;
     using R = float;
+    static constexpr bool SHIFTED = false;
     __device__ __forceinline__ static float dec(T v, float) { return v; }
     __device__ __forceinline__ static T enc(float v, float) { return v; }
+    __device__ __forceinline__ static float dec_f(T v, float) { return v; }
+    __device__ __forceinline__ static T enc_f(float v, float) { return v; }
 };
 template <> struct Codec<ST_FP16> {  // R16F: IEEE half of f
     using T = __half;
     using R = float;
+    static constexpr bool SHIFTED = false;
     __device__ __forceinline__ static float dec(T v, float) { return __half2float(v); }
     __device__ __forceinline__ static T enc(float v, float) { return __float2half_rn(v); }
+    __device__ __forceinline__ static float dec_f(T v, float) { return __half2float(v); }
+    __device__ __forceinline__ static T enc_f(float v, float) { return __float2half_rn(v); }
 };
-template <> struct Codec<ST_FP16S> {  // IEEE half of f - w
+template <> struct Codec<ST_FP16S> {  // IEEE half of g = f - w
     using T = __half;
     using R = float;
-    __device__ __forceinline__ static float dec(T v, float w) { return __fadd_rn(__half2float(v), w); }
-    __device__ __forceinline__ static T enc(float v, float w) { return __float2half_rn(__fsub_rn(v, w)); }
+    static constexpr bool SHIFTED = true;
+    __device__ __forceinline__ static float dec(T v, float) { return __half2float(v); }
+    __device__ __forceinline__ static T enc(float g, float) { return __float2half_rn(g); }
+    __device__ __forceinline__ static float dec_f(T v, float w) { return __fadd_rn(__half2float(v), w); }
+    __device__ __forceinline__ static T enc_f(float v, float w) { return __float2half_rn(__fsub_rn(v, w)); }
 };
-template <> struct Codec<ST_FP16C> {  // custom 16-bit of (f - w)/w
+template <> struct Codec<ST_FP16C> {  // custom 16-bit of g/w = (f - w)/w
     using T = uint16_t;
     using R = float;
-    __device__ __forceinline__ static float dec(T v, float w) { return fmaf(decode_c16(v), w, w); }
-    __device__ __forceinline__ static T enc(float v, float w) { return encode_c16(__fmul_rn(__fsub_rn(v, w), 1.0f / w)); }
+    static constexpr bool SHIFTED = true;
+    __device__ __forceinline__ static float dec(T v, float w) { return __fmul_rn(decode_c16(v), w); }
+    __device__ __forceinline__ static T enc(float g, float w) { return encode_c16(__fmul_rn(g, 1.0f / w)); }
+    __device__ __forceinline__ static float dec_f(T v, float w) { return fmaf(decode_c16(v), w, w); }
+    __device__ __forceinline__ static T enc_f(float v, float w) { return encode_c16(__fmul_rn(__fsub_rn(v, w), 1.0f / w)); }
 };
 template <> struct Codec<ST_FP64> {  // FP64 reference stepper: populations and arithmetic in double
     using T = double;
     using R = double;
+    static constexpr bool SHIFTED = false;
     __device__ __forceinline__ static double dec(T v, double) { return v; }
     __device__ __forceinline__ static T enc(double v, double) { return v; }
+    __device__ __forceinline__ static double dec_f(T v, double) { return v; }
+    __device__ __forceinline__ static T enc_f(double v, double) { return v; }
 };
 
 // ---------------------------------------------------------------------------
@@ -299,6 +318,9 @@ cudaError_t launch_reduce_finish(const double* partials, uint32_t n_blocks, doub
 // sets the thread's message returned by bf_last_error()
 void record_error(const std::string& msg);
 
-constexpr int kStepBlock = 256;
+#ifndef BF_STEP_BLOCK
+#define BF_STEP_BLOCK 256
+#endif
+constexpr int kStepBlock = BF_STEP_BLOCK;  // threads per block of the step kernels (along x)
 
 }  // namespace bf

@@ -249,7 +249,9 @@ __device__ __forceinline__ void velocity_and_limit(const double (&f)[Q], Moments
 // with the Guo term split into its even part (1-omega+/2) w ((F.c)(u.c)/cs4 - F.u/cs2)
 // and odd part (1-omega-/2) w F.c/cs2.  Above the extreme velocity limit the
 // populations become the equilibrium (BGK: feq, TRT: e+ +- e-).
-template <int Q, class Emit>
+// SH (shifted storage): f holds g = f - w and every equilibrium is formed
+// as g_eq = fma(w rho, bracket, -w); the rest of the update is unchanged.
+template <int Q, bool SH, class Emit>
 __device__ __forceinline__ void collide_emit(const float (&f)[Q], const Moments& m, const StepParams& p, bool trt,
                                              bool src, bool to_equilibrium, Emit emit) {
     using L = Lattice<Q>;
@@ -261,7 +263,8 @@ __device__ __forceinline__ void collide_emit(const float (&f)[Q], const Moments&
             const Dir c = L::c(i);
             const float w = L::w(i);
             const float cu = cdot_rt(c, m.ux, m.uy, m.uz);
-            const float fe = FMUL(FMUL(w, m.rho), bracket(cu, one_m, p.R2, p.R4h));
+            const float br = bracket(cu, one_m, p.R2, p.R4h);
+            const float fe = SH ? FFMA(FMUL(w, m.rho), br, -w) : FMUL(FMUL(w, m.rho), br);
             float v = FFMA(FSUB(fe, f[i]), p.Rtau, f[i]);  // old + (-(old - feq)/tau)
             if (src) {
                 const float fc = cdot_rt(c, m.Fx, m.Fy, m.Fz);
@@ -273,7 +276,7 @@ __device__ __forceinline__ void collide_emit(const float (&f)[Q], const Moments&
     }
     {
         const float w0 = L::w(0);
-        const float fe0 = FMUL(FMUL(w0, m.rho), one_m);
+        const float fe0 = SH ? FFMA(FMUL(w0, m.rho), one_m, -w0) : FMUL(FMUL(w0, m.rho), one_m);
         float v = FFMA(FSUB(fe0, f[0]), p.Rtau, f[0]);
         if (src) v = FFMA(FMUL(p.Pp, w0), -fuR2, v);
         emit(0, m.out_ext ? fe0 : v);
@@ -285,7 +288,8 @@ __device__ __forceinline__ void collide_emit(const float (&f)[Q], const Moments&
         const float w = L::w(i);
         const float cu = cdot_rt(c, m.ux, m.uy, m.uz);
         const float wr = FMUL(w, m.rho);
-        const float ep = FMUL(wr, FFMA(FMUL(cu, cu), p.R4h, one_m));
+        const float be = FFMA(FMUL(cu, cu), p.R4h, one_m);
+        const float ep = SH ? FFMA(wr, be, -w) : FMUL(wr, be);
         const float em = FMUL(FMUL(wr, p.R2), cu);
         const float Pd = FFMA(pair_sum<Q>(f, i), 0.5f, -ep);
         const float Md = FFMA(pair_diff<Q>(f, i), 0.5f, -em);
@@ -317,7 +321,7 @@ __device__ __forceinline__ Coef<double> coef_of(const StepParams& p, double) {
 // branches once per cell on the rare extreme case instead of selecting per
 // population); R = float is the canonical FP32 evaluation, R = double the
 // FP64 reference stepper.
-template <int Q, bool TRT, bool SRC, bool EXT, class R, class Emit>
+template <int Q, bool TRT, bool SRC, bool EXT, bool SH, class R, class Emit>
 __device__ __forceinline__ void collide_fixed(const R (&f)[Q], const MomentsT<R>& m, const Coef<R>& k, Emit emit) {
     using L = Lattice<Q>;
     using W = LatticeW<Q, R>;
@@ -329,7 +333,8 @@ __device__ __forceinline__ void collide_fixed(const R (&f)[Q], const MomentsT<R>
             const Dir c = L::c(i);
             const R w = W::w(i);
             const R cu = cdot_rt(c, m.ux, m.uy, m.uz);
-            const R fe = FMUL(FMUL(w, m.rho), bracket(cu, one_m, k.R2, k.R4h));
+            const R br = bracket(cu, one_m, k.R2, k.R4h);
+            const R fe = SH ? FFMA(FMUL(w, m.rho), br, -w) : FMUL(FMUL(w, m.rho), br);
             if (EXT) { emit(i, fe); continue; }
             R v = FFMA(FSUB(fe, f[i]), k.Rtau, f[i]);
             if (SRC) {
@@ -342,7 +347,7 @@ __device__ __forceinline__ void collide_fixed(const R (&f)[Q], const MomentsT<R>
     }
     {
         const R w0 = W::w(0);
-        const R fe0 = FMUL(FMUL(w0, m.rho), one_m);
+        const R fe0 = SH ? FFMA(FMUL(w0, m.rho), one_m, -w0) : FMUL(FMUL(w0, m.rho), one_m);
         if (EXT) {
             emit(0, fe0);
         } else {
@@ -358,7 +363,8 @@ __device__ __forceinline__ void collide_fixed(const R (&f)[Q], const MomentsT<R>
         const R w = W::w(i);
         const R cu = cdot_rt(c, m.ux, m.uy, m.uz);
         const R wr = FMUL(w, m.rho);
-        const R ep = FMUL(wr, FFMA(FMUL(cu, cu), k.R4h, one_m));
+        const R be = FFMA(FMUL(cu, cu), k.R4h, one_m);
+        const R ep = SH ? FFMA(wr, be, -w) : FMUL(wr, be);
         const R em = FMUL(FMUL(wr, k.R2), cu);
         if (EXT) {
             emit(i, FADD(ep, em));
@@ -430,7 +436,19 @@ __device__ __forceinline__ void prefetch_block_rows(const StepParams& p, uint32_
 // pf_blocks ahead in launch order, so that the block's own loads mostly hit
 // L2 and 16-bit storage needs fewer loads in flight to saturate HBM.
 // ---------------------------------------------------------------------------
-constexpr int kFastMinBlocks = 4;  // 256 threads x 4 blocks: at most 64 registers (FP64: 2 blocks, 128)
+#ifndef BF_FAST_MIN_BLOCKS
+#define BF_FAST_MIN_BLOCKS 4
+#endif
+#ifndef BF_FAST_MIN_BLOCKS_16
+#define BF_FAST_MIN_BLOCKS_16 5
+#endif
+// resident blocks per SM the fast kernel is compiled for: 256 threads x 4
+// blocks allow at most 64 registers (FP32 storage); the 16-bit storages,
+// which are issue-bound rather than bandwidth-bound, fit 48 registers and 5
+// blocks up to D3Q19 (measured faster at 512^3; D3Q27 would spill); FP64:
+// 2 blocks, 128 registers
+constexpr int kFastMinBlocks = BF_FAST_MIN_BLOCKS;
+constexpr int kFastMinBlocks16 = BF_FAST_MIN_BLOCKS_16;
 
 // One cell of the fast step.  EDGE: the block's row lies on a y or z face of
 // the box, so the y/z neighbour offsets wrap and are computed in the block;
@@ -477,6 +495,7 @@ __device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepP
     asm volatile("" : "+r"(n_st), "+r"(oxm_st), "+r"(oxp_st));
     MomentsT<R> m;
     m.rho = density_of<Q>(f);
+    if (C::SHIFTED) m.rho = FADD(R(1), m.rho);  // sum of g plus sum of w
     if (!(m.rho == m.rho)) atomicOr(p.err, 1u);
     m.rho = m.rho < R(0.01) ? R(0.01) : m.rho;
     constexpr bool F64 = sizeof(R) == 8;
@@ -488,8 +507,8 @@ __device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepP
     if (p.flags & F_UPDATE) {
         const Coef<R> k = coef_of(p, R(0));
         auto emit = [&](int i, R v) { base[slot(opp(i), n_st, oxm_st, oxp_st)] = C::enc(v, W::w(i)); };
-        if (m.out_ext) collide_fixed<Q, TRT, FORCED, true>(f, m, k, emit);
-        else collide_fixed<Q, TRT, FORCED, false>(f, m, k, emit);
+        if (m.out_ext) collide_fixed<Q, TRT, FORCED, true, C::SHIFTED>(f, m, k, emit);
+        else collide_fixed<Q, TRT, FORCED, false, C::SHIFTED>(f, m, k, emit);
     }
     if (p.flags & F_SAVE) {
         p.vel_den[n] = make_float4((float)m.ux, (float)m.uy, (float)m.uz, (float)m.rho);
@@ -504,7 +523,8 @@ __device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepP
 }
 
 template <int Q, int ST, int MODE, bool TRT, bool FORCED>
-__global__ void __launch_bounds__(kStepBlock, ST == ST_FP64 ? 2 : kFastMinBlocks)
+__global__ void __launch_bounds__(kStepBlock,
+                                  ST == ST_FP64 ? 2 : ((ST == ST_FP32 || Q == 27) ? kFastMinBlocks : kFastMinBlocks16))
     fast_step_kernel(const __grid_constant__ StepParams p) {
     if (p.pf_blocks != 0u && threadIdx.x == 0) {
         const uint32_t b = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z) + p.pf_blocks;
@@ -572,7 +592,8 @@ __device__ __forceinline__ CellSum cell_update(const StepParams& p, int x, int y
                 // population entering from outside the domain: f_eq(rho_b, u_b)
                 const float cu = cdot_rt(c, bv.y, bv.z, bv.w);
                 const float one_mb = FSUB(1.0f, FMUL(uu_of(bv.y, bv.z, bv.w), p.R2h));
-                f[i] = FMUL(FMUL(w, bv.x), bracket(cu, one_mb, p.R2, p.R4h));
+                const float br = bracket(cu, one_mb, p.R2, p.R4h);
+                f[i] = C::SHIFTED ? FFMA(FMUL(w, bv.x), br, -w) : FMUL(FMUL(w, bv.x), br);
                 done = true;
             } else if ((flags & F_BOUNCE_BACK) && !sopen && (flags & F_BOUNDARIES)) {
                 const uint32_t sid = boundary_id(p.bnd, p.bits, sn);
@@ -590,7 +611,8 @@ __device__ __forceinline__ CellSum cell_update(const StepParams& p, int x, int y
             }
         }
         if (!done) {
-            if (MODE == AA_EVEN) f[i] = sopen ? 0.01f : C::dec(plane(i)[sn], w);
+            // out-of-domain reads give 0.01 (collide.comp:278-298), g = 0.01 - w when shifted
+            if (MODE == AA_EVEN) f[i] = sopen ? (C::SHIFTED ? FSUB(0.01f, w) : 0.01f) : C::dec(plane(i)[sn], w);
             else if (MODE == AA_ODD) f[i] = C::dec(plane(opp(i))[n], w);
             else f[i] = C::dec(plane(i)[n], w);
         }
@@ -599,6 +621,7 @@ __device__ __forceinline__ CellSum cell_update(const StepParams& p, int x, int y
     // ---- moments and forces (collide.comp:702-725) ----
     Moments m;
     m.rho = density_of<Q>(f);
+    if (C::SHIFTED) m.rho = FADD(1.0f, m.rho);  // sum of g plus sum of w
     if (!(m.rho == m.rho)) atomicOr(p.err, 1u);
     m.rho = m.rho < 0.01f ? 0.01f : m.rho;  // max(density, 0.01), NaN kept
     m.Fx = m.Fy = m.Fz = 0.f;
@@ -641,7 +664,7 @@ __device__ __forceinline__ CellSum cell_update(const StepParams& p, int x, int y
 
     // ---- collision + AA store (collide.comp:727-760) ----
     if (flags & F_UPDATE) {
-        collide_emit<Q>(f, m, p, (flags & F_TRT) != 0, (flags & F_SOURCE) != 0, eqb, [&](int i, float v) {
+        collide_emit<Q, C::SHIFTED>(f, m, p, (flags & F_TRT) != 0, (flags & F_SOURCE) != 0, eqb, [&](int i, float v) {
             const Dir c = L::c(i);
             const float w = L::w(i);
             if (MODE == AA_EVEN) {
@@ -718,7 +741,7 @@ __global__ void __launch_bounds__(kStepBlock) stream_kernel(const __grid_constan
         int sx = x - c.x, sy = y - c.y, sz = z - c.z;
         bool open;
         coords_wrap<Q>(sx, sy, sz, p.nx, p.ny, p.nz, open, p.flags);
-        if (open) { dst[(uint64_t)i * S + n] = C::enc(0.01f, w); continue; }
+        if (open) { dst[(uint64_t)i * S + n] = C::enc(C::SHIFTED ? __fsub_rn(0.01f, w) : 0.01f, w); continue; }
         const uint32_t sn = (uint32_t)sx + (uint32_t)p.nx * ((uint32_t)sy + (uint32_t)p.ny * (uint32_t)sz);
         uint32_t sid = (p.flags & F_BOUNDARIES) ? boundary_id(p.bnd, p.bits, sn) : 0u;
         if (sid != 0u && solid_id(p.obj_kind, sid)) {
@@ -802,7 +825,7 @@ __global__ void init_kernel(const __grid_constant__ InitParams p) {
         const Dir c = L::c(i);
         const R w = LatticeW<Q, R>::w(i);
         const R cu = feq_init_dot(R(c.x), R(c.y), R(c.z), ux, uy, uz);
-        F[i * p.stride + n] = C::enc(feq_init_literal(w, r, cu, uu), w);
+        F[i * p.stride + n] = C::enc_f(feq_init_literal(w, r, cu, uu), w);
     }
 }
 
@@ -836,7 +859,7 @@ __global__ void decode_kernel(const void* f, uint64_t stride, uint32_t n_cells, 
     const T* F = static_cast<const T*>(f);
 #pragma unroll
     for (int i = 0; i < Q; i++)
-        out[(uint64_t)i * n_cells + n] = (float)C::dec(F[(uint64_t)i * stride + n], LatticeW<Q, typename C::R>::w(i));
+        out[(uint64_t)i * n_cells + n] = (float)C::dec_f(F[(uint64_t)i * stride + n], LatticeW<Q, typename C::R>::w(i));
 }
 template <int Q, int ST>
 __global__ void encode_kernel(void* f, uint64_t stride, uint32_t n_cells, const float* in) {
@@ -847,7 +870,7 @@ __global__ void encode_kernel(void* f, uint64_t stride, uint32_t n_cells, const 
     T* F = static_cast<T*>(f);
 #pragma unroll
     for (int i = 0; i < Q; i++)
-        F[(uint64_t)i * stride + n] = C::enc(in[(uint64_t)i * n_cells + n], LatticeW<Q, typename C::R>::w(i));
+        F[(uint64_t)i * stride + n] = C::enc_f(in[(uint64_t)i * n_cells + n], LatticeW<Q, typename C::R>::w(i));
 }
 
 // ---------------------------------------------------------------------------

@@ -33,3 +33,53 @@ def spinodal(res, rho0=0.69, amplitude=0.01, seed=4):
     n = int(res[0]) * int(res[1]) * int(res[2])
     rng = np.random.default_rng(seed)
     return (rho0 + amplitude * rng.uniform(-1, 1, n)).astype(np.float32)
+
+
+def rayleigh_benard(res, ra=1e5, pr=0.71, kappa=0.008, beta=0.5, seed=5, storage=None):
+    """Hot bottom (T = 1) and cold top (T = 0) walls at z = 0 and z = nz-1,
+    periodic x and y; gravity along -z sized for Rayleigh number `ra` with
+    H = nz - 2 fluid layers, D3Q7 diffusivity kappa = (tau_T - 1/2)/4 and
+    nu = pr kappa; Boussinesq force F (1 - beta (T - 1)) from the solver's
+    thermal coupling (the reference's buoyancy form).
+    -> (solver, kappa, h)."""
+    from . import lbm as bf
+    if storage is None:
+        storage = bf.FloatingPointAccuracy.fp32
+    nx, ny, nz = res
+    n = nx * ny * nz
+    h = nz - 2
+    nu = pr * kappa
+    tau, tau_t = 3 * nu + 0.5, 4 * kappa + 0.5
+    # buoyancy contrast across the layer: g beta dT with dT = 1
+    g = ra * nu * kappa / (beta * h ** 3)
+    z = np.repeat(np.arange(nz), nx * ny)
+    ids = np.zeros(n, np.uint32)
+    ids[z == 0] = 1
+    ids[z == nz - 1] = 2
+    rng = np.random.default_rng(seed)
+    zf = (z - 0.5) / h
+    temp = (1.0 - np.clip(zf, 0, 1) + 1e-3 * rng.uniform(-1, 1, n)).astype(np.float32)
+    force = np.zeros((n, 3), np.float32)
+    force[:, 2] = -g
+    s = bf.LBM()
+    s.is_collide_esoteric = True
+    s.boundary_mode = bf.BoundaryMode.bounce_back
+    s.collision = bf.Collision.trt
+    s.thermal_relaxation_time = tau_t
+    s.thermal_expansion_coefficient = beta
+    s.thermal_init_equilibrium = True
+    s.set_boundry_properties(1, velocity_translational=(0, 0, 0), temperature=1.0)
+    s.set_boundry_properties(2, velocity_translational=(0, 0, 0), temperature=0.0)
+    s.initialize_fields_from_arrays(res, tau, force=force, temperature=temp, boundry_id=ids,
+                                    periodic=(True, True, False), velocity_set=bf.VelocitySet.D3Q19,
+                                    fp_accuracy=storage)
+    return s, kappa, h
+
+
+def nusselt(s, kappa, h):
+    nx, ny, nz = s.get_resolution()
+    vd = s.get_velocity_density_texture().reshape(nz, ny, nx, 4)
+    ft = s.get_force_temperature_texture().reshape(nz, ny, nx, 4)
+    uz, T = vd[1:-1, :, :, 2].astype(np.float64), ft[1:-1, :, :, 3].astype(np.float64)
+    # conductive profile dT/dz = -1/h: Nu = 1 + <u_z T> h / kappa
+    return 1.0 + (uz * T).mean() * h / kappa

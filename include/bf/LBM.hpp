@@ -239,6 +239,31 @@ public:
     }
     void synchronize(int32_t timeout_ms = 0) { check(bf_synchronize(s_, timeout_ms)); }
 
+    // ---- volume rendering (LBM.h render3d_*, LBM.cpp:1207-1376), headless ----
+    // view / projection: column-major 4x4 (glm::value_ptr of the camera's
+    // matrices); rgba_device: width*height*4 floats on the device
+    void render3d_density(const float* view, const float* projection, int32_t width, int32_t height,
+                          int32_t sample_count, float* rgba_device, void* stream = nullptr) {
+        check(bf_render3d(s_, BF_RENDER_DENSITY, view, projection, width, height, sample_count, rgba_device, stream));
+    }
+    void render3d_velocity(const float* view, const float* projection, int32_t width, int32_t height,
+                           int32_t sample_count, float* rgba_device, void* stream = nullptr) {
+        check(bf_render3d(s_, BF_RENDER_VELOCITY, view, projection, width, height, sample_count, rgba_device, stream));
+    }
+    void render3d_boundries(const float* view, const float* projection, int32_t width, int32_t height,
+                            int32_t sample_count, float* rgba_device, void* stream = nullptr) {
+        check(bf_render3d(s_, BF_RENDER_BOUNDRIES, view, projection, width, height, sample_count, rgba_device, stream));
+    }
+    void render3d_forces(const float* view, const float* projection, int32_t width, int32_t height,
+                         int32_t sample_count, float* rgba_device, void* stream = nullptr) {
+        check(bf_render3d(s_, BF_RENDER_FORCES, view, projection, width, height, sample_count, rgba_device, stream));
+    }
+    void render3d_temperature(const float* view, const float* projection, int32_t width, int32_t height,
+                              int32_t sample_count, float* rgba_device, void* stream = nullptr) {
+        check(bf_render3d(s_, BF_RENDER_TEMPERATURE, view, projection, width, height, sample_count, rgba_device,
+                          stream));
+    }
+
     // ---- public knobs (LBM.h:139-145, :242-243, :257) + extensions ----
     bool is_lattice_texture3d = false;  // storage layout of the GL path: no effect here
     bool is_collide_esoteric = false;
@@ -272,5 +297,57 @@ private:
     FloatingPointAccuracy fp_ = fp32;
     bool periodic_[3] = {true, true, true};
 };
+
+// MarchingCubes (BoltzmannFluids/Source/MarchingCubes/MarchingCubes.h): the
+// triangle list of a device scalar field, on the GPU.
+class MarchingCubes {
+public:
+    MarchingCubes() { check(bf_mc_create(&m_)); }
+    ~MarchingCubes() { bf_mc_destroy(m_); }
+    MarchingCubes(const MarchingCubes&) = delete;
+    MarchingCubes& operator=(const MarchingCubes&) = delete;
+
+    // the density of an LBM's velocity/density field; returns the triangle count
+    uint64_t compute(const Field& velocity_density, float threshold = 1.0f, vec3 mesh_scale = vec3(1, 1, 1),
+                     void* stream = nullptr) {
+        const float sc[3] = {mesh_scale.x, mesh_scale.y, mesh_scale.z};
+        uint64_t n = 0;
+        check(bf_mc_compute(m_, static_cast<const float*>(velocity_density.desc.device_ptr), 4, 3,
+                            velocity_density.desc.resolution, threshold, sc, stream, &n));
+        return n;
+    }
+    // device vertices: triangle_count * 9 floats, valid until the next compute
+    const float* vertices(uint64_t* triangle_count) {
+        const float* v = nullptr;
+        check(bf_mc_get_vertices(m_, &v, triangle_count));
+        return v;
+    }
+    std::vector<float> vertices_host() {
+        uint64_t n = 0;
+        vertices(&n);
+        std::vector<float> out(n * 9);
+        uint64_t w = 0;
+        check(bf_mc_copy_vertices_to_host(m_, out.data(), n, &w));
+        return out;
+    }
+
+private:
+    static void check(int code) {
+        if (code != BF_OK) throw LBMError(code, bf_last_error());
+    }
+    bf_marching_cubes* m_ = nullptr;
+};
+
+// MeshRasterizer3D::rasterize (MeshRasterizer3D.h:16-19) as a GPU ray-parity
+// voxeliser: mask[nx*ny*nz] = 1 for voxels inside the closed mesh
+inline std::vector<uint8_t> rasterize_mesh(const std::vector<float>& triangle_vertices, ivec3 resolution,
+                                           const float* model_matrix = nullptr, int32_t samples_per_voxel = 64) {
+    const int32_t res[3] = {resolution.x, resolution.y, resolution.z};
+    std::vector<uint8_t> mask((size_t)resolution.x * resolution.y * resolution.z);
+    const int code = bf_voxelize_mesh(triangle_vertices.data(), triangle_vertices.size() / 9, model_matrix, res,
+                                      samples_per_voxel, mask.data());
+    if (code != BF_OK) throw LBMError(code, bf_last_error());
+    return mask;
+}
 
 }  // namespace bf

@@ -187,21 +187,45 @@ typedef struct { REAL x, y, z; } v3;
 static v3 mk3(REAL x, REAL y, REAL z) { v3 r = {x, y, z}; return r; }
 static REAL dot3(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 
-static REAL store_round(const orc_t* s, REAL v, int i) {
+/* DDF storage emulation.  The lattice array holds what the device stores,
+ * decoded to a float: f itself for fp32 and fp16 (rounded to half);
+ * the shifted population g = f - w (rounded to half) for fp16s; the custom
+ * 16-bit value a of (f - w)/w for fp16c.  The shifted storages run the
+ * update on g (see collide), as the kernels do. */
+static int shifted(const orc_t* s) {
+    return IS_F32 && (s->d.storage == ORC_STORE_FP16S || s->d.storage == ORC_STORE_FP16C);
+}
+static float c16_round(float v) { return c16_to_f32(f32_to_c16(v)); }
+/* stored value of slot i -> the value the update works on (g when shifted) */
+static REAL lat_load(const orc_t* s, REAL raw, int i) {
+    if (IS_F32 && s->d.storage == ORC_STORE_FP16C) return (REAL)((float)raw * (float)s->V[i].w);
+    return raw;
+}
+/* value the update produced -> stored value */
+static REAL lat_store(const orc_t* s, REAL v, int i) {
     if (!IS_F32) return v;
     switch (s->d.storage) {
-    case ORC_STORE_FP16: return (REAL)f16_to_f32(f32_to_f16_rne((float)v));
-    case ORC_STORE_FP16S: {
-        float w = (float)s->V[i].w;
-        return (REAL)(f16_to_f32(f32_to_f16_rne((float)v - w)) + w);
-    }
-    case ORC_STORE_FP16C: {
-        float w = (float)s->V[i].w;
-        float winv = 1.0f / w;
-        return (REAL)fmaf(c16_to_f32(f32_to_c16(((float)v - w) * winv)), w, w);
-    }
+    case ORC_STORE_FP16:
+    case ORC_STORE_FP16S: return (REAL)f16_to_f32(f32_to_f16_rne((float)v));
+    case ORC_STORE_FP16C: return (REAL)c16_round((float)v * (1.0f / (float)s->V[i].w));
     default: return v;
     }
+}
+/* population f -> stored value (initialisation, set_lattice) */
+static REAL lat_from_f(const orc_t* s, REAL f, int i) {
+    if (shifted(s)) {
+        float w = (float)s->V[i].w;
+        if (s->d.storage == ORC_STORE_FP16S) return (REAL)f16_to_f32(f32_to_f16_rne((float)f - w));
+        return (REAL)c16_round(((float)f - w) * (1.0f / w));
+    }
+    return lat_store(s, f, i);
+}
+/* stored value -> population f (get_lattice) */
+static REAL lat_to_f(const orc_t* s, REAL raw, int i) {
+    if (!shifted(s)) return raw;
+    float w = (float)s->V[i].w;
+    if (s->d.storage == ORC_STORE_FP16S) return (REAL)((float)raw + w);
+    return (REAL)fmaf((float)raw, w, w);
 }
 
 static int opp(int i) { /* collide.comp:219-222 */
@@ -372,6 +396,7 @@ static void collide(orc_t* s, int save, int update) {
     REAL* L = LSRC(s);
     const size_t N = s->N;
     const int bb = s->d.esoteric && s->d.boundary_mode == ORC_BOUNDARY_BOUNCE_BACK;
+    const int sh = shifted(s);
     /* cells are independent within one dispatch: the AA step reads and
      * writes the same private set of slots per cell, so the loop is safe to
      * run in parallel exactly as the GPU dispatch is. */
@@ -398,8 +423,8 @@ static void collide(orc_t* s, int save, int update) {
                 if (eqb && sopen) {
                     REAL rb = (REAL)s->bvals[cell * 4 + 0];
                     v3 ub = mk3((REAL)s->bvals[cell * 4 + 1], (REAL)s->bvals[cell * 4 + 2], (REAL)s->bvals[cell * 4 + 3]);
-                    f[i] = ((REAL)s->V[i].w * rb) * bracket(s, cdot(s->V[i].cx, s->V[i].cy, s->V[i].cz, ub),
-                                                             (REAL)1 - uu_of(ub) * s->R2h);
+                    REAL br = bracket(s, cdot(s->V[i].cx, s->V[i].cy, s->V[i].cz, ub), (REAL)1 - uu_of(ub) * s->R2h);
+                    f[i] = sh ? FMA((REAL)s->V[i].w * rb, br, -(REAL)s->V[i].w) : ((REAL)s->V[i].w * rb) * br;
                     continue;
                 }
                 if (bb && !sopen && is_solid(s, sid)) {
@@ -410,11 +435,12 @@ static void collide(orc_t* s, int save, int update) {
                     const float* ob = &s->objects[sid * 12];
                     v3 uw = mk3((REAL)ob[0], (REAL)ob[1], (REAL)ob[2]);
                     v3 co = mk3((REAL)s->V[oi].cx, (REAL)s->V[oi].cy, (REAL)s->V[oi].cz);
-                    f[i] = L[(size_t)os * N + oc] + (REAL)(-2) * (REAL)s->V[oi].w * (REAL)1.0 * dot3(co, uw) * (REAL)3;
+                    f[i] = lat_load(s, L[(size_t)os * N + oc], os) + (REAL)(-2) * (REAL)s->V[oi].w * (REAL)1.0 * dot3(co, uw) * (REAL)3;
                     continue;
                 }
             }
-            f[i] = open ? (REAL)0.01 : L[(size_t)rs * N + rc];
+            /* out-of-domain reads give 0.01 (collide.comp:278-298); g = 0.01 - w when shifted */
+            f[i] = open ? (sh ? (REAL)0.01 - (REAL)s->V[i].w : (REAL)0.01) : lat_load(s, L[(size_t)rs * N + rc], rs);
         }
         /* ---- canonical FP32 evaluation (shared with the CUDA kernels) ----
          * opposite populations pair as (i, i+1), i odd:  s = f_i + f_i+1,
@@ -423,6 +449,7 @@ static void collide(orc_t* s, int save, int update) {
         for (int i = 1; i < Q; i += 2) { sp[i / 2] = f[i] + f[i + 1]; dp_[i / 2] = f[i] - f[i + 1]; }
         REAL density = f[0];
         for (int i = 1; i < Q; i += 2) density = density + sp[i / 2];
+        if (sh) density = (REAL)1 + density; /* sum of g plus sum of w */
         if (density < (REAL)0.01) density = (REAL)0.01; /* max(density, 0.01) */
         v3 force = get_force(s, cell);
         REAL temperature = 0;
@@ -483,7 +510,9 @@ static void collide(orc_t* s, int save, int update) {
                 for (int i = 0; i < Q; i++) {
                     REAL w = (REAL)s->V[i].w;
                     REAL cu = cdot(s->V[i].cx, s->V[i].cy, s->V[i].cz, vel);
-                    REAL fe = (w * density) * bracket(s, cu, one_m);
+                    /* shifted storages form g_eq = fma(w rho, bracket, -w) */
+                    REAL br = bracket(s, cu, one_m);
+                    REAL fe = sh ? FMA(w * density, br, -w) : (w * density) * br;
                     REAL v = FMA(fe - f[i], s->Rtau, f[i]); /* old + (-(old - feq)/tau) */
                     if (s->src_on) {
                         REAL fc = cdot(s->V[i].cx, s->V[i].cy, s->V[i].cz, force);
@@ -502,7 +531,7 @@ static void collide(orc_t* s, int save, int update) {
                  * velocity limit the populations become e+ +- e-. */
                 {
                     REAL w0 = (REAL)s->V[0].w;
-                    REAL fe0 = (w0 * density) * one_m;
+                    REAL fe0 = sh ? FMA(w0 * density, one_m, -w0) : (w0 * density) * one_m;
                     REAL v = FMA(fe0 - f[0], s->Rtau, f[0]);
                     if (s->src_on) v = FMA(s->Pp * w0, -fuR2, v);
                     fn[0] = out_ext ? fe0 : v;
@@ -512,7 +541,8 @@ static void collide(orc_t* s, int save, int update) {
                     REAL w = (REAL)s->V[i].w;
                     REAL cu = cdot(s->V[i].cx, s->V[i].cy, s->V[i].cz, vel);
                     REAL wr = w * density;
-                    REAL ep = wr * FMA(cu * cu, s->R4h, one_m);
+                    REAL be = FMA(cu * cu, s->R4h, one_m);
+                    REAL ep = sh ? FMA(wr, be, -w) : wr * be;
                     REAL em = (wr * s->R2) * cu;
                     REAL Pd = FMA(sp[i / 2], (REAL)0.5, -ep);
                     REAL Md = FMA(dp_[i / 2], (REAL)0.5, -em);
@@ -532,7 +562,7 @@ static void collide(orc_t* s, int save, int update) {
             for (int i = 0; i < Q; i++) {
                 size_t wc; int ws;
                 if (aa_write_addr(s, x, y, z, i, odd, &wc, &ws)) continue;
-                L[(size_t)ws * N + wc] = store_round(s, fn[i], ws);
+                L[(size_t)ws * N + wc] = lat_store(s, fn[i], ws);
             }
         }
         if (s->d.multiphase) {
@@ -580,7 +610,10 @@ static void stream(orc_t* s) {
         int inv = (i == 0 || i >= Q) ? 0 : ((i % 2 == 1) ? i + 1 : i - 1);
         if (is_solid(s, get_boundry(s, cell))) continue;
         int sx = x - s->V[i].cx, sy = y - s->V[i].cy, sz = z - s->V[i].cz;
-        if (wrap(s, &sx, &sy, &sz)) { T[(size_t)i * N + cell] = store_round(s, (REAL)0.01, i); continue; }
+        if (wrap(s, &sx, &sy, &sz)) {
+            T[(size_t)i * N + cell] = lat_store(s, shifted(s) ? (REAL)0.01 - (REAL)s->V[i].w : (REAL)0.01, i);
+            continue;
+        }
         size_t sc = cid(s, sx, sy, sz);
         uint32_t sid = get_boundry(s, sc);
         if (is_solid(s, sid)) {
@@ -588,7 +621,7 @@ static void stream(orc_t* s) {
             v3 uw = mk3((REAL)ob[0], (REAL)ob[1], (REAL)ob[2]);
             v3 c = mk3((REAL)s->V[inv].cx, (REAL)s->V[inv].cy, (REAL)s->V[inv].cz);
             REAL corr = (REAL)(-2) * (REAL)s->V[inv].w * (REAL)1.0 * dot3(c, uw) * (REAL)3;
-            T[(size_t)i * N + cell] = store_round(s, S[(size_t)inv * N + cell] + corr, i);
+            T[(size_t)i * N + cell] = lat_store(s, lat_load(s, S[(size_t)inv * N + cell], inv) + corr, i);
         } else {
             T[(size_t)i * N + cell] = S[(size_t)i * N + sc];
         }
@@ -764,7 +797,7 @@ orc_t* ORC(create)(const orc_desc* d, const float* rho, const float* u, const fl
         v3 uc = mk3(0, 0, 0);
         if (u && !is_solid(s, id)) uc = mk3((REAL)u[c * 3], (REAL)u[c * 3 + 1], (REAL)u[c * 3 + 2]);
         REAL r = rho ? (REAL)rho[c] : (REAL)1;
-        for (int i = 0; i < s->Q; i++) L[(size_t)i * N + c] = store_round(s, feq_init(s, r, uc, i), i);
+        for (int i = 0; i < s->Q; i++) L[(size_t)i * N + c] = lat_from_f(s, feq_init(s, r, uc, i), i);
     }
     if (s->thermal) {
         s->th[0] = (REAL*)calloc(N * s->Qt, sizeof(REAL));
@@ -815,11 +848,11 @@ void ORC(get_fields)(orc_t* s, double* vel_den, double* force_temp, float* bnd) 
 /* copies the raw DDF buffer (source lattice, SoA i*N+cell) */
 void ORC(get_lattice)(orc_t* s, double* out) {
     REAL* L = LSRC(s);
-    for (size_t k = 0; k < s->N * (size_t)s->Q; k++) out[k] = (double)L[k];
+    for (size_t k = 0; k < s->N * (size_t)s->Q; k++) out[k] = (double)lat_to_f(s, L[k], (int)(k / s->N));
 }
 void ORC(set_lattice)(orc_t* s, const double* in) {
     REAL* L = LSRC(s);
-    for (size_t k = 0; k < s->N * (size_t)s->Q; k++) L[k] = (REAL)in[k];
+    for (size_t k = 0; k < s->N * (size_t)s->Q; k++) L[k] = lat_from_f(s, (REAL)in[k], (int)(k / s->N));
 }
 void ORC(get_thermal)(orc_t* s, double* out) {
     if (!s->thermal) return;

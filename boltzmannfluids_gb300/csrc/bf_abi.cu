@@ -105,6 +105,7 @@ struct bf_solver {
     std::map<int, cudaGraphExec_t> graphs;
     bool graphs_enabled = true;
     uint32_t pf_blocks = 0;  // L2 prefetch distance of the fast kernel, in blocks (0 = off)
+    bool tma_step = true;    // 16-bit fast step with loads staged by bulk copies
 };
 
 namespace {
@@ -251,7 +252,9 @@ cudaError_t collide(bf_solver* s, bool save, bool update, bool reduce, bool meas
     p.err = s->err.as<unsigned int>();
 
     int mode = s->desc.esoteric ? ((s->ticks % 2 == 1) ? AA_ODD : AA_EVEN) : AA_LOCAL;
-    const uint32_t heavy = F_BOUNDARIES | F_FORCE_FIELD | F_THERMAL | F_MULTIPHASE | F_EQ_BOUNDARIES;
+    // the fast kernel covers periodic boxes without objects, force fields or a
+    // thermal lattice; a constant force and the Shan-Chen force are in it
+    const uint32_t heavy = F_BOUNDARIES | F_FORCE_FIELD | F_THERMAL | F_EQ_BOUNDARIES;
     const bool all_periodic = (p.flags & (F_PERIODIC_X | F_PERIODIC_Y | F_PERIODIC_Z)) ==
                               (F_PERIODIC_X | F_PERIODIC_Y | F_PERIODIC_Z);
     // the fast kernel indexes every slot with 32 bits off the first plane
@@ -262,6 +265,7 @@ cudaError_t collide(bf_solver* s, bool save, bool update, bool reduce, bool meas
     const size_t plane_bytes = (size_t)s->N * storage_bytes(s->desc.storage);
     if (!generic && plane_bytes % 16 == 0 && reinterpret_cast<uintptr_t>(lat_src(s)) % 16 == 0)
         p.pf_blocks = s->pf_blocks;
+    p.tma = s->tma_step ? 1u : 0u;
     switch (s->Q) {
     case 9: fill_uoff<9>(p); break;
     case 15: fill_uoff<15>(p); break;
@@ -482,6 +486,8 @@ int bf_create(bf_solver** out) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
     s->pf_blocks = (uint32_t)std::max(sms, 1) * 4u;
     if (const char* env = std::getenv("BF_PREFETCH_BLOCKS")) s->pf_blocks = (uint32_t)std::strtoul(env, nullptr, 10);
+    // BF_TMA_STEP=0 selects the plain 16-bit fast step (A/B comparisons)
+    if (const char* env = std::getenv("BF_TMA_STEP")) s->tma_step = std::strtoul(env, nullptr, 10) != 0;
     *out = s;
     return BF_OK;
 }
@@ -747,6 +753,7 @@ int bf_synchronize(bf_solver* s, int32_t timeout_ms) {
         unsigned int h = 0;
         BF_CUDA(cudaMemcpy(&h, s->err.p, sizeof(h), cudaMemcpyDeviceToHost));
         if (h & 1u) return fail(BF_ERR_UNSTABLE, "a step computed a NaN density (simulation unstable)");
+        if (h & 2u) return fail(BF_ERR_TIMEOUT, "a step's copy pipeline gave up waiting for its loads");
     }
     return BF_OK;
 }

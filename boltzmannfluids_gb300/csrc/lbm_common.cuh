@@ -166,7 +166,13 @@ template <> struct Codec<ST_FP16C> {  // custom 16-bit of g/w = (f - w)/w
     using T = uint16_t;
     using R = float;
     static constexpr bool SHIFTED = true;
-    __device__ __forceinline__ static float dec(T v, float w) { return __fmul_rn(decode_c16(v), w); }
+    // = decode_c16(v) * w with one rounding: the 15 code bits and the sign
+    // placed in an FP32 pattern from the sign-extended code (shift, one AND),
+    // times the exact constant w * 2^114
+    __device__ __forceinline__ static float dec(T v, float w) {
+        const uint32_t a = ((uint32_t)(int32_t)(int16_t)v << 12) & 0x87fff000u;
+        return __fmul_rn(__uint_as_float(a), w * 0x1p114f);
+    }
     __device__ __forceinline__ static T enc(float g, float w) { return encode_c16(__fmul_rn(g, 1.0f / w)); }
     __device__ __forceinline__ static float dec_f(T v, float w) { return fmaf(decode_c16(v), w, w); }
     __device__ __forceinline__ static T enc_f(float v, float w) { return encode_c16(__fmul_rn(__fsub_rn(v, w), 1.0f / w)); }
@@ -217,6 +223,9 @@ struct alignas(16) StepParams {
     // block prefetches into L2 with bulk copies; 0 = off.  Only set when every
     // population plane starts and ends on a 16-byte boundary.
     uint32_t pf_blocks;
+    // 1: the 16-bit fast step may stage its loads through shared memory with
+    // bulk copies (lbm_tma.cuh); set by the host when the planes allow it
+    uint32_t tma;
     // fast kernel, even step, rows off the y/z faces: element offset of the
     // slot read for direction i relative to the cell, without its x part:
     // i * stride - (c_y nx + c_z nx ny), modulo 2^32

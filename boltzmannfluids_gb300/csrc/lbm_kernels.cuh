@@ -14,6 +14,8 @@
 #pragma once
 #include "lbm_common.cuh"
 
+#include <algorithm>
+
 namespace bf {
 
 template <class R> struct CellSumT { R m, px, py, pz, ke; };
@@ -454,8 +456,12 @@ constexpr int kFastMinBlocks16 = BF_FAST_MIN_BLOCKS_16;
 // the box, so the y/z neighbour offsets wrap and are computed in the block;
 // otherwise they are the launch constants p.uoff (plane offset minus
 // c_y nx + c_z nx ny), one constant-bank operand per index.
-template <int Q, int ST, int MODE, bool TRT, bool FORCED, bool EDGE>
-__device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepParams& p, int x, int y, int z) {
+// load(i, slot) returns the stored element of direction i; slot(k) is the
+// element index of the slot read for direction k (the plain kernel loads
+// base[slot(i)], the staged kernel reads shared memory and never calls it)
+template <int Q, int ST, int MODE, bool TRT, bool FORCED, bool MP, bool EDGE, class Load>
+__device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepParams& p, int x, int y, int z,
+                                                                     Load&& load) {
     using L = Lattice<Q>;
     using C = Codec<ST>;
     using T = typename C::T;
@@ -486,8 +492,9 @@ __device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepP
         return nn + (uint32_t)opp(i) * S;
     };
     R f[Q];
+    auto slot_of = [&](int k) -> uint32_t { return slot(k, n, oxm, oxp); };
 #pragma unroll
-    for (int i = 0; i < Q; i++) f[i] = C::dec(base[slot(i, n, oxm, oxp)], W::w(i));
+    for (int i = 0; i < Q; i++) f[i] = C::dec(load(i, slot_of), W::w(i));
     // the store phase recomputes its indices (one add each) from opaque
     // copies of the per-thread terms instead of keeping Q indices live
     uint32_t n_st = n;
@@ -502,6 +509,25 @@ __device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepP
     m.Fx = FORCED ? (F64 ? R(p.k64.fconst[0]) : R(p.fconst[0])) : R(0);
     m.Fy = FORCED ? (F64 ? R(p.k64.fconst[1]) : R(p.fconst[1])) : R(0);
     m.Fz = FORCED ? (F64 ? R(p.k64.fconst[2]) : R(p.fconst[2])) : R(0);
+    if constexpr (MP && !F64) {
+        // Shan-Chen pseudopotential force (collide.comp:534-584), the generic
+        // kernel's arithmetic: psi of the previous step at the periodic
+        // neighbours x + c_i, summed as w_i psi c_i in direction order
+        const float self_psi = FSUB(1.0f, exp_f32(-m.rho));
+        float sx = 0.f, sy = 0.f, sz = 0.f;
+#pragma unroll
+        for (int i = 1; i < Q; i++) {
+            const Dir c = L::c(i);
+            const uint32_t a = n + (uint32_t)((c.x > 0 ? oxp : (c.x < 0 ? oxm : 0)) + (c.y > 0 ? oyp : (c.y < 0 ? oym : 0)) +
+                                              (c.z > 0 ? ozp : (c.z < 0 ? ozm : 0)));
+            const float wp = FMUL(L::w(i), __ldg(p.psi_src + a));
+            if (c.x) sx = FADD(sx, c.x > 0 ? wp : -wp);
+            if (c.y) sy = FADD(sy, c.y > 0 ? wp : -wp);
+            if (c.z) sz = FADD(sz, c.z > 0 ? wp : -wp);
+        }
+        const float k = FMUL(-self_psi, p.G);
+        m.Fx = FFMA(sx, k, m.Fx); m.Fy = FFMA(sy, k, m.Fy); m.Fz = FFMA(sz, k, m.Fz);
+    }
     if constexpr (F64) velocity_and_limit<Q>(f, m, FORCED, p.k64.vlim, p.k64.vlim_ext);
     else velocity_and_limit<Q>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
     if (p.flags & F_UPDATE) {
@@ -509,6 +535,10 @@ __device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepP
         auto emit = [&](int i, R v) { base[slot(opp(i), n_st, oxm_st, oxp_st)] = C::enc(v, W::w(i)); };
         if (m.out_ext) collide_fixed<Q, TRT, FORCED, true, C::SHIFTED>(f, m, k, emit);
         else collide_fixed<Q, TRT, FORCED, false, C::SHIFTED>(f, m, k, emit);
+    }
+    if constexpr (MP && !F64) {
+        // psi of this step's density for the next step (collide.comp:763-769)
+        if (!(p.flags & F_MEASURE)) p.psi_tgt[n] = FSUB(1.0f, exp_f32(-m.rho));
     }
     if (p.flags & F_SAVE) {
         p.vel_den[n] = make_float4((float)m.ux, (float)m.uy, (float)m.uz, (float)m.rho);
@@ -522,7 +552,7 @@ __device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepP
     return cs;
 }
 
-template <int Q, int ST, int MODE, bool TRT, bool FORCED>
+template <int Q, int ST, int MODE, bool TRT, bool FORCED, bool MP>
 __global__ void __launch_bounds__(kStepBlock,
                                   ST == ST_FP64 ? 2 : ((ST == ST_FP32 || Q == 27) ? kFastMinBlocks : kFastMinBlocks16))
     fast_step_kernel(const __grid_constant__ StepParams p) {
@@ -538,8 +568,11 @@ __global__ void __launch_bounds__(kStepBlock,
         // block-uniform choice: rows on a y or z face wrap their neighbour offsets
         const bool edge = MODE == AA_EVEN &&
                           (y == 0 || y == p.ny - 1 || (Lattice<Q>::D == 3 && (z == 0 || z == p.nz - 1)));
-        if (edge) cs = fast_cell<Q, ST, MODE, TRT, FORCED, true>(p, x, y, z);
-        else cs = fast_cell<Q, ST, MODE, TRT, FORCED, false>(p, x, y, z);
+        using T = typename Codec<ST>::T;
+        const T* base = static_cast<const T*>(p.plane[0]);
+        auto load = [&](int i, auto&& slot_of) -> T { return base[slot_of(i)]; };
+        if (edge) cs = fast_cell<Q, ST, MODE, TRT, FORCED, MP, true>(p, x, y, z, load);
+        else cs = fast_cell<Q, ST, MODE, TRT, FORCED, MP, false>(p, x, y, z, load);
     }
     if (p.flags & F_REDUCE) block_reduce_store(cs, p.red_partials);
 }
@@ -873,6 +906,10 @@ __global__ void encode_kernel(void* f, uint64_t stride, uint32_t n_cells, const 
         F[(uint64_t)i * stride + n] = C::enc_f(in[(uint64_t)i * n_cells + n], LatticeW<Q, typename C::R>::w(i));
 }
 
+}  // namespace bf
+#include "lbm_tma.cuh"
+namespace bf {
+
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
@@ -881,29 +918,59 @@ inline dim3 cell_grid(int nx, int ny, int nz, int& block) {
     return dim3((unsigned)((nx + block - 1) / block), (unsigned)ny, (unsigned)nz);
 }
 
+// persistent grid of the staged kernel: every SM filled with resident blocks
+template <int Q, int ST, int MODE, bool TRT, bool FORCED>
+cudaError_t launch_tma(const StepParams& p, cudaStream_t st) {
+    auto kernel = tma_step_kernel<Q, ST, MODE, TRT, FORCED>;
+    constexpr size_t smem = tma_smem_bytes<Q, ST>();
+    static int per_sm = -1, sms = 0;  // per instantiation, first device
+    if (per_sm < 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kTmaTile, smem);
+        if (per_sm < 1) per_sm = 1;
+    }
+    const uint32_t tiles = ((uint32_t)p.nx / kTmaTile) * (uint32_t)p.ny * (uint32_t)p.nz;
+    const uint32_t blocks = std::min<uint32_t>(tiles, (uint32_t)(sms * per_sm));
+    kernel<<<blocks, kTmaTile, smem, st>>>(p);
+    return cudaGetLastError();
+}
+
 template <int Q, int ST>
 cudaError_t launch_step_st(const StepParams& p, int mode, bool generic, cudaStream_t st) {
     int block;
     dim3 grid = cell_grid(p.nx, p.ny, p.nz, block);
-    if (!generic) {
-        const bool trt = (p.flags & F_TRT) != 0, forced = (p.flags & F_FORCE_CONST) != 0;
-        if (mode == AA_EVEN) {
-            if (trt) {
-                if (forced) fast_step_kernel<Q, ST, AA_EVEN, true, true><<<grid, block, 0, st>>>(p);
-                else fast_step_kernel<Q, ST, AA_EVEN, true, false><<<grid, block, 0, st>>>(p);
-            } else {
-                if (forced) fast_step_kernel<Q, ST, AA_EVEN, false, true><<<grid, block, 0, st>>>(p);
-                else fast_step_kernel<Q, ST, AA_EVEN, false, false><<<grid, block, 0, st>>>(p);
+    // staged loads: 16-bit storage, an update step without reduction or
+    // multiphase, whole 256-cell tiles per row, 16-byte aligned planes
+    if constexpr (ST == ST_FP16 || ST == ST_FP16S || ST == ST_FP16C) {
+        if (!generic && p.tma && (p.flags & F_UPDATE) && !(p.flags & (F_REDUCE | F_MULTIPHASE)) &&
+            p.nx % kTmaTile == 0 && reinterpret_cast<uintptr_t>(p.plane[0]) % 16 == 0) {
+            const bool trt = (p.flags & F_TRT) != 0, forced = (p.flags & F_FORCE_CONST) != 0;
+            if (mode == AA_EVEN) {
+                if (trt) return forced ? launch_tma<Q, ST, AA_EVEN, true, true>(p, st) : launch_tma<Q, ST, AA_EVEN, true, false>(p, st);
+                return forced ? launch_tma<Q, ST, AA_EVEN, false, true>(p, st) : launch_tma<Q, ST, AA_EVEN, false, false>(p, st);
             }
-        } else {
-            if (trt) {
-                if (forced) fast_step_kernel<Q, ST, AA_ODD, true, true><<<grid, block, 0, st>>>(p);
-                else fast_step_kernel<Q, ST, AA_ODD, true, false><<<grid, block, 0, st>>>(p);
-            } else {
-                if (forced) fast_step_kernel<Q, ST, AA_ODD, false, true><<<grid, block, 0, st>>>(p);
-                else fast_step_kernel<Q, ST, AA_ODD, false, false><<<grid, block, 0, st>>>(p);
-            }
+            if (trt) return forced ? launch_tma<Q, ST, AA_ODD, true, true>(p, st) : launch_tma<Q, ST, AA_ODD, true, false>(p, st);
+            return forced ? launch_tma<Q, ST, AA_ODD, false, true>(p, st) : launch_tma<Q, ST, AA_ODD, false, false>(p, st);
         }
+    }
+    if (!generic) {
+        // multiphase flow is forced (the pseudopotential) with the source term on
+        const bool trt = (p.flags & F_TRT) != 0, mp = (p.flags & F_MULTIPHASE) != 0;
+        const bool forced = (p.flags & F_FORCE_CONST) != 0 || mp;
+        auto go = [&](auto kernel) { kernel<<<grid, block, 0, st>>>(p); };
+#define BF_FAST(MODE_, TRT_, F_, MP_) go(fast_step_kernel<Q, ST, MODE_, TRT_, F_, MP_>)
+        if (mode == AA_EVEN) {
+            if (mp) { if (trt) BF_FAST(AA_EVEN, true, true, true); else BF_FAST(AA_EVEN, false, true, true); }
+            else if (trt) { if (forced) BF_FAST(AA_EVEN, true, true, false); else BF_FAST(AA_EVEN, true, false, false); }
+            else { if (forced) BF_FAST(AA_EVEN, false, true, false); else BF_FAST(AA_EVEN, false, false, false); }
+        } else {
+            if (mp) { if (trt) BF_FAST(AA_ODD, true, true, true); else BF_FAST(AA_ODD, false, true, true); }
+            else if (trt) { if (forced) BF_FAST(AA_ODD, true, true, false); else BF_FAST(AA_ODD, true, false, false); }
+            else { if (forced) BF_FAST(AA_ODD, false, true, false); else BF_FAST(AA_ODD, false, false, false); }
+        }
+#undef BF_FAST
     } else {
         // the FP64 reference stepper covers the fast path only
         if constexpr (ST == ST_FP64) return cudaErrorInvalidValue;

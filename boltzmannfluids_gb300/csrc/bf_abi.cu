@@ -105,7 +105,7 @@ struct bf_solver {
     std::map<int, cudaGraphExec_t> graphs;
     bool graphs_enabled = true;
     uint32_t pf_blocks = 0;  // L2 prefetch distance of the fast kernel, in blocks (0 = off)
-    bool tma_step = true;    // 16-bit fast step with loads staged by bulk copies
+    bool tma_step = false;   // 16-bit fast step with loads staged by bulk copies
 };
 
 namespace {
@@ -486,7 +486,7 @@ int bf_create(bf_solver** out) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
     s->pf_blocks = (uint32_t)std::max(sms, 1) * 4u;
     if (const char* env = std::getenv("BF_PREFETCH_BLOCKS")) s->pf_blocks = (uint32_t)std::strtoul(env, nullptr, 10);
-    // BF_TMA_STEP=0 selects the plain 16-bit fast step (A/B comparisons)
+    // BF_TMA_STEP=1 selects the staged 16-bit fast step, 0 the plain one
     if (const char* env = std::getenv("BF_TMA_STEP")) s->tma_step = std::strtoul(env, nullptr, 10) != 0;
     *out = s;
     return BF_OK;

@@ -1,0 +1,212 @@
+// lbm_tma.cuh -- the fast AA step with its population loads staged through
+// shared memory by the bulk-copy (TMA) engine, for the 16-bit storages.
+//
+// The 16-bit steps are issue-bound: half of a plain step's instructions are
+// load/store addressing and memory operations.  Here a persistent block walks
+// over row tiles of 256 cells (x0 .. x0+255 of one (y, z) row); for each tile
+// one warp issues, per direction i, a bulk copy of the row segment the tile
+// reads -- on an even step row (y - c_y, z - c_z) of plane i widened by 8
+// cells each side (the c_x shift), on an odd step row (y, z) of plane opp(i)
+// -- into one of kTmaStages shared-memory stages, completing on the stage's
+// mbarrier.  Threads read their 19 populations from the stage with constant
+// offsets (no address arithmetic), run the same update as the plain kernel
+// (fast_cell) and store to global memory.  The copies of the next tiles are
+// in flight while a tile is computed.
+//
+// Alignment: a bulk copy needs 16-byte aligned addresses and sizes.  Row
+// starts are multiples of nx elements with nx % 256 == 0, planes start at
+// multiples of N = nx*ny*nz, so every row segment [x0 - 8, x0 + 264) of
+// 16-bit data starts on a 16-byte boundary; at the two ends of a row the
+// 8-cell halos wrap to the other end of the same row (periodic in x) and are
+// copied separately (16 bytes each).  Every wait on an mbarrier is bounded:
+// past the limit the block sets bit 1 of the error word (reported as
+// BF_ERR_TIMEOUT), waits, again bounded, for its copies still in flight, and
+// returns.
+#pragma once
+
+namespace bf {
+
+constexpr int kTmaTile = 256;                        // cells per tile = threads per block
+constexpr int kTmaHalo = 8;                          // halo cells each side: 16 bytes of 16-bit data
+constexpr int kTmaRow = kTmaTile + 2 * kTmaHalo;     // staged elements per row
+constexpr int kTmaStages = 3;
+constexpr uint32_t kTmaWaitLimit = 1u << 24;         // try_wait polls before giving up
+
+__device__ __forceinline__ uint32_t smem_addr(const void* ptr) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(ptr));
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred P;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, P;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait for the phase with the given parity; false = gave up
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+    for (uint32_t k = 0; k < kTmaWaitLimit; k++)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+// bulk copy global -> shared, completing `bytes` on the mbarrier
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+
+// direction components packed 2 bits per direction (component + 1), so a
+// lane can look up its direction without a table in memory
+template <int Q>
+struct DirBits {
+    static constexpr uint64_t pack(int axis) {
+        uint64_t v = 0;
+        for (int i = 0; i < Q; i++) {
+            const Dir c = Lattice<Q>::c(i);
+            const int comp = axis == 0 ? c.x : (axis == 1 ? c.y : c.z);
+            v |= (uint64_t)(comp + 1) << (2 * i);
+        }
+        return v;
+    }
+    static constexpr uint64_t X = pack(0), Y = pack(1), Z = pack(2);
+    __device__ __forceinline__ static int cx(int i) { return (int)((X >> (2 * i)) & 3u) - 1; }
+    __device__ __forceinline__ static int cy(int i) { return (int)((Y >> (2 * i)) & 3u) - 1; }
+    __device__ __forceinline__ static int cz(int i) { return (int)((Z >> (2 * i)) & 3u) - 1; }
+};
+
+struct TmaTile {
+    int x0, y, z;
+};
+__device__ __forceinline__ TmaTile tma_tile(const StepParams& p, uint32_t t) {
+    const uint32_t tx = (uint32_t)p.nx / kTmaTile;
+    TmaTile r;
+    r.x0 = (int)(t % tx) * kTmaTile;
+    const uint32_t yz = t / tx;
+    r.y = (int)(yz % (uint32_t)p.ny);
+    r.z = (int)(yz / (uint32_t)p.ny);
+    return r;
+}
+
+// Warp 0 issues the copies of tile t into the stage at `stage` (shared
+// address), completing on `bar`: lane i < Q copies direction i's row.
+template <int Q, int ST, int MODE>
+__device__ __forceinline__ void tma_issue(const StepParams& p, uint32_t t, uint32_t stage, uint32_t bar, int lane) {
+    using T = typename Codec<ST>::T;
+    constexpr uint32_t sz = sizeof(T);
+    constexpr uint32_t row_bytes = (MODE == AA_EVEN ? kTmaRow : kTmaTile) * sz;
+    if (lane == 0) mbar_arrive_expect_tx(bar, (uint32_t)Q * row_bytes);
+    __syncwarp();
+    if (lane >= Q) return;
+    const TmaTile tl = tma_tile(p, t);
+    const int i = lane;
+    int ys = tl.y, zs = tl.z, plane = i;
+    if (MODE == AA_EVEN) {
+        ys -= DirBits<Q>::cy(i);
+        zs -= DirBits<Q>::cz(i);
+        ys = ys < 0 ? ys + p.ny : (ys >= p.ny ? ys - p.ny : ys);
+        zs = zs < 0 ? zs + p.nz : (zs >= p.nz ? zs - p.nz : zs);
+    } else {
+        plane = opp(i);
+    }
+    const T* row = static_cast<const T*>(p.plane[0]) + (size_t)plane * p.stride +
+                   (size_t)p.nx * ((size_t)ys + (size_t)p.ny * (size_t)zs);
+    const uint32_t dst = stage + (uint32_t)i * kTmaRow * sz;
+    if (MODE == AA_EVEN) {
+        const int x0 = tl.x0;
+        if (x0 > 0 && x0 + kTmaTile < p.nx) {
+            bulk_g2s(dst, row + (x0 - kTmaHalo), kTmaRow * sz, bar);
+        } else {  // the halo of a row end wraps to the other end of the same row
+            const int left = x0 == 0 ? p.nx - kTmaHalo : x0 - kTmaHalo;
+            const int right = x0 + kTmaTile == p.nx ? 0 : x0 + kTmaTile;
+            bulk_g2s(dst, row + left, kTmaHalo * sz, bar);
+            bulk_g2s(dst + kTmaHalo * sz, row + x0, kTmaTile * sz, bar);
+            bulk_g2s(dst + (kTmaHalo + kTmaTile) * sz, row + right, kTmaHalo * sz, bar);
+        }
+    } else {
+        bulk_g2s(dst + kTmaHalo * sz, row + tl.x0, kTmaTile * sz, bar);
+    }
+}
+
+#ifndef BF_TMA_MIN_BLOCKS
+#define BF_TMA_MIN_BLOCKS 4
+#endif
+// 64 registers: the staged even step spills at 48
+template <int Q, int ST, int MODE, bool TRT, bool FORCED>
+__global__ void __launch_bounds__(kTmaTile, BF_TMA_MIN_BLOCKS) tma_step_kernel(const __grid_constant__ StepParams p) {
+    using C = Codec<ST>;
+    using T = typename C::T;
+    using L = Lattice<Q>;
+    extern __shared__ __align__(128) unsigned char tma_smem[];
+    T* const stages = reinterpret_cast<T*>(tma_smem);
+    uint64_t* const bars = reinterpret_cast<uint64_t*>(tma_smem + (size_t)kTmaStages * Q * kTmaRow * sizeof(T));
+    const uint32_t stage0 = smem_addr(stages), bar0 = smem_addr(bars);
+    constexpr uint32_t stage_bytes = (uint32_t)Q * kTmaRow * sizeof(T);
+    const uint32_t n_tiles = ((uint32_t)p.nx / kTmaTile) * (uint32_t)p.ny * (uint32_t)p.nz;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+    if (tid == 0) {
+        for (int s = 0; s < kTmaStages; s++) mbar_init(bar0 + 8u * s, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (warp == 0) {
+        for (int s = 0; s < kTmaStages; s++) {
+            const uint32_t t = blockIdx.x + (uint32_t)s * gridDim.x;
+            if (t < n_tiles) tma_issue<Q, ST, MODE>(p, t, stage0 + s * stage_bytes, bar0 + 8u * s, lane);
+        }
+    }
+    for (uint32_t k = 0;; k++) {
+        const uint32_t t = blockIdx.x + k * gridDim.x;
+        if (t >= n_tiles) break;
+        const int s = (int)(k % kTmaStages);
+        const uint32_t parity = (k / kTmaStages) & 1u;
+        // the block agrees on the outcome, so that no thread leaves while
+        // others wait at a barrier
+        const bool ok = mbar_wait_bounded(bar0 + 8u * s, parity);
+        if (__syncthreads_or(!ok)) {
+            // give up: report, let the copies already issued land, return
+            if (tid == 0) atomicOr(p.err, 2u);
+            for (uint32_t j = k; j < k + kTmaStages; j++) {
+                const uint32_t tj = blockIdx.x + j * gridDim.x;
+                if (tj >= n_tiles) break;
+                mbar_wait_bounded(bar0 + 8u * (j % kTmaStages), (j / kTmaStages) & 1u);
+            }
+            return;
+        }
+        const TmaTile tl = tma_tile(p, t);
+        const T* st = stages + (size_t)s * Q * kTmaRow;
+        auto load = [&](int i, auto&&) -> T {
+            const Dir c = L::c(i);
+            return st[i * kTmaRow + kTmaHalo + tid - (MODE == AA_EVEN ? c.x : 0)];
+        };
+        const bool edge = MODE == AA_EVEN && (tl.y == 0 || tl.y == p.ny - 1 || (L::D == 3 && (tl.z == 0 || tl.z == p.nz - 1)));
+        if (edge) fast_cell<Q, ST, MODE, TRT, FORCED, false, true>(p, tl.x0 + tid, tl.y, tl.z, load);
+        else fast_cell<Q, ST, MODE, TRT, FORCED, false, false>(p, tl.x0 + tid, tl.y, tl.z, load);
+        __syncthreads();  // every thread is done with stage s
+        if (warp == 0) {
+            const uint32_t tn = t + (uint32_t)kTmaStages * gridDim.x;
+            if (tn < n_tiles) {
+                // order this block's reads of the stage before the copy engine overwrites it
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                tma_issue<Q, ST, MODE>(p, tn, stage0 + s * stage_bytes, bar0 + 8u * s, lane);
+            }
+        }
+    }
+}
+
+template <int Q, int ST>
+constexpr size_t tma_smem_bytes() {
+    return (size_t)kTmaStages * Q * kTmaRow * sizeof(typename Codec<ST>::T) + kTmaStages * sizeof(uint64_t);
+}
+
+}  // namespace bf

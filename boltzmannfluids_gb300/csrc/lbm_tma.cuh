@@ -19,9 +19,9 @@
 // 16-bit data starts on a 16-byte boundary; at the two ends of a row the
 // 8-cell halos wrap to the other end of the same row (periodic in x) and are
 // copied separately (16 bytes each).  Every wait on an mbarrier is bounded:
-// past the limit the block sets bit 1 of the error word (reported as
-// BF_ERR_TIMEOUT), waits, again bounded, for its copies still in flight, and
-// returns.
+// past the limit a warp sets bit 1 of the error word (reported as
+// BF_ERR_TIMEOUT), waits, again bounded, on the stages' copies, and returns;
+// no block-wide barrier follows the start, so no warp waits on one that left.
 #pragma once
 
 namespace bf {
@@ -29,7 +29,10 @@ namespace bf {
 constexpr int kTmaTile = 256;                        // cells per tile = threads per block
 constexpr int kTmaHalo = 8;                          // halo cells each side: 16 bytes of 16-bit data
 constexpr int kTmaRow = kTmaTile + 2 * kTmaHalo;     // staged elements per row
-constexpr int kTmaStages = 3;
+#ifndef BF_TMA_STAGES
+#define BF_TMA_STAGES 3
+#endif
+constexpr int kTmaStages = BF_TMA_STAGES;
 constexpr uint32_t kTmaWaitLimit = 1u << 24;         // try_wait polls before giving up
 
 __device__ __forceinline__ uint32_t smem_addr(const void* ptr) {
@@ -52,6 +55,9 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
 // bounded wait for the phase with the given parity; false = gave up
 __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
     for (uint32_t k = 0; k < kTmaWaitLimit; k++)
@@ -63,6 +69,18 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
                  "l"(src), "r"(bytes), "r"(bar)
                  : "memory");
+}
+
+// 16-bit load from a shared-memory address (explicit shared state space: a
+// generic pointer into the stage would go through the generic load path)
+template <class T>
+__device__ __forceinline__ T lds16(uint32_t addr) {
+    static_assert(sizeof(T) == 2, "16-bit storage only");
+    unsigned short v;
+    asm volatile("ld.shared.u16 %0, [%1];" : "=h"(v) : "r"(addr));
+    T out;
+    memcpy(&out, &v, 2);
+    return out;
 }
 
 // direction components packed 2 bits per direction (component + 1), so a
@@ -140,73 +158,85 @@ __device__ __forceinline__ void tma_issue(const StepParams& p, uint32_t t, uint3
 #ifndef BF_TMA_MIN_BLOCKS
 #define BF_TMA_MIN_BLOCKS 4
 #endif
-// 64 registers: the staged even step spills at 48
+// Pipeline per stage s: full[s] completes when the stage's copies have
+// landed (one arrival with the byte count, then the copies' bytes); empty[s]
+// completes when all eight warps are done with the tile in it.  Warp 0 also
+// produces: after its own part of tile k it waits for empty[s] and issues
+// tile k + kTmaStages into stage s, while the other warps go on to the next
+// tile without a block-wide barrier.  64 registers (the even step spills at 48).
 template <int Q, int ST, int MODE, bool TRT, bool FORCED>
 __global__ void __launch_bounds__(kTmaTile, BF_TMA_MIN_BLOCKS) tma_step_kernel(const __grid_constant__ StepParams p) {
     using C = Codec<ST>;
     using T = typename C::T;
     using L = Lattice<Q>;
+    constexpr int kWarps = kTmaTile / 32;
     extern __shared__ __align__(128) unsigned char tma_smem[];
-    T* const stages = reinterpret_cast<T*>(tma_smem);
     uint64_t* const bars = reinterpret_cast<uint64_t*>(tma_smem + (size_t)kTmaStages * Q * kTmaRow * sizeof(T));
-    const uint32_t stage0 = smem_addr(stages), bar0 = smem_addr(bars);
+    const uint32_t stage0 = smem_addr(tma_smem), full0 = smem_addr(bars), empty0 = full0 + 8u * kTmaStages;
     constexpr uint32_t stage_bytes = (uint32_t)Q * kTmaRow * sizeof(T);
-    const uint32_t n_tiles = ((uint32_t)p.nx / kTmaTile) * (uint32_t)p.ny * (uint32_t)p.nz;
+    const uint32_t tiles_x = (uint32_t)p.nx / kTmaTile;
+    const uint32_t n_tiles = tiles_x * (uint32_t)p.ny * (uint32_t)p.nz;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
     if (tid == 0) {
-        for (int s = 0; s < kTmaStages; s++) mbar_init(bar0 + 8u * s, 1);
+        for (int s = 0; s < kTmaStages; s++) {
+            mbar_init(full0 + 8u * s, 1);
+            mbar_init(empty0 + 8u * s, kWarps);
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
     if (warp == 0) {
         for (int s = 0; s < kTmaStages; s++) {
             const uint32_t t = blockIdx.x + (uint32_t)s * gridDim.x;
-            if (t < n_tiles) tma_issue<Q, ST, MODE>(p, t, stage0 + s * stage_bytes, bar0 + 8u * s, lane);
+            if (t < n_tiles) tma_issue<Q, ST, MODE>(p, t, stage0 + s * stage_bytes, full0 + 8u * s, lane);
         }
     }
-    for (uint32_t k = 0;; k++) {
-        const uint32_t t = blockIdx.x + k * gridDim.x;
-        if (t >= n_tiles) break;
+    // tile coordinates, advanced by the grid stride without divisions
+    TmaTile tl = tma_tile(p, blockIdx.x);
+    const TmaTile step = tma_tile(p, gridDim.x);
+    bool failed = false;
+    for (uint32_t k = 0, t = blockIdx.x; t < n_tiles; k++, t += gridDim.x) {
         const int s = (int)(k % kTmaStages);
         const uint32_t parity = (k / kTmaStages) & 1u;
-        // the block agrees on the outcome, so that no thread leaves while
-        // others wait at a barrier
-        const bool ok = mbar_wait_bounded(bar0 + 8u * s, parity);
-        if (__syncthreads_or(!ok)) {
-            // give up: report, let the copies already issued land, return
-            if (tid == 0) atomicOr(p.err, 2u);
-            for (uint32_t j = k; j < k + kTmaStages; j++) {
-                const uint32_t tj = blockIdx.x + j * gridDim.x;
-                if (tj >= n_tiles) break;
-                mbar_wait_bounded(bar0 + 8u * (j % kTmaStages), (j / kTmaStages) & 1u);
-            }
-            return;
-        }
-        const TmaTile tl = tma_tile(p, t);
-        const T* st = stages + (size_t)s * Q * kTmaRow;
+        if (!mbar_wait_bounded(full0 + 8u * s, parity)) { failed = true; break; }
+        const uint32_t sbase = stage0 + (uint32_t)s * stage_bytes + (uint32_t)(kTmaHalo + tid) * (uint32_t)sizeof(T);
         auto load = [&](int i, auto&&) -> T {
             const Dir c = L::c(i);
-            return st[i * kTmaRow + kTmaHalo + tid - (MODE == AA_EVEN ? c.x : 0)];
+            return lds16<T>(sbase + (uint32_t)((i * kTmaRow - (MODE == AA_EVEN ? c.x : 0)) * (int)sizeof(T)));
         };
         const bool edge = MODE == AA_EVEN && (tl.y == 0 || tl.y == p.ny - 1 || (L::D == 3 && (tl.z == 0 || tl.z == p.nz - 1)));
         if (edge) fast_cell<Q, ST, MODE, TRT, FORCED, false, true>(p, tl.x0 + tid, tl.y, tl.z, load);
         else fast_cell<Q, ST, MODE, TRT, FORCED, false, false>(p, tl.x0 + tid, tl.y, tl.z, load);
-        __syncthreads();  // every thread is done with stage s
+        __syncwarp();
+        if (lane == 0) mbar_arrive(empty0 + 8u * s);  // this warp is done with stage s
         if (warp == 0) {
             const uint32_t tn = t + (uint32_t)kTmaStages * gridDim.x;
             if (tn < n_tiles) {
-                // order this block's reads of the stage before the copy engine overwrites it
+                if (!mbar_wait_bounded(empty0 + 8u * s, parity)) { failed = true; break; }
+                // order the block's reads of the stage before the copy engine overwrites it
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                tma_issue<Q, ST, MODE>(p, tn, stage0 + s * stage_bytes, bar0 + 8u * s, lane);
+                tma_issue<Q, ST, MODE>(p, tn, stage0 + s * stage_bytes, full0 + 8u * s, lane);
             }
         }
+        // next tile: x0 += step.x0 (carry into y), y += step.y (carry into z), z += step.z
+        tl.x0 += step.x0;
+        int cy = 0;
+        if (tl.x0 >= p.nx) { tl.x0 -= p.nx; cy = 1; }
+        tl.y += step.y + cy;
+        if (tl.y >= p.ny) { tl.y -= p.ny; tl.z += 1; }
+        tl.z += step.z;
+    }
+    if (failed) {
+        // give up: report, let this warp's view of the copies in flight land, return
+        if (lane == 0) atomicOr(p.err, 2u);
+        for (int s = 0; s < kTmaStages; s++) mbar_wait_bounded(full0 + 8u * s, 0u), mbar_wait_bounded(full0 + 8u * s, 1u);
     }
 }
 
 template <int Q, int ST>
 constexpr size_t tma_smem_bytes() {
-    return (size_t)kTmaStages * Q * kTmaRow * sizeof(typename Codec<ST>::T) + kTmaStages * sizeof(uint64_t);
+    return (size_t)kTmaStages * Q * kTmaRow * sizeof(typename Codec<ST>::T) + 2 * kTmaStages * sizeof(uint64_t);
 }
 
 }  // namespace bf

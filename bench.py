@@ -321,6 +321,35 @@ def run_multiphysics_leg(bf, full=False):
     return out
 
 
+def run_sphere_leg(bf, steps=1000):
+    """3D plain-method configuration: D3Q19 TRT (1/4, tau 0.55) flow past a
+    sphere r 16 at (64, 64, 64), 256x128x128, velocity inlet 0.05, density
+    outlet 1, periodic y/z, equilibrium start with u noise 1e-4; MLUPs of the
+    generic step (objects, open boundaries, bounce-back) by CUDA events."""
+    from boltzmannfluids_gb300.workloads import sphere_channel
+    res = (256, 128, 128)
+    n = res[0] * res[1] * res[2]
+    rho, u, ids, objs = sphere_channel(res)
+    s = bf.LBM()
+    s.is_collide_esoteric = True
+    s.collision = bf.Collision.trt
+    s.boundary_mode = bf.BoundaryMode.bounce_back
+    for k, o in objs.items():
+        s.set_boundry_properties(k, velocity_translational=(0, 0, 0), kind=o["kind"])
+    s.initialize_fields_from_arrays(res, 0.55, density=rho, velocity=u, boundry_id=ids, periodic=(False, True, True),
+                                    velocity_set=bf.VelocitySet.D3Q19)
+    s.iterate_time(steps=3, save=False)
+    ms = s.benchmark_steps(steps)
+    s.reduce()
+    vd = s.get_velocity_density_texture().reshape(res[2], res[1], res[0], 4)
+    out = {"workload": "D3Q19 TRT flow past a sphere r16, 256x128x128, inlet u 0.05, outlet rho 1, periodic y/z",
+           "steps_timed": steps, "mlups": round(n * steps / (ms * 1e-3) / 1e6, 1),
+           "achieved_gbs": round(153 * n * steps / (ms * 1e-3) / 1e9, 1),
+           "wake_ux_behind_sphere": float(vd[64, 64, 88, 0])}
+    del s
+    return out
+
+
 def run_gpu(args):
     rank, world, local = dist_env()
     if world > 1:
@@ -394,6 +423,9 @@ def run_gpu(args):
     multi = None
     if not args.no_multiphysics:
         multi = run_multiphysics_leg(bf, args.multiphysics_full)
+    sphere = None
+    if not args.no_sphere:
+        sphere = run_sphere_leg(bf)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         mlups_cpu, threads, sample = cpu_baseline_sample()
@@ -419,6 +451,7 @@ def run_gpu(args):
             "adjoint": adj,
             "precision": prec,
             "multiphysics": multi,
+            "sphere": sphere,
             "gpu_launches": args.steps,
             "clocks": clock_info,
         }
@@ -448,6 +481,7 @@ def main():
     ap.add_argument("--precision-steps", type=int, default=2000)
     ap.add_argument("--no-multiphysics", action="store_true", help="skip the Shan-Chen / Rayleigh-Benard leg")
     ap.add_argument("--multiphysics-full", action="store_true", help="run the multiphysics configurations at full size")
+    ap.add_argument("--no-sphere", action="store_true", help="skip the flow-past-a-sphere leg")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -20,6 +20,27 @@ SOURCES = ["lbm_q9.cu", "lbm_q15.cu", "lbm_q19.cu", "lbm_q27.cu", "lbm_aux.cu", 
            "marching_cubes.cu", "voxelize.cu", "render3d.cu"]
 
 
+# the step kernels of each (velocity set, storage) pair: one generated
+# translation unit each, so that the heaviest templates compile in parallel
+STEP_UNITS = [(q, st) for q in (9, 15, 19, 27) for st in range(5)]
+
+
+def _generated_units():
+    gen = os.path.join(BUILD, "gen")
+    os.makedirs(gen, exist_ok=True)
+    out = []
+    for q, st in STEP_UNITS:
+        path = os.path.join(gen, f"step_q{q}_s{st}.cu")
+        text = ("// generated by boltzmannfluids_gb300/build.py: step kernels of one velocity set and storage\n"
+                f'#include "{os.path.join(CSRC, "lbm_kernels.cuh")}"\n'
+                f"namespace bf {{\nBF_INSTANTIATE_STEP({q}, {st})\n}}\n")
+        if not os.path.exists(path) or open(path).read() != text:
+            with open(path, "w") as f:
+                f.write(text)
+        out.append(path)
+    return out
+
+
 def nvcc():
     for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
         if cand and os.path.exists(cand):
@@ -47,15 +68,17 @@ def build(verbose=False, force=False):
     flags += [f for f in os.environ.get("BF_NVCC_DEFINES", "").split() if f.startswith("-D")]
 
     def compile_one(src):
-        obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
-        cmd = [nvcc(), *flags, "-c", os.path.join(CSRC, src), "-o", obj]
+        path = src if os.path.isabs(src) else os.path.join(CSRC, src)
+        obj = os.path.join(BUILD, os.path.splitext(os.path.basename(src))[0] + ".o")
+        cmd = [nvcc(), *flags, "-c", path, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
         return obj, r.stderr
 
-    with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        results = list(ex.map(compile_one, SOURCES))
+    units = SOURCES + _generated_units()
+    with cf.ThreadPoolExecutor(max_workers=min(len(units), max(4, (os.cpu_count() or 4)))) as ex:
+        results = list(ex.map(compile_one, units))
     if verbose:
         for obj, err in results:
             print(obj)

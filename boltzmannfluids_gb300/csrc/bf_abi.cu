@@ -96,6 +96,7 @@ struct bf_solver {
     // device memory
     DeviceBuf lat[2], bnd, objs, kinds, force, bvals, th[2], psi[2];
     DeviceBuf vel_den, force_temp, bnd_tex, partials, red_out, err, decode_tmp;
+    DeviceBuf nmask;  // per-cell masks of the boundary-aware fast step
     uint32_t n_blocks = 0;
     // buffer roles (LBM.h:280-291)
     int lat0_src = 1, th0_src = 1, psi0_src = 1;
@@ -106,6 +107,7 @@ struct bf_solver {
     bool graphs_enabled = true;
     uint32_t pf_blocks = 0;  // L2 prefetch distance of the fast kernel, in blocks (0 = off)
     bool tma_step = false;   // 16-bit fast step with loads staged by bulk copies
+    bool masked_step = true; // boundary-aware fast step for objects and open faces
 };
 
 namespace {
@@ -119,7 +121,7 @@ void release_all(bf_solver* s) {
     clear_graphs(s);
     DeviceBuf* bufs[] = {&s->lat[0], &s->lat[1], &s->bnd, &s->objs, &s->kinds, &s->force, &s->bvals,
                          &s->th[0], &s->th[1], &s->psi[0], &s->psi[1], &s->vel_den, &s->force_temp,
-                         &s->bnd_tex, &s->partials, &s->red_out, &s->err, &s->decode_tmp};
+                         &s->bnd_tex, &s->partials, &s->red_out, &s->err, &s->decode_tmp, &s->nmask};
     for (auto* b : bufs) b->release();
     s->initialized = false;
 }
@@ -131,12 +133,12 @@ float* th_tgt(bf_solver* s) { return s->th[s->th0_src ? 1 : 0].as<float>(); }
 float* psi_src(bf_solver* s) { return s->psi[s->psi0_src ? 0 : 1].as<float>(); }
 float* psi_tgt(bf_solver* s) { return s->psi[s->psi0_src ? 1 : 0].as<float>(); }
 
-cudaError_t dispatch_step(bf_solver* s, const StepParams& p, int mode, bool generic) {
+cudaError_t dispatch_step(bf_solver* s, const StepParams& p, int mode, int path) {
     switch (s->Q) {
-    case 9: return launch_step<9>(p, s->desc.storage, mode, generic, s->stream);
-    case 15: return launch_step<15>(p, s->desc.storage, mode, generic, s->stream);
-    case 19: return launch_step<19>(p, s->desc.storage, mode, generic, s->stream);
-    case 27: return launch_step<27>(p, s->desc.storage, mode, generic, s->stream);
+    case 9: return launch_step<9>(p, s->desc.storage, mode, path, s->stream);
+    case 15: return launch_step<15>(p, s->desc.storage, mode, path, s->stream);
+    case 19: return launch_step<19>(p, s->desc.storage, mode, path, s->stream);
+    case 27: return launch_step<27>(p, s->desc.storage, mode, path, s->stream);
     }
     return cudaErrorInvalidValue;
 }
@@ -260,6 +262,14 @@ cudaError_t collide(bf_solver* s, bool save, bool update, bool reduce, bool meas
     // the fast kernel indexes every slot with 32 bits off the first plane
     const bool idx32 = (uint64_t)s->N * (uint64_t)s->Q < (1ull << 32);
     const bool generic = mode == AA_LOCAL || (p.flags & heavy) || !all_periodic || !idx32;
+    // objects and open faces without thermal, force-field or multiphase
+    // flow: the boundary-aware fast kernel, with its masks
+    const uint32_t masked_excl = F_FORCE_FIELD | F_THERMAL | F_MULTIPHASE;
+    int path = generic ? PATH_GENERIC : PATH_FAST;
+    if (generic && mode != AA_LOCAL && idx32 && !(p.flags & masked_excl) && s->nmask.p &&
+        s->desc.storage != BF_STORE_FP64 && s->masked_step)
+        path = PATH_MASKED;
+    p.nmask = s->nmask.as<uint32_t>();
     // the prefetch rounds each row range out to 16 bytes, which stays inside
     // the plane only when every plane starts and ends on a 16-byte boundary
     const size_t plane_bytes = (size_t)s->N * storage_bytes(s->desc.storage);
@@ -272,7 +282,7 @@ cudaError_t collide(bf_solver* s, bool save, bool update, bool reduce, bool meas
     case 19: fill_uoff<19>(p); break;
     default: fill_uoff<27>(p); break;
     }
-    cudaError_t e = dispatch_step(s, p, mode, generic);
+    cudaError_t e = dispatch_step(s, p, mode, path);
     if (e != cudaSuccess) return e;
     if (measure) return cudaSuccess;
     if (!s->desc.esoteric && update && !s->desc.two_buffer_fixed) s->lat0_src = !s->lat0_src;
@@ -486,6 +496,8 @@ int bf_create(bf_solver** out) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
     s->pf_blocks = (uint32_t)std::max(sms, 1) * 4u;
     if (const char* env = std::getenv("BF_PREFETCH_BLOCKS")) s->pf_blocks = (uint32_t)std::strtoul(env, nullptr, 10);
+    // BF_MASKED_STEP=0 sends objects and open faces to the generic kernel (A/B comparisons)
+    if (const char* env = std::getenv("BF_MASKED_STEP")) s->masked_step = std::strtoul(env, nullptr, 10) != 0;
     // BF_TMA_STEP=1 selects the staged 16-bit fast step, 0 the plain one
     if (const char* env = std::getenv("BF_TMA_STEP")) s->tma_step = std::strtoul(env, nullptr, 10) != 0;
     *out = s;
@@ -715,6 +727,24 @@ int bf_initialize_fields(bf_solver* s, const bf_init_desc* d, const float* densi
         }
         // As the reference reads it, set_equilibrium_populations_thermal.comp:101-107
         // writes past the end of the thermal buffer, which keeps its zero contents.
+    }
+    // masks of the boundary-aware fast step: built once, the geometry is fixed
+    if (d->esoteric && (s->boundaries || !(d->periodic[0] && d->periodic[1] && d->periodic[2])) &&
+        d->storage != BF_STORE_FP64) {
+        BF_CUDA(s->nmask.alloc((size_t)N * sizeof(uint32_t)));
+        StepParams mp{};
+        mp.nx = rx; mp.ny = ry; mp.nz = rz;
+        mp.flags = base_flags(s);
+        mp.bnd = s->bnd.as<uint32_t>();
+        mp.bits = s->bits;
+        mp.obj_kind = s->kinds.as<uint8_t>();
+        switch (Q) {
+        case 9: e = launch_build_mask<9>(mp, s->nmask.as<uint32_t>(), s->stream); break;
+        case 15: e = launch_build_mask<15>(mp, s->nmask.as<uint32_t>(), s->stream); break;
+        case 19: e = launch_build_mask<19>(mp, s->nmask.as<uint32_t>(), s->stream); break;
+        default: e = launch_build_mask<27>(mp, s->nmask.as<uint32_t>(), s->stream); break;
+        }
+        if (e != cudaSuccess) return fail(BF_ERR_CUDA, std::string("mask kernel: ") + cudaGetErrorString(e));
     }
     // LBM.cpp:502: _iterate_time(true, false)
     e = iterate_once(s, true, false, false);

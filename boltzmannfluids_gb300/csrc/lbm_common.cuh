@@ -226,6 +226,11 @@ struct alignas(16) StepParams {
     // 1: the 16-bit fast step may stage its loads through shared memory with
     // bulk copies (lbm_tma.cuh); set by the host when the planes allow it
     uint32_t tma;
+    // per-cell masks of the boundary-aware fast step (build_mask_kernel):
+    // bit i (1..Q-1) = the AA source x - c_i needs special handling (outside
+    // the domain, or a solid cell under bounce-back); bit 31 = the cell is
+    // solid; bit 30 = the cell is an equilibrium-boundary cell
+    const uint32_t* nmask;
     // fast kernel, even step, rows off the y/z faces: element offset of the
     // slot read for direction i relative to the cell, without its x part:
     // i * stride - (c_y nx + c_z nx ny), modulo 2^32
@@ -314,7 +319,11 @@ __device__ __forceinline__ uint32_t boundary_id(const uint32_t* __restrict__ bnd
 }
 
 // launchers (one translation unit per Q instantiates them)
-template <int Q> cudaError_t launch_step(const StepParams& p, int storage, int mode, bool generic, cudaStream_t st);
+// kernel choice of one step: the periodic fast kernel, the boundary-aware
+// (masked) fast kernel, or the generic kernel
+enum StepPath { PATH_FAST = 0, PATH_MASKED = 1, PATH_GENERIC = 2 };
+template <int Q> cudaError_t launch_step(const StepParams& p, int storage, int mode, int path, cudaStream_t st);
+template <int Q> cudaError_t launch_build_mask(const StepParams& p, uint32_t* mask, cudaStream_t st);
 template <int Q> cudaError_t launch_stream(const StreamParams& p, int storage, cudaStream_t st);
 template <int Q> cudaError_t launch_init(const InitParams& p, int storage, cudaStream_t st);
 template <int Q> cudaError_t launch_decode(const void* f, uint64_t stride, uint32_t n, int storage, float* out, cudaStream_t st);

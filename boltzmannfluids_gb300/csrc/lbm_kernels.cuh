@@ -578,6 +578,175 @@ __global__ void __launch_bounds__(kStepBlock,
 }
 
 // ---------------------------------------------------------------------------
+// boundary-aware fast step: objects (solid cells, halfway bounce-back with
+// moving walls, equilibrium velocity/density cells), open (non-periodic)
+// domain faces and a constant force, in the esoteric-pull modes.  A per-cell
+// mask built once at initialisation marks the directions whose AA source
+// needs the generic treatment; every other direction uses the fast kernel's
+// addressing, and the arithmetic is the generic kernel's, so results agree
+// bit for bit.
+// ---------------------------------------------------------------------------
+template <int Q>
+__global__ void build_mask_kernel(const __grid_constant__ StepParams p, uint32_t* __restrict__ mask) {
+    using L = Lattice<Q>;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
+    if (x >= p.nx) return;
+    const int nx = p.nx, ny = p.ny, nz = p.nz;
+    const uint32_t flags = p.flags;
+    const uint32_t n = (uint32_t)x + (uint32_t)nx * ((uint32_t)y + (uint32_t)ny * (uint32_t)z);
+    const uint32_t bid = (flags & F_BOUNDARIES) ? boundary_id(p.bnd, p.bits, n) : 0u;
+    uint32_t m = 0u;
+    if (solid_id(p.obj_kind, bid)) m |= 1u << 31;
+    else if (bid != 0u) m |= 1u << 30;
+#pragma unroll
+    for (int i = 1; i < Q; i++) {
+        const Dir c = L::c(i);
+        int sx = x - c.x, sy = y - c.y, sz = z - c.z;
+        bool sopen;
+        coords_wrap<Q>(sx, sy, sz, nx, ny, nz, sopen, flags);
+        bool special = sopen;
+        if (!sopen && (flags & F_BOUNCE_BACK) && (flags & F_BOUNDARIES)) {
+            const uint32_t sn = (uint32_t)sx + (uint32_t)nx * ((uint32_t)sy + (uint32_t)ny * (uint32_t)sz);
+            special = solid_id(p.obj_kind, boundary_id(p.bnd, p.bits, sn));
+        }
+        if (special) m |= 1u << i;
+    }
+    mask[n] = m;
+}
+
+template <int Q, int ST, int MODE, bool TRT, bool FORCED, bool EDGE>
+__device__ __forceinline__ CellSum masked_cell(const StepParams& p, int x, int y, int z) {
+    using L = Lattice<Q>;
+    using C = Codec<ST>;
+    using T = typename C::T;
+    CellSum cs = {0.f, 0.f, 0.f, 0.f, 0.f};
+    const int nx = p.nx, ny = p.ny, nz = p.nz, nxy = nx * ny;
+    const uint32_t flags = p.flags;
+    const uint32_t n = (uint32_t)x + (uint32_t)nx * ((uint32_t)y + (uint32_t)ny * (uint32_t)z);
+    const uint32_t mask = __ldg(p.nmask + n);
+    if (mask >> 31) {  // solid cell (collide.comp:696-700)
+        if (flags & F_SAVE) {
+            p.vel_den[n] = make_float4(0.f, 0.f, 0.f, 0.f);
+            p.force_temp[n] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (p.bnd_tex) p.bnd_tex[n] = (uint8_t)boundary_id(p.bnd, p.bits, n);
+        }
+        return cs;
+    }
+    const bool eqb = (mask >> 30) & 1u;
+    const uint32_t bid = eqb ? boundary_id(p.bnd, p.bits, n) : 0u;
+    float4 bv = make_float4(1.f, 0.f, 0.f, 0.f);
+    if (eqb && p.bvals) bv = __ldg(p.bvals + n);
+    T* const base = static_cast<T*>(p.plane[0]);
+    const uint32_t S = (uint32_t)p.stride;
+    const int oxm = x == 0 ? nx - 1 : -1, oxp = x == nx - 1 ? 1 - nx : 1;
+    const int oym = y == 0 ? (ny - 1) * nx : -nx, oyp = y == ny - 1 ? (1 - ny) * nx : nx;
+    const int ozm = z == 0 ? (nz - 1) * nxy : -nxy, ozp = z == nz - 1 ? (1 - nz) * nxy : nxy;
+    auto slot = [&](int i, uint32_t nn, int xm, int xp) -> uint32_t {
+        if (MODE == AA_EVEN) {
+            const Dir c = L::c(i);
+            const uint32_t u = EDGE ? (uint32_t)i * S + (uint32_t)((c.y > 0 ? oym : (c.y < 0 ? oyp : 0)) +
+                                                                   (c.z > 0 ? ozm : (c.z < 0 ? ozp : 0)))
+                                    : p.uoff[i];
+            return nn + u + (uint32_t)(c.x > 0 ? xm : (c.x < 0 ? xp : 0));
+        }
+        return nn + (uint32_t)opp(i) * S;
+    };
+    float f[Q];
+#pragma unroll
+    for (int i = 0; i < Q; i++) {
+        const float w = L::w(i);
+        if (i == 0 || !((mask >> i) & 1u)) {
+            f[i] = C::dec(base[slot(i, n, oxm, oxp)], w);
+            continue;
+        }
+        // the generic kernel's treatment of a source outside the domain or solid
+        const Dir c = L::c(i);
+        int sx = x - c.x, sy = y - c.y, sz = z - c.z;
+        bool sopen;
+        coords_wrap<Q>(sx, sy, sz, nx, ny, nz, sopen, flags);
+        const uint32_t sn = sopen ? 0u : (uint32_t)sx + (uint32_t)nx * ((uint32_t)sy + (uint32_t)ny * (uint32_t)sz);
+        if (eqb && sopen) {  // population entering from outside: f_eq(rho_b, u_b)
+            const float cu = cdot_rt(c, bv.y, bv.z, bv.w);
+            const float one_mb = FSUB(1.0f, FMUL(uu_of(bv.y, bv.z, bv.w), p.R2h));
+            const float br = bracket(cu, one_mb, p.R2, p.R4h);
+            f[i] = C::SHIFTED ? FFMA(FMUL(w, bv.x), br, -w) : FMUL(FMUL(w, bv.x), br);
+        } else if (!sopen) {  // solid source under bounce-back (stream.comp:487-496, rho_wall = 1)
+            const uint32_t sid = boundary_id(p.bnd, p.bits, sn);
+            const float4 uw = __ldg(p.objects + 3u * sid);
+            const Dir co = L::c(opp(i));
+            const float wall = FMUL(FMUL(-2.f * w, co.x * uw.x + co.y * uw.y + co.z * uw.z), 3.f);
+            const float v = (MODE == AA_EVEN) ? C::dec(base[(uint32_t)opp(i) * S + n], w)
+                                              : C::dec(base[(uint32_t)i * S + sn], w);
+            f[i] = FADD(v, wall);
+        } else if (MODE == AA_EVEN) {  // out-of-domain read (collide.comp:278-298)
+            f[i] = C::SHIFTED ? FSUB(0.01f, w) : 0.01f;
+        } else {  // odd steps read the cell's own slot whatever lies outside
+            f[i] = C::dec(base[slot(i, n, oxm, oxp)], w);
+        }
+    }
+    uint32_t n_st = n;
+    int oxm_st = oxm, oxp_st = oxp;
+    asm volatile("" : "+r"(n_st), "+r"(oxm_st), "+r"(oxp_st));
+
+    Moments m;
+    m.rho = density_of<Q>(f);
+    if (C::SHIFTED) m.rho = FADD(1.0f, m.rho);
+    if (!(m.rho == m.rho)) atomicOr(p.err, 1u);
+    m.rho = m.rho < 0.01f ? 0.01f : m.rho;
+    m.Fx = FORCED ? p.fconst[0] : 0.f;
+    m.Fy = FORCED ? p.fconst[1] : 0.f;
+    m.Fz = FORCED ? p.fconst[2] : 0.f;
+    velocity_and_limit<Q>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
+    if (eqb) {
+        const int kind = __ldg(p.obj_kind + bid);
+        if (kind == 1) { m.ux = bv.y; m.uy = bv.z; m.uz = bv.w; } else { m.rho = bv.x; }
+        m.Fx = m.Fy = m.Fz = 0.f;
+    }
+    if (flags & F_UPDATE) {
+        const Coef<float> k = coef_of(p, 0.0f);
+        auto emit = [&](int i, float v) {
+            if (MODE == AA_EVEN && ((mask >> opp(i)) & 1u)) {
+                // the destination x + c_i is the source of opp(i): dropped when outside
+                const Dir c = L::c(i);
+                int dx = x + c.x, dy = y + c.y, dz = z + c.z;
+                bool dopen;
+                coords_wrap<Q>(dx, dy, dz, nx, ny, nz, dopen, flags);
+                if (dopen) return;
+            }
+            base[slot(opp(i), n_st, oxm_st, oxp_st)] = C::enc(v, L::w(i));
+        };
+        if (eqb) collide_fixed<Q, false, false, true, C::SHIFTED>(f, m, k, emit);  // f_eq of the cell
+        else if (m.out_ext) collide_fixed<Q, TRT, FORCED, true, C::SHIFTED>(f, m, k, emit);
+        else collide_fixed<Q, TRT, FORCED, false, C::SHIFTED>(f, m, k, emit);
+    }
+    if (flags & F_SAVE) {
+        p.vel_den[n] = make_float4(m.ux, m.uy, m.uz, m.rho);
+        p.force_temp[n] = make_float4(m.Fx, m.Fy, m.Fz, 0.f);
+        if (p.bnd_tex) p.bnd_tex[n] = (uint8_t)bid;
+    }
+    if (flags & F_REDUCE) {
+        const float uu = uu_of(m.ux, m.uy, m.uz);
+        cs.m = m.rho; cs.px = m.rho * m.ux; cs.py = m.rho * m.uy; cs.pz = m.rho * m.uz;
+        cs.ke = 0.5f * m.rho * uu;
+    }
+    return cs;
+}
+
+template <int Q, int ST, int MODE, bool TRT, bool FORCED>
+__global__ void __launch_bounds__(kStepBlock, kFastMinBlocks) masked_step_kernel(const __grid_constant__ StepParams p) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    CellSum cs = {0.f, 0.f, 0.f, 0.f, 0.f};
+    if (x < p.nx) {
+        const bool edge = MODE == AA_EVEN &&
+                          (y == 0 || y == p.ny - 1 || (Lattice<Q>::D == 3 && (z == 0 || z == p.nz - 1)));
+        if (edge) cs = masked_cell<Q, ST, MODE, TRT, FORCED, true>(p, x, y, z);
+        else cs = masked_cell<Q, ST, MODE, TRT, FORCED, false>(p, x, y, z);
+    }
+    if (p.flags & F_REDUCE) block_reduce_store(cs, p.red_partials);
+}
+
+// ---------------------------------------------------------------------------
 // generic AA / two-buffer step: open boundaries, packed boundary ids, solid
 // skipping or bounce-back, equilibrium boundary cells, force fields, thermal
 // lattice, Shan-Chen pseudopotential, field saving and reductions
@@ -938,12 +1107,26 @@ cudaError_t launch_tma(const StepParams& p, cudaStream_t st) {
 }
 
 template <int Q, int ST>
-cudaError_t launch_step_st(const StepParams& p, int mode, bool generic, cudaStream_t st) {
+cudaError_t launch_step_st(const StepParams& p, int mode, int path, cudaStream_t st) {
     int block;
     dim3 grid = cell_grid(p.nx, p.ny, p.nz, block);
+    const bool generic = path != PATH_FAST;
+    if constexpr (ST != ST_FP64) {
+        if (path == PATH_MASKED && mode != AA_LOCAL) {
+            const bool trt = (p.flags & F_TRT) != 0, forced = (p.flags & F_FORCE_CONST) != 0;
+            if (mode == AA_EVEN) {
+                if (trt) { if (forced) masked_step_kernel<Q, ST, AA_EVEN, true, true><<<grid, block, 0, st>>>(p); else masked_step_kernel<Q, ST, AA_EVEN, true, false><<<grid, block, 0, st>>>(p); }
+                else { if (forced) masked_step_kernel<Q, ST, AA_EVEN, false, true><<<grid, block, 0, st>>>(p); else masked_step_kernel<Q, ST, AA_EVEN, false, false><<<grid, block, 0, st>>>(p); }
+            } else {
+                if (trt) { if (forced) masked_step_kernel<Q, ST, AA_ODD, true, true><<<grid, block, 0, st>>>(p); else masked_step_kernel<Q, ST, AA_ODD, true, false><<<grid, block, 0, st>>>(p); }
+                else { if (forced) masked_step_kernel<Q, ST, AA_ODD, false, true><<<grid, block, 0, st>>>(p); else masked_step_kernel<Q, ST, AA_ODD, false, false><<<grid, block, 0, st>>>(p); }
+            }
+            return cudaGetLastError();
+        }
+    }
     // staged loads: 16-bit storage, an update step without reduction or
     // multiphase, whole 256-cell tiles per row, 16-byte aligned planes
-    if constexpr (ST == ST_FP16 || ST == ST_FP16S || ST == ST_FP16C) {
+    if constexpr (ST == ST_FP16S) {  // the staged variant exists for fp16s only
         if (!generic && p.tma && (p.flags & F_UPDATE) && !(p.flags & (F_REDUCE | F_MULTIPHASE)) &&
             p.nx % kTmaTile == 0 && reinterpret_cast<uintptr_t>(p.plane[0]) % 16 == 0) {
             const bool trt = (p.flags & F_TRT) != 0, forced = (p.flags & F_FORCE_CONST) != 0;
@@ -961,12 +1144,14 @@ cudaError_t launch_step_st(const StepParams& p, int mode, bool generic, cudaStre
         const bool forced = (p.flags & F_FORCE_CONST) != 0 || mp;
         auto go = [&](auto kernel) { kernel<<<grid, block, 0, st>>>(p); };
 #define BF_FAST(MODE_, TRT_, F_, MP_) go(fast_step_kernel<Q, ST, MODE_, TRT_, F_, MP_>)
+        if (ST == ST_FP64 && mp) return cudaErrorInvalidValue;  // rejected at initialisation
+        constexpr bool MPX = ST != ST_FP64;  // no multiphase variants of the FP64 stepper
         if (mode == AA_EVEN) {
-            if (mp) { if (trt) BF_FAST(AA_EVEN, true, true, true); else BF_FAST(AA_EVEN, false, true, true); }
+            if (mp) { if (trt) BF_FAST(AA_EVEN, true, true, MPX); else BF_FAST(AA_EVEN, false, true, MPX); }
             else if (trt) { if (forced) BF_FAST(AA_EVEN, true, true, false); else BF_FAST(AA_EVEN, true, false, false); }
             else { if (forced) BF_FAST(AA_EVEN, false, true, false); else BF_FAST(AA_EVEN, false, false, false); }
         } else {
-            if (mp) { if (trt) BF_FAST(AA_ODD, true, true, true); else BF_FAST(AA_ODD, false, true, true); }
+            if (mp) { if (trt) BF_FAST(AA_ODD, true, true, MPX); else BF_FAST(AA_ODD, false, true, MPX); }
             else if (trt) { if (forced) BF_FAST(AA_ODD, true, true, false); else BF_FAST(AA_ODD, true, false, false); }
             else { if (forced) BF_FAST(AA_ODD, false, true, false); else BF_FAST(AA_ODD, false, false, false); }
         }
@@ -982,15 +1167,23 @@ cudaError_t launch_step_st(const StepParams& p, int mode, bool generic, cudaStre
 }
 
 template <int Q>
-cudaError_t launch_step(const StepParams& p, int storage, int mode, bool generic, cudaStream_t st) {
+cudaError_t launch_step(const StepParams& p, int storage, int mode, int path, cudaStream_t st) {
     switch (storage) {
-    case ST_FP32: return launch_step_st<Q, ST_FP32>(p, mode, generic, st);
-    case ST_FP16: return launch_step_st<Q, ST_FP16>(p, mode, generic, st);
-    case ST_FP16S: return launch_step_st<Q, ST_FP16S>(p, mode, generic, st);
-    case ST_FP16C: return launch_step_st<Q, ST_FP16C>(p, mode, generic, st);
-    case ST_FP64: return launch_step_st<Q, ST_FP64>(p, mode, generic, st);
+    case ST_FP32: return launch_step_st<Q, ST_FP32>(p, mode, path, st);
+    case ST_FP16: return launch_step_st<Q, ST_FP16>(p, mode, path, st);
+    case ST_FP16S: return launch_step_st<Q, ST_FP16S>(p, mode, path, st);
+    case ST_FP16C: return launch_step_st<Q, ST_FP16C>(p, mode, path, st);
+    case ST_FP64: return launch_step_st<Q, ST_FP64>(p, mode, path, st);
     }
     return cudaErrorInvalidValue;
+}
+
+template <int Q>
+cudaError_t launch_build_mask(const StepParams& p, uint32_t* mask, cudaStream_t st) {
+    int block;
+    dim3 grid = cell_grid(p.nx, p.ny, p.nz, block);
+    build_mask_kernel<Q><<<grid, block, 0, st>>>(p, mask);
+    return cudaGetLastError();
 }
 
 template <int Q>
@@ -1048,8 +1241,21 @@ cudaError_t launch_encode(void* f, uint64_t stride, uint32_t n, int storage, con
     return cudaGetLastError();
 }
 
+// The step kernels of one (velocity set, storage) pair are instantiated in
+// their own translation unit (generated by build.py, compiled in parallel);
+// the velocity set's main unit declares them extern.
+#define BF_INSTANTIATE_STEP(Q, ST) template cudaError_t launch_step_st<Q, ST>(const StepParams&, int, int, cudaStream_t);
+#define BF_EXTERN_STEP(Q)                                                                                     \
+    extern template cudaError_t launch_step_st<Q, ST_FP32>(const StepParams&, int, int, cudaStream_t);       \
+    extern template cudaError_t launch_step_st<Q, ST_FP16>(const StepParams&, int, int, cudaStream_t);       \
+    extern template cudaError_t launch_step_st<Q, ST_FP16S>(const StepParams&, int, int, cudaStream_t);      \
+    extern template cudaError_t launch_step_st<Q, ST_FP16C>(const StepParams&, int, int, cudaStream_t);      \
+    extern template cudaError_t launch_step_st<Q, ST_FP64>(const StepParams&, int, int, cudaStream_t);
+
 #define BF_INSTANTIATE_Q(Q)                                                                                   \
-    template cudaError_t launch_step<Q>(const StepParams&, int, int, bool, cudaStream_t);                    \
+    BF_EXTERN_STEP(Q)                                                                                         \
+    template cudaError_t launch_step<Q>(const StepParams&, int, int, int, cudaStream_t);                     \
+    template cudaError_t launch_build_mask<Q>(const StepParams&, uint32_t*, cudaStream_t);                   \
     template cudaError_t launch_stream<Q>(const StreamParams&, int, cudaStream_t);                           \
     template cudaError_t launch_init<Q>(const InitParams&, int, cudaStream_t);                               \
     template cudaError_t launch_decode<Q>(const void*, uint64_t, uint32_t, int, float*, cudaStream_t);        \

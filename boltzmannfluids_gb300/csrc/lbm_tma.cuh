@@ -1,5 +1,5 @@
 // lbm_tma.cuh -- the fast AA step with its population loads staged through
-// shared memory by the bulk-copy (TMA) engine, for the 16-bit storages.
+// shared memory by the bulk-copy (TMA) engine, for fp16s storage.
 //
 // The 16-bit steps are issue-bound: half of a plain step's instructions are
 // load/store addressing and memory operations.  Here a persistent block walks

@@ -83,3 +83,26 @@ def nusselt(s, kappa, h):
     uz, T = vd[1:-1, :, :, 2].astype(np.float64), ft[1:-1, :, :, 3].astype(np.float64)
     # conductive profile dT/dz = -1/h: Nu = 1 + <u_z T> h / kappa
     return 1.0 + (uz * T).mean() * h / kappa
+
+
+def sphere_channel(res=(256, 128, 128), radius=16.0, center=(64.0, 64.0, 64.0), u_in=0.05, noise=1e-4, seed=2):
+    """Flow past a sphere: velocity inlet (equilibrium object, u = (u_in, 0, 0))
+    on the x = 0 layer, density outlet (equilibrium object, rho = 1) on the
+    x = nx-1 layer, a solid sphere, periodic y and z; equilibrium start at
+    u_in plus seeded uniform noise of `noise` on u.  Returns (rho, u, ids,
+    objects) for LBM.initialize_fields_from_arrays / set_boundry_properties
+    (ids 1 inlet, 2 outlet, 3 sphere)."""
+    nx, ny, nz = (int(v) for v in res)
+    n = nx * ny * nz
+    z, y, x = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    ids = np.zeros((nz, ny, nx), np.uint32)
+    ids[:, :, 0] = 1
+    ids[:, :, -1] = 2
+    cx, cy, cz = center
+    ids[(x - cx) ** 2 + (y - cy) ** 2 + (z - cz) ** 2 <= radius * radius] = 3
+    rng = np.random.default_rng(seed)
+    u = rng.uniform(-noise, noise, (n, 3)).astype(np.float32)
+    u[:, 0] += np.float32(u_in)
+    rho = np.ones(n, np.float32)
+    objects = {1: dict(kind=1), 2: dict(kind=2), 3: dict(kind=0)}
+    return rho, u, ids.reshape(-1), objects

@@ -1,6 +1,7 @@
 """The staged 16-bit fast step (row tiles in shared memory by bulk copies)
 against the oracle, bit for bit: single-tile and multi-tile rows (halo wrap
-at both row ends), every velocity set, the three 16-bit storages."""
+at both row ends), every velocity set (fp16s storage; the other storages take
+the plain step, checked the same way)."""
 import os
 
 import numpy as np
@@ -20,11 +21,11 @@ def staged(monkeypatch):
 
 @pytest.mark.parametrize("vs,res,storage,collision,forced", [
     (bf.VelocitySet.D3Q19, (256, 6, 5), bf.FloatingPointAccuracy.fp16s, 1, False),
-    (bf.VelocitySet.D3Q19, (512, 4, 3), bf.FloatingPointAccuracy.fp16c, 0, True),
-    (bf.VelocitySet.D3Q19, (768, 3, 2), bf.FloatingPointAccuracy.fp16, 1, True),
+    (bf.VelocitySet.D3Q19, (512, 4, 3), bf.FloatingPointAccuracy.fp16s, 0, True),
+    (bf.VelocitySet.D3Q19, (768, 3, 2), bf.FloatingPointAccuracy.fp16s, 1, True),
     (bf.VelocitySet.D2Q9, (256, 10, 1), bf.FloatingPointAccuracy.fp16s, 0, False),
     (bf.VelocitySet.D3Q15, (256, 4, 4), bf.FloatingPointAccuracy.fp16s, 1, False),
-    (bf.VelocitySet.D3Q27, (256, 4, 3), bf.FloatingPointAccuracy.fp16c, 1, False),
+    (bf.VelocitySet.D3Q27, (256, 4, 3), bf.FloatingPointAccuracy.fp16s, 1, False),
 ])
 def test_staged_step_matches_oracle(staged, vs, res, storage, collision, forced, product_lib):
     dims = 2 if vs == bf.VelocitySet.D2Q9 else 3

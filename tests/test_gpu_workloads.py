@@ -69,3 +69,32 @@ def test_rayleigh_benard_convects_with_plausible_nusselt(product_lib):
     # FP32 mass drift (the FP64 oracle conserves this flow's mass to 1e-13 and
     # its FP32 restatement gains ~2.7e-8 per step, bit-exact with the GPU)
     assert abs(m1 - m0) / m0 < 2e-3, (m0, m1)
+
+
+def test_flow_past_sphere_full_size(product_lib):
+    """The 3D plain-method configuration: D3Q19 TRT (1/4, tau 0.55) flow past a
+    sphere r 16 at (64, 64, 64) in 256x128x128, velocity inlet 0.05, density
+    outlet 1, periodic y/z, 5000 steps: stable, a wake behind the sphere, a
+    stagnation point in front, the outlet at rho 1."""
+    from boltzmannfluids_gb300.workloads import sphere_channel
+    res = (256, 128, 128)
+    rho, u, ids, objs = sphere_channel(res)
+    s = bf.LBM()
+    s.is_collide_esoteric = True
+    s.collision = bf.Collision.trt
+    s.boundary_mode = bf.BoundaryMode.bounce_back
+    for k, o in objs.items():
+        s.set_boundry_properties(k, velocity_translational=(0, 0, 0), kind=o["kind"])
+    s.initialize_fields_from_arrays(res, 0.55, density=rho, velocity=u, boundry_id=ids, periodic=(False, True, True),
+                                    velocity_set=bf.VelocitySet.D3Q19)
+    s.iterate_time(steps=5000, save=True)
+    s.synchronize()
+    vd = s.get_velocity_density_texture().reshape(128, 128, 256, 4)
+    assert np.isfinite(vd).all()
+    ux = vd[..., 0]
+    assert ux[64, 64, 64 + 24] < 0.5 * 0.05          # wake just behind the sphere
+    assert abs(ux[64, 64, 64 - 20]) < 0.8 * 0.05     # slowed ahead of the stagnation point
+    # the mass flux through cross-sections up- and downstream agrees (steady flow)
+    flux = (vd[..., 3] * ux).sum(axis=(0, 1))
+    assert abs(flux[40] - flux[200]) / flux[40] < 0.02, (flux[40], flux[200])
+    assert np.abs(vd[:, :, -2, 3] - 1.0).max() < 0.02  # next to the density outlet

@@ -44,6 +44,23 @@ def dist_env():
     return rank, world, local
 
 
+def slowest_rank_time(t_local, dist, device):
+    """Max over ranks of a per-rank step time (the whole job runs at the
+    slowest replica's pace); the local value without a process group."""
+    if dist is None:
+        return float(t_local)
+    import torch
+    t = torch.tensor([float(t_local)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_mlups(cells_per_rank, world, t_step_ms):
+    """Whole-job throughput of `world` replicas: all ranks' cell updates over
+    the slowest rank's step time."""
+    return world * cells_per_rank / (t_step_ms * 1e-3) / 1e6
+
+
 class ClockSampler:
     """Samples nvidia-smi clocks and throttle reasons every 50 ms."""
 
@@ -382,13 +399,8 @@ def run_gpu(args):
     ms = s.benchmark_steps(args.steps)
     clock_info = clocks.stop()
     s.synchronize()
-    t_step = ms / args.steps
-    if dist:
-        import torch
-        t = torch.tensor([t_step], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_step = float(t.item())
-    mlups = world * n / (t_step * 1e-3) / 1e6
+    t_step = slowest_rank_time(ms / args.steps, dist, "cuda")
+    mlups = job_mlups(n, world, t_step)
     peak, peak_kind = measured_peak()
     achieved = BYTES_PER_CELL[int(main_st)] * n / (t_step * 1e-3) / 1e9
     # KE / mass after the timed run (FP64 reductions)

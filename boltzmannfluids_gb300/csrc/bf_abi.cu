@@ -262,9 +262,9 @@ cudaError_t collide(bf_solver* s, bool save, bool update, bool reduce, bool meas
     // the fast kernel indexes every slot with 32 bits off the first plane
     const bool idx32 = (uint64_t)s->N * (uint64_t)s->Q < (1ull << 32);
     const bool generic = mode == AA_LOCAL || (p.flags & heavy) || !all_periodic || !idx32;
-    // objects and open faces without thermal, force-field or multiphase
-    // flow: the boundary-aware fast kernel, with its masks
-    const uint32_t masked_excl = F_FORCE_FIELD | F_THERMAL | F_MULTIPHASE;
+    // objects and open faces (thermal flow included) without force-field or
+    // multiphase flow: the boundary-aware fast kernel, with its masks
+    const uint32_t masked_excl = F_FORCE_FIELD | F_MULTIPHASE;
     int path = generic ? PATH_GENERIC : PATH_FAST;
     if (generic && mode != AA_LOCAL && idx32 && !(p.flags & masked_excl) && s->nmask.p &&
         s->desc.storage != BF_STORE_FP64 && s->masked_step)

@@ -614,7 +614,7 @@ __global__ void build_mask_kernel(const __grid_constant__ StepParams p, uint32_t
     mask[n] = m;
 }
 
-template <int Q, int ST, int MODE, bool TRT, bool FORCED, bool EDGE>
+template <int Q, int ST, int MODE, bool TRT, bool FORCED, bool THERMAL, bool EDGE>
 __device__ __forceinline__ CellSum masked_cell(const StepParams& p, int x, int y, int z) {
     using L = Lattice<Q>;
     using C = Codec<ST>;
@@ -696,7 +696,17 @@ __device__ __forceinline__ CellSum masked_cell(const StepParams& p, int x, int y
     m.Fx = FORCED ? p.fconst[0] : 0.f;
     m.Fy = FORCED ? p.fconst[1] : 0.f;
     m.Fz = FORCED ? p.fconst[2] : 0.f;
-    velocity_and_limit<Q>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
+    constexpr int QT = L::D == 2 ? 5 : 7;
+    float temperature = 0.f;
+    if (THERMAL) {  // Boussinesq buoyancy of the generic kernel (collide.comp:709-716)
+#pragma unroll
+        for (int i = 0; i < QT; i++) temperature = FADD(temperature, __ldg(p.th_src + (uint64_t)i * p.stride + n));
+        const float k = FMUL(-p.beta, FSUB(temperature, 1.0f));
+        m.Fx = FFMA(k, m.Fx, m.Fx); m.Fy = FFMA(k, m.Fy, m.Fy); m.Fz = FFMA(k, m.Fz, m.Fz);
+    }
+    // thermal flow is forced with the source term on, as in the generic kernel
+    constexpr bool FRC = FORCED || THERMAL;
+    velocity_and_limit<Q>(f, m, FRC, p.vlim, p.t_lim, p.t_ext);
     if (eqb) {
         const int kind = __ldg(p.obj_kind + bid);
         if (kind == 1) { m.ux = bv.y; m.uy = bv.z; m.uz = bv.w; } else { m.rho = bv.x; }
@@ -716,12 +726,24 @@ __device__ __forceinline__ CellSum masked_cell(const StepParams& p, int x, int y
             base[slot(opp(i), n_st, oxm_st, oxp_st)] = C::enc(v, L::w(i));
         };
         if (eqb) collide_fixed<Q, false, false, true, C::SHIFTED>(f, m, k, emit);  // f_eq of the cell
-        else if (m.out_ext) collide_fixed<Q, TRT, FORCED, true, C::SHIFTED>(f, m, k, emit);
-        else collide_fixed<Q, TRT, FORCED, false, C::SHIFTED>(f, m, k, emit);
+        else if (m.out_ext) collide_fixed<Q, TRT, FRC, true, C::SHIFTED>(f, m, k, emit);
+        else collide_fixed<Q, TRT, FRC, false, C::SHIFTED>(f, m, k, emit);
+    }
+    if (THERMAL && !(flags & F_MEASURE)) {  // thermal BGK (collide.comp:771-782)
+        const float one_m = FSUB(1.0f, FMUL(uu_of(m.ux, m.uy, m.uz), p.R2h));
+#pragma unroll
+        for (int i = 0; i < QT; i++) {
+            const Dir c = ThermalLattice<QT>::c(i);
+            const float w = ThermalLattice<QT>::w(i);
+            const float cu = cdot_rt(c, m.ux, m.uy, m.uz);
+            const float geq = FMUL(FMUL(w, temperature), bracket(cu, one_m, p.R2, p.R4h));
+            const float g = __ldg(p.th_src + (uint64_t)i * p.stride + n);
+            p.th_tgt[(uint64_t)i * p.stride + n] = FFMA(FSUB(geq, g), p.Rtau_t, g);
+        }
     }
     if (flags & F_SAVE) {
         p.vel_den[n] = make_float4(m.ux, m.uy, m.uz, m.rho);
-        p.force_temp[n] = make_float4(m.Fx, m.Fy, m.Fz, 0.f);
+        p.force_temp[n] = make_float4(m.Fx, m.Fy, m.Fz, temperature);
         if (p.bnd_tex) p.bnd_tex[n] = (uint8_t)bid;
     }
     if (flags & F_REDUCE) {
@@ -732,16 +754,18 @@ __device__ __forceinline__ CellSum masked_cell(const StepParams& p, int x, int y
     return cs;
 }
 
-template <int Q, int ST, int MODE, bool TRT, bool FORCED>
-__global__ void __launch_bounds__(kStepBlock, kFastMinBlocks) masked_step_kernel(const __grid_constant__ StepParams p) {
+// 64 registers (4 blocks of 256 per SM); D3Q27 gets 80 (3 blocks), below which it spills
+template <int Q, int ST, int MODE, bool TRT, bool FORCED, bool THERMAL>
+__global__ void __launch_bounds__(kStepBlock, Q == 27 ? 3 : kFastMinBlocks)
+    masked_step_kernel(const __grid_constant__ StepParams p) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y, z = blockIdx.z;
     CellSum cs = {0.f, 0.f, 0.f, 0.f, 0.f};
     if (x < p.nx) {
         const bool edge = MODE == AA_EVEN &&
                           (y == 0 || y == p.ny - 1 || (Lattice<Q>::D == 3 && (z == 0 || z == p.nz - 1)));
-        if (edge) cs = masked_cell<Q, ST, MODE, TRT, FORCED, true>(p, x, y, z);
-        else cs = masked_cell<Q, ST, MODE, TRT, FORCED, false>(p, x, y, z);
+        if (edge) cs = masked_cell<Q, ST, MODE, TRT, FORCED, THERMAL, true>(p, x, y, z);
+        else cs = masked_cell<Q, ST, MODE, TRT, FORCED, THERMAL, false>(p, x, y, z);
     }
     if (p.flags & F_REDUCE) block_reduce_store(cs, p.red_partials);
 }
@@ -1114,13 +1138,16 @@ cudaError_t launch_step_st(const StepParams& p, int mode, int path, cudaStream_t
     if constexpr (ST != ST_FP64) {
         if (path == PATH_MASKED && mode != AA_LOCAL) {
             const bool trt = (p.flags & F_TRT) != 0, forced = (p.flags & F_FORCE_CONST) != 0;
-            if (mode == AA_EVEN) {
-                if (trt) { if (forced) masked_step_kernel<Q, ST, AA_EVEN, true, true><<<grid, block, 0, st>>>(p); else masked_step_kernel<Q, ST, AA_EVEN, true, false><<<grid, block, 0, st>>>(p); }
-                else { if (forced) masked_step_kernel<Q, ST, AA_EVEN, false, true><<<grid, block, 0, st>>>(p); else masked_step_kernel<Q, ST, AA_EVEN, false, false><<<grid, block, 0, st>>>(p); }
-            } else {
-                if (trt) { if (forced) masked_step_kernel<Q, ST, AA_ODD, true, true><<<grid, block, 0, st>>>(p); else masked_step_kernel<Q, ST, AA_ODD, true, false><<<grid, block, 0, st>>>(p); }
-                else { if (forced) masked_step_kernel<Q, ST, AA_ODD, false, true><<<grid, block, 0, st>>>(p); else masked_step_kernel<Q, ST, AA_ODD, false, false><<<grid, block, 0, st>>>(p); }
-            }
+            const bool thermal = (p.flags & F_THERMAL) != 0;
+#define BF_MASKED(MODE_, TRT_, F_, TH_) masked_step_kernel<Q, ST, MODE_, TRT_, F_, TH_><<<grid, block, 0, st>>>(p)
+#define BF_MASKED_MODE(MODE_)                                                                       \
+    if (thermal) { if (trt) BF_MASKED(MODE_, true, true, true); else BF_MASKED(MODE_, false, true, true); } \
+    else if (trt) { if (forced) BF_MASKED(MODE_, true, true, false); else BF_MASKED(MODE_, true, false, false); } \
+    else { if (forced) BF_MASKED(MODE_, false, true, false); else BF_MASKED(MODE_, false, false, false); }
+            if (mode == AA_EVEN) { BF_MASKED_MODE(AA_EVEN) }
+            else { BF_MASKED_MODE(AA_ODD) }
+#undef BF_MASKED_MODE
+#undef BF_MASKED
             return cudaGetLastError();
         }
     }

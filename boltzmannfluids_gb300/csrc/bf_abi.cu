@@ -214,11 +214,14 @@ void fill_constants(bf_solver* s, StepParams& p) {
 }
 
 template <int Q>
-void fill_uoff(StepParams& p) {
+void fill_uoff(StepParams& p, size_t elem) {
     const uint32_t nx = (uint32_t)p.nx, nxy = (uint32_t)p.nx * (uint32_t)p.ny;
     for (int i = 0; i < Q; i++) {
         const Dir c = Lattice<Q>::c(i);
         p.uoff[i] = (uint32_t)i * (uint32_t)p.stride - ((uint32_t)c.y * nx + (uint32_t)c.z * nxy);
+        const int64_t e = (int64_t)i * (int64_t)p.stride - ((int64_t)c.y * nx + (int64_t)c.z * nxy);
+        p.uoff_b[i] = e * (int64_t)elem;
+        p.poff_b[i] = (int64_t)i * (int64_t)p.stride * (int64_t)elem;
     }
 }
 
@@ -277,10 +280,10 @@ cudaError_t collide(bf_solver* s, bool save, bool update, bool reduce, bool meas
         p.pf_blocks = s->pf_blocks;
     p.tma = s->tma_step ? 1u : 0u;
     switch (s->Q) {
-    case 9: fill_uoff<9>(p); break;
-    case 15: fill_uoff<15>(p); break;
-    case 19: fill_uoff<19>(p); break;
-    default: fill_uoff<27>(p); break;
+    case 9: fill_uoff<9>(p, storage_bytes(s->desc.storage)); break;
+    case 15: fill_uoff<15>(p, storage_bytes(s->desc.storage)); break;
+    case 19: fill_uoff<19>(p, storage_bytes(s->desc.storage)); break;
+    default: fill_uoff<27>(p, storage_bytes(s->desc.storage)); break;
     }
     cudaError_t e = dispatch_step(s, p, mode, path);
     if (e != cudaSuccess) return e;

@@ -235,6 +235,10 @@ struct alignas(16) StepParams {
     // slot read for direction i relative to the cell, without its x part:
     // i * stride - (c_y nx + c_z nx ny), modulo 2^32
     uint32_t uoff[27];
+    // the same in bytes, signed (uoff_b), and the byte offset of plane i
+    // (poff_b): the fast kernel adds them to per-thread byte pointers
+    int64_t uoff_b[27];
+    int64_t poff_b[27];
     // FP64 reference stepper: the launch constants in double, computed as the
     // FP64 oracle does (cs = 1/sqrt(3), tau and the limits from the FP32 inputs)
     struct {

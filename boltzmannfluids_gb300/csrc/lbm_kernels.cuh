@@ -456,9 +456,9 @@ constexpr int kFastMinBlocks16 = BF_FAST_MIN_BLOCKS_16;
 // the box, so the y/z neighbour offsets wrap and are computed in the block;
 // otherwise they are the launch constants p.uoff (plane offset minus
 // c_y nx + c_z nx ny), one constant-bank operand per index.
-// load(i, slot) returns the stored element of direction i; slot(k) is the
-// element index of the slot read for direction k (the plain kernel loads
-// base[slot(i)], the staged kernel reads shared memory and never calls it)
+// load(i, ptr_of) returns the stored element of direction i; ptr_of(k) is
+// the address of the slot read for direction k (the plain kernel loads
+// *ptr_of(i), the staged kernel reads shared memory and never calls it)
 template <int Q, int ST, int MODE, bool TRT, bool FORCED, bool MP, bool EDGE, class Load>
 __device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepParams& p, int x, int y, int z,
                                                                      Load&& load) {
@@ -491,15 +491,45 @@ __device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepP
         }
         return nn + (uint32_t)opp(i) * S;
     };
-    R f[Q];
-    auto slot_of = [&](int k) -> uint32_t { return slot(k, n, oxm, oxp); };
-#pragma unroll
-    for (int i = 0; i < Q; i++) f[i] = C::dec(load(i, slot_of), W::w(i));
+#ifndef BF_PTR_ADDR
+#define BF_PTR_ADDR 1
+#endif
+#if BF_PTR_ADDR
+    // byte pointers to this cell in plane 0 and to its x neighbours
+    // (periodic); a slot is one of them plus a launch constant, a 64-bit
+    // add of a uniform value (interior rows of even steps, all odd steps)
+    const char* const cb = reinterpret_cast<const char*>(base) + (size_t)n * sizeof(T);
+    const char* const cbm = cb + (ptrdiff_t)oxm * (ptrdiff_t)sizeof(T);
+    const char* const cbp = cb + (ptrdiff_t)oxp * (ptrdiff_t)sizeof(T);
+    auto make_ptr = [&](int i, const char* c0, const char* cm, const char* cp, uint32_t nn, int xm, int xp) -> T* {
+        if (MODE == AA_EVEN && EDGE) return base + slot(i, nn, xm, xp);
+        if (MODE == AA_EVEN) {
+            const Dir c = L::c(i);
+            const char* b = c.x > 0 ? cm : (c.x < 0 ? cp : c0);
+            return reinterpret_cast<T*>(const_cast<char*>(b) + p.uoff_b[i]);
+        }
+        return reinterpret_cast<T*>(const_cast<char*>(c0) + p.poff_b[opp(i)]);
+    };
+    auto ptr_of = [&](int i) -> T* { return make_ptr(i, cb, cbm, cbp, n, oxm, oxp); };
+    // the store phase recomputes its addresses from opaque copies of the
+    // per-thread pointers instead of keeping Q addresses live
+    const char *cb_st = cb, *cbm_st = cbm, *cbp_st = cbp;
+    uint32_t n_st = n;
+    int oxm_st = oxm, oxp_st = oxp;
+    asm volatile("" : "+l"(cb_st), "+l"(cbm_st), "+l"(cbp_st), "+r"(n_st), "+r"(oxm_st), "+r"(oxp_st));
+    auto ptr_st = [&](int i) -> T* { return make_ptr(i, cb_st, cbm_st, cbp_st, n_st, oxm_st, oxp_st); };
+#else
+    auto ptr_of = [&](int k) -> T* { return base + slot(k, n, oxm, oxp); };
     // the store phase recomputes its indices (one add each) from opaque
     // copies of the per-thread terms instead of keeping Q indices live
     uint32_t n_st = n;
     int oxm_st = oxm, oxp_st = oxp;
     asm volatile("" : "+r"(n_st), "+r"(oxm_st), "+r"(oxp_st));
+    auto ptr_st = [&](int k) -> T* { return base + slot(k, n_st, oxm_st, oxp_st); };
+#endif
+    R f[Q];
+#pragma unroll
+    for (int i = 0; i < Q; i++) f[i] = C::dec(load(i, ptr_of), W::w(i));
     MomentsT<R> m;
     m.rho = density_of<Q>(f);
     if (C::SHIFTED) m.rho = FADD(R(1), m.rho);  // sum of g plus sum of w
@@ -532,7 +562,7 @@ __device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepP
     else velocity_and_limit<Q>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
     if (p.flags & F_UPDATE) {
         const Coef<R> k = coef_of(p, R(0));
-        auto emit = [&](int i, R v) { base[slot(opp(i), n_st, oxm_st, oxp_st)] = C::enc(v, W::w(i)); };
+        auto emit = [&](int i, R v) { *ptr_st(opp(i)) = C::enc(v, W::w(i)); };
         if (m.out_ext) collide_fixed<Q, TRT, FORCED, true, C::SHIFTED>(f, m, k, emit);
         else collide_fixed<Q, TRT, FORCED, false, C::SHIFTED>(f, m, k, emit);
     }
@@ -569,8 +599,7 @@ __global__ void __launch_bounds__(kStepBlock,
         const bool edge = MODE == AA_EVEN &&
                           (y == 0 || y == p.ny - 1 || (Lattice<Q>::D == 3 && (z == 0 || z == p.nz - 1)));
         using T = typename Codec<ST>::T;
-        const T* base = static_cast<const T*>(p.plane[0]);
-        auto load = [&](int i, auto&& slot_of) -> T { return base[slot_of(i)]; };
+        auto load = [&](int i, auto&& ptr_of) -> T { return *ptr_of(i); };
         if (edge) cs = fast_cell<Q, ST, MODE, TRT, FORCED, MP, true>(p, x, y, z, load);
         else cs = fast_cell<Q, ST, MODE, TRT, FORCED, MP, false>(p, x, y, z, load);
     }

@@ -216,9 +216,12 @@ __global__ void mc_total_kernel(const McParams p, const uint32_t* __restrict__ o
 }
 
 __global__ void __launch_bounds__(256) mc_generate_kernel(const McParams p, const uint32_t* __restrict__ offsets,
-                                                          float* __restrict__ out) {
+                                                          const uint64_t* __restrict__ total, float* __restrict__ out) {
     const uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= p.voxels) return;
+    // empty voxels (equal consecutive offsets) leave before reading their corners
+    const uint64_t next = v + 1 < p.voxels ? (uint64_t)offsets[v + 1] : *total;
+    if (next == (uint64_t)offsets[v]) return;
     int x, y, z;
     voxel_xyz(p, v, x, y, z);
     float val[8];
@@ -371,7 +374,8 @@ int bf_mc_compute(bf_marching_cubes* m, const float* field, int32_t components, 
         MCUDA(cudaMalloc(&m->vertices, tris * 9 * sizeof(float)));
         m->vertex_capacity = tris;
     }
-    if (tris > 0) mc_generate_kernel<<<(unsigned)((voxels + 255) / 256), 256, 0, st>>>(p, m->scan.levels[0], m->vertices);
+    if (tris > 0)
+        mc_generate_kernel<<<(unsigned)((voxels + 255) / 256), 256, 0, st>>>(p, m->scan.levels[0], m->total, m->vertices);
     MCUDA(cudaGetLastError());
     MCUDA(cudaStreamSynchronize(st));
     m->triangles = tris;

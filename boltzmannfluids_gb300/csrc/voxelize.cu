@@ -18,7 +18,7 @@
 // z = -1 + 2(k + (s + 1/2)/samples)/nz.  (The reference's camera looks down
 // -z from z = +1, so its layer 0 is at the top; here layer k grows with z.)
 //
-// Passes: transform the triangles; each triangle visits the column centres
+// Passes: transform the triangles; each triangle (one warp) visits the column centres
 // inside its projection (edge functions with a top-left rule, so a centre on
 // an edge shared by two triangles is counted once and a silhouette edge
 // twice or never, which keeps the parity) and counts a crossing per column;
@@ -61,9 +61,10 @@ __device__ __forceinline__ bool owns(float ax, float ay, float bx, float by) {
     return dy < 0.0f || (dy == 0.0f && dx < 0.0f);
 }
 
-// Visits the column centres covered by triangle t; f(column, depth).
+// Visits the column centres covered by triangle t; f(column, depth).  The
+// lanes of a warp share the triangle's bounding box (lane, lane + 32, ...).
 template <class F>
-__device__ __forceinline__ void visit_triangle(const VoxParams& p, uint64_t t, F f) {
+__device__ __forceinline__ void visit_triangle(const VoxParams& p, uint64_t t, int lane, F f) {
     const float* v = p.tri + t * 9;
     float ax = v[0], ay = v[1], az = v[2];
     float bx = v[3], by = v[4], bz = v[5];
@@ -87,9 +88,13 @@ __device__ __forceinline__ void visit_triangle(const VoxParams& p, uint64_t t, F
     i0 = max(i0, 0); j0 = max(j0, 0);
     i1 = min(i1, p.nx - 1); j1 = min(j1, p.ny - 1);
     const bool oa = owns(bx, by, cx, cy), ob = owns(cx, cy, ax, ay), oc = owns(ax, ay, bx, by);
-    for (int j = j0; j <= j1; j++) {
+    if (i1 < i0 || j1 < j0) return;
+    const int bw = i1 - i0 + 1;
+    const int64_t cells = (int64_t)bw * (int64_t)(j1 - j0 + 1);
+    for (int64_t k = lane; k < cells; k += 32) {
+        const int i = i0 + (int)(k % bw), j = j0 + (int)(k / bw);
         const float py = __fsub_rn(__fdiv_rn((float)(2 * j + 1), (float)p.ny), 1.0f);
-        for (int i = i0; i <= i1; i++) {
+        {
             const float px = __fsub_rn(__fdiv_rn((float)(2 * i + 1), (float)p.nx), 1.0f);
             const float wa = edge_fn(bx, by, cx, cy, px, py);  // weight of a
             const float wb = edge_fn(cx, cy, ax, ay, px, py);
@@ -121,17 +126,18 @@ __global__ void vox_transform_kernel(const float* __restrict__ in, uint64_t tris
     }
 }
 
+// one warp per triangle
 __global__ void vox_count_kernel(const VoxParams p, uint32_t* __restrict__ counts) {
-    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t t = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
     if (t >= p.tris) return;
-    visit_triangle(p, t, [&](uint64_t col, float) { atomicAdd(counts + col, 1u); });
+    visit_triangle(p, t, threadIdx.x & 31, [&](uint64_t col, float) { atomicAdd(counts + col, 1u); });
 }
 
 __global__ void vox_fill_kernel(const VoxParams p, const uint32_t* __restrict__ offsets, uint32_t* __restrict__ cursor,
                                 float* __restrict__ depths) {
-    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t t = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
     if (t >= p.tris) return;
-    visit_triangle(p, t, [&](uint64_t col, float z) {
+    visit_triangle(p, t, threadIdx.x & 31, [&](uint64_t col, float z) {
         const uint32_t slot = offsets[col] + atomicAdd(cursor + col, 1u);
         depths[slot] = z;
     });
@@ -235,9 +241,10 @@ extern "C" int bf_voxelize_mesh(const float* vertices, uint64_t triangle_count, 
     p.nx = nx; p.ny = ny; p.nz = nz;
     p.samples = samples_per_voxel;
     const unsigned tb = (unsigned)((triangle_count + 127) / 128);
+    const unsigned wb = (unsigned)((triangle_count + 3) / 4);  // 4 warps (triangles) per 128-thread block
     if (triangle_count) {
         vox_transform_kernel<<<tb, 128>>>(d_in, triangle_count, d_m, d_tri);
-        vox_count_kernel<<<tb, 128>>>(p, d_count);
+        vox_count_kernel<<<wb, 128>>>(p, d_count);
     }
     // offsets = exclusive scan of the counts (scan level 0 is the offsets array)
     VCUDA(cudaMemcpy(scan.levels[0], d_count, ncol * sizeof(uint32_t), cudaMemcpyDeviceToDevice));
@@ -247,7 +254,7 @@ extern "C" int bf_voxelize_mesh(const float* vertices, uint64_t triangle_count, 
     VCUDA(cudaMemcpy(&last_cnt, d_count + (ncol - 1), 4, cudaMemcpyDeviceToHost));
     const uint64_t crossings = (uint64_t)last_off + last_cnt;
     VCUDA(mem.alloc((void**)&d_depth, crossings * sizeof(float)));
-    if (triangle_count) vox_fill_kernel<<<tb, 128>>>(p, scan.levels[0], d_cursor, d_depth);
+    if (triangle_count) vox_fill_kernel<<<wb, 128>>>(p, scan.levels[0], d_cursor, d_depth);
     vox_resolve_kernel<<<(unsigned)((ncol + 127) / 128), 128>>>(p, scan.levels[0], d_count, d_depth, d_mask);
     VCUDA(cudaGetLastError());
     VCUDA(cudaMemcpy(mask, d_mask, nvox, cudaMemcpyDeviceToHost));

@@ -108,6 +108,7 @@ struct bf_solver {
     uint32_t pf_blocks = 0;  // L2 prefetch distance of the fast kernel, in blocks (0 = off)
     bool tma_step = false;   // 16-bit fast step with loads staged by bulk copies
     bool masked_step = true; // boundary-aware fast step for objects and open faces
+    bool two_cell = true;    // 16-bit fast step with two cells per thread
 };
 
 namespace {
@@ -279,6 +280,7 @@ cudaError_t collide(bf_solver* s, bool save, bool update, bool reduce, bool meas
     if (!generic && plane_bytes % 16 == 0 && reinterpret_cast<uintptr_t>(lat_src(s)) % 16 == 0)
         p.pf_blocks = s->pf_blocks;
     p.tma = s->tma_step ? 1u : 0u;
+    p.two_cell = s->two_cell ? 1u : 0u;
     switch (s->Q) {
     case 9: fill_uoff<9>(p, storage_bytes(s->desc.storage)); break;
     case 15: fill_uoff<15>(p, storage_bytes(s->desc.storage)); break;
@@ -499,6 +501,8 @@ int bf_create(bf_solver** out) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
     s->pf_blocks = (uint32_t)std::max(sms, 1) * 4u;
     if (const char* env = std::getenv("BF_PREFETCH_BLOCKS")) s->pf_blocks = (uint32_t)std::strtoul(env, nullptr, 10);
+    // BF_TWO_CELL=0 keeps the 16-bit fast step at one cell per thread (A/B comparisons)
+    if (const char* env = std::getenv("BF_TWO_CELL")) s->two_cell = std::strtoul(env, nullptr, 10) != 0;
     // BF_MASKED_STEP=0 sends objects and open faces to the generic kernel (A/B comparisons)
     if (const char* env = std::getenv("BF_MASKED_STEP")) s->masked_step = std::strtoul(env, nullptr, 10) != 0;
     // BF_TMA_STEP=1 selects the staged 16-bit fast step, 0 the plain one

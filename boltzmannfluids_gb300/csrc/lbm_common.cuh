@@ -226,6 +226,8 @@ struct alignas(16) StepParams {
     // 1: the 16-bit fast step may stage its loads through shared memory with
     // bulk copies (lbm_tma.cuh); set by the host when the planes allow it
     uint32_t tma;
+    // 1: 16-bit update steps may run two cells per thread (fast2_step_kernel)
+    uint32_t two_cell;
     // per-cell masks of the boundary-aware fast step (build_mask_kernel):
     // bit i (1..Q-1) = the AA source x - c_i needs special handling (outside
     // the domain, or a solid cell under bounce-back); bit 31 = the cell is

@@ -395,48 +395,59 @@ __device__ __forceinline__ void l2_prefetch_bulk(const void* ptr, uint32_t bytes
     asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(ptr), "r"(bytes) : "memory");
 }
 
+// c_y + 1 (axis 1) or c_z + 1 (axis 2) of every direction, two bits each
+template <int Q>
+__host__ __device__ constexpr uint64_t packed_axis(int axis) {
+    uint64_t k = 0;
+    for (int i = 0; i < Q; i++) {
+        const Dir c = Lattice<Q>::c(i);
+        k |= (uint64_t)((axis == 1 ? c.y : c.z) + 1) << (2 * i);
+    }
+    return k;
+}
+
 // Prefetch into L2 the population rows that block `b` (linear launch order,
-// x fastest) reads: on an even step row (y - c_y, z - c_z) of plane i over
-// the block's x range widened by 8 cells each side (the c_x shift), on an odd
-// step row (y, z) of every plane.  Ranges are clipped to the row and rounded
-// out to 16 bytes; that stays inside the plane because planes start and end
-// on 16-byte boundaries whenever pf_blocks is set.
+// x fastest) reads, one plane per lane of the calling warp (lanes >= Q do
+// nothing): on an even step lane i takes row (y - c_y, z - c_z) of plane i
+// over the block's x range widened by 8 cells each side (the c_x shift), on
+// an odd step row (y, z) of plane i.  `tile` is the block's width in cells.
+// Ranges are clipped to the row and rounded out to 16 bytes; that stays
+// inside the plane because planes start and end on 16-byte boundaries
+// whenever pf_blocks is set.  Planes lie `stride` elements apart.
 template <int Q, int ST, int MODE>
-__device__ __forceinline__ void prefetch_block_rows(const StepParams& p, uint32_t b) {
-    using L = Lattice<Q>;
+__device__ __forceinline__ void prefetch_block_rows(const StepParams& p, uint32_t b, int lane, int tile) {
     using T = typename Codec<ST>::T;
+    if (lane >= Q) return;
     const uint32_t gx = gridDim.x, gy = gridDim.y;
     const uint32_t bx = b % gx, yz = b / gx;
-    const int y = (int)(yz % gy), z = (int)(yz / gy);
+    int ys = (int)(yz % gy), zs = (int)(yz / gy);
     const int nx = p.nx, ny = p.ny, nz = p.nz;
-    const int x0 = (int)(bx * blockDim.x);
+    const int x0 = (int)bx * tile;
     const int xlo = MODE == AA_EVEN ? max(x0 - 8, 0) : x0;
-    const int xhi = min(x0 + (int)blockDim.x + (MODE == AA_EVEN ? 8 : 0), nx);
-    const uintptr_t plane_bytes = (uintptr_t)p.n_cells * sizeof(T);
-#pragma unroll
-    for (int i = 0; i < Q; i++) {
-        const Dir c = L::c(i);
-        int ys = y, zs = z;
-        if (MODE == AA_EVEN) {
-            ys -= c.y; ys = ys < 0 ? ys + ny : (ys >= ny ? ys - ny : ys);
-            zs -= c.z; zs = zs < 0 ? zs + nz : (zs >= nz ? zs - nz : zs);
-        }
-        const int slot = MODE == AA_EVEN ? i : opp(i);
-        const uintptr_t base = reinterpret_cast<uintptr_t>(p.plane[slot]);
-        const uintptr_t row = (uintptr_t)nx * ((uintptr_t)ys + (uintptr_t)ny * (uintptr_t)zs);
-        const uintptr_t lo = (base + (row + (uintptr_t)xlo) * sizeof(T)) & ~(uintptr_t)15;
-        uintptr_t hi = (base + (row + (uintptr_t)xhi) * sizeof(T) + 15) & ~(uintptr_t)15;
-        hi = min(hi, base + plane_bytes);
-        if (hi > lo) l2_prefetch_bulk(reinterpret_cast<const void*>(lo), (uint32_t)(hi - lo));
+    const int xhi = min(x0 + tile + (MODE == AA_EVEN ? 8 : 0), nx);
+    if (MODE == AA_EVEN) {
+        constexpr uint64_t ky = packed_axis<Q>(1), kz = packed_axis<Q>(2);
+        ys -= (int)((ky >> (2 * lane)) & 3u) - 1;
+        zs -= (int)((kz >> (2 * lane)) & 3u) - 1;
+        ys = ys < 0 ? ys + ny : (ys >= ny ? ys - ny : ys);
+        zs = zs < 0 ? zs + nz : (zs >= nz ? zs - nz : zs);
     }
+    const uintptr_t plane_bytes = (uintptr_t)p.n_cells * sizeof(T);
+    const uintptr_t base = reinterpret_cast<uintptr_t>(p.plane[0]) + (uintptr_t)lane * (uintptr_t)p.stride * sizeof(T);
+    const uintptr_t row = (uintptr_t)nx * ((uintptr_t)ys + (uintptr_t)ny * (uintptr_t)zs);
+    const uintptr_t lo = (base + (row + (uintptr_t)xlo) * sizeof(T)) & ~(uintptr_t)15;
+    uintptr_t hi = (base + (row + (uintptr_t)xhi) * sizeof(T) + 15) & ~(uintptr_t)15;
+    hi = min(hi, base + plane_bytes);
+    if (hi > lo) l2_prefetch_bulk(reinterpret_cast<const void*>(lo), (uint32_t)(hi - lo));
 }
 
 // ---------------------------------------------------------------------------
 // fast AA step: fully periodic box, no objects, no thermal / Shan-Chen /
 // force field (constant force allowed; TRT and forcing fixed per launch).
-// Slots are addressed by 32-bit element indices off the first plane.  Thread 0 of each block prefetches into L2 the rows of the block
-// pf_blocks ahead in launch order, so that the block's own loads mostly hit
-// L2 and 16-bit storage needs fewer loads in flight to saturate HBM.
+// Slots are addressed by byte offsets off the first plane.  The first warp of
+// each block prefetches into L2 the rows of the block pf_blocks ahead in
+// launch order (one plane per lane), so that the block's own loads mostly
+// hit L2 and 16-bit storage needs fewer loads in flight to saturate HBM.
 // ---------------------------------------------------------------------------
 #ifndef BF_FAST_MIN_BLOCKS
 #define BF_FAST_MIN_BLOCKS 4
@@ -586,9 +597,9 @@ template <int Q, int ST, int MODE, bool TRT, bool FORCED, bool MP>
 __global__ void __launch_bounds__(kStepBlock,
                                   ST == ST_FP64 ? 2 : ((ST == ST_FP32 || Q == 27) ? kFastMinBlocks : kFastMinBlocks16))
     fast_step_kernel(const __grid_constant__ StepParams p) {
-    if (p.pf_blocks != 0u && threadIdx.x == 0) {
+    if (p.pf_blocks != 0u && threadIdx.x < 32) {
         const uint32_t b = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z) + p.pf_blocks;
-        if (b < gridDim.x * gridDim.y * gridDim.z) prefetch_block_rows<Q, ST, MODE>(p, b);
+        if (b < gridDim.x * gridDim.y * gridDim.z) prefetch_block_rows<Q, ST, MODE>(p, b, (int)threadIdx.x, (int)blockDim.x);
     }
     using R = typename Codec<ST>::R;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -604,6 +615,135 @@ __global__ void __launch_bounds__(kStepBlock,
         else cs = fast_cell<Q, ST, MODE, TRT, FORCED, MP, false>(p, x, y, z, load);
     }
     if (p.flags & F_REDUCE) block_reduce_store(cs, p.red_partials);
+}
+
+// ---------------------------------------------------------------------------
+// fast step, two cells per thread (16-bit storage): a thread updates the
+// cells x and x+1 (x even) of one row.  Directions with c_x = 0 move both
+// cells' populations as one aligned 32-bit word (one address, one load, one
+// store, one packed conversion); directions with c_x != 0 load and store the
+// two 16-bit values through one address.  The arithmetic of each cell is the
+// one-cell kernel's (fast_cell), so results agree bit for bit.
+// ---------------------------------------------------------------------------
+template <int Q, int ST, int MODE, bool TRT, bool FORCED, bool EDGE>
+__device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, int z) {
+    using L = Lattice<Q>;
+    using C = Codec<ST>;
+    using T = typename C::T;
+    static_assert(sizeof(T) == 2, "16-bit storage only");
+    const int nx = p.nx, ny = p.ny, nz = p.nz, nxy = nx * ny;
+    const uint32_t n = (uint32_t)x + (uint32_t)nx * ((uint32_t)y + (uint32_t)ny * (uint32_t)z);
+    const uint64_t S = p.stride;
+    char* const base = static_cast<char*>(p.plane[0]);
+    // byte pointers (plane 0, this row): cell x, x + 1, and the wrapped x - 1, x + 2
+    char* const c0 = base + (size_t)n * 2;
+    char* const cm = base + (size_t)(n + (uint32_t)(x == 0 ? nx - 1 : -1)) * 2;
+    char* const cq = base + (size_t)(n + (uint32_t)(x + 2 == nx ? 2 - nx : 2)) * 2;
+    const int oym = y == 0 ? (ny - 1) * nx : -nx, oyp = y == ny - 1 ? (1 - ny) * nx : nx;
+    const int ozm = z == 0 ? (nz - 1) * nxy : -nxy, ozp = z == nz - 1 ? (1 - nz) * nxy : nxy;
+    // byte offset of the slot read for direction i from a plane-0 pointer at the source's x
+    auto uoff = [&](int i) -> int64_t {
+        if (MODE == AA_ODD) return p.poff_b[opp(i)];
+        if (!EDGE) return p.uoff_b[i];
+        const Dir c = L::c(i);
+        return ((int64_t)i * (int64_t)S + (int64_t)((c.y > 0 ? oym : (c.y < 0 ? oyp : 0)) +
+                                                    (c.z > 0 ? ozm : (c.z < 0 ? ozp : 0)))) * 2;
+    };
+    // sources of direction i for cells x (a) and x + 1 (b): even step x - c_i, odd step x
+    auto src_a = [&](int i) -> char* {
+        const Dir c = L::c(i);
+        if (MODE == AA_ODD || c.x == 0) return c0 + uoff(i);
+        return (c.x > 0 ? cm : c0 + 2) + uoff(i);
+    };
+    auto src_b = [&](int i) -> char* {
+        const Dir c = L::c(i);
+        if (MODE == AA_ODD || c.x == 0) return c0 + 2 + uoff(i);
+        return (c.x > 0 ? c0 : cq) + uoff(i);
+    };
+    auto paired = [&](int i) -> bool { return MODE == AA_ODD || L::c(i).x == 0; };
+    // ---- loads: every population of both cells before any arithmetic ----
+    uint32_t ld[Q];
+#pragma unroll
+    for (int i = 0; i < Q; i++) {
+        if (paired(i)) {
+            ld[i] = __ldg(reinterpret_cast<const unsigned int*>(src_a(i)));
+        } else {
+            const uint32_t a = __ldg(reinterpret_cast<const unsigned short*>(src_a(i)));
+            const uint32_t b = __ldg(reinterpret_cast<const unsigned short*>(src_b(i)));
+            ld[i] = a | (b << 16);
+        }
+    }
+    // the stores recompute their addresses from opaque copies of the pointers
+    char *c0s = c0, *cms = cm, *cqs = cq;
+    asm volatile("" : "+l"(c0s), "+l"(cms), "+l"(cqs));
+    // store of population i goes to the slot read for opp(i)
+    auto dst_a = [&](int i) -> char* {
+        const int o = opp(i);
+        const Dir c = L::c(o);
+        if (MODE == AA_ODD || c.x == 0) return c0s + uoff(o);
+        return (c.x > 0 ? cms : c0s + 2) + uoff(o);
+    };
+    auto dst_b = [&](int i) -> char* {
+        const int o = opp(i);
+        const Dir c = L::c(o);
+        if (MODE == AA_ODD || c.x == 0) return c0s + 2 + uoff(o);
+        return (c.x > 0 ? c0s : cqs) + uoff(o);
+    };
+    auto to16 = [](uint32_t v) -> T { const unsigned short u = (unsigned short)v; T t; memcpy(&t, &u, 2); return t; };
+    auto bits16 = [](T t) -> uint32_t { unsigned short u; memcpy(&u, &t, 2); return u; };
+    uint32_t keep[Q];  // cell a's encoded populations of the paired directions
+    const Coef<float> k = coef_of(p, 0.0f);
+#pragma unroll
+    for (int half = 0; half < 2; half++) {
+        float f[Q];
+#pragma unroll
+        for (int i = 0; i < Q; i++) f[i] = C::dec(to16(half ? (ld[i] >> 16) : ld[i]), L::w(i));
+        Moments m;
+        m.rho = density_of<Q>(f);
+        if (C::SHIFTED) m.rho = FADD(1.0f, m.rho);
+        if (!(m.rho == m.rho)) atomicOr(p.err, 1u);
+        m.rho = m.rho < 0.01f ? 0.01f : m.rho;
+        m.Fx = FORCED ? p.fconst[0] : 0.f;
+        m.Fy = FORCED ? p.fconst[1] : 0.f;
+        m.Fz = FORCED ? p.fconst[2] : 0.f;
+        velocity_and_limit<Q>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
+        auto emit = [&](int i, float v) {
+            const uint32_t e = bits16(C::enc(v, L::w(i)));
+            const int o = opp(i);
+            if (paired(o)) {
+                if (half == 0) keep[i] = e;
+                else *reinterpret_cast<unsigned int*>(dst_a(i)) = keep[i] | (e << 16);
+            } else {
+                *reinterpret_cast<unsigned short*>(half ? dst_b(i) : dst_a(i)) = (unsigned short)e;
+            }
+        };
+        if (m.out_ext) collide_fixed<Q, TRT, FORCED, true, C::SHIFTED>(f, m, k, emit);
+        else collide_fixed<Q, TRT, FORCED, false, C::SHIFTED>(f, m, k, emit);
+        if (p.flags & F_SAVE) {
+            p.vel_den[n + half] = make_float4(m.ux, m.uy, m.uz, m.rho);
+            if (p.force_temp) p.force_temp[n + half] = make_float4(m.Fx, m.Fy, m.Fz, 0.f);
+        }
+    }
+}
+
+#ifndef BF_FAST2_MIN_BLOCKS
+#define BF_FAST2_MIN_BLOCKS 4
+#endif
+// 64 registers (4 blocks of 256 per SM): a thread holds both cells' loads; a few
+// TRT and forced variants spill a handful of words, which measured cheaper than
+// the latency of running at 3 blocks
+template <int Q, int ST, int MODE, bool TRT, bool FORCED>
+__global__ void __launch_bounds__(kStepBlock, BF_FAST2_MIN_BLOCKS) fast2_step_kernel(const __grid_constant__ StepParams p) {
+    if (p.pf_blocks != 0u && threadIdx.x < 32) {
+        const uint32_t b = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z) + p.pf_blocks;
+        if (b < gridDim.x * gridDim.y * gridDim.z) prefetch_block_rows<Q, ST, MODE>(p, b, (int)threadIdx.x, 2 * (int)blockDim.x);
+    }
+    const int x = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= p.nx) return;
+    const bool edge = MODE == AA_EVEN && (y == 0 || y == p.ny - 1 || (Lattice<Q>::D == 3 && (z == 0 || z == p.nz - 1)));
+    if (edge) fast2_cells<Q, ST, MODE, TRT, FORCED, true>(p, x, y, z);
+    else fast2_cells<Q, ST, MODE, TRT, FORCED, false>(p, x, y, z);
 }
 
 // ---------------------------------------------------------------------------
@@ -1192,6 +1332,26 @@ cudaError_t launch_step_st(const StepParams& p, int mode, int path, cudaStream_t
             }
             if (trt) return forced ? launch_tma<Q, ST, AA_ODD, true, true>(p, st) : launch_tma<Q, ST, AA_ODD, true, false>(p, st);
             return forced ? launch_tma<Q, ST, AA_ODD, false, true>(p, st) : launch_tma<Q, ST, AA_ODD, false, false>(p, st);
+        }
+    }
+    // two cells per thread: 16-bit update steps without reduction or multiphase, even nx
+    if constexpr ((ST == ST_FP16S || ST == ST_FP16C) && Q != 27) {
+        if (!generic && p.two_cell && (p.flags & F_UPDATE) && !(p.flags & (F_REDUCE | F_MULTIPHASE)) &&
+            p.nx % 2 == 0) {
+            // one block spans a row where the row is shorter than 2 x kStepBlock cells
+            const int threads = min(kStepBlock, (p.nx / 2 + 31) / 32 * 32);
+            const dim3 g2((unsigned)((p.nx / 2 + threads - 1) / threads), (unsigned)p.ny, (unsigned)p.nz);
+            const bool trt = (p.flags & F_TRT) != 0, forced = (p.flags & F_FORCE_CONST) != 0;
+#define BF_FAST2(MODE_, TRT_, F_) fast2_step_kernel<Q, ST, MODE_, TRT_, F_><<<g2, threads, 0, st>>>(p)
+            if (mode == AA_EVEN) {
+                if (trt) { if (forced) BF_FAST2(AA_EVEN, true, true); else BF_FAST2(AA_EVEN, true, false); }
+                else { if (forced) BF_FAST2(AA_EVEN, false, true); else BF_FAST2(AA_EVEN, false, false); }
+            } else {
+                if (trt) { if (forced) BF_FAST2(AA_ODD, true, true); else BF_FAST2(AA_ODD, true, false); }
+                else { if (forced) BF_FAST2(AA_ODD, false, true); else BF_FAST2(AA_ODD, false, false); }
+            }
+#undef BF_FAST2
+            return cudaGetLastError();
         }
     }
     if (!generic) {

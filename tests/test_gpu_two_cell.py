@@ -1,0 +1,49 @@
+"""The 16-bit fast step with two cells per thread against the oracle, bit
+for bit: paired 32-bit moves of the c_x = 0 directions, 16-bit moves of the
+others, x wrap at both row ends, rows on and off the y/z faces, block widths from
+one warp to rows of several blocks."""
+import numpy as np
+import pytest
+
+import boltzmannfluids_gb300 as bf
+from gpu_helpers import make_pair, seeded_fields, step_and_compare
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("vs,res,storage,collision,forced", [
+    (bf.VelocitySet.D3Q19, (24, 20, 16), bf.FloatingPointAccuracy.fp16s, 1, False),
+    (bf.VelocitySet.D3Q19, (2, 6, 5), bf.FloatingPointAccuracy.fp16s, 0, True),
+    (bf.VelocitySet.D3Q19, (34, 3, 4), bf.FloatingPointAccuracy.fp16c, 1, True),
+    (bf.VelocitySet.D3Q15, (16, 12, 10), bf.FloatingPointAccuracy.fp16c, 0, False),
+    (bf.VelocitySet.D2Q9, (40, 24, 1), bf.FloatingPointAccuracy.fp16s, 1, True),
+    (bf.VelocitySet.D2Q9, (4, 8, 1), bf.FloatingPointAccuracy.fp16c, 0, False),
+    # rows of several blocks (the last one partly filled) and a block of 96 threads
+    (bf.VelocitySet.D3Q19, (600, 3, 2), bf.FloatingPointAccuracy.fp16s, 1, False),
+    (bf.VelocitySet.D3Q19, (170, 6, 4), bf.FloatingPointAccuracy.fp16c, 1, True),
+])
+def test_two_cell_step_matches_oracle(vs, res, storage, collision, forced, product_lib):
+    dims = 2 if vs == bf.VelocitySet.D2Q9 else 3
+    rho, u = seeded_fields(res, 11, dims=dims)
+    n = res[0] * res[1] * res[2]
+    force = None
+    if forced:
+        force = np.zeros((n, 3), np.float32)
+        force[:, 1] = -2e-5
+    s, o = make_pair(res, 0.56, vs, density=rho, velocity=u, force=force, storage=storage, collision=collision,
+                     esoteric=True)
+    step_and_compare(s, o, [1, 2, 3, 8, 17])
+    assert np.array_equal(s.get_populations(), o.lattice().astype(np.float32))
+
+
+def test_two_cell_equals_one_cell(monkeypatch, product_lib):
+    res = (64, 12, 10)
+    rho, u = seeded_fields(res, 12)
+    out = []
+    for flag in ("1", "0"):
+        monkeypatch.setenv("BF_TWO_CELL", flag)
+        s, _ = make_pair(res, 0.55, bf.VelocitySet.D3Q19, density=rho, velocity=u,
+                         storage=bf.FloatingPointAccuracy.fp16s, collision=1, esoteric=True)
+        s.iterate_time(steps=33, save=True)
+        out.append(s.get_populations())
+    assert np.array_equal(out[0], out[1])

@@ -437,7 +437,7 @@ def run_gpu(args):
         multi = run_multiphysics_leg(bf, args.multiphysics_full)
     sphere = None
     if not args.no_sphere:
-        sphere = run_sphere_leg(bf)
+        sphere = run_sphere_leg(bf, args.sphere_steps)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         mlups_cpu, threads, sample = cpu_baseline_sample()
@@ -494,6 +494,7 @@ def main():
     ap.add_argument("--no-multiphysics", action="store_true", help="skip the Shan-Chen / Rayleigh-Benard leg")
     ap.add_argument("--multiphysics-full", action="store_true", help="run the multiphysics configurations at full size")
     ap.add_argument("--no-sphere", action="store_true", help="skip the flow-past-a-sphere leg")
+    ap.add_argument("--sphere-steps", type=int, default=1000, help="timed steps of the flow-past-a-sphere leg")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -16,6 +16,7 @@
 
 #include "../../include/bf_lbm.h"
 #include "lbm_common.cuh"
+#include "scan.cuh"
 
 using namespace bf;
 
@@ -97,6 +98,8 @@ struct bf_solver {
     DeviceBuf lat[2], bnd, objs, kinds, force, bvals, th[2], psi[2];
     DeviceBuf vel_den, force_temp, bnd_tex, partials, red_out, err, decode_tmp;
     DeviceBuf nmask;  // per-cell masks of the boundary-aware fast step
+    DeviceBuf special;        // the cells with a nonzero mask, in index order
+    uint32_t n_special = 0;
     uint32_t n_blocks = 0;
     // buffer roles (LBM.h:280-291)
     int lat0_src = 1, th0_src = 1, psi0_src = 1;
@@ -109,9 +112,52 @@ struct bf_solver {
     bool tma_step = false;   // 16-bit fast step with loads staged by bulk copies
     bool masked_step = true; // boundary-aware fast step for objects and open faces
     bool two_cell = true;    // 16-bit fast step with two cells per thread
+    bool masked_split = true; // boundary-aware step as two launches: plain cells, then the listed ones
 };
 
 namespace {
+
+__global__ void special_flags_kernel(const uint32_t* __restrict__ mask, uint64_t n, uint32_t* __restrict__ flag) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) flag[i] = mask[i] != 0u ? 1u : 0u;
+}
+
+__global__ void special_scatter_kernel(const uint32_t* __restrict__ mask, const uint32_t* __restrict__ offset,
+                                       uint64_t n, uint32_t* __restrict__ list) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && mask[i] != 0u) list[offset[i]] = (uint32_t)i;
+}
+
+// the list of cells with a nonzero mask, in increasing index order (an
+// exclusive scan of the 0/1 flags gives each listed cell its position)
+cudaError_t build_special_list(bf_solver* s, uint64_t n) {
+    s->special.release();
+    s->n_special = 0;
+    if (n == 0) return cudaSuccess;
+    ScanLevels scan;
+    cudaError_t e = scan.reserve(n);
+    if (e != cudaSuccess) return e;
+    const uint32_t* mask = s->nmask.as<uint32_t>();
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    special_flags_kernel<<<blocks, 256, 0, s->stream>>>(mask, n, scan.levels[0]);
+    e = scan.scan(0, n, s->stream);
+    uint32_t last[2] = {0u, 0u};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&last[0], scan.levels[0] + (n - 1), 4, cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&last[1], mask + (n - 1), 4, cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    const uint32_t count = last[0] + (last[1] != 0u ? 1u : 0u);
+    if (e == cudaSuccess && count > 0) {
+        e = s->special.alloc((size_t)count * sizeof(uint32_t));
+        if (e == cudaSuccess) {
+            special_scatter_kernel<<<blocks, 256, 0, s->stream>>>(mask, scan.levels[0], n, s->special.as<uint32_t>());
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    }
+    scan.release();
+    if (e == cudaSuccess) s->n_special = count;
+    return e;
+}
 
 void clear_graphs(bf_solver* s) {
     for (auto& kv : s->graphs) cudaGraphExecDestroy(kv.second);
@@ -122,8 +168,10 @@ void release_all(bf_solver* s) {
     clear_graphs(s);
     DeviceBuf* bufs[] = {&s->lat[0], &s->lat[1], &s->bnd, &s->objs, &s->kinds, &s->force, &s->bvals,
                          &s->th[0], &s->th[1], &s->psi[0], &s->psi[1], &s->vel_den, &s->force_temp,
-                         &s->bnd_tex, &s->partials, &s->red_out, &s->err, &s->decode_tmp, &s->nmask};
+                         &s->bnd_tex, &s->partials, &s->red_out, &s->err, &s->decode_tmp, &s->nmask,
+                         &s->special};
     for (auto* b : bufs) b->release();
+    s->n_special = 0;
     s->initialized = false;
 }
 
@@ -274,6 +322,10 @@ cudaError_t collide(bf_solver* s, bool save, bool update, bool reduce, bool meas
         s->desc.storage != BF_STORE_FP64 && s->masked_step)
         path = PATH_MASKED;
     p.nmask = s->nmask.as<uint32_t>();
+    if (s->masked_split && s->n_special > 0) {
+        p.special = s->special.as<uint32_t>();
+        p.n_special = s->n_special;
+    }
     // the prefetch rounds each row range out to 16 bytes, which stays inside
     // the plane only when every plane starts and ends on a 16-byte boundary
     const size_t plane_bytes = (size_t)s->N * storage_bytes(s->desc.storage);
@@ -505,6 +557,7 @@ int bf_create(bf_solver** out) {
     if (const char* env = std::getenv("BF_TWO_CELL")) s->two_cell = std::strtoul(env, nullptr, 10) != 0;
     // BF_MASKED_STEP=0 sends objects and open faces to the generic kernel (A/B comparisons)
     if (const char* env = std::getenv("BF_MASKED_STEP")) s->masked_step = std::strtoul(env, nullptr, 10) != 0;
+    if (const char* env = std::getenv("BF_MASKED_SPLIT")) s->masked_split = std::strtoul(env, nullptr, 10) != 0;
     // BF_TMA_STEP=1 selects the staged 16-bit fast step, 0 the plain one
     if (const char* env = std::getenv("BF_TMA_STEP")) s->tma_step = std::strtoul(env, nullptr, 10) != 0;
     *out = s;
@@ -752,6 +805,9 @@ int bf_initialize_fields(bf_solver* s, const bf_init_desc* d, const float* densi
         default: e = launch_build_mask<27>(mp, s->nmask.as<uint32_t>(), s->stream); break;
         }
         if (e != cudaSuccess) return fail(BF_ERR_CUDA, std::string("mask kernel: ") + cudaGetErrorString(e));
+        e = build_special_list(s, (uint64_t)N);
+        if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? BF_ERR_OUT_OF_MEMORY : BF_ERR_CUDA,
+                                          std::string("special-cell list: ") + cudaGetErrorString(e));
     }
     // LBM.cpp:502: _iterate_time(true, false)
     e = iterate_once(s, true, false, false);

@@ -233,6 +233,12 @@ struct alignas(16) StepParams {
     // the domain, or a solid cell under bounce-back); bit 31 = the cell is
     // solid; bit 30 = the cell is an equilibrium-boundary cell
     const uint32_t* nmask;
+    // the cells whose mask is nonzero, in increasing index order: when set
+    // (n_special > 0 or special non-null), the boundary-aware step updates
+    // the other cells with the periodic kernel's cell update in one launch
+    // and these cells in a second one
+    const uint32_t* special;
+    uint32_t n_special;
     // fast kernel, even step, rows off the y/z faces: element offset of the
     // slot read for direction i relative to the cell, without its x part:
     // i * stride - (c_y nx + c_z nx ny), modulo 2^32

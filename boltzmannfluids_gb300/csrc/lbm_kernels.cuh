@@ -784,7 +784,7 @@ __global__ void build_mask_kernel(const __grid_constant__ StepParams p, uint32_t
 }
 
 template <int Q, int ST, int MODE, bool TRT, bool FORCED, bool THERMAL, bool EDGE>
-__device__ __forceinline__ CellSum masked_cell(const StepParams& p, int x, int y, int z) {
+__device__ __forceinline__ CellSum masked_cell(const StepParams& p, int x, int y, int z, uint32_t mask) {
     using L = Lattice<Q>;
     using C = Codec<ST>;
     using T = typename C::T;
@@ -792,7 +792,6 @@ __device__ __forceinline__ CellSum masked_cell(const StepParams& p, int x, int y
     const int nx = p.nx, ny = p.ny, nz = p.nz, nxy = nx * ny;
     const uint32_t flags = p.flags;
     const uint32_t n = (uint32_t)x + (uint32_t)nx * ((uint32_t)y + (uint32_t)ny * (uint32_t)z);
-    const uint32_t mask = __ldg(p.nmask + n);
     if (mask >> 31) {  // solid cell (collide.comp:696-700)
         if (flags & F_SAVE) {
             p.vel_den[n] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -931,12 +930,62 @@ __global__ void __launch_bounds__(kStepBlock, Q == 27 ? 3 : kFastMinBlocks)
     const int y = blockIdx.y, z = blockIdx.z;
     CellSum cs = {0.f, 0.f, 0.f, 0.f, 0.f};
     if (x < p.nx) {
+        const uint32_t n = (uint32_t)x + (uint32_t)p.nx * ((uint32_t)y + (uint32_t)p.ny * (uint32_t)z);
+        const uint32_t mask = __ldg(p.nmask + n);
         const bool edge = MODE == AA_EVEN &&
                           (y == 0 || y == p.ny - 1 || (Lattice<Q>::D == 3 && (z == 0 || z == p.nz - 1)));
-        if (edge) cs = masked_cell<Q, ST, MODE, TRT, FORCED, THERMAL, true>(p, x, y, z);
-        else cs = masked_cell<Q, ST, MODE, TRT, FORCED, THERMAL, false>(p, x, y, z);
+        if (!THERMAL && !edge && mask == 0u) {
+            // no special source, no boundary id: every source and destination
+            // is an ordinary in-domain slot (x +- 1 never wraps here), so the
+            // periodic kernel's cell update applies as it is
+            using T = typename Codec<ST>::T;
+            auto load = [&](int i, auto&& ptr_of) -> T { return *ptr_of(i); };
+            cs = fast_cell<Q, ST, MODE, TRT, FORCED, false, false>(p, x, y, z, load);
+            if ((p.flags & F_SAVE) && p.bnd_tex) p.bnd_tex[n] = 0;
+        } else if (edge) {
+            cs = masked_cell<Q, ST, MODE, TRT, FORCED, THERMAL, true>(p, x, y, z, mask);
+        } else {
+            cs = masked_cell<Q, ST, MODE, TRT, FORCED, THERMAL, false>(p, x, y, z, mask);
+        }
     }
     if (p.flags & F_REDUCE) block_reduce_store(cs, p.red_partials);
+}
+
+// The boundary-aware step split in two launches (no reduction, no thermal
+// lattice).  In an AA step every slot is read and written by exactly one
+// cell, so cells are independent within a step and any partition of them
+// over launches gives the same result.  The first launch updates the cells
+// with an empty mask in the periodic kernel's cell update and leaves the
+// others; the second walks the list of the others, so that warps of the
+// first launch never wait for a lane on the special treatment (every row of
+// a channel with inlet and outlet faces starts and ends with such a cell).
+template <int Q, int ST, int MODE, bool TRT, bool FORCED>
+__global__ void __launch_bounds__(kStepBlock, kFastMinBlocks) masked_main_kernel(const __grid_constant__ StepParams p) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= p.nx) return;
+    const uint32_t n = (uint32_t)x + (uint32_t)p.nx * ((uint32_t)y + (uint32_t)p.ny * (uint32_t)z);
+    if (__ldg(p.nmask + n) != 0u) return;
+    using T = typename Codec<ST>::T;
+    auto load = [&](int i, auto&& ptr_of) -> T { return *ptr_of(i); };
+    // rows on a y or z face (block-uniform) wrap their neighbour offsets;
+    // a cell there with an empty mask lies on a periodic face
+    const bool edge = MODE == AA_EVEN && (y == 0 || y == p.ny - 1 || (Lattice<Q>::D == 3 && (z == 0 || z == p.nz - 1)));
+    if (edge) fast_cell<Q, ST, MODE, TRT, FORCED, false, true>(p, x, y, z, load);
+    else fast_cell<Q, ST, MODE, TRT, FORCED, false, false>(p, x, y, z, load);
+    if ((p.flags & F_SAVE) && p.bnd_tex) p.bnd_tex[n] = 0;
+}
+
+template <int Q, int ST, int MODE, bool TRT, bool FORCED>
+__global__ void __launch_bounds__(kStepBlock, Q == 27 ? 3 : kFastMinBlocks) masked_list_kernel(const __grid_constant__ StepParams p) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= p.n_special) return;
+    const uint32_t n = __ldg(p.special + t);
+    const uint32_t nx = (uint32_t)p.nx, ny = (uint32_t)p.ny;
+    const int x = (int)(n % nx), y = (int)((n / nx) % ny), z = (int)(n / (nx * ny));
+    // the face-row variant computes every neighbour offset with its wrap,
+    // which is right for any cell
+    masked_cell<Q, ST, MODE, TRT, FORCED, false, true>(p, x, y, z, __ldg(p.nmask + n));
 }
 
 // ---------------------------------------------------------------------------
@@ -1308,6 +1357,22 @@ cudaError_t launch_step_st(const StepParams& p, int mode, int path, cudaStream_t
         if (path == PATH_MASKED && mode != AA_LOCAL) {
             const bool trt = (p.flags & F_TRT) != 0, forced = (p.flags & F_FORCE_CONST) != 0;
             const bool thermal = (p.flags & F_THERMAL) != 0;
+            if (p.special && !thermal && !(p.flags & F_REDUCE)) {
+                const unsigned lb = (unsigned)((p.n_special + kStepBlock - 1) / kStepBlock);
+#define BF_SPLIT(MODE_, TRT_, F_)                                                            \
+    do {                                                                                     \
+        masked_main_kernel<Q, ST, MODE_, TRT_, F_><<<grid, block, 0, st>>>(p);               \
+        if (lb) masked_list_kernel<Q, ST, MODE_, TRT_, F_><<<lb, kStepBlock, 0, st>>>(p);    \
+    } while (0)
+#define BF_SPLIT_MODE(MODE_)                                                                 \
+    if (trt) { if (forced) BF_SPLIT(MODE_, true, true); else BF_SPLIT(MODE_, true, false); } \
+    else { if (forced) BF_SPLIT(MODE_, false, true); else BF_SPLIT(MODE_, false, false); }
+                if (mode == AA_EVEN) { BF_SPLIT_MODE(AA_EVEN) }
+                else { BF_SPLIT_MODE(AA_ODD) }
+#undef BF_SPLIT_MODE
+#undef BF_SPLIT
+                return cudaGetLastError();
+            }
 #define BF_MASKED(MODE_, TRT_, F_, TH_) masked_step_kernel<Q, ST, MODE_, TRT_, F_, TH_><<<grid, block, 0, st>>>(p)
 #define BF_MASKED_MODE(MODE_)                                                                       \
     if (thermal) { if (trt) BF_MASKED(MODE_, true, true, true); else BF_MASKED(MODE_, false, true, true); } \

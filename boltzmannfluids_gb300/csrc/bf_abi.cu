@@ -100,6 +100,10 @@ struct bf_solver {
     DeviceBuf nmask;  // per-cell masks of the boundary-aware fast step
     DeviceBuf special;        // the cells with a nonzero mask, in index order
     uint32_t n_special = 0;
+    // the special-cell launch of the split boundary-aware step runs on a
+    // high-priority side stream beside the main launch (fork/join by events)
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     uint32_t n_blocks = 0;
     // buffer roles (LBM.h:280-291)
     int lat0_src = 1, th0_src = 1, psi0_src = 1;
@@ -156,6 +160,13 @@ cudaError_t build_special_list(bf_solver* s, uint64_t n) {
     }
     scan.release();
     if (e == cudaSuccess) s->n_special = count;
+    if (e == cudaSuccess && count > 0 && !s->side) {
+        int least = 0, greatest = 0;
+        e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+        if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&s->side, cudaStreamNonBlocking, greatest);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming);
+    }
     return e;
 }
 
@@ -182,14 +193,32 @@ float* th_tgt(bf_solver* s) { return s->th[s->th0_src ? 1 : 0].as<float>(); }
 float* psi_src(bf_solver* s) { return s->psi[s->psi0_src ? 0 : 1].as<float>(); }
 float* psi_tgt(bf_solver* s) { return s->psi[s->psi0_src ? 1 : 0].as<float>(); }
 
-cudaError_t dispatch_step(bf_solver* s, const StepParams& p, int mode, int path) {
+cudaError_t launch_on(bf_solver* s, const StepParams& p, int mode, int path, cudaStream_t st) {
     switch (s->Q) {
-    case 9: return launch_step<9>(p, s->desc.storage, mode, path, s->stream);
-    case 15: return launch_step<15>(p, s->desc.storage, mode, path, s->stream);
-    case 19: return launch_step<19>(p, s->desc.storage, mode, path, s->stream);
-    case 27: return launch_step<27>(p, s->desc.storage, mode, path, s->stream);
+    case 9: return launch_step<9>(p, s->desc.storage, mode, path, st);
+    case 15: return launch_step<15>(p, s->desc.storage, mode, path, st);
+    case 19: return launch_step<19>(p, s->desc.storage, mode, path, st);
+    case 27: return launch_step<27>(p, s->desc.storage, mode, path, st);
     }
     return cudaErrorInvalidValue;
+}
+
+cudaError_t dispatch_step(bf_solver* s, const StepParams& p, int mode, int path) {
+    // split boundary-aware step: the special cells (a partial wave of long
+    // threads) on the side stream while the main launch streams the rest;
+    // the two touch disjoint slots, and the join orders the next step after
+    // both (inside a captured graph this becomes a fork/join of two nodes)
+    if (path == PATH_MASKED && mode != AA_LOCAL && p.special && s->side &&
+        !(p.flags & (F_THERMAL | F_REDUCE))) {
+        cudaError_t e = cudaEventRecord(s->ev_fork, s->stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s->side, s->ev_fork, 0);
+        if (e == cudaSuccess) e = launch_on(s, p, mode, PATH_MASKED_LIST, s->side);
+        if (e == cudaSuccess) e = cudaEventRecord(s->ev_join, s->side);
+        if (e == cudaSuccess) e = launch_on(s, p, mode, PATH_MASKED_MAIN, s->stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s->stream, s->ev_join, 0);
+        return e;
+    }
+    return launch_on(s, p, mode, path, s->stream);
 }
 
 uint32_t base_flags(bf_solver* s) {
@@ -569,6 +598,12 @@ int bf_destroy(bf_solver* s) {
     cudaSetDevice(s->device);
     cudaStreamSynchronize(s->stream);
     release_all(s);
+    if (s->side) {
+        cudaStreamSynchronize(s->side);
+        cudaStreamDestroy(s->side);
+        cudaEventDestroy(s->ev_fork);
+        cudaEventDestroy(s->ev_join);
+    }
     cudaStreamDestroy(s->stream);
     delete s;
     return BF_OK;

@@ -333,7 +333,9 @@ __device__ __forceinline__ uint32_t boundary_id(const uint32_t* __restrict__ bnd
 // launchers (one translation unit per Q instantiates them)
 // kernel choice of one step: the periodic fast kernel, the boundary-aware
 // (masked) fast kernel, or the generic kernel
-enum StepPath { PATH_FAST = 0, PATH_MASKED = 1, PATH_GENERIC = 2 };
+// PATH_MASKED_MAIN / PATH_MASKED_LIST: one of the two launches of the split
+// boundary-aware step (the caller puts them on two streams)
+enum StepPath { PATH_FAST = 0, PATH_MASKED = 1, PATH_GENERIC = 2, PATH_MASKED_MAIN = 3, PATH_MASKED_LIST = 4 };
 template <int Q> cudaError_t launch_step(const StepParams& p, int storage, int mode, int path, cudaStream_t st);
 template <int Q> cudaError_t launch_build_mask(const StepParams& p, uint32_t* mask, cudaStream_t st);
 template <int Q> cudaError_t launch_stream(const StreamParams& p, int storage, cudaStream_t st);

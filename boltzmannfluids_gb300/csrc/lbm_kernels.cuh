@@ -1354,15 +1354,16 @@ cudaError_t launch_step_st(const StepParams& p, int mode, int path, cudaStream_t
     dim3 grid = cell_grid(p.nx, p.ny, p.nz, block);
     const bool generic = path != PATH_FAST;
     if constexpr (ST != ST_FP64) {
-        if (path == PATH_MASKED && mode != AA_LOCAL) {
+        if ((path == PATH_MASKED || path == PATH_MASKED_MAIN || path == PATH_MASKED_LIST) && mode != AA_LOCAL) {
             const bool trt = (p.flags & F_TRT) != 0, forced = (p.flags & F_FORCE_CONST) != 0;
             const bool thermal = (p.flags & F_THERMAL) != 0;
             if (p.special && !thermal && !(p.flags & F_REDUCE)) {
                 const unsigned lb = (unsigned)((p.n_special + kStepBlock - 1) / kStepBlock);
-#define BF_SPLIT(MODE_, TRT_, F_)                                                            \
-    do {                                                                                     \
-        masked_main_kernel<Q, ST, MODE_, TRT_, F_><<<grid, block, 0, st>>>(p);               \
-        if (lb) masked_list_kernel<Q, ST, MODE_, TRT_, F_><<<lb, kStepBlock, 0, st>>>(p);    \
+                const bool main_part = path != PATH_MASKED_LIST, list_part = path != PATH_MASKED_MAIN;
+#define BF_SPLIT(MODE_, TRT_, F_)                                                                          \
+    do {                                                                                                   \
+        if (main_part) masked_main_kernel<Q, ST, MODE_, TRT_, F_><<<grid, block, 0, st>>>(p);              \
+        if (list_part && lb) masked_list_kernel<Q, ST, MODE_, TRT_, F_><<<lb, kStepBlock, 0, st>>>(p);     \
     } while (0)
 #define BF_SPLIT_MODE(MODE_)                                                                 \
     if (trt) { if (forced) BF_SPLIT(MODE_, true, true); else BF_SPLIT(MODE_, true, false); } \

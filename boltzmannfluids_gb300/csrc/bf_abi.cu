@@ -99,11 +99,8 @@ struct bf_solver {
     DeviceBuf vel_den, force_temp, bnd_tex, partials, red_out, err, decode_tmp;
     DeviceBuf nmask;  // per-cell masks of the boundary-aware fast step
     DeviceBuf special;        // the cells with a nonzero mask, in index order
+    DeviceBuf special_ptr;    // per block of the cell grid: its range of `special`
     uint32_t n_special = 0;
-    // the special-cell launch of the split boundary-aware step runs on a
-    // high-priority side stream beside the main launch (fork/join by events)
-    cudaStream_t side = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     uint32_t n_blocks = 0;
     // buffer roles (LBM.h:280-291)
     int lat0_src = 1, th0_src = 1, psi0_src = 1;
@@ -116,7 +113,7 @@ struct bf_solver {
     bool tma_step = false;   // 16-bit fast step with loads staged by bulk copies
     bool masked_step = true; // boundary-aware fast step for objects and open faces
     bool two_cell = true;    // 16-bit fast step with two cells per thread
-    bool masked_split = true; // boundary-aware step as two launches: plain cells, then the listed ones
+    bool masked_split = true; // boundary-aware step with the special cells in blocks of their own
 };
 
 namespace {
@@ -132,10 +129,28 @@ __global__ void special_scatter_kernel(const uint32_t* __restrict__ mask, const 
     if (i < n && mask[i] != 0u) list[offset[i]] = (uint32_t)i;
 }
 
+// first list position of each block of the cell grid (lower bound of the
+// block's first cell index in the sorted list); entry n_blocks = count
+__global__ void special_ptr_kernel(const uint32_t* __restrict__ list, uint32_t count, uint32_t n_blocks,
+                                   uint32_t grid_x, uint32_t block, uint32_t nx, uint32_t* __restrict__ ptr) {
+    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b > n_blocks) return;
+    if (b == n_blocks) { ptr[b] = count; return; }
+    const uint64_t first = (uint64_t)(b % grid_x) * block + (uint64_t)(b / grid_x) * nx;
+    uint32_t lo = 0, hi = count;
+    while (lo < hi) {
+        const uint32_t mid = lo + (hi - lo) / 2;
+        if ((uint64_t)list[mid] < first) lo = mid + 1; else hi = mid;
+    }
+    ptr[b] = lo;
+}
+
 // the list of cells with a nonzero mask, in increasing index order (an
-// exclusive scan of the 0/1 flags gives each listed cell its position)
+// exclusive scan of the 0/1 flags gives each listed cell its position),
+// and each cell-grid block's range of it
 cudaError_t build_special_list(bf_solver* s, uint64_t n) {
     s->special.release();
+    s->special_ptr.release();
     s->n_special = 0;
     if (n == 0) return cudaSuccess;
     ScanLevels scan;
@@ -159,14 +174,21 @@ cudaError_t build_special_list(bf_solver* s, uint64_t n) {
         if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
     }
     scan.release();
-    if (e == cudaSuccess) s->n_special = count;
-    if (e == cudaSuccess && count > 0 && !s->side) {
-        int least = 0, greatest = 0;
-        e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
-        if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&s->side, cudaStreamNonBlocking, greatest);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming);
+    if (e == cudaSuccess && count > 0) {
+        // the step kernels' cell grid (cell_grid() in lbm_kernels.cuh)
+        const uint32_t nx = (uint32_t)s->desc.resolution[0];
+        const uint32_t block = nx >= (uint32_t)kStepBlock ? (uint32_t)kStepBlock : (nx + 31) / 32 * 32;
+        const uint32_t grid_x = (nx + block - 1) / block;
+        const uint32_t n_blocks = grid_x * (uint32_t)s->desc.resolution[1] * (uint32_t)s->desc.resolution[2];
+        e = s->special_ptr.alloc(((size_t)n_blocks + 1) * sizeof(uint32_t));
+        if (e == cudaSuccess) {
+            special_ptr_kernel<<<(unsigned)((n_blocks + 1 + 255) / 256), 256, 0, s->stream>>>(
+                s->special.as<uint32_t>(), count, n_blocks, grid_x, block, nx, s->special_ptr.as<uint32_t>());
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
     }
+    if (e == cudaSuccess) s->n_special = count;
     return e;
 }
 
@@ -180,7 +202,7 @@ void release_all(bf_solver* s) {
     DeviceBuf* bufs[] = {&s->lat[0], &s->lat[1], &s->bnd, &s->objs, &s->kinds, &s->force, &s->bvals,
                          &s->th[0], &s->th[1], &s->psi[0], &s->psi[1], &s->vel_den, &s->force_temp,
                          &s->bnd_tex, &s->partials, &s->red_out, &s->err, &s->decode_tmp, &s->nmask,
-                         &s->special};
+                         &s->special, &s->special_ptr};
     for (auto* b : bufs) b->release();
     s->n_special = 0;
     s->initialized = false;
@@ -193,32 +215,14 @@ float* th_tgt(bf_solver* s) { return s->th[s->th0_src ? 1 : 0].as<float>(); }
 float* psi_src(bf_solver* s) { return s->psi[s->psi0_src ? 0 : 1].as<float>(); }
 float* psi_tgt(bf_solver* s) { return s->psi[s->psi0_src ? 1 : 0].as<float>(); }
 
-cudaError_t launch_on(bf_solver* s, const StepParams& p, int mode, int path, cudaStream_t st) {
+cudaError_t dispatch_step(bf_solver* s, const StepParams& p, int mode, int path) {
     switch (s->Q) {
-    case 9: return launch_step<9>(p, s->desc.storage, mode, path, st);
-    case 15: return launch_step<15>(p, s->desc.storage, mode, path, st);
-    case 19: return launch_step<19>(p, s->desc.storage, mode, path, st);
-    case 27: return launch_step<27>(p, s->desc.storage, mode, path, st);
+    case 9: return launch_step<9>(p, s->desc.storage, mode, path, s->stream);
+    case 15: return launch_step<15>(p, s->desc.storage, mode, path, s->stream);
+    case 19: return launch_step<19>(p, s->desc.storage, mode, path, s->stream);
+    case 27: return launch_step<27>(p, s->desc.storage, mode, path, s->stream);
     }
     return cudaErrorInvalidValue;
-}
-
-cudaError_t dispatch_step(bf_solver* s, const StepParams& p, int mode, int path) {
-    // split boundary-aware step: the special cells (a partial wave of long
-    // threads) on the side stream while the main launch streams the rest;
-    // the two touch disjoint slots, and the join orders the next step after
-    // both (inside a captured graph this becomes a fork/join of two nodes)
-    if (path == PATH_MASKED && mode != AA_LOCAL && p.special && s->side &&
-        !(p.flags & (F_THERMAL | F_REDUCE))) {
-        cudaError_t e = cudaEventRecord(s->ev_fork, s->stream);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(s->side, s->ev_fork, 0);
-        if (e == cudaSuccess) e = launch_on(s, p, mode, PATH_MASKED_LIST, s->side);
-        if (e == cudaSuccess) e = cudaEventRecord(s->ev_join, s->side);
-        if (e == cudaSuccess) e = launch_on(s, p, mode, PATH_MASKED_MAIN, s->stream);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(s->stream, s->ev_join, 0);
-        return e;
-    }
-    return launch_on(s, p, mode, path, s->stream);
 }
 
 uint32_t base_flags(bf_solver* s) {
@@ -353,7 +357,7 @@ cudaError_t collide(bf_solver* s, bool save, bool update, bool reduce, bool meas
     p.nmask = s->nmask.as<uint32_t>();
     if (s->masked_split && s->n_special > 0) {
         p.special = s->special.as<uint32_t>();
-        p.n_special = s->n_special;
+        p.special_ptr = s->special_ptr.as<uint32_t>();
     }
     // the prefetch rounds each row range out to 16 bytes, which stays inside
     // the plane only when every plane starts and ends on a 16-byte boundary
@@ -598,12 +602,6 @@ int bf_destroy(bf_solver* s) {
     cudaSetDevice(s->device);
     cudaStreamSynchronize(s->stream);
     release_all(s);
-    if (s->side) {
-        cudaStreamSynchronize(s->side);
-        cudaStreamDestroy(s->side);
-        cudaEventDestroy(s->ev_fork);
-        cudaEventDestroy(s->ev_join);
-    }
     cudaStreamDestroy(s->stream);
     delete s;
     return BF_OK;

@@ -233,12 +233,14 @@ struct alignas(16) StepParams {
     // the domain, or a solid cell under bounce-back); bit 31 = the cell is
     // solid; bit 30 = the cell is an equilibrium-boundary cell
     const uint32_t* nmask;
-    // the cells whose mask is nonzero, in increasing index order: when set
-    // (n_special > 0 or special non-null), the boundary-aware step updates
-    // the other cells with the periodic kernel's cell update in one launch
-    // and these cells in a second one
+    // the cells whose mask is nonzero, in increasing index order, and per
+    // block of the cell grid (linear index b) its range of them,
+    // special[special_ptr[b] .. special_ptr[b + 1]): when set, the
+    // boundary-aware step updates the cells with an empty mask in the
+    // periodic kernel's cell update and the listed cells in blocks of their
+    // own (masked_mixed_kernel)
     const uint32_t* special;
-    uint32_t n_special;
+    const uint32_t* special_ptr;
     // fast kernel, even step, rows off the y/z faces: element offset of the
     // slot read for direction i relative to the cell, without its x part:
     // i * stride - (c_y nx + c_z nx ny), modulo 2^32
@@ -333,9 +335,7 @@ __device__ __forceinline__ uint32_t boundary_id(const uint32_t* __restrict__ bnd
 // launchers (one translation unit per Q instantiates them)
 // kernel choice of one step: the periodic fast kernel, the boundary-aware
 // (masked) fast kernel, or the generic kernel
-// PATH_MASKED_MAIN / PATH_MASKED_LIST: one of the two launches of the split
-// boundary-aware step (the caller puts them on two streams)
-enum StepPath { PATH_FAST = 0, PATH_MASKED = 1, PATH_GENERIC = 2, PATH_MASKED_MAIN = 3, PATH_MASKED_LIST = 4 };
+enum StepPath { PATH_FAST = 0, PATH_MASKED = 1, PATH_GENERIC = 2 };
 template <int Q> cudaError_t launch_step(const StepParams& p, int storage, int mode, int path, cudaStream_t st);
 template <int Q> cudaError_t launch_build_mask(const StepParams& p, uint32_t* mask, cudaStream_t st);
 template <int Q> cudaError_t launch_stream(const StreamParams& p, int storage, cudaStream_t st);

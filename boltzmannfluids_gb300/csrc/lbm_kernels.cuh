@@ -951,42 +951,60 @@ __global__ void __launch_bounds__(kStepBlock, Q == 27 ? 3 : kFastMinBlocks)
     if (p.flags & F_REDUCE) block_reduce_store(cs, p.red_partials);
 }
 
-// The boundary-aware step split in two launches (no reduction, no thermal
-// lattice).  In an AA step every slot is read and written by exactly one
-// cell, so cells are independent within a step and any partition of them
-// over launches gives the same result.  The first launch updates the cells
-// with an empty mask in the periodic kernel's cell update and leaves the
-// others; the second walks the list of the others, so that warps of the
-// first launch never wait for a lane on the special treatment (every row of
-// a channel with inlet and outlet faces starts and ends with such a cell).
-template <int Q, int ST, int MODE, bool TRT, bool FORCED>
-__global__ void __launch_bounds__(kStepBlock, kFastMinBlocks) masked_main_kernel(const __grid_constant__ StepParams p) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y, z = blockIdx.z;
-    if (x >= p.nx) return;
-    const uint32_t n = (uint32_t)x + (uint32_t)p.nx * ((uint32_t)y + (uint32_t)p.ny * (uint32_t)z);
-    if (__ldg(p.nmask + n) != 0u) return;
-    using T = typename Codec<ST>::T;
-    auto load = [&](int i, auto&& ptr_of) -> T { return *ptr_of(i); };
-    // rows on a y or z face (block-uniform) wrap their neighbour offsets;
-    // a cell there with an empty mask lies on a periodic face
-    const bool edge = MODE == AA_EVEN && (y == 0 || y == p.ny - 1 || (Lattice<Q>::D == 3 && (z == 0 || z == p.nz - 1)));
-    if (edge) fast_cell<Q, ST, MODE, TRT, FORCED, false, true>(p, x, y, z, load);
-    else fast_cell<Q, ST, MODE, TRT, FORCED, false, false>(p, x, y, z, load);
-    if ((p.flags & F_SAVE) && p.bnd_tex) p.bnd_tex[n] = 0;
-}
+// The boundary-aware step with the special cells taken out of the lanes (no
+// reduction, no thermal lattice).  In an AA step every slot is read and
+// written by exactly one cell, so the cells of a step are independent and any
+// partition of them over blocks gives the same result.  Plain blocks update
+// the cells whose mask is empty, in the periodic kernel's cell update, and
+// leave the others: their warps never wait for one lane's special treatment
+// (every row of a channel with inlet and outlet faces starts and ends with a
+// special cell).  After every kSpecialEvery plain blocks in launch order
+// comes one block that updates the listed special cells of those blocks'
+// rows.  Blocks are dispatched about in launch order, so the special cells
+// are updated right after their neighbours streamed the same 32-byte sectors
+// through L2, in blocks of their own; small groups keep those blocks short.
+// groups of 4 to 512 plain blocks measured 31.1k to 14.4k MLUPs on flow
+// past a sphere (256x128x128 D3Q19), best at 32 (33.3k)
+#ifndef BF_SPECIAL_EVERY
+#define BF_SPECIAL_EVERY 32
+#endif
+constexpr uint32_t kSpecialEvery = BF_SPECIAL_EVERY;
 
 template <int Q, int ST, int MODE, bool TRT, bool FORCED>
-__global__ void __launch_bounds__(kStepBlock, Q == 27 ? 3 : kFastMinBlocks) masked_list_kernel(const __grid_constant__ StepParams p) {
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= p.n_special) return;
-    const uint32_t n = __ldg(p.special + t);
-    const uint32_t nx = (uint32_t)p.nx, ny = (uint32_t)p.ny;
-    const int x = (int)(n % nx), y = (int)((n / nx) % ny), z = (int)(n / (nx * ny));
-    // the face-row variant computes every neighbour offset with its wrap,
-    // which is right for any cell
-    masked_cell<Q, ST, MODE, TRT, FORCED, false, true>(p, x, y, z, __ldg(p.nmask + n));
+__global__ void __launch_bounds__(kStepBlock, kFastMinBlocks) masked_mixed_kernel(const __grid_constant__ StepParams p) {
+    const uint32_t nx = (uint32_t)p.nx, ny = (uint32_t)p.ny, nz = (uint32_t)p.nz;
+    const uint32_t gx = (nx + blockDim.x - 1) / blockDim.x;
+    const uint32_t n_main = gx * ny * nz;
+    const uint32_t g = blockIdx.x / (kSpecialEvery + 1), r = blockIdx.x % (kSpecialEvery + 1);
+    if (r < kSpecialEvery) {
+        const uint32_t mb = g * kSpecialEvery + r;
+        if (mb >= n_main) return;
+        const uint32_t yz = mb / gx;
+        const int x = (int)((mb - yz * gx) * blockDim.x + threadIdx.x);
+        const int y = (int)(yz % ny), z = (int)(yz / ny);
+        if (x >= p.nx) return;
+        const uint32_t n = (uint32_t)x + nx * yz;
+        if (__ldg(p.nmask + n) != 0u) return;
+        using T = typename Codec<ST>::T;
+        auto load = [&](int i, auto&& ptr_of) -> T { return *ptr_of(i); };
+        const bool edge = MODE == AA_EVEN && (y == 0 || y == p.ny - 1 || (Lattice<Q>::D == 3 && (z == 0 || z == p.nz - 1)));
+        if (edge) fast_cell<Q, ST, MODE, TRT, FORCED, false, true>(p, x, y, z, load);
+        else fast_cell<Q, ST, MODE, TRT, FORCED, false, false>(p, x, y, z, load);
+        if ((p.flags & F_SAVE) && p.bnd_tex) p.bnd_tex[n] = 0;
+        return;
+    }
+    const uint32_t m0 = g * kSpecialEvery, m1 = min(m0 + kSpecialEvery, n_main);
+    const uint32_t hi = __ldg(p.special_ptr + m1);
+    for (uint32_t k = __ldg(p.special_ptr + m0) + threadIdx.x; k < hi; k += blockDim.x) {
+        const uint32_t n = __ldg(p.special + k);
+        const uint32_t yz = n / nx;
+        const int x = (int)(n - yz * nx), y = (int)(yz % ny), z = (int)(yz / ny);
+        // the face-row variant computes every neighbour offset with its wrap,
+        // which is right for any row
+        masked_cell<Q, ST, MODE, TRT, FORCED, false, true>(p, x, y, z, __ldg(p.nmask + n));
+    }
 }
+
 
 // ---------------------------------------------------------------------------
 // generic AA / two-buffer step: open boundaries, packed boundary ids, solid
@@ -1354,24 +1372,20 @@ cudaError_t launch_step_st(const StepParams& p, int mode, int path, cudaStream_t
     dim3 grid = cell_grid(p.nx, p.ny, p.nz, block);
     const bool generic = path != PATH_FAST;
     if constexpr (ST != ST_FP64) {
-        if ((path == PATH_MASKED || path == PATH_MASKED_MAIN || path == PATH_MASKED_LIST) && mode != AA_LOCAL) {
+        if (path == PATH_MASKED && mode != AA_LOCAL) {
             const bool trt = (p.flags & F_TRT) != 0, forced = (p.flags & F_FORCE_CONST) != 0;
             const bool thermal = (p.flags & F_THERMAL) != 0;
             if (p.special && !thermal && !(p.flags & F_REDUCE)) {
-                const unsigned lb = (unsigned)((p.n_special + kStepBlock - 1) / kStepBlock);
-                const bool main_part = path != PATH_MASKED_LIST, list_part = path != PATH_MASKED_MAIN;
-#define BF_SPLIT(MODE_, TRT_, F_)                                                                          \
-    do {                                                                                                   \
-        if (main_part) masked_main_kernel<Q, ST, MODE_, TRT_, F_><<<grid, block, 0, st>>>(p);              \
-        if (list_part && lb) masked_list_kernel<Q, ST, MODE_, TRT_, F_><<<lb, kStepBlock, 0, st>>>(p);     \
-    } while (0)
-#define BF_SPLIT_MODE(MODE_)                                                                 \
-    if (trt) { if (forced) BF_SPLIT(MODE_, true, true); else BF_SPLIT(MODE_, true, false); } \
-    else { if (forced) BF_SPLIT(MODE_, false, true); else BF_SPLIT(MODE_, false, false); }
-                if (mode == AA_EVEN) { BF_SPLIT_MODE(AA_EVEN) }
-                else { BF_SPLIT_MODE(AA_ODD) }
-#undef BF_SPLIT_MODE
-#undef BF_SPLIT
+                const uint32_t n_main = grid.x * grid.y * grid.z;
+                const unsigned total = (unsigned)(((n_main + kSpecialEvery - 1) / kSpecialEvery) * (kSpecialEvery + 1));
+#define BF_MIXED(MODE_, TRT_, F_) masked_mixed_kernel<Q, ST, MODE_, TRT_, F_><<<total, block, 0, st>>>(p)
+#define BF_MIXED_MODE(MODE_)                                                                 \
+    if (trt) { if (forced) BF_MIXED(MODE_, true, true); else BF_MIXED(MODE_, true, false); } \
+    else { if (forced) BF_MIXED(MODE_, false, true); else BF_MIXED(MODE_, false, false); }
+                if (mode == AA_EVEN) { BF_MIXED_MODE(AA_EVEN) }
+                else { BF_MIXED_MODE(AA_ODD) }
+#undef BF_MIXED_MODE
+#undef BF_MIXED
                 return cudaGetLastError();
             }
 #define BF_MASKED(MODE_, TRT_, F_, TH_) masked_step_kernel<Q, ST, MODE_, TRT_, F_, TH_><<<grid, block, 0, st>>>(p)

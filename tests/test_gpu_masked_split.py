@@ -1,7 +1,7 @@
 """The boundary-aware step with the special cells taken out of the lanes
 (cells with an empty mask in the periodic kernel's cell update, the listed
-special cells in a launch of their own) against the oracle, bit for bit, and
-against the single-pass masked kernel."""
+special cells in blocks of their own, interleaved in launch order) against
+the oracle, bit for bit, and against the single-pass masked kernel."""
 import numpy as np
 import pytest
 

@@ -335,6 +335,36 @@ def run_multiphysics_leg(bf, full=False):
         "nusselt": float(nu_num), "mass_rel_drift": float((m1 - m0) / m0),
         "mlups": round(rn * rsteps / (ms * 1e-3) / 1e6, 1)}
     del s
+    if not full:
+        out["throughput_full_size"] = multiphysics_throughput(bf)
+    return out
+
+
+def multiphysics_throughput(bf, steps=300):
+    """MLUPs of the multiphysics configuration's step at its own sizes
+    (Shan-Chen 256^3 in each storage, Rayleigh-Benard 256x256x130), a few
+    hundred timed steps each after the start-up steps."""
+    from boltzmannfluids_gb300.workloads import rayleigh_benard, spinodal
+    res = (256, 256, 256)
+    n = res[0] * res[1] * res[2]
+    out = {"steps_timed": steps}
+    rho = spinodal(res, 0.69, 0.01, 4)
+    for name in ("fp32", "fp16s", "fp16c"):
+        s = bf.LBM()
+        s.is_collide_esoteric = True
+        s.intermolecular_interaction_strength = -5.0
+        s.initialize_fields_from_arrays(res, 1.0, density=rho, velocity_set=bf.VelocitySet.D3Q19,
+                                        fp_accuracy=getattr(bf.FloatingPointAccuracy, name), is_flow_multiphase=True)
+        s.iterate_time(steps=4, save=False)
+        ms = s.benchmark_steps(steps)
+        out[f"shan_chen_256^3_{name}_mlups"] = round(n * steps / (ms * 1e-3) / 1e6, 1)
+        del s
+    rres = (256, 256, 130)
+    s, _, _ = rayleigh_benard(rres, kappa=0.02)
+    s.iterate_time(steps=4, save=False)
+    ms = s.benchmark_steps(steps)
+    out["rayleigh_benard_256x256x130_fp32_mlups"] = round(rres[0] * rres[1] * rres[2] * steps / (ms * 1e-3) / 1e6, 1)
+    del s
     return out
 
 

@@ -416,6 +416,9 @@ cudaError_t stream_thermal(bf_solver* s) {
     p.bnd = s->bnd.as<uint32_t>();
     p.objects = s->objs.as<float4>();
     p.obj_kind = s->kinds.as<uint8_t>();
+    // the flow masks mark solid sources under bounce-back only; the thermal
+    // stream treats every solid source (anti-bounce-back)
+    if (s->nmask.p && ((p.flags & F_BOUNCE_BACK) || !(p.flags & F_BOUNDARIES))) p.nmask = s->nmask.as<uint32_t>();
     cudaError_t e = s->QT == 5 ? launch_stream_thermal<5>(p, s->stream) : launch_stream_thermal<7>(p, s->stream);
     s->th0_src = !s->th0_src;
     return e;

@@ -95,6 +95,21 @@ template <> struct ThermalLattice<7> {
     __host__ __device__ static constexpr float w(int i) { return i == 0 ? float(1.0 / 4) : float(1.0 / 8); }
 };
 
+// the thermal set's directions are the velocity set's first QT directions,
+// in the same order, so a flow-lattice source mask also marks the thermal
+// lattice's special sources (bits 1 .. QT-1)
+template <int Q, int QT>
+constexpr bool thermal_dirs_lead() {
+    for (int i = 0; i < QT; i++) {
+        const Dir a = Lattice<Q>::c(i), b = ThermalLattice<QT>::c(i);
+        if (a.x != b.x || a.y != b.y || a.z != b.z) return false;
+    }
+    return true;
+}
+static_assert(thermal_dirs_lead<9, 5>() && thermal_dirs_lead<15, 7>() && thermal_dirs_lead<19, 7>() &&
+                  thermal_dirs_lead<27, 7>(),
+              "thermal directions must lead the velocity set");
+
 // weight of direction i in the arithmetic type R (float: the reference's
 // FP32 constants; double: the FP64 reference stepper)
 template <int Q, class R> struct LatticeW;
@@ -310,6 +325,10 @@ struct ThermalStreamParams {
     const uint32_t* bnd;
     const float4* objects;
     const uint8_t* obj_kind;
+    // the flow lattice's per-cell source masks (build_mask_kernel), set when
+    // they mark every special thermal source too (bounce-back mode, or no
+    // boundary ids); null: every cell looks its neighbours up
+    const uint32_t* nmask;
 };
 
 struct InitParams {

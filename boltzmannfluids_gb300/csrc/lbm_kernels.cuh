@@ -1228,7 +1228,24 @@ __global__ void __launch_bounds__(kStepBlock) stream_thermal_kernel(const __grid
     if (x >= p.nx) return;
     const uint64_t S = p.stride;
     const uint32_t n = (uint32_t)x + (uint32_t)p.nx * ((uint32_t)y + (uint32_t)p.ny * (uint32_t)z);
-    if (p.flags & F_BOUNDARIES) {
+    if (p.nmask) {
+        const uint32_t m = __ldg(p.nmask + n);
+        if (m >> 31) return;  // solid cell
+        if ((m & ((1u << QT) - 2u)) == 0u) {
+            // every source in the domain and fluid: the plain pull, no
+            // boundary lookups (periodic wrap only where the domain wraps)
+#pragma unroll
+            for (int i = 0; i < QT; i++) {
+                const Dir c = TL::c(i);
+                int sx = x - c.x, sy = y - c.y, sz = z - c.z;
+                bool open;
+                coords_wrap<QT>(sx, sy, sz, p.nx, p.ny, p.nz, open, p.flags);
+                const uint32_t sn = (uint32_t)sx + (uint32_t)p.nx * ((uint32_t)sy + (uint32_t)p.ny * (uint32_t)sz);
+                p.dst[(uint64_t)i * S + n] = __ldg(p.src + (uint64_t)i * S + sn);
+            }
+            return;
+        }
+    } else if (p.flags & F_BOUNDARIES) {
         if (solid_id(p.obj_kind, boundary_id(p.bnd, p.bits, n))) return;
     }
 #pragma unroll

@@ -155,10 +155,13 @@ def test_trt_collision():
     step_and_compare(s, o, [1, 2, 30])
 
 
+@pytest.mark.parametrize("bb", [0, 1])
 @pytest.mark.parametrize("q", [9, 19])
-def test_thermal_lattice(q):
+def test_thermal_lattice(q, bb):
     """Thermal D2Q5/D3Q7 lattice with Dirichlet walls (stream_thermal.comp)
-    and Boussinesq buoyancy; both the as-read zero start and the equilibrium start."""
+    and Boussinesq buoyancy; both the as-read zero start and the equilibrium
+    start; walls skipped as read (bb 0) or under bounce-back (bb 1, where the
+    thermal stream takes its sources from the flow lattice's masks)."""
     res = (32, 24, 1) if q == 9 else (16, 14, 10)
     nx, ny, nz = res
     ids = np.zeros((nz, ny, nx), np.uint32)
@@ -170,7 +173,7 @@ def test_thermal_lattice(q):
     fluid = ids.reshape(-1) == 0
     for eq in (False, True):
         s, o = make_pair(res, 0.6, VS[q], ids=ids, objects=objs, force=f, periodic=(True, False, True),
-                         thermal_init_equilibrium=eq, tau_t=0.8, beta=0.5)
+                         thermal_init_equilibrium=eq, tau_t=0.8, beta=0.5, boundary_mode=bb)
         assert s.get_is_flow_thermal()
         step_and_compare(s, o, [1, 2, 25, 80], mask=fluid, check_temperature=True)
 

@@ -248,14 +248,16 @@ struct alignas(16) StepParams {
     // the domain, or a solid cell under bounce-back); bit 31 = the cell is
     // solid; bit 30 = the cell is an equilibrium-boundary cell
     const uint32_t* nmask;
-    // the cells whose mask is nonzero, in increasing index order, and per
-    // block of the cell grid (linear index b) its range of them,
-    // special[special_ptr[b] .. special_ptr[b + 1]): when set, the
-    // boundary-aware step updates the cells with an empty mask in the
-    // periodic kernel's cell update and the listed cells in blocks of their
-    // own (masked_mixed_kernel)
+    // the cells whose mask is nonzero, in increasing index order
+    // (n_special), and a launch schedule (n_sched entries, one per block of
+    // masked_mixed_kernel): entry e < 2^31 is block e of the cell grid,
+    // which updates its cells with an empty mask in the periodic kernel's
+    // cell update; entry 2^31 + k updates the listed cells
+    // special[k * special_chunk ..] (special_chunk of them, one per thread).
+    // When set, the boundary-aware step runs this way.
     const uint32_t* special;
-    const uint32_t* special_ptr;
+    const uint32_t* sched;
+    uint32_t n_special, n_sched, special_chunk;
     // fast kernel, even step, rows off the y/z faces: element offset of the
     // slot read for direction i relative to the cell, without its x part:
     // i * stride - (c_y nx + c_z nx ny), modulo 2^32

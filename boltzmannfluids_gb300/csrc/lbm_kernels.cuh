@@ -470,7 +470,44 @@ constexpr int kFastMinBlocks16 = BF_FAST_MIN_BLOCKS_16;
 // load(i, ptr_of) returns the stored element of direction i; ptr_of(k) is
 // the address of the slot read for direction k (the plain kernel loads
 // *ptr_of(i), the staged kernel reads shared memory and never calls it)
-template <int Q, int ST, int MODE, bool TRT, bool FORCED, bool MP, bool EDGE, class Load>
+// Boussinesq buoyancy of the thermal lattice (collide.comp:709-716): the
+// temperature T = sum of the cell's thermal populations scales the force by
+// 1 - beta (T - 1); returns T
+template <int Q>
+__device__ __forceinline__ float thermal_buoyancy(const StepParams& p, uint32_t n, Moments& m) {
+    constexpr int QT = Lattice<Q>::D == 2 ? 5 : 7;
+    float temperature = 0.f;
+#pragma unroll
+    for (int i = 0; i < QT; i++) temperature = FADD(temperature, __ldg(p.th_src + (uint64_t)i * p.stride + n));
+    const float k = FMUL(-p.beta, FSUB(temperature, 1.0f));
+    m.Fx = FFMA(k, m.Fx, m.Fx); m.Fy = FFMA(k, m.Fy, m.Fy); m.Fz = FFMA(k, m.Fz, m.Fz);
+    return temperature;
+}
+
+// thermal BGK towards g_eq(T, u) (collide.comp:771-782)
+template <int Q>
+__device__ __forceinline__ void thermal_collide(const StepParams& p, uint32_t n, const Moments& m, float temperature) {
+    constexpr int QT = Lattice<Q>::D == 2 ? 5 : 7;
+    const float one_m = FSUB(1.0f, FMUL(uu_of(m.ux, m.uy, m.uz), p.R2h));
+#pragma unroll
+    for (int i = 0; i < QT; i++) {
+        const Dir c = ThermalLattice<QT>::c(i);
+        const float w = ThermalLattice<QT>::w(i);
+        const float cu = cdot_rt(c, m.ux, m.uy, m.uz);
+        const float geq = FMUL(FMUL(w, temperature), bracket(cu, one_m, p.R2, p.R4h));
+        const float g = __ldg(p.th_src + (uint64_t)i * p.stride + n);
+        p.th_tgt[(uint64_t)i * p.stride + n] = FFMA(FSUB(geq, g), p.Rtau_t, g);
+    }
+}
+
+// THERMAL (FP32 and 16-bit storage; FORCED set with it): the buoyancy and
+// the thermal collision of the boundary-aware kernel, for cells whose
+// sources are all plain.  GUARD: the cell's mask is loaded beside its
+// populations and a cell with a nonzero mask stops after the loads (the
+// periodic addresses stay inside the lattice), so that the mask costs no
+// round trip of its own; returns whether the cell was updated.
+template <int Q, int ST, int MODE, bool TRT, bool FORCED, bool MP, bool EDGE, bool THERMAL = false,
+          bool GUARD = false, class Load>
 __device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepParams& p, int x, int y, int z,
                                                                      Load&& load) {
     using L = Lattice<Q>;
@@ -538,9 +575,11 @@ __device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepP
     asm volatile("" : "+r"(n_st), "+r"(oxm_st), "+r"(oxp_st));
     auto ptr_st = [&](int k) -> T* { return base + slot(k, n_st, oxm_st, oxp_st); };
 #endif
+    const uint32_t guard_mask = GUARD ? __ldg(p.nmask + n) : 0u;
     R f[Q];
 #pragma unroll
     for (int i = 0; i < Q; i++) f[i] = C::dec(load(i, ptr_of), W::w(i));
+    if (GUARD && guard_mask != 0u) return cs;
     MomentsT<R> m;
     m.rho = density_of<Q>(f);
     if (C::SHIFTED) m.rho = FADD(R(1), m.rho);  // sum of g plus sum of w
@@ -569,6 +608,11 @@ __device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepP
         const float k = FMUL(-self_psi, p.G);
         m.Fx = FFMA(sx, k, m.Fx); m.Fy = FFMA(sy, k, m.Fy); m.Fz = FFMA(sz, k, m.Fz);
     }
+    float temperature = 0.f;
+    if constexpr (THERMAL && !F64) {
+        static_assert(FORCED, "thermal flow runs with the source term on");
+        temperature = thermal_buoyancy<Q>(p, n, m);
+    }
     if constexpr (F64) velocity_and_limit<Q>(f, m, FORCED, p.k64.vlim, p.k64.vlim_ext);
     else velocity_and_limit<Q>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
     if (p.flags & F_UPDATE) {
@@ -581,9 +625,12 @@ __device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepP
         // psi of this step's density for the next step (collide.comp:763-769)
         if (!(p.flags & F_MEASURE)) p.psi_tgt[n] = FSUB(1.0f, exp_f32(-m.rho));
     }
+    if constexpr (THERMAL && !F64) {
+        if (!(p.flags & F_MEASURE)) thermal_collide<Q>(p, n, m, temperature);
+    }
     if (p.flags & F_SAVE) {
         p.vel_den[n] = make_float4((float)m.ux, (float)m.uy, (float)m.uz, (float)m.rho);
-        if (p.force_temp) p.force_temp[n] = make_float4((float)m.Fx, (float)m.Fy, (float)m.Fz, 0.f);
+        if (p.force_temp) p.force_temp[n] = make_float4((float)m.Fx, (float)m.Fy, (float)m.Fz, temperature);
     }
     if (p.flags & F_REDUCE) {
         const R uu = uu_of(m.ux, m.uy, m.uz);
@@ -864,14 +911,8 @@ __device__ __forceinline__ CellSum masked_cell(const StepParams& p, int x, int y
     m.Fx = FORCED ? p.fconst[0] : 0.f;
     m.Fy = FORCED ? p.fconst[1] : 0.f;
     m.Fz = FORCED ? p.fconst[2] : 0.f;
-    constexpr int QT = L::D == 2 ? 5 : 7;
     float temperature = 0.f;
-    if (THERMAL) {  // Boussinesq buoyancy of the generic kernel (collide.comp:709-716)
-#pragma unroll
-        for (int i = 0; i < QT; i++) temperature = FADD(temperature, __ldg(p.th_src + (uint64_t)i * p.stride + n));
-        const float k = FMUL(-p.beta, FSUB(temperature, 1.0f));
-        m.Fx = FFMA(k, m.Fx, m.Fx); m.Fy = FFMA(k, m.Fy, m.Fy); m.Fz = FFMA(k, m.Fz, m.Fz);
-    }
+    if (THERMAL) temperature = thermal_buoyancy<Q>(p, n, m);  // the generic kernel's buoyancy
     // thermal flow is forced with the source term on, as in the generic kernel
     constexpr bool FRC = FORCED || THERMAL;
     velocity_and_limit<Q>(f, m, FRC, p.vlim, p.t_lim, p.t_ext);
@@ -897,18 +938,7 @@ __device__ __forceinline__ CellSum masked_cell(const StepParams& p, int x, int y
         else if (m.out_ext) collide_fixed<Q, TRT, FRC, true, C::SHIFTED>(f, m, k, emit);
         else collide_fixed<Q, TRT, FRC, false, C::SHIFTED>(f, m, k, emit);
     }
-    if (THERMAL && !(flags & F_MEASURE)) {  // thermal BGK (collide.comp:771-782)
-        const float one_m = FSUB(1.0f, FMUL(uu_of(m.ux, m.uy, m.uz), p.R2h));
-#pragma unroll
-        for (int i = 0; i < QT; i++) {
-            const Dir c = ThermalLattice<QT>::c(i);
-            const float w = ThermalLattice<QT>::w(i);
-            const float cu = cdot_rt(c, m.ux, m.uy, m.uz);
-            const float geq = FMUL(FMUL(w, temperature), bracket(cu, one_m, p.R2, p.R4h));
-            const float g = __ldg(p.th_src + (uint64_t)i * p.stride + n);
-            p.th_tgt[(uint64_t)i * p.stride + n] = FFMA(FSUB(geq, g), p.Rtau_t, g);
-        }
-    }
+    if (THERMAL && !(flags & F_MEASURE)) thermal_collide<Q>(p, n, m, temperature);
     if (flags & F_SAVE) {
         p.vel_den[n] = make_float4(m.ux, m.uy, m.uz, m.rho);
         p.force_temp[n] = make_float4(m.Fx, m.Fy, m.Fz, temperature);
@@ -952,56 +982,49 @@ __global__ void __launch_bounds__(kStepBlock, Q == 27 ? 3 : kFastMinBlocks)
 }
 
 // The boundary-aware step with the special cells taken out of the lanes (no
-// reduction, no thermal lattice).  In an AA step every slot is read and
-// written by exactly one cell, so the cells of a step are independent and any
-// partition of them over blocks gives the same result.  Plain blocks update
-// the cells whose mask is empty, in the periodic kernel's cell update, and
-// leave the others: their warps never wait for one lane's special treatment
-// (every row of a channel with inlet and outlet faces starts and ends with a
-// special cell).  After every kSpecialEvery plain blocks in launch order
-// comes one block that updates the listed special cells of those blocks'
-// rows.  Blocks are dispatched about in launch order, so the special cells
-// are updated right after their neighbours streamed the same 32-byte sectors
-// through L2, in blocks of their own; small groups keep those blocks short.
-// groups of 4 to 512 plain blocks measured 31.1k to 14.4k MLUPs on flow
-// past a sphere (256x128x128 D3Q19), best at 32 (33.3k)
-#ifndef BF_SPECIAL_EVERY
-#define BF_SPECIAL_EVERY 32
-#endif
-constexpr uint32_t kSpecialEvery = BF_SPECIAL_EVERY;
-
-template <int Q, int ST, int MODE, bool TRT, bool FORCED>
+// reduction).  In an AA step every slot is read and written by exactly one
+// cell, so the cells of a step are independent and any partition of them
+// over blocks gives the same result.  Plain blocks update the cells whose
+// mask is empty, in the periodic kernel's cell update, and leave the others:
+// their warps never wait for one lane's special treatment (every row of a
+// channel with inlet and outlet faces starts and ends with a special cell).
+// Blocks of special_chunk listed cells follow in launch order as soon as the
+// plain blocks of their rows have been launched (the host's schedule).
+// Blocks are dispatched about in launch order, so the special cells are
+// updated right after their neighbours streamed the same 32-byte sectors
+// through L2, in short blocks of their own, however dense they lie (a wall
+// plane is a run of special blocks).
+template <int Q, int ST, int MODE, bool TRT, bool FORCED, bool THERMAL>
 __global__ void __launch_bounds__(kStepBlock, kFastMinBlocks) masked_mixed_kernel(const __grid_constant__ StepParams p) {
-    const uint32_t nx = (uint32_t)p.nx, ny = (uint32_t)p.ny, nz = (uint32_t)p.nz;
-    const uint32_t gx = (nx + blockDim.x - 1) / blockDim.x;
-    const uint32_t n_main = gx * ny * nz;
-    const uint32_t g = blockIdx.x / (kSpecialEvery + 1), r = blockIdx.x % (kSpecialEvery + 1);
-    if (r < kSpecialEvery) {
-        const uint32_t mb = g * kSpecialEvery + r;
-        if (mb >= n_main) return;
+    const uint32_t nx = (uint32_t)p.nx, ny = (uint32_t)p.ny;
+    const uint32_t e = __ldg(p.sched + blockIdx.x);
+    if (!(e >> 31)) {
+        const uint32_t gx = (nx + blockDim.x - 1) / blockDim.x;
+        const uint32_t mb = e;
         const uint32_t yz = mb / gx;
         const int x = (int)((mb - yz * gx) * blockDim.x + threadIdx.x);
         const int y = (int)(yz % ny), z = (int)(yz / ny);
         if (x >= p.nx) return;
-        const uint32_t n = (uint32_t)x + nx * yz;
-        if (__ldg(p.nmask + n) != 0u) return;
         using T = typename Codec<ST>::T;
         auto load = [&](int i, auto&& ptr_of) -> T { return *ptr_of(i); };
         const bool edge = MODE == AA_EVEN && (y == 0 || y == p.ny - 1 || (Lattice<Q>::D == 3 && (z == 0 || z == p.nz - 1)));
-        if (edge) fast_cell<Q, ST, MODE, TRT, FORCED, false, true>(p, x, y, z, load);
-        else fast_cell<Q, ST, MODE, TRT, FORCED, false, false>(p, x, y, z, load);
-        if ((p.flags & F_SAVE) && p.bnd_tex) p.bnd_tex[n] = 0;
+        if (edge) fast_cell<Q, ST, MODE, TRT, FORCED, false, true, THERMAL, true>(p, x, y, z, load);
+        else fast_cell<Q, ST, MODE, TRT, FORCED, false, false, THERMAL, true>(p, x, y, z, load);
+        if ((p.flags & F_SAVE) && p.bnd_tex) {
+            const uint32_t n = (uint32_t)x + nx * yz;
+            if (__ldg(p.nmask + n) == 0u) p.bnd_tex[n] = 0;
+        }
         return;
     }
-    const uint32_t m0 = g * kSpecialEvery, m1 = min(m0 + kSpecialEvery, n_main);
-    const uint32_t hi = __ldg(p.special_ptr + m1);
-    for (uint32_t k = __ldg(p.special_ptr + m0) + threadIdx.x; k < hi; k += blockDim.x) {
+    if (threadIdx.x < p.special_chunk) {
+        const uint32_t k = (e & 0x7fffffffu) * p.special_chunk + threadIdx.x;
+        if (k >= p.n_special) return;
         const uint32_t n = __ldg(p.special + k);
         const uint32_t yz = n / nx;
         const int x = (int)(n - yz * nx), y = (int)(yz % ny), z = (int)(yz / ny);
         // the face-row variant computes every neighbour offset with its wrap,
         // which is right for any row
-        masked_cell<Q, ST, MODE, TRT, FORCED, false, true>(p, x, y, z, __ldg(p.nmask + n));
+        masked_cell<Q, ST, MODE, TRT, FORCED, THERMAL, true>(p, x, y, z, __ldg(p.nmask + n));
     }
 }
 
@@ -1392,13 +1415,13 @@ cudaError_t launch_step_st(const StepParams& p, int mode, int path, cudaStream_t
         if (path == PATH_MASKED && mode != AA_LOCAL) {
             const bool trt = (p.flags & F_TRT) != 0, forced = (p.flags & F_FORCE_CONST) != 0;
             const bool thermal = (p.flags & F_THERMAL) != 0;
-            if (p.special && !thermal && !(p.flags & F_REDUCE)) {
-                const uint32_t n_main = grid.x * grid.y * grid.z;
-                const unsigned total = (unsigned)(((n_main + kSpecialEvery - 1) / kSpecialEvery) * (kSpecialEvery + 1));
-#define BF_MIXED(MODE_, TRT_, F_) masked_mixed_kernel<Q, ST, MODE_, TRT_, F_><<<total, block, 0, st>>>(p)
-#define BF_MIXED_MODE(MODE_)                                                                 \
-    if (trt) { if (forced) BF_MIXED(MODE_, true, true); else BF_MIXED(MODE_, true, false); } \
-    else { if (forced) BF_MIXED(MODE_, false, true); else BF_MIXED(MODE_, false, false); }
+            if (p.special && p.sched && !(p.flags & F_REDUCE)) {
+                const unsigned total = p.n_sched;
+#define BF_MIXED(MODE_, TRT_, F_, TH_) masked_mixed_kernel<Q, ST, MODE_, TRT_, F_, TH_><<<total, block, 0, st>>>(p)
+#define BF_MIXED_MODE(MODE_)                                                                                          \
+    if (thermal) { if (trt) BF_MIXED(MODE_, true, true, true); else BF_MIXED(MODE_, false, true, true); }              \
+    else if (trt) { if (forced) BF_MIXED(MODE_, true, true, false); else BF_MIXED(MODE_, true, false, false); }       \
+    else { if (forced) BF_MIXED(MODE_, false, true, false); else BF_MIXED(MODE_, false, false, false); }
                 if (mode == AA_EVEN) { BF_MIXED_MODE(AA_EVEN) }
                 else { BF_MIXED_MODE(AA_ODD) }
 #undef BF_MIXED_MODE

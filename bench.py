@@ -34,6 +34,11 @@ sys.path.insert(0, ROOT)
 RES = (512, 512, 512)
 TAU = 0.55
 BYTES_PER_CELL = {0: 152, 2: 76, 3: 76}  # algorithmic: 19 reads + 19 writes (periodic box, no flag field)
+# DRAM bytes (read + write) per launch of fast_step_kernel<19, fp32, *, TRT> on
+# the 512^3 box, from one single-pass ncu capture of dram__bytes_read.sum and
+# dram__bytes_write.sum (odd 20.465e9, even 20.515e9; algorithmic 20.401e9):
+# profiles/fast_step_kernel_d3q19_512_traffic.md
+TRAFFIC_512_FP32 = 20.49e9
 METRIC = "D3Q19 MLUPs, % HBM peak: FP32 vs FP16-storage @ stated err; adjoint ms/grad"
 
 
@@ -485,7 +490,9 @@ def run_gpu(args):
                              f"DDF vs 129 MB L2), no flush",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                         "frac": round(achieved / peak, 4), "traffic": None,
+                         "frac": round(achieved / peak, 4),
+                         "traffic": (TRAFFIC_512_FP32 if args.size == 512 and args.storage == "fp32" else None),
+                         "traffic_unit": "DRAM bytes per launch (ncu capture of this workload)",
                          "peak_kind": peak_kind, "bytes_per_cell": BYTES_PER_CELL[int(main_st)]},
             "storage_sweep": sweep,
             "conservation_fp64": {"mass": red[0], "momentum": list(red[1:4]), "kinetic_energy": red[4]},

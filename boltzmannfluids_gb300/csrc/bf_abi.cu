@@ -43,6 +43,12 @@ constexpr int kGraphSteps = 16;   // steps per captured graph (even: the AA stat
 struct DeviceBuf {
     void* p = nullptr;
     size_t bytes = 0;
+    DeviceBuf() = default;
+    DeviceBuf(const DeviceBuf&) = delete;
+    DeviceBuf& operator=(const DeviceBuf&) = delete;
+    // a buffer is freed when it goes out of scope (staging buffers of an
+    // initialisation; the solver releases its own explicitly as well)
+    ~DeviceBuf() { release(); }
     cudaError_t alloc(size_t n) {
         release();
         if (n == 0) return cudaSuccess;
@@ -114,9 +120,38 @@ struct bf_solver {
     bool masked_step = true; // boundary-aware fast step for objects and open faces
     bool two_cell = true;    // 16-bit fast step with two cells per thread
     bool masked_split = true; // boundary-aware step with the special cells in blocks of their own
+    bool zero_copy = true;    // kernels read/write pinned host buffers directly (initial velocity, field read-back)
 };
 
 namespace {
+
+// device address of a page-locked, mapped host buffer (cudaHostAlloc or
+// cudaHostRegister, as torch's pin_memory does), or null for any other
+// pointer: kernels read and write such buffers directly over the CPU-GPU link
+const void* mapped_host_ptr(const void* p) {
+    cudaPointerAttributes at{};
+    if (!p || cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
+// 16-byte copy between device memory and a mapped host buffer
+__global__ void copy16_kernel(const uint4* __restrict__ src, uint4* __restrict__ dst, uint64_t n16) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += (uint64_t)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+
+__global__ void ids_to_bytes_kernel(const uint32_t* __restrict__ ids, uint32_t n, uint8_t* __restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (uint8_t)ids[i];
+}
+
+__global__ void fill_f32_kernel(float* __restrict__ p, uint32_t n, float v) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = v;
+}
 
 __global__ void special_flags_kernel(const uint32_t* __restrict__ mask, uint64_t n, uint32_t* __restrict__ flag) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -634,6 +669,8 @@ int bf_create(bf_solver** out) {
     // BF_MASKED_STEP=0 sends objects and open faces to the generic kernel (A/B comparisons)
     if (const char* env = std::getenv("BF_MASKED_STEP")) s->masked_step = std::strtoul(env, nullptr, 10) != 0;
     if (const char* env = std::getenv("BF_MASKED_SPLIT")) s->masked_split = std::strtoul(env, nullptr, 10) != 0;
+    // BF_ZERO_COPY=0: stage pinned host buffers through cudaMemcpy like any other (A/B comparisons)
+    if (const char* env = std::getenv("BF_ZERO_COPY")) s->zero_copy = std::strtoul(env, nullptr, 10) != 0;
     // BF_TMA_STEP=1 selects the staged 16-bit fast step, 0 the plain one
     if (const char* env = std::getenv("BF_TMA_STEP")) s->tma_step = std::strtoul(env, nullptr, 10) != 0;
     *out = s;
@@ -705,9 +742,17 @@ int bf_initialize_fields(bf_solver* s, const bf_init_desc* d, const float* densi
     fluid.temperature = 1.0f; fluid.effective_density = 1.0f;
     if (s->objects.empty()) s->objects.resize(1);
     s->objects[0] = fluid;
-    // LBM.cpp:523-556 -- one host pass over the lambda results
+    // LBM.cpp:523-556 -- host passes over the given arrays only (an absent
+    // array is the reference's default value everywhere)
     uint32_t maxid = 0;
-    if (ids) for (uint32_t c = 0; c < N; c++) maxid = std::max(maxid, ids[c]);
+    std::vector<uint8_t> id_present(256, 0);
+    if (ids) {
+        for (uint32_t c = 0; c < N; c++) {
+            const uint32_t v = ids[c];
+            maxid = std::max(maxid, v);
+            if (v < 256u) id_present[v] = 1;
+        }
+    }
     if (maxid > 255) return fail(BF_ERR_INVALID_ARGUMENT, "initialize_fields(): boundry ids above 255");
     if (maxid + 1 > s->objects.size()) {
         bf_object def{};
@@ -719,13 +764,23 @@ int bf_initialize_fields(bf_solver* s, const bf_init_desc* d, const float* densi
     s->fconst[0] = force ? force[0] : 0.f; s->fconst[1] = force ? force[1] : 0.f; s->fconst[2] = force ? force[2] : 0.f;
     s->thermal = false;
     const float T0 = temperature ? temperature[0] : 1.0f;
-    for (uint32_t c = 0; c < N; c++) {
-        if (force && (force[3 * (uint64_t)c] != s->fconst[0] || force[3 * (uint64_t)c + 1] != s->fconst[1] || force[3 * (uint64_t)c + 2] != s->fconst[2]))
-            s->constant_force = false;
-        if (temperature && temperature[c] != T0) s->thermal = true;
-        const uint32_t id = ids ? ids[c] : 0u;
-        if (id != 0 && s->objects[id].temperature != T0) s->thermal = true;
+    if (force) {
+        for (uint32_t c = 0; c < N; c++) {
+            if (force[3 * (uint64_t)c] != s->fconst[0] || force[3 * (uint64_t)c + 1] != s->fconst[1] ||
+                force[3 * (uint64_t)c + 2] != s->fconst[2]) {
+                s->constant_force = false;
+                break;
+            }
+        }
     }
+    if (temperature) {
+        for (uint32_t c = 0; c < N; c++) {
+            if (temperature[c] != T0) { s->thermal = true; break; }
+        }
+    }
+    // a cell whose object's temperature differs from the first cell's
+    for (uint32_t id = 1; id < 256u && id < s->objects.size(); id++)
+        if (id_present[id] && s->objects[id].temperature != T0) s->thermal = true;
     s->forcing = !(s->constant_force && s->fconst[0] == 0.f && s->fconst[1] == 0.f && s->fconst[2] == 0.f);
     s->boundaries = nobj > 1;
     s->bits = bits_per_boundry(nobj);
@@ -756,37 +811,51 @@ int bf_initialize_fields(bf_solver* s, const bf_init_desc* d, const float* densi
     BF_CUDA(s->kinds.alloc(kinds_h.size()));
     BF_CUDA(cudaMemcpy(s->objs.p, objs_h.data(), objs_h.size() * sizeof(float4), cudaMemcpyHostToDevice));
     BF_CUDA(cudaMemcpy(s->kinds.p, kinds_h.data(), kinds_h.size(), cudaMemcpyHostToDevice));
-    std::vector<uint8_t> tex_h(N, 0);
     if (s->boundaries) {
         s->bnd_words = ((uint64_t)N * s->bits + 31) / 32;
         std::vector<uint32_t> words(s->bnd_words + 1, 0u);
         if (ids) {
             size_t nw = 0;
             bf_pack_boundries(ids, N, s->bits, words.data(), words.size(), &nw);
-            for (uint64_t c = 0; c < N; c++) tex_h[c] = (uint8_t)ids[c];
         }
         BF_CUDA(s->bnd.alloc(words.size() * 4));
         BF_CUDA(cudaMemcpy(s->bnd.p, words.data(), words.size() * 4, cudaMemcpyHostToDevice));
     } else {
         s->bnd_words = 0;
     }
-    BF_CUDA(s->bnd_tex.alloc(N));
-    BF_CUDA(cudaMemcpy(s->bnd_tex.p, tex_h.data(), N, cudaMemcpyHostToDevice));
 
-    // host staging of the lambda results
+    // the given arrays on the device; an absent density or velocity is the
+    // init kernel's default (1, 0), so nothing is staged for it
     DeviceBuf d_rho, d_u, d_ids;
-    BF_CUDA(d_rho.alloc((size_t)N * 4));
-    BF_CUDA(d_u.alloc((size_t)N * 12));
-    {
-        std::vector<float> tmp;
-        if (density) BF_CUDA(cudaMemcpy(d_rho.p, density, (size_t)N * 4, cudaMemcpyHostToDevice));
-        else { tmp.assign(N, 1.0f); BF_CUDA(cudaMemcpy(d_rho.p, tmp.data(), (size_t)N * 4, cudaMemcpyHostToDevice)); }
-        if (velocity) BF_CUDA(cudaMemcpy(d_u.p, velocity, (size_t)N * 12, cudaMemcpyHostToDevice));
-        else BF_CUDA(cudaMemset(d_u.p, 0, (size_t)N * 12));
+    // a pinned density / velocity array is read by the init kernel in place
+    const float* rho_in = nullptr;
+    const float* u_in = nullptr;
+    if (density) {
+        rho_in = s->zero_copy ? static_cast<const float*>(mapped_host_ptr(density)) : nullptr;
+        if (!rho_in) {
+            BF_CUDA(d_rho.alloc((size_t)N * 4));
+            BF_CUDA(cudaMemcpy(d_rho.p, density, (size_t)N * 4, cudaMemcpyHostToDevice));
+            rho_in = d_rho.as<float>();
+        }
     }
+    if (velocity) {
+        u_in = s->zero_copy ? static_cast<const float*>(mapped_host_ptr(velocity)) : nullptr;
+        if (!u_in) {
+            BF_CUDA(d_u.alloc((size_t)N * 12));
+            BF_CUDA(cudaMemcpy(d_u.p, velocity, (size_t)N * 12, cudaMemcpyHostToDevice));
+            u_in = d_u.as<float>();
+        }
+    }
+    // the boundary-id field (LBM.cpp:957-1003): the ids as bytes
+    BF_CUDA(s->bnd_tex.alloc(N));
     if (ids) {
         BF_CUDA(d_ids.alloc((size_t)N * 4));
         BF_CUDA(cudaMemcpy(d_ids.p, ids, (size_t)N * 4, cudaMemcpyHostToDevice));
+        ids_to_bytes_kernel<<<(unsigned)((N + 255u) / 256u), 256, 0, s->stream>>>(d_ids.as<uint32_t>(), N,
+                                                                                 s->bnd_tex.as<uint8_t>());
+        BF_CUDA(cudaGetLastError());
+    } else {
+        BF_CUDA(cudaMemsetAsync(s->bnd_tex.p, 0, N, s->stream));
     }
     // force field (LBM.cpp:693-717), vec4 per cell
     if (s->forcing && !s->constant_force) {
@@ -830,8 +899,8 @@ int bf_initialize_fields(bf_solver* s, const bf_init_desc* d, const float* densi
     ip.f = s->lat[0].p;
     ip.stride = N;
     ip.n_cells = N;
-    ip.rho = d_rho.as<float>();
-    ip.u = d_u.as<float>();
+    ip.rho = rho_in;
+    ip.u = u_in;
     ip.ids = d_ids.as<uint32_t>();
     ip.obj_kind = s->kinds.as<uint8_t>();
     cudaError_t e;
@@ -850,9 +919,12 @@ int bf_initialize_fields(bf_solver* s, const bf_init_desc* d, const float* densi
         if (d->thermal_init_equilibrium) {
             DeviceBuf d_Tb;
             BF_CUDA(d_Tb.alloc((size_t)N * 4));
-            std::vector<float> tmp;
-            if (temperature) BF_CUDA(cudaMemcpy(d_Tb.p, temperature, (size_t)N * 4, cudaMemcpyHostToDevice));
-            else { tmp.assign(N, 1.0f); BF_CUDA(cudaMemcpy(d_Tb.p, tmp.data(), (size_t)N * 4, cudaMemcpyHostToDevice)); }
+            if (temperature) {
+                BF_CUDA(cudaMemcpy(d_Tb.p, temperature, (size_t)N * 4, cudaMemcpyHostToDevice));
+            } else {
+                fill_f32_kernel<<<(unsigned)((N + 255u) / 256u), 256, 0, s->stream>>>(d_Tb.as<float>(), N, 1.0f);
+                BF_CUDA(cudaGetLastError());
+            }
             InitParams tp = ip;
             tp.th = th_src(s);
             tp.T = d_Tb.as<float>();
@@ -1043,7 +1115,24 @@ int bf_copy_field_to_host(bf_solver* s, int32_t kind, void* dst, size_t bytes) {
     int r = bf_get_field(s, kind, &f);
     if (r != BF_OK) return r;
     if (bytes < f.bytes) return fail(BF_ERR_INVALID_ARGUMENT, "copy_field_to_host(): destination too small");
-    BF_CUDA(cudaMemcpyAsync(dst, f.device_ptr, f.bytes, cudaMemcpyDeviceToHost, s->stream));
+    // a pinned destination is written by a copy kernel (several times the
+    // copy engine's rate over the CPU-GPU link); any other by cudaMemcpy
+    void* mapped = s->zero_copy ? const_cast<void*>(mapped_host_ptr(dst)) : nullptr;
+    const size_t n16 = f.bytes / 16;
+    if (mapped && reinterpret_cast<uintptr_t>(mapped) % 16 == 0 && reinterpret_cast<uintptr_t>(f.device_ptr) % 16 == 0 &&
+        n16 > 0) {
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
+        const uint64_t blocks = std::min<uint64_t>((n16 + 255) / 256, (uint64_t)std::max(sms, 1) * 8);
+        copy16_kernel<<<(unsigned)blocks, 256, 0, s->stream>>>(static_cast<const uint4*>(f.device_ptr),
+                                                              static_cast<uint4*>(mapped), n16);
+        BF_CUDA(cudaGetLastError());
+        if (f.bytes % 16)
+            BF_CUDA(cudaMemcpyAsync(static_cast<char*>(dst) + n16 * 16, static_cast<const char*>(f.device_ptr) + n16 * 16,
+                                    f.bytes % 16, cudaMemcpyDeviceToHost, s->stream));
+    } else {
+        BF_CUDA(cudaMemcpyAsync(dst, f.device_ptr, f.bytes, cudaMemcpyDeviceToHost, s->stream));
+    }
     BF_CUDA(cudaStreamSynchronize(s->stream));
     return BF_OK;
 }

@@ -174,7 +174,10 @@ int bf_clear_boundry_properties(bf_solver* s);
  *   boundry_id[N] (NULL: all 0)
  * Derives the forcing/constant-force/thermal switches and the packed boundary
  * bits exactly as LBM.cpp:523-569, uploads, writes equilibrium populations
- * and runs the reference's save-only first pass (LBM.cpp:502). */
+ * and runs the reference's save-only first pass (LBM.cpp:502).  A density or
+ * velocity array in page-locked memory (cudaHostAlloc / cudaHostRegister) is
+ * read in place by the initialisation kernel; others are copied first.  The
+ * arrays are not used after the call returns. */
 int bf_initialize_fields(bf_solver* s, const bf_init_desc* desc,
                          const float* density, const float* velocity, const float* force,
                          const float* temperature, const uint32_t* boundry_id);
@@ -209,7 +212,9 @@ int bf_get_scheme_flags(bf_solver* s, int32_t* flags, int32_t* bits_per_boundry)
 /* ---- field readback (LBM.h:97-99, LBM.cpp:1444-1457) -------------------- */
 /* device pointer + shape of a field; valid until the next bf_initialize_fields/bf_destroy */
 int bf_get_field(bf_solver* s, int32_t kind, bf_field* out);
-/* copies a field to host memory (bytes must be at least the field's size) */
+/* copies a field to host memory (bytes must be at least the field's size);
+ * a 16-byte aligned page-locked destination is written by a copy kernel over
+ * the CPU-GPU link, any other by cudaMemcpy; returns when the copy is done */
 int bf_copy_field_to_host(bf_solver* s, int32_t kind, void* dst, size_t bytes);
 /* packed boundary words as built by LBM.cpp:634-659 (count in *words) */
 int bf_copy_boundry_bits_to_host(bf_solver* s, uint32_t* dst, size_t capacity_words, size_t* words);

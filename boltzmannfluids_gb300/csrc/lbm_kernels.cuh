@@ -738,7 +738,10 @@ __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, i
     };
     auto to16 = [](uint32_t v) -> T { const unsigned short u = (unsigned short)v; T t; memcpy(&t, &u, 2); return t; };
     auto bits16 = [](T t) -> uint32_t { unsigned short u; memcpy(&u, &t, 2); return u; };
-    uint32_t keep[Q];  // cell a's encoded populations of the paired directions
+    // cell a's populations of the paired directions until cell b's are known:
+    // encoded (fp16c), or as floats that one cvt.rn.f16x2.f32 converts
+    // together with cell b's (fp16s; the same rounding as two conversions)
+    uint32_t keep[Q];
     const Coef<float> k = coef_of(p, 0.0f);
 #pragma unroll
     for (int half = 0; half < 2; half++) {
@@ -755,8 +758,21 @@ __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, i
         m.Fz = FORCED ? p.fconst[2] : 0.f;
         velocity_and_limit<Q>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
         auto emit = [&](int i, float v) {
-            const uint32_t e = bits16(C::enc(v, L::w(i)));
             const int o = opp(i);
+            if constexpr (ST == ST_FP16S) {
+                if (paired(o)) {
+                    if (half == 0) {
+                        keep[i] = __float_as_uint(v);
+                    } else {
+                        const __half2 h = __floats2half2_rn(__uint_as_float(keep[i]), v);
+                        uint32_t w2;
+                        memcpy(&w2, &h, 4);
+                        *reinterpret_cast<unsigned int*>(dst_a(i)) = w2;
+                    }
+                    return;
+                }
+            }
+            const uint32_t e = bits16(C::enc(v, L::w(i)));
             if (paired(o)) {
                 if (half == 0) keep[i] = e;
                 else *reinterpret_cast<unsigned int*>(dst_a(i)) = keep[i] | (e << 16);

@@ -437,7 +437,7 @@ cudaError_t collide(bf_solver* s, bool save, bool update, bool reduce, bool meas
     // the prefetch rounds each row range out to 16 bytes, which stays inside
     // the plane only when every plane starts and ends on a 16-byte boundary
     const size_t plane_bytes = (size_t)s->N * storage_bytes(s->desc.storage);
-    if (!generic && plane_bytes % 16 == 0 && reinterpret_cast<uintptr_t>(lat_src(s)) % 16 == 0)
+    if ((!generic || p.sched) && plane_bytes % 16 == 0 && reinterpret_cast<uintptr_t>(lat_src(s)) % 16 == 0)
         p.pf_blocks = s->pf_blocks;
     p.tma = s->tma_step ? 1u : 0u;
     p.two_cell = s->two_cell ? 1u : 0u;

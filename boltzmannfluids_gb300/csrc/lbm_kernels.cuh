@@ -415,10 +415,10 @@ __host__ __device__ constexpr uint64_t packed_axis(int axis) {
 // inside the plane because planes start and end on 16-byte boundaries
 // whenever pf_blocks is set.  Planes lie `stride` elements apart.
 template <int Q, int ST, int MODE>
-__device__ __forceinline__ void prefetch_block_rows(const StepParams& p, uint32_t b, int lane, int tile) {
+__device__ __forceinline__ void prefetch_block_rows(const StepParams& p, uint32_t b, int lane, int tile,
+                                                    uint32_t gx = gridDim.x, uint32_t gy = gridDim.y) {
     using T = typename Codec<ST>::T;
     if (lane >= Q) return;
-    const uint32_t gx = gridDim.x, gy = gridDim.y;
     const uint32_t bx = b % gx, yz = b / gx;
     int ys = (int)(yz % gy), zs = (int)(yz / gy);
     const int nx = p.nx, ny = p.ny, nz = p.nz;
@@ -1016,6 +1016,12 @@ __global__ void __launch_bounds__(kStepBlock, kFastMinBlocks) masked_mixed_kerne
     const uint32_t e = __ldg(p.sched + blockIdx.x);
     if (!(e >> 31)) {
         const uint32_t gx = (nx + blockDim.x - 1) / blockDim.x;
+        // the first warp prefetches the rows of the plain block pf_blocks
+        // entries ahead in the schedule (one plane per lane)
+        if (p.pf_blocks != 0u && threadIdx.x < 32 && blockIdx.x + p.pf_blocks < p.n_sched) {
+            const uint32_t ahead = __ldg(p.sched + blockIdx.x + p.pf_blocks);
+            if (!(ahead >> 31)) prefetch_block_rows<Q, ST, MODE>(p, ahead, (int)threadIdx.x, (int)blockDim.x, gx, ny);
+        }
         const uint32_t mb = e;
         const uint32_t yz = mb / gx;
         const int x = (int)((mb - yz * gx) * blockDim.x + threadIdx.x);

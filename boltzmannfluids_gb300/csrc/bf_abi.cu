@@ -116,6 +116,7 @@ struct bf_solver {
     std::map<int, cudaGraphExec_t> graphs;
     bool graphs_enabled = true;
     uint32_t pf_blocks = 0;  // L2 prefetch distance of the fast kernel, in blocks (0 = off)
+    uint32_t pf_blocks_masked = 0;  // the same for the boundary-aware step, in schedule entries
     bool tma_step = false;   // 16-bit fast step with loads staged by bulk copies
     bool masked_step = true; // boundary-aware fast step for objects and open faces
     bool two_cell = true;    // 16-bit fast step with two cells per thread
@@ -438,7 +439,7 @@ cudaError_t collide(bf_solver* s, bool save, bool update, bool reduce, bool meas
     // the plane only when every plane starts and ends on a 16-byte boundary
     const size_t plane_bytes = (size_t)s->N * storage_bytes(s->desc.storage);
     if ((!generic || p.sched) && plane_bytes % 16 == 0 && reinterpret_cast<uintptr_t>(lat_src(s)) % 16 == 0)
-        p.pf_blocks = s->pf_blocks;
+        p.pf_blocks = generic ? s->pf_blocks_masked : s->pf_blocks;
     p.tma = s->tma_step ? 1u : 0u;
     p.two_cell = s->two_cell ? 1u : 0u;
     switch (s->Q) {
@@ -663,7 +664,11 @@ int bf_create(bf_solver** out) {
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
     s->pf_blocks = (uint32_t)std::max(sms, 1) * 4u;
-    if (const char* env = std::getenv("BF_PREFETCH_BLOCKS")) s->pf_blocks = (uint32_t)std::strtoul(env, nullptr, 10);
+    // the boundary-aware step: half a wave (flow past a sphere 256x128x128:
+    // 0.5 / 1 / 1.5 / 2 waves measured 35.1k / 34.8k / 34.3k / 33.6k MLUPs)
+    s->pf_blocks_masked = (uint32_t)std::max(sms, 1) * 2u;
+    if (const char* env = std::getenv("BF_PREFETCH_BLOCKS"))
+        s->pf_blocks = s->pf_blocks_masked = (uint32_t)std::strtoul(env, nullptr, 10);
     // BF_TWO_CELL=0 keeps the 16-bit fast step at one cell per thread (A/B comparisons)
     if (const char* env = std::getenv("BF_TWO_CELL")) s->two_cell = std::strtoul(env, nullptr, 10) != 0;
     // BF_MASKED_STEP=0 sends objects and open faces to the generic kernel (A/B comparisons)

@@ -468,7 +468,9 @@ def run_gpu(args):
     if not args.no_precision:
         prec = run_precision_leg(bf, args.precision_size, args.precision_steps)
     multi = None
-    if not args.no_multiphysics:
+    if args.multiphysics_throughput_steps:
+        multi = {"throughput_full_size": multiphysics_throughput(bf, args.multiphysics_throughput_steps)}
+    elif not args.no_multiphysics:
         multi = run_multiphysics_leg(bf, args.multiphysics_full)
     sphere = None
     if not args.no_sphere:
@@ -530,6 +532,8 @@ def main():
     ap.add_argument("--precision-steps", type=int, default=2000)
     ap.add_argument("--no-multiphysics", action="store_true", help="skip the Shan-Chen / Rayleigh-Benard leg")
     ap.add_argument("--multiphysics-full", action="store_true", help="run the multiphysics configurations at full size")
+    ap.add_argument("--multiphysics-throughput-steps", type=int, default=0,
+                    help="instead of the multiphysics leg, only its full-size throughput part with this many timed steps")
     ap.add_argument("--no-sphere", action="store_true", help="skip the flow-past-a-sphere leg")
     ap.add_argument("--sphere-steps", type=int, default=1000, help="timed steps of the flow-past-a-sphere leg")
     args = ap.parse_args()

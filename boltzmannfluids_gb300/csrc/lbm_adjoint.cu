@@ -22,13 +22,14 @@
 // FP64 (per-cell terms are summed in FP32 first).  The forward trajectory is
 // checkpointed every K steps; the forward leaves the last segment's states in
 // a segment buffer and every earlier segment is recomputed from its
-// checkpoint.  Two segment buffers alternate: the recomputation of segment
-// k-1 runs on a second stream while the adjoint sweep of segment k runs on
-// the first (both are captured into one graph with event edges), so the
-// recomputation is hidden behind the sweep as far as the GPU has room.
+// checkpoint.  Two segment buffers alternate: while the adjoint sweeps
+// segment k, segment k-1 is recomputed into the other buffer, each adjoint
+// step sharing one launch with one recomputation step, so the recomputation
+// runs beside the latency-bound sweep.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -57,6 +58,21 @@ struct AdjParams {
     double* grad_out;       // ny*nz, from the x = nx-1 cells
     double* partials;       // one per block (objective)
 };
+
+// c . u for a lattice vector (components -1, 0, 1): only the nonzero terms
+__device__ __forceinline__ float lattice_dot(const Dir c, float ux, float uy, float uz) {
+    float r = 0.f;
+    bool any = false;
+    if (c.x) { r = c.x > 0 ? ux : -ux; any = true; }
+    if (c.y) { r = any ? (c.y > 0 ? r + uy : r - uy) : (c.y > 0 ? uy : -uy); any = true; }
+    if (c.z) { r = any ? (c.z > 0 ? r + uz : r - uz) : (c.z > 0 ? uz : -uz); }
+    return r;
+}
+// acc += c v for a lattice component c in {-1, 0, 1}
+__device__ __forceinline__ void lattice_axpy(int c, float v, float& acc) {
+    if (c > 0) acc += v;
+    else if (c < 0) acc -= v;
+}
 
 template <int Q>
 __device__ __forceinline__ float feq_plain(int i, float rho, float ux, float uy, float uz) {
@@ -126,11 +142,10 @@ __global__ void __launch_bounds__(kAdjBlock) adj_init_kernel(AdjParams p) {
 }
 
 template <int Q, bool FINAL>
-__global__ void __launch_bounds__(kAdjBlock) adj_forward_kernel(AdjParams p) {
+__device__ __forceinline__ double adj_forward_cell(const AdjParams& p, int x, int y, int z) {
     using L = Lattice<Q>;
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
     double contrib = 0.0;
-    if (x < p.nx) {
+    {
         const uint32_t n = adj_cell(p, x, y, z);
         float g[Q];
         adj_pull<Q>(p, x, y, z, n, g);
@@ -157,14 +172,19 @@ __global__ void __launch_bounds__(kAdjBlock) adj_forward_kernel(AdjParams p) {
             }
         }
     }
+    return contrib;
+}
+
+template <int Q, bool FINAL>
+__global__ void __launch_bounds__(kAdjBlock) adj_forward_kernel(AdjParams p) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
+    const double contrib = x < p.nx ? adj_forward_cell<Q, FINAL>(p, x, y, z) : 0.0;
     if (FINAL) block_sum_store(contrib, p.partials);
 }
 
 template <int Q, bool FINAL>
-__global__ void __launch_bounds__(kAdjBlock) adj_backward_kernel(AdjParams p) {
+__device__ __forceinline__ void adj_backward_cell(const AdjParams& p, int x, int y, int z) {
     using L = Lattice<Q>;
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
-    if (x >= p.nx) return;
     const uint32_t n = adj_cell(p, x, y, z);
     // every load of the step is issued before any arithmetic, so the step
     // waits on memory once: the pulled state, the incoming adjoint, the
@@ -199,33 +219,54 @@ __global__ void __launch_bounds__(kAdjBlock) adj_backward_kernel(AdjParams p) {
         }
         gs = (double)p.wd * 2.0 * (double)jx;
     } else {
+        // The lattice components are -1, 0 or 1 and known per unrolled
+        // direction: terms with a zero component are left out and the others
+        // added or subtracted (IEEE arithmetic does not let the compiler drop
+        // x * 0 or x + 0 itself).  With B_k = 1 + 3 cu_k + 4.5 cu_k^2 - 1.5 uu
+        // (shared by A0 and the equilibrium) and L_k = (1 - s) lam_k w_k:
+        //   A0 = sum_k L_k B_k,  V = sum_k L_k (3 + 9 cu_k) c_k - 3 u sum_k L_k.
         const float om = p.omega, oms = 1.0f - s;
-        const float uu = ux * ux + uy * uy + uz * uz;
-        float A0 = 0.f, Vx = 0.f, Vy = 0.f, Vz = 0.f, gsf = 0.f;
+        const float base = 1.0f - 1.5f * (ux * ux + uy * uy + uz * uz);
+        float A0 = 0.f, Lsum = 0.f, Vx = 0.f, Vy = 0.f, Vz = 0.f, gsf = 0.f;
 #pragma unroll
         for (int k = 0; k < Q; k++) {
             const Dir c = L::c(k);
-            const float w = L::w(k);
-            const float cu = c.x * ux + c.y * uy + c.z * uz;
-            const float Lk = oms * lam[k] * w;
-            A0 += Lk * (1.0f + 3.0f * cu + 4.5f * cu * cu - 1.5f * uu);
-            const float t9 = 9.0f * cu;
-            Vx += Lk * (3.0f * c.x + t9 * c.x - 3.0f * ux);
-            Vy += Lk * (3.0f * c.y + t9 * c.y - 3.0f * uy);
-            Vz += Lk * (3.0f * c.z + t9 * c.z - 3.0f * uz);
-            const float gck = g[k] + (feq_plain<Q>(k, rho, ux, uy, uz) - g[k]) * om;
+            const float cu = lattice_dot(c, ux, uy, uz);
+            const float Bk = fmaf(fmaf(4.5f, cu, 3.0f), cu, base);
+            const float Lk = oms * lam[k] * L::w(k);
+            A0 = fmaf(Lk, Bk, A0);
+            Lsum += Lk;
+            const float q = Lk * fmaf(9.0f, cu, 3.0f);
+            lattice_axpy(c.x, q, Vx); lattice_axpy(c.y, q, Vy); lattice_axpy(c.z, q, Vz);
+            const float feq = L::w(k) * rho * Bk;
+            const float gck = g[k] + (feq - g[k]) * om;
             gsf += lam[k] * (g[opp(k)] - gck);
         }
+        Vx = fmaf(-3.0f * ux, Lsum, Vx); Vy = fmaf(-3.0f * uy, Lsum, Vy); Vz = fmaf(-3.0f * uz, Lsum, Vz);
         gs = (double)gsf;  // per-cell sum in FP32, accumulated over steps in FP64
+        // mu_i = (1 - om)(1 - s) lam_i + om (A0 + (c_i - u).V) + s lam_opp(i)
+        const float a1 = (1.0f - om) * oms, a0 = om * (A0 - (ux * Vx + uy * Vy + uz * Vz));
 #pragma unroll
         for (int i = 0; i < Q; i++) {
             const Dir c = L::c(i);
-            const float dot = (c.x - ux) * Vx + (c.y - uy) * Vy + (c.z - uz) * Vz;
-            mu[i] = (1.0f - om) * oms * lam[i] + om * (A0 + dot) + s * lam[opp(i)];
+            float cv = 0.f;
+            lattice_axpy(c.x, Vx, cv); lattice_axpy(c.y, Vy, cv); lattice_axpy(c.z, Vz, cv);
+            mu[i] = fmaf(a1, lam[i], fmaf(om, cv, a0)) + s * lam[opp(i)];
         }
     }
     p.grad_s[n] = gs_prev + gs;
-    // transpose of the pull
+    // transpose of the pull; cells off the walls and the inlet/outlet layers
+    // push every adjoint population to an interior neighbour (z periodic)
+    if (x > 0 && x < p.nx - 1 && y > 0 && y < p.ny - 1) {
+        const int zm = z == 0 ? p.nz - 1 : z - 1, zp = z == p.nz - 1 ? 0 : z + 1;
+#pragma unroll
+        for (int i = 0; i < Q; i++) {
+            const Dir c = L::c(i);
+            const int Z = c.z > 0 ? zm : (c.z < 0 ? zp : z);
+            p.lam_out[(uint64_t)i * p.n + adj_cell(p, x - c.x, y - c.y, Z)] = mu[i];
+        }
+        return;
+    }
     const float ui = p.uin[(uint32_t)z * p.ny + y];
     float guf = 0.f;
     bool eq_source = false;
@@ -249,6 +290,30 @@ __global__ void __launch_bounds__(kAdjBlock) adj_backward_kernel(AdjParams p) {
         if (x == 0) p.grad_in[row] += (double)guf;
         else p.grad_out[row] += (double)guf;
     }
+}
+
+// D2Q9: 48 registers, 5 blocks per SM (the 512x256 channel's backward
+// measured 13.3 ms against 16.0 ms at 64 registers); D3Q19 keeps its
+// registers (at 48 it spills over 120 bytes)
+template <int Q>
+constexpr int adj_min_blocks() { return Q == 9 ? 5 : 1; }
+
+template <int Q, bool FINAL>
+__global__ void __launch_bounds__(kAdjBlock, adj_min_blocks<Q>()) adj_backward_kernel(AdjParams p) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
+    if (x < p.nx) adj_backward_cell<Q, FINAL>(p, x, y, z);
+}
+
+// One adjoint step (blocks z < nz, first in launch order: the longer of the
+// two) and one step of the recomputation of the previous segment (blocks
+// z >= nz) in one launch.  The two read and write disjoint buffers, so their
+// blocks run side by side; stream order keeps each chain in sequence.
+template <int Q>
+__global__ void __launch_bounds__(kAdjBlock, adj_min_blocks<Q>()) adj_sweep_recompute_kernel(AdjParams pb, AdjParams pf) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
+    if (x >= pb.nx) return;
+    if (z < pb.nz) adj_backward_cell<Q, false>(pb, x, y, z);
+    else adj_forward_cell<Q, false>(pf, x, y, z - pb.nz);
 }
 
 // d f^0 / d u_in: grad[row] += sum_x sum_i lam^0_i(x) dfeq_i/du, one block per (y, z) row
@@ -296,8 +361,7 @@ struct bf_adjoint {
     int Q = 0;
     uint32_t n = 0, rows = 0, nblocks = 0;
     int nseg = 0;
-    cudaStream_t stream = nullptr, side = nullptr;
-    std::vector<cudaEvent_t> events;  // fork, join, then per segment: recomputed, swept
+    cudaStream_t stream = nullptr;
     std::vector<void*> allocs;
     float *s = nullptr, *uin = nullptr, *ustar = nullptr;
     std::vector<float*> ckpt, seg[2];
@@ -374,52 +438,44 @@ cudaError_t enqueue_backward(bf_adjoint* a) {
     cudaMemsetAsync(a->grad_s, 0, (size_t)a->n * sizeof(double), a->stream);
     cudaMemsetAsync(a->grad_in, 0, (size_t)a->rows * sizeof(double), a->stream);
     cudaMemsetAsync(a->grad_out, 0, (size_t)a->rows * sizeof(double), a->stream);
-    cudaEvent_t ev_fork = a->events[0], ev_join = a->events[1];
-    auto ev_recomputed = [&](int k) { return a->events[2 + 2 * k]; };
-    auto ev_swept = [&](int k) { return a->events[3 + 2 * k]; };
-    // recompute f^(t0+1) .. f^(t1-1) of segment k into its buffer, on the side stream
-    auto recompute = [&](int k) {
-        const int t0 = k * K, t1 = std::min(t0 + K, T);
-        AdjParams q = p;
-        const float* prev = a->ckpt[k];
-        for (int j = 1; j <= t1 - 1 - t0; j++) {
-            q.f_prev = prev;
-            q.f_next = a->seg[k & 1][j];
-            adj_forward_kernel<Q, false><<<grid, block, 0, a->side>>>(q);
-            prev = q.f_next;
-        }
-        cudaEventRecord(ev_recomputed(k), a->side);
-    };
-    cudaEventRecord(ev_fork, a->stream);
-    cudaStreamWaitEvent(a->side, ev_fork, 0);
-    if (nseg >= 2) recompute(nseg - 2);  // the forward left segment nseg-1 in place
-    int cur_lam = -1;  // index of the buffer holding the adjoint of f^t
+    // one stream: adjoint step i of segment k together with step i + 1
+    // of the recomputation of segment k - 1 (into the other segment
+    // buffer, which the sweep of segment k + 1 has finished with)
+    const dim3 grid2(grid.x, grid.y, grid.z * 2);
+    int cur = -1;
     for (int k = nseg - 1; k >= 0; k--) {
         const int t0 = k * K, t1 = std::min(t0 + K, T);
-        if (k != nseg - 1) cudaStreamWaitEvent(a->stream, ev_recomputed(k), 0);
+        const int r = k - 1;  // segment being recomputed, if any
+        const int r_steps = r >= 0 ? K - 1 : 0;
+        AdjParams q = p;
+        const float* rprev = r >= 0 ? a->ckpt[r] : nullptr;
+        int j = 1;  // next recomputation step, f^(r K + j)
         for (int t = t1; t >= t0 + 1; t--) {
             p.f_prev = (t - 1 == t0) ? a->ckpt[k] : a->seg[k & 1][t - 1 - t0];
-            const int out = cur_lam == 0 ? 1 : 0;
+            const int out = cur == 0 ? 1 : 0;
             p.lam_out = a->lam[out];
-            if (t == T) {
-                p.lam_in = nullptr;
+            p.lam_in = t == T ? nullptr : a->lam[cur];
+            if (t != T && j <= r_steps) {
+                q.f_prev = rprev;
+                q.f_next = a->seg[r & 1][j];
+                adj_sweep_recompute_kernel<Q><<<grid2, block, 0, a->stream>>>(p, q);
+                rprev = q.f_next;
+                j++;
+            } else if (t == T) {
                 adj_backward_kernel<Q, true><<<grid, block, 0, a->stream>>>(p);
             } else {
-                p.lam_in = a->lam[cur_lam];
                 adj_backward_kernel<Q, false><<<grid, block, 0, a->stream>>>(p);
             }
-            cur_lam = out;
+            cur = out;
         }
-        cudaEventRecord(ev_swept(k), a->stream);
-        // segment k-2 reuses this segment's buffer once its sweep is done
-        if (k - 2 >= 0) {
-            cudaStreamWaitEvent(a->side, ev_swept(k), 0);
-            recompute(k - 2);
+        for (; j <= r_steps; j++) {  // a short last segment leaves recomputation steps over
+            q.f_prev = rprev;
+            q.f_next = a->seg[r & 1][j];
+            adj_forward_kernel<Q, false><<<grid, block, 0, a->stream>>>(q);
+            rprev = q.f_next;
         }
     }
-    cudaEventRecord(ev_join, a->side);
-    cudaStreamWaitEvent(a->stream, ev_join, 0);
-    p.lam_in = a->lam[cur_lam];
+    p.lam_in = a->lam[cur];
     adj_init_grad_kernel<Q><<<dim3((unsigned)a->d.resolution[1], (unsigned)a->d.resolution[2]), kAdjBlock, 0, a->stream>>>(p);
     return cudaGetLastError();
 }
@@ -466,8 +522,6 @@ int bf_adjoint_destroy(bf_adjoint* a) {
     if (a->fwd_graph) cudaGraphExecDestroy(a->fwd_graph);
     if (a->bwd_graph) cudaGraphExecDestroy(a->bwd_graph);
     for (void* p : a->allocs) cudaFree(p);
-    for (cudaEvent_t ev : a->events) if (ev) cudaEventDestroy(ev);
-    if (a->side) cudaStreamDestroy(a->side);
     if (a->stream) cudaStreamDestroy(a->stream);
     delete a;
     return BF_OK;
@@ -516,14 +570,10 @@ int bf_adjoint_create(bf_adjoint** out, const bf_adjoint_desc* d) {
     if (e == cudaSuccess) e = alloc((size_t)a->n * 12, (void**)&a->ustar);
     a->ckpt.assign(a->nseg, nullptr);
     for (int k = 0; k < a->nseg && e == cudaSuccess; k++) e = alloc(state, (void**)&a->ckpt[k]);
-    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&a->side, cudaStreamNonBlocking, prio_low);
     for (int b = 0; b < (a->nseg >= 2 ? 2 : 1); b++) {
         a->seg[b].assign(d->checkpoint_interval, nullptr);
         for (int j = 1; j < d->checkpoint_interval && e == cudaSuccess; j++) e = alloc(state, (void**)&a->seg[b][j]);
     }
-    a->events.assign(2 + 2 * (size_t)a->nseg, nullptr);
-    for (size_t k = 0; k < a->events.size() && e == cudaSuccess; k++)
-        e = cudaEventCreateWithFlags(&a->events[k], cudaEventDisableTiming);
     for (int k = 0; k < 2 && e == cudaSuccess; k++) e = alloc(state, (void**)&a->pp[k]);
     for (int k = 0; k < 2 && e == cudaSuccess; k++) e = alloc(state, (void**)&a->lam[k]);
     if (e == cudaSuccess) e = alloc((size_t)a->n * 8, (void**)&a->grad_s);

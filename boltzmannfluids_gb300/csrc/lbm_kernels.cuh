@@ -470,6 +470,30 @@ constexpr int kFastMinBlocks16 = BF_FAST_MIN_BLOCKS_16;
 // load(i, ptr_of) returns the stored element of direction i; ptr_of(k) is
 // the address of the slot read for direction k (the plain kernel loads
 // *ptr_of(i), the staged kernel reads shared memory and never calls it)
+// Shan-Chen pseudopotential force (collide.comp:534-584) with the generic
+// kernel's arithmetic: psi of the previous step at the periodic neighbours
+// x + c_i (offsets ox*/oy*/oz* from cell n to x -+ 1, y -+ 1, z -+ 1),
+// summed as w_i psi c_i in direction order, times -G psi(rho) of the cell
+template <int Q>
+__device__ __forceinline__ void sc_force(const StepParams& p, uint32_t n, int oxm, int oxp, int oym, int oyp, int ozm,
+                                         int ozp, Moments& m) {
+    using L = Lattice<Q>;
+    const float self_psi = FSUB(1.0f, exp_f32(-m.rho));
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+#pragma unroll
+    for (int i = 1; i < Q; i++) {
+        const Dir c = L::c(i);
+        const uint32_t a = n + (uint32_t)((c.x > 0 ? oxp : (c.x < 0 ? oxm : 0)) + (c.y > 0 ? oyp : (c.y < 0 ? oym : 0)) +
+                                          (c.z > 0 ? ozp : (c.z < 0 ? ozm : 0)));
+        const float wp = FMUL(L::w(i), __ldg(p.psi_src + a));
+        if (c.x) sx = FADD(sx, c.x > 0 ? wp : -wp);
+        if (c.y) sy = FADD(sy, c.y > 0 ? wp : -wp);
+        if (c.z) sz = FADD(sz, c.z > 0 ? wp : -wp);
+    }
+    const float k = FMUL(-self_psi, p.G);
+    m.Fx = FFMA(sx, k, m.Fx); m.Fy = FFMA(sy, k, m.Fy); m.Fz = FFMA(sz, k, m.Fz);
+}
+
 // Boussinesq buoyancy of the thermal lattice (collide.comp:709-716): the
 // temperature T = sum of the cell's thermal populations scales the force by
 // 1 - beta (T - 1); returns T
@@ -589,25 +613,7 @@ __device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepP
     m.Fx = FORCED ? (F64 ? R(p.k64.fconst[0]) : R(p.fconst[0])) : R(0);
     m.Fy = FORCED ? (F64 ? R(p.k64.fconst[1]) : R(p.fconst[1])) : R(0);
     m.Fz = FORCED ? (F64 ? R(p.k64.fconst[2]) : R(p.fconst[2])) : R(0);
-    if constexpr (MP && !F64) {
-        // Shan-Chen pseudopotential force (collide.comp:534-584), the generic
-        // kernel's arithmetic: psi of the previous step at the periodic
-        // neighbours x + c_i, summed as w_i psi c_i in direction order
-        const float self_psi = FSUB(1.0f, exp_f32(-m.rho));
-        float sx = 0.f, sy = 0.f, sz = 0.f;
-#pragma unroll
-        for (int i = 1; i < Q; i++) {
-            const Dir c = L::c(i);
-            const uint32_t a = n + (uint32_t)((c.x > 0 ? oxp : (c.x < 0 ? oxm : 0)) + (c.y > 0 ? oyp : (c.y < 0 ? oym : 0)) +
-                                              (c.z > 0 ? ozp : (c.z < 0 ? ozm : 0)));
-            const float wp = FMUL(L::w(i), __ldg(p.psi_src + a));
-            if (c.x) sx = FADD(sx, c.x > 0 ? wp : -wp);
-            if (c.y) sy = FADD(sy, c.y > 0 ? wp : -wp);
-            if (c.z) sz = FADD(sz, c.z > 0 ? wp : -wp);
-        }
-        const float k = FMUL(-self_psi, p.G);
-        m.Fx = FFMA(sx, k, m.Fx); m.Fy = FFMA(sy, k, m.Fy); m.Fz = FFMA(sz, k, m.Fz);
-    }
+    if constexpr (MP && !F64) sc_force<Q>(p, n, oxm, oxp, oym, oyp, ozm, ozp, m);
     float temperature = 0.f;
     if constexpr (THERMAL && !F64) {
         static_assert(FORCED, "thermal flow runs with the source term on");
@@ -672,7 +678,7 @@ __global__ void __launch_bounds__(kStepBlock,
 // two 16-bit values through one address.  The arithmetic of each cell is the
 // one-cell kernel's (fast_cell), so results agree bit for bit.
 // ---------------------------------------------------------------------------
-template <int Q, int ST, int MODE, bool TRT, bool FORCED, bool EDGE>
+template <int Q, int ST, int MODE, bool TRT, bool FORCED, bool MP, bool EDGE>
 __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, int z) {
     using L = Lattice<Q>;
     using C = Codec<ST>;
@@ -756,6 +762,13 @@ __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, i
         m.Fx = FORCED ? p.fconst[0] : 0.f;
         m.Fy = FORCED ? p.fconst[1] : 0.f;
         m.Fz = FORCED ? p.fconst[2] : 0.f;
+        if constexpr (MP) {
+            // x neighbours of cell x (half 0) and x + 1 (half 1): only x - 1
+            // of the first and x + 2 of the second can wrap (x even, nx even)
+            const int oxm = half ? -1 : (x == 0 ? nx - 1 : -1);
+            const int oxp = half ? (x + 2 == nx ? 1 - nx : 1) : 1;
+            sc_force<Q>(p, n + half, oxm, oxp, oym, oyp, ozm, ozp, m);
+        }
         velocity_and_limit<Q>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
         auto emit = [&](int i, float v) {
             const int o = opp(i);
@@ -782,6 +795,10 @@ __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, i
         };
         if (m.out_ext) collide_fixed<Q, TRT, FORCED, true, C::SHIFTED>(f, m, k, emit);
         else collide_fixed<Q, TRT, FORCED, false, C::SHIFTED>(f, m, k, emit);
+        if constexpr (MP) {
+            // psi of this step's density for the next step (collide.comp:763-769)
+            if (!(p.flags & F_MEASURE)) p.psi_tgt[n + half] = FSUB(1.0f, exp_f32(-m.rho));
+        }
         if (p.flags & F_SAVE) {
             p.vel_den[n + half] = make_float4(m.ux, m.uy, m.uz, m.rho);
             if (p.force_temp) p.force_temp[n + half] = make_float4(m.Fx, m.Fy, m.Fz, 0.f);
@@ -795,8 +812,12 @@ __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, i
 // 64 registers (4 blocks of 256 per SM): a thread holds both cells' loads; a few
 // TRT and forced variants spill a handful of words, which measured cheaper than
 // the latency of running at 3 blocks
-template <int Q, int ST, int MODE, bool TRT, bool FORCED>
-__global__ void __launch_bounds__(kStepBlock, BF_FAST2_MIN_BLOCKS) fast2_step_kernel(const __grid_constant__ StepParams p) {
+#ifndef BF_FAST2_MP_MIN_BLOCKS
+#define BF_FAST2_MP_MIN_BLOCKS BF_FAST2_MIN_BLOCKS
+#endif
+template <int Q, int ST, int MODE, bool TRT, bool FORCED, bool MP>
+__global__ void __launch_bounds__(kStepBlock, MP ? BF_FAST2_MP_MIN_BLOCKS : BF_FAST2_MIN_BLOCKS)
+    fast2_step_kernel(const __grid_constant__ StepParams p) {
     if (p.pf_blocks != 0u && threadIdx.x < 32) {
         const uint32_t b = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z) + p.pf_blocks;
         if (b < gridDim.x * gridDim.y * gridDim.z) prefetch_block_rows<Q, ST, MODE>(p, b, (int)threadIdx.x, 2 * (int)blockDim.x);
@@ -805,8 +826,8 @@ __global__ void __launch_bounds__(kStepBlock, BF_FAST2_MIN_BLOCKS) fast2_step_ke
     const int y = blockIdx.y, z = blockIdx.z;
     if (x >= p.nx) return;
     const bool edge = MODE == AA_EVEN && (y == 0 || y == p.ny - 1 || (Lattice<Q>::D == 3 && (z == 0 || z == p.nz - 1)));
-    if (edge) fast2_cells<Q, ST, MODE, TRT, FORCED, true>(p, x, y, z);
-    else fast2_cells<Q, ST, MODE, TRT, FORCED, false>(p, x, y, z);
+    if (edge) fast2_cells<Q, ST, MODE, TRT, FORCED, MP, true>(p, x, y, z);
+    else fast2_cells<Q, ST, MODE, TRT, FORCED, MP, false>(p, x, y, z);
 }
 
 // ---------------------------------------------------------------------------
@@ -1478,20 +1499,21 @@ cudaError_t launch_step_st(const StepParams& p, int mode, int path, cudaStream_t
     }
     // two cells per thread: 16-bit update steps without reduction or multiphase, even nx
     if constexpr ((ST == ST_FP16S || ST == ST_FP16C) && Q != 27) {
-        if (!generic && p.two_cell && (p.flags & F_UPDATE) && !(p.flags & (F_REDUCE | F_MULTIPHASE)) &&
-            p.nx % 2 == 0) {
+        if (!generic && p.two_cell && (p.flags & F_UPDATE) && !(p.flags & F_REDUCE) && p.nx % 2 == 0) {
             // one block spans a row where the row is shorter than 2 x kStepBlock cells
             const int threads = min(kStepBlock, (p.nx / 2 + 31) / 32 * 32);
             const dim3 g2((unsigned)((p.nx / 2 + threads - 1) / threads), (unsigned)p.ny, (unsigned)p.nz);
-            const bool trt = (p.flags & F_TRT) != 0, forced = (p.flags & F_FORCE_CONST) != 0;
-#define BF_FAST2(MODE_, TRT_, F_) fast2_step_kernel<Q, ST, MODE_, TRT_, F_><<<g2, threads, 0, st>>>(p)
-            if (mode == AA_EVEN) {
-                if (trt) { if (forced) BF_FAST2(AA_EVEN, true, true); else BF_FAST2(AA_EVEN, true, false); }
-                else { if (forced) BF_FAST2(AA_EVEN, false, true); else BF_FAST2(AA_EVEN, false, false); }
-            } else {
-                if (trt) { if (forced) BF_FAST2(AA_ODD, true, true); else BF_FAST2(AA_ODD, true, false); }
-                else { if (forced) BF_FAST2(AA_ODD, false, true); else BF_FAST2(AA_ODD, false, false); }
-            }
+            // multiphase flow is forced (the pseudopotential) with the source term on
+            const bool trt = (p.flags & F_TRT) != 0, mp = (p.flags & F_MULTIPHASE) != 0;
+            const bool forced = (p.flags & F_FORCE_CONST) != 0 || mp;
+#define BF_FAST2(MODE_, TRT_, F_, MP_) fast2_step_kernel<Q, ST, MODE_, TRT_, F_, MP_><<<g2, threads, 0, st>>>(p)
+#define BF_FAST2_MODE(MODE_)                                                                                  \
+    if (mp) { if (trt) BF_FAST2(MODE_, true, true, true); else BF_FAST2(MODE_, false, true, true); }          \
+    else if (trt) { if (forced) BF_FAST2(MODE_, true, true, false); else BF_FAST2(MODE_, true, false, false); } \
+    else { if (forced) BF_FAST2(MODE_, false, true, false); else BF_FAST2(MODE_, false, false, false); }
+            if (mode == AA_EVEN) { BF_FAST2_MODE(AA_EVEN) }
+            else { BF_FAST2_MODE(AA_ODD) }
+#undef BF_FAST2_MODE
 #undef BF_FAST2
             return cudaGetLastError();
         }

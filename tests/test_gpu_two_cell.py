@@ -47,3 +47,35 @@ def test_two_cell_equals_one_cell(monkeypatch, product_lib):
         s.iterate_time(steps=33, save=True)
         out.append(s.get_populations())
     assert np.array_equal(out[0], out[1])
+
+
+@pytest.mark.parametrize("vs,res,storage", [
+    (bf.VelocitySet.D3Q19, (24, 20, 16), bf.FloatingPointAccuracy.fp16s),
+    (bf.VelocitySet.D3Q19, (34, 6, 4), bf.FloatingPointAccuracy.fp16c),
+    (bf.VelocitySet.D2Q9, (40, 24, 1), bf.FloatingPointAccuracy.fp16s),
+])
+def test_two_cell_shan_chen_matches_oracle(vs, res, storage, product_lib):
+    """The pseudopotential force per cell of the pair: psi of the previous
+    step at the neighbours, with the x wrap of each cell."""
+    n = res[0] * res[1] * res[2]
+    rng = np.random.default_rng(31)
+    rho = (0.69 + 0.01 * rng.uniform(-1, 1, n)).astype(np.float32)
+    s, o = make_pair(res, 1.0, vs, density=rho, storage=storage, multiphase=True, G=-5.0, esoteric=True)
+    step_and_compare(s, o, [1, 2, 3, 8, 17])
+    assert np.array_equal(s.get_populations(), o.lattice().astype(np.float32))
+
+
+def test_two_cell_shan_chen_equals_one_cell(monkeypatch, product_lib):
+    res = (64, 12, 10)
+    n = res[0] * res[1] * res[2]
+    rng = np.random.default_rng(32)
+    rho = (0.69 + 0.01 * rng.uniform(-1, 1, n)).astype(np.float32)
+    out = []
+    for flag in ("1", "0"):
+        monkeypatch.setenv("BF_TWO_CELL", flag)
+        s, _ = make_pair(res, 1.0, bf.VelocitySet.D3Q19, density=rho, storage=bf.FloatingPointAccuracy.fp16s,
+                         multiphase=True, G=-5.0, esoteric=True)
+        s.iterate_time(steps=33, save=True)
+        out.append((s.get_populations(), s.get_velocity_density_texture().copy()))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])

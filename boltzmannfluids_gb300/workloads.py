@@ -106,3 +106,17 @@ def sphere_channel(res=(256, 128, 128), radius=16.0, center=(64.0, 64.0, 64.0), 
     rho = np.ones(n, np.float32)
     objects = {1: dict(kind=1), 2: dict(kind=2), 3: dict(kind=0)}
     return rho, u, ids.reshape(-1), objects
+
+
+def uv_sphere(n_lon=256, n_lat=128, radius=0.8):
+    """Closed triangle mesh of a sphere centred at the origin (latitude /
+    longitude grid, two triangles per quad) as (T, 3, 3)
+    float32, for voxelize_mesh."""
+    th = np.linspace(0.0, np.pi, n_lat + 1)
+    ph = np.linspace(0.0, 2.0 * np.pi, n_lon + 1)
+    pts = np.stack([np.sin(th)[:, None] * np.cos(ph)[None, :],
+                    np.sin(th)[:, None] * np.sin(ph)[None, :],
+                    np.cos(th)[:, None] * np.ones_like(ph)[None, :]], -1) * radius
+    a, b, c, d = pts[:-1, :-1], pts[1:, :-1], pts[1:, 1:], pts[:-1, 1:]
+    tris = np.concatenate([np.stack([a, b, c], 2).reshape(-1, 3, 3), np.stack([a, c, d], 2).reshape(-1, 3, 3)])
+    return tris.astype(np.float32)

@@ -236,19 +236,25 @@ def run_adjoint_leg(bf):
     64x64 box, T = 2000 steps, checkpoints every 100 steps; ms per gradient
     (forward + backward) against the forward solve, device time by CUDA events."""
     from boltzmannfluids_gb300.adjoint import AdjointChannel, channel_setup
-    res = (512, 256, 1)
-    s, u_in, tgt = channel_setup(res)
-    out = {"workload": "D2Q9 BGK channel 512x256, PSM obstacle, T=2000"}
-    for K, key in ((100, "checkpoint_every_100"), (2000, "all_states_stored")):
-        g = AdjointChannel(res, 0.6, bf.VelocitySet.D2Q9, 2000, K)
+
+    def timed(res, vs, K, reps):
+        s, u_in, tgt = channel_setup(res)
+        g = AdjointChannel(res, 0.6, vs, 2000, K)
         g.set_parameters(s, u_in)
         g.set_target(tgt)
         g.forward()
         g.backward()
-        f_ms, b_ms = g.time(5)
-        out[key] = {"forward_ms": round(f_ms, 3), "backward_ms": round(b_ms, 3),
-                    "ms_per_gradient": round(f_ms + b_ms, 3), "gradient_over_forward": round((f_ms + b_ms) / f_ms, 3)}
+        f_ms, b_ms = g.time(reps)
         del g
+        return {"forward_ms": round(f_ms, 3), "backward_ms": round(b_ms, 3),
+                "ms_per_gradient": round(f_ms + b_ms, 3), "gradient_over_forward": round((f_ms + b_ms) / f_ms, 3)}
+
+    out = {"workload": "D2Q9 BGK channel 512x256, PSM obstacle, T=2000"}
+    for K, key in ((100, "checkpoint_every_100"), (2000, "all_states_stored")):
+        out[key] = timed((512, 256, 1), bf.VelocitySet.D2Q9, K, 5)
+    # the configuration's 3D case: D3Q19 channel 128^3 (periodic z), checkpoints every 100 steps
+    out["d3q19_128"] = {"workload": "D3Q19 BGK channel 128x128x128 (periodic z), PSM obstacle, T=2000, K=100",
+                        **timed((128, 128, 128), bf.VelocitySet.D3Q19, 100, 2)}
     return out
 
 

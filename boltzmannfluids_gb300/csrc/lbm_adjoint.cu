@@ -205,18 +205,18 @@ __device__ __forceinline__ void adj_backward_cell(const AdjParams& p, int x, int
     }
     const float rr = 1.0f / rho;
     const float ux = jx * rr, uy = jy * rr, uz = jz * rr;
-    float mu[Q];
+    // the cell's transposed Jacobian as a few scalars; mu_i is formed where
+    // it is stored (no array of Q adjoint populations held in registers)
     double gs;
-    if (FINAL) {
+    float fdx = 0.f, fdy = 0.f, fdz = 0.f;        // final step
+    float a0 = 0.f, a1 = 0.f;                     // other steps
+    const float om = p.omega;
+    float Vx = 0.f, Vy = 0.f, Vz = 0.f;
+    if constexpr (FINAL) {
         // dJ/dg_i = wd 2 s c_ix + wm sum_a 2 (u_a - u*_a)(c_ia - u_a)/rho,  dJ/ds = wd 2 j_x
-        const float dx = 2.0f * p.wm * (ux - p.ustar[3 * (uint64_t)n]) * rr;
-        const float dy = 2.0f * p.wm * (uy - p.ustar[3 * (uint64_t)n + 1]) * rr;
-        const float dz = 2.0f * p.wm * (uz - p.ustar[3 * (uint64_t)n + 2]) * rr;
-#pragma unroll
-        for (int i = 0; i < Q; i++) {
-            const Dir c = L::c(i);
-            mu[i] = 2.0f * p.wd * s * c.x + dx * (c.x - ux) + dy * (c.y - uy) + dz * (c.z - uz);
-        }
+        fdx = 2.0f * p.wm * (ux - p.ustar[3 * (uint64_t)n]) * rr;
+        fdy = 2.0f * p.wm * (uy - p.ustar[3 * (uint64_t)n + 1]) * rr;
+        fdz = 2.0f * p.wm * (uz - p.ustar[3 * (uint64_t)n + 2]) * rr;
         gs = (double)p.wd * 2.0 * (double)jx;
     } else {
         // The lattice components are -1, 0 or 1 and known per unrolled
@@ -225,9 +225,9 @@ __device__ __forceinline__ void adj_backward_cell(const AdjParams& p, int x, int
         // x * 0 or x + 0 itself).  With B_k = 1 + 3 cu_k + 4.5 cu_k^2 - 1.5 uu
         // (shared by A0 and the equilibrium) and L_k = (1 - s) lam_k w_k:
         //   A0 = sum_k L_k B_k,  V = sum_k L_k (3 + 9 cu_k) c_k - 3 u sum_k L_k.
-        const float om = p.omega, oms = 1.0f - s;
+        const float oms = 1.0f - s;
         const float base = 1.0f - 1.5f * (ux * ux + uy * uy + uz * uz);
-        float A0 = 0.f, Lsum = 0.f, Vx = 0.f, Vy = 0.f, Vz = 0.f, gsf = 0.f;
+        float A0 = 0.f, Lsum = 0.f, gsf = 0.f;
 #pragma unroll
         for (int k = 0; k < Q; k++) {
             const Dir c = L::c(k);
@@ -245,15 +245,19 @@ __device__ __forceinline__ void adj_backward_cell(const AdjParams& p, int x, int
         Vx = fmaf(-3.0f * ux, Lsum, Vx); Vy = fmaf(-3.0f * uy, Lsum, Vy); Vz = fmaf(-3.0f * uz, Lsum, Vz);
         gs = (double)gsf;  // per-cell sum in FP32, accumulated over steps in FP64
         // mu_i = (1 - om)(1 - s) lam_i + om (A0 + (c_i - u).V) + s lam_opp(i)
-        const float a1 = (1.0f - om) * oms, a0 = om * (A0 - (ux * Vx + uy * Vy + uz * Vz));
-#pragma unroll
-        for (int i = 0; i < Q; i++) {
-            const Dir c = L::c(i);
+        a1 = (1.0f - om) * oms;
+        a0 = om * (A0 - (ux * Vx + uy * Vy + uz * Vz));
+    }
+    auto mu_of = [&](int i) -> float {
+        const Dir c = L::c(i);
+        if constexpr (FINAL) {
+            return 2.0f * p.wd * s * c.x + fdx * (c.x - ux) + fdy * (c.y - uy) + fdz * (c.z - uz);
+        } else {
             float cv = 0.f;
             lattice_axpy(c.x, Vx, cv); lattice_axpy(c.y, Vy, cv); lattice_axpy(c.z, Vz, cv);
-            mu[i] = fmaf(a1, lam[i], fmaf(om, cv, a0)) + s * lam[opp(i)];
+            return fmaf(a1, lam[i], fmaf(om, cv, a0)) + s * lam[opp(i)];
         }
-    }
+    };
     p.grad_s[n] = gs_prev + gs;
     // transpose of the pull; cells off the walls and the inlet/outlet layers
     // push every adjoint population to an interior neighbour (z periodic)
@@ -263,7 +267,7 @@ __device__ __forceinline__ void adj_backward_cell(const AdjParams& p, int x, int
         for (int i = 0; i < Q; i++) {
             const Dir c = L::c(i);
             const int Z = c.z > 0 ? zm : (c.z < 0 ? zp : z);
-            p.lam_out[(uint64_t)i * p.n + adj_cell(p, x - c.x, y - c.y, Z)] = mu[i];
+            p.lam_out[(uint64_t)i * p.n + adj_cell(p, x - c.x, y - c.y, Z)] = mu_of(i);
         }
         return;
     }
@@ -274,9 +278,10 @@ __device__ __forceinline__ void adj_backward_cell(const AdjParams& p, int x, int
     for (int i = 0; i < Q; i++) {
         int X, Y, Z;
         const int kind = adj_source<Q>(p, x, y, z, i, X, Y, Z);
-        if (kind == 0) p.lam_out[(uint64_t)i * p.n + adj_cell(p, X, Y, Z)] = mu[i];
-        else if (kind == 1) p.lam_out[(uint64_t)opp(i) * p.n + n] = mu[i];
-        else { guf += mu[i] * dfeq_du<Q>(i, ui); eq_source = true; }
+        const float mi = mu_of(i);
+        if (kind == 0) p.lam_out[(uint64_t)i * p.n + adj_cell(p, X, Y, Z)] = mi;
+        else if (kind == 1) p.lam_out[(uint64_t)opp(i) * p.n + n] = mi;
+        else { guf += mi * dfeq_du<Q>(i, ui); eq_source = true; }
     }
     // populations of f^(t-1) that leave through the inlet or outlet feed nothing
 #pragma unroll
@@ -292,11 +297,18 @@ __device__ __forceinline__ void adj_backward_cell(const AdjParams& p, int x, int
     }
 }
 
-// D2Q9: 48 registers, 5 blocks per SM (the 512x256 channel's backward
-// measured 13.3 ms against 16.0 ms at 64 registers); D3Q19 keeps its
-// registers (at 48 it spills over 120 bytes)
+// blocks per SM of the adjoint step: D2Q9 5 (48 registers; the 512x256
+// channel's backward measured 13.3 ms, 14.0 ms at 4 blocks); D3Q19 4 (64
+// registers; the 128^3 channel's backward measured 474 / 394 / 351 / 362 ms
+// at 2 / 3 / 4 / 5 blocks, 640 ms at 1)
+#ifndef BF_ADJ_MIN_BLOCKS_Q19
+#define BF_ADJ_MIN_BLOCKS_Q19 4
+#endif
+#ifndef BF_ADJ_MIN_BLOCKS_Q9
+#define BF_ADJ_MIN_BLOCKS_Q9 5
+#endif
 template <int Q>
-constexpr int adj_min_blocks() { return Q == 9 ? 5 : 1; }
+constexpr int adj_min_blocks() { return Q == 9 ? BF_ADJ_MIN_BLOCKS_Q9 : BF_ADJ_MIN_BLOCKS_Q19; }
 
 template <int Q, bool FINAL>
 __global__ void __launch_bounds__(kAdjBlock, adj_min_blocks<Q>()) adj_backward_kernel(AdjParams p) {
@@ -429,6 +441,16 @@ cudaError_t enqueue_forward(bf_adjoint* a) {
     return cudaGetLastError();
 }
 
+// D2Q9 merges each adjoint step with a recomputation step; D3Q19's adjoint
+// kernel holds many more registers than its forward, so there the
+// recomputation runs as its own launches at the forward's occupancy (the
+// 128^3 channel's backward: 351 ms against 527 ms merged)
+#ifndef BF_ADJ_MERGE_Q19
+#define BF_ADJ_MERGE_Q19 0
+#endif
+template <int Q>
+constexpr bool kMergeRecompute = Q == 9 || BF_ADJ_MERGE_Q19;
+
 template <int Q>
 cudaError_t enqueue_backward(bf_adjoint* a) {
     int block;
@@ -455,7 +477,7 @@ cudaError_t enqueue_backward(bf_adjoint* a) {
             const int out = cur == 0 ? 1 : 0;
             p.lam_out = a->lam[out];
             p.lam_in = t == T ? nullptr : a->lam[cur];
-            if (t != T && j <= r_steps) {
+            if (kMergeRecompute<Q> && t != T && j <= r_steps) {
                 q.f_prev = rprev;
                 q.f_next = a->seg[r & 1][j];
                 adj_sweep_recompute_kernel<Q><<<grid2, block, 0, a->stream>>>(p, q);

@@ -473,10 +473,11 @@ constexpr int kFastMinBlocks16 = BF_FAST_MIN_BLOCKS_16;
 // Shan-Chen pseudopotential force (collide.comp:534-584) with the generic
 // kernel's arithmetic: psi of the previous step at the periodic neighbours
 // x + c_i (offsets ox*/oy*/oz* from cell n to x -+ 1, y -+ 1, z -+ 1),
-// summed as w_i psi c_i in direction order, times -G psi(rho) of the cell
+// summed as w_i psi c_i in direction order, times -G psi(rho) of the cell;
+// returns psi(rho), which is also this step's psi field value of the cell
 template <int Q>
-__device__ __forceinline__ void sc_force(const StepParams& p, uint32_t n, int oxm, int oxp, int oym, int oyp, int ozm,
-                                         int ozp, Moments& m) {
+__device__ __forceinline__ float sc_force(const StepParams& p, uint32_t n, int oxm, int oxp, int oym, int oyp, int ozm,
+                                          int ozp, Moments& m) {
     using L = Lattice<Q>;
     const float self_psi = FSUB(1.0f, exp_f32(-m.rho));
     float sx = 0.f, sy = 0.f, sz = 0.f;
@@ -492,6 +493,7 @@ __device__ __forceinline__ void sc_force(const StepParams& p, uint32_t n, int ox
     }
     const float k = FMUL(-self_psi, p.G);
     m.Fx = FFMA(sx, k, m.Fx); m.Fy = FFMA(sy, k, m.Fy); m.Fz = FFMA(sz, k, m.Fz);
+    return self_psi;
 }
 
 // Boussinesq buoyancy of the thermal lattice (collide.comp:709-716): the
@@ -613,7 +615,10 @@ __device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepP
     m.Fx = FORCED ? (F64 ? R(p.k64.fconst[0]) : R(p.fconst[0])) : R(0);
     m.Fy = FORCED ? (F64 ? R(p.k64.fconst[1]) : R(p.fconst[1])) : R(0);
     m.Fz = FORCED ? (F64 ? R(p.k64.fconst[2]) : R(p.fconst[2])) : R(0);
-    if constexpr (MP && !F64) sc_force<Q>(p, n, oxm, oxp, oym, oyp, ozm, ozp, m);
+    // psi(rho) of the cell: the force's factor and, unchanged (rho is not
+    // modified after it), this step's psi field value
+    float psi_self = 0.f;
+    if constexpr (MP && !F64) psi_self = sc_force<Q>(p, n, oxm, oxp, oym, oyp, ozm, ozp, m);
     float temperature = 0.f;
     if constexpr (THERMAL && !F64) {
         static_assert(FORCED, "thermal flow runs with the source term on");
@@ -629,7 +634,7 @@ __device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepP
     }
     if constexpr (MP && !F64) {
         // psi of this step's density for the next step (collide.comp:763-769)
-        if (!(p.flags & F_MEASURE)) p.psi_tgt[n] = FSUB(1.0f, exp_f32(-m.rho));
+        if (!(p.flags & F_MEASURE)) p.psi_tgt[n] = psi_self;
     }
     if constexpr (THERMAL && !F64) {
         if (!(p.flags & F_MEASURE)) thermal_collide<Q>(p, n, m, temperature);
@@ -762,12 +767,13 @@ __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, i
         m.Fx = FORCED ? p.fconst[0] : 0.f;
         m.Fy = FORCED ? p.fconst[1] : 0.f;
         m.Fz = FORCED ? p.fconst[2] : 0.f;
+        float psi_self = 0.f;
         if constexpr (MP) {
             // x neighbours of cell x (half 0) and x + 1 (half 1): only x - 1
             // of the first and x + 2 of the second can wrap (x even, nx even)
             const int oxm = half ? -1 : (x == 0 ? nx - 1 : -1);
             const int oxp = half ? (x + 2 == nx ? 1 - nx : 1) : 1;
-            sc_force<Q>(p, n + half, oxm, oxp, oym, oyp, ozm, ozp, m);
+            psi_self = sc_force<Q>(p, n + half, oxm, oxp, oym, oyp, ozm, ozp, m);
         }
         velocity_and_limit<Q>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
         auto emit = [&](int i, float v) {
@@ -797,7 +803,7 @@ __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, i
         else collide_fixed<Q, TRT, FORCED, false, C::SHIFTED>(f, m, k, emit);
         if constexpr (MP) {
             // psi of this step's density for the next step (collide.comp:763-769)
-            if (!(p.flags & F_MEASURE)) p.psi_tgt[n + half] = FSUB(1.0f, exp_f32(-m.rho));
+            if (!(p.flags & F_MEASURE)) p.psi_tgt[n + half] = psi_self;
         }
         if (p.flags & F_SAVE) {
             p.vel_den[n + half] = make_float4(m.ux, m.uy, m.uz, m.rho);
@@ -1031,8 +1037,14 @@ __global__ void __launch_bounds__(kStepBlock, Q == 27 ? 3 : kFastMinBlocks)
 // updated right after their neighbours streamed the same 32-byte sectors
 // through L2, in short blocks of their own, however dense they lie (a wall
 // plane is a run of special blocks).
+// 4 blocks per SM (64 registers; some even-step variants spill 12-56 bytes):
+// 3 blocks without spills measured 31.4k against 35.1k MLUPs on flow past a
+// sphere, 18.6k against 20.8k on Rayleigh-Benard
+#ifndef BF_MIXED_MIN_BLOCKS
+#define BF_MIXED_MIN_BLOCKS kFastMinBlocks
+#endif
 template <int Q, int ST, int MODE, bool TRT, bool FORCED, bool THERMAL>
-__global__ void __launch_bounds__(kStepBlock, kFastMinBlocks) masked_mixed_kernel(const __grid_constant__ StepParams p) {
+__global__ void __launch_bounds__(kStepBlock, BF_MIXED_MIN_BLOCKS) masked_mixed_kernel(const __grid_constant__ StepParams p) {
     const uint32_t nx = (uint32_t)p.nx, ny = (uint32_t)p.ny;
     const uint32_t e = __ldg(p.sched + blockIdx.x);
     if (!(e >> 31)) {

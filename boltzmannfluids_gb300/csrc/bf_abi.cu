@@ -122,6 +122,8 @@ struct bf_solver {
     bool two_cell = true;    // 16-bit fast step with two cells per thread
     bool masked_split = true; // boundary-aware step with the special cells in blocks of their own
     bool zero_copy = true;    // kernels read/write pinned host buffers directly (initial velocity, field read-back)
+    bool thermal_push = true; // split boundary-aware step: thermal stream folded into the collision
+    bool pushed_thermal = false;  // the last collide pushed (no thermal stream pass to follow)
 };
 
 namespace {
@@ -435,6 +437,15 @@ cudaError_t collide(bf_solver* s, bool save, bool update, bool reduce, bool meas
         p.n_sched = s->n_sched;
         p.special_chunk = s->special_chunk;
     }
+    // the split kernel (masked_mixed_kernel) runs the thermal collision as a
+    // push when the masks mark every special thermal source: solid sources
+    // are marked under bounce-back, and without boundary ids only open ones exist
+    s->pushed_thermal = false;
+    if (s->thermal && s->thermal_push && path == PATH_MASKED && mode != AA_LOCAL && p.special && !reduce &&
+        !measure && ((p.flags & F_BOUNCE_BACK) || !(p.flags & F_BOUNDARIES))) {
+        p.thermal_push = 1u;
+        s->pushed_thermal = true;
+    }
     // the prefetch rounds each row range out to 16 bytes, which stays inside
     // the plane only when every plane starts and ends on a 16-byte boundary
     const size_t plane_bytes = (size_t)s->N * storage_bytes(s->desc.storage);
@@ -505,7 +516,7 @@ cudaError_t iterate_once(bf_solver* s, bool save, bool update, bool reduce) {
     cudaError_t e = collide(s, save, update, reduce, false);
     if (e != cudaSuccess) return e;
     if (!s->desc.esoteric) { e = stream(s); if (e != cudaSuccess) return e; }
-    if (s->thermal) { e = stream_thermal(s); if (e != cudaSuccess) return e; }
+    if (s->thermal && !s->pushed_thermal) { e = stream_thermal(s); if (e != cudaSuccess) return e; }
     return cudaSuccess;
 }
 
@@ -676,6 +687,8 @@ int bf_create(bf_solver** out) {
     if (const char* env = std::getenv("BF_MASKED_SPLIT")) s->masked_split = std::strtoul(env, nullptr, 10) != 0;
     // BF_ZERO_COPY=0: stage pinned host buffers through cudaMemcpy like any other (A/B comparisons)
     if (const char* env = std::getenv("BF_ZERO_COPY")) s->zero_copy = std::strtoul(env, nullptr, 10) != 0;
+    // BF_THERMAL_PUSH=0: a separate thermal stream pass after every collision (A/B comparisons)
+    if (const char* env = std::getenv("BF_THERMAL_PUSH")) s->thermal_push = std::strtoul(env, nullptr, 10) != 0;
     // BF_TMA_STEP=1 selects the staged 16-bit fast step, 0 the plain one
     if (const char* env = std::getenv("BF_TMA_STEP")) s->tma_step = std::strtoul(env, nullptr, 10) != 0;
     *out = s;
@@ -936,6 +949,9 @@ int bf_initialize_fields(bf_solver* s, const bf_init_desc* d, const float* densi
             tp.stride = N;
             e = s->QT == 5 ? launch_init_thermal<5>(tp, s->stream) : launch_init_thermal<7>(tp, s->stream);
             if (e != cudaSuccess) return fail(BF_ERR_CUDA, std::string("thermal init kernel: ") + cudaGetErrorString(e));
+            // both buffers start alike: slots nothing writes (solid cells) then
+            // read the same whichever buffer holds the current state
+            BF_CUDA(cudaMemcpyAsync(th_tgt(s), th_src(s), (size_t)N * s->QT * 4, cudaMemcpyDeviceToDevice, s->stream));
             BF_CUDA(cudaStreamSynchronize(s->stream));
         }
         // As the reference reads it, set_equilibrium_populations_thermal.comp:101-107

@@ -243,6 +243,12 @@ struct alignas(16) StepParams {
     uint32_t tma;
     // 1: 16-bit update steps may run two cells per thread (fast2_step_kernel)
     uint32_t two_cell;
+    // 1: the thermal collision pushes each post-collision thermal population
+    // to the slot the thermal pull stream would fill with it (th_tgt becomes
+    // the next step's pre-collision state; no stream pass).  Set by the host
+    // for the split boundary-aware step when the masks mark every special
+    // thermal source.
+    uint32_t thermal_push;
     // per-cell masks of the boundary-aware fast step (build_mask_kernel):
     // bit i (1..Q-1) = the AA source x - c_i needs special handling (outside
     // the domain, or a solid cell under bounce-back); bit 31 = the cell is

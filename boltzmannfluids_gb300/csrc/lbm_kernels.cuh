@@ -526,6 +526,60 @@ __device__ __forceinline__ void thermal_collide(const StepParams& p, uint32_t n,
     }
 }
 
+// The thermal BGK with the thermal pull stream (stream_thermal.comp:457-526)
+// folded in as a push.  The stream fills slot i of fluid cell m with
+// B_i(m - c_i) when that source is a fluid cell in the domain, with
+// -B_opp(i)(m) + 2 w_opp T_wall when it is solid (anti-bounce-back), and
+// leaves it as it was (the pre-collision value) when it lies outside.  Here
+// cell n writes its post-collision b_i to slot i of n + c_i unless that
+// destination is outside or solid (mask bit opp(i): the source n - c_opp(i)
+// is special), and fills its own slot i itself when its source n - c_i is
+// special (mask bit i).  Every slot of the target keeps exactly one writer;
+// solid cells write nothing, as in the stream.  The values are the stream's.
+template <int Q>
+__device__ __forceinline__ void thermal_collide_push(const StepParams& p, uint32_t n, int x, int y, int z, uint32_t mask,
+                                                     const Moments& m, float temperature) {
+    constexpr int QT = Lattice<Q>::D == 2 ? 5 : 7;
+    using TL = ThermalLattice<QT>;
+    const uint64_t S = p.stride;
+    const float one_m = FSUB(1.0f, FMUL(uu_of(m.ux, m.uy, m.uz), p.R2h));
+    float a[QT], b[QT];
+#pragma unroll
+    for (int i = 0; i < QT; i++) {
+        const Dir c = TL::c(i);
+        const float w = TL::w(i);
+        const float cu = cdot_rt(c, m.ux, m.uy, m.uz);
+        const float geq = FMUL(FMUL(w, temperature), bracket(cu, one_m, p.R2, p.R4h));
+        a[i] = __ldg(p.th_src + (uint64_t)i * S + n);
+        b[i] = FFMA(FSUB(geq, a[i]), p.Rtau_t, a[i]);
+    }
+    p.th_tgt[n] = b[0];
+#pragma unroll
+    for (int i = 1; i < QT; i++) {
+        const Dir c = TL::c(i);
+        if (!((mask >> opp(i)) & 1u)) {
+            int dx = x + c.x, dy = y + c.y, dz = z + c.z;
+            bool open;
+            coords_wrap<Q>(dx, dy, dz, p.nx, p.ny, p.nz, open, p.flags);
+            p.th_tgt[(uint64_t)i * S + (uint32_t)dx + (uint32_t)p.nx * ((uint32_t)dy + (uint32_t)p.ny * (uint32_t)dz)] = b[i];
+        }
+        if ((mask >> i) & 1u) {
+            int sx = x - c.x, sy = y - c.y, sz = z - c.z;
+            bool open;
+            coords_wrap<Q>(sx, sy, sz, p.nx, p.ny, p.nz, open, p.flags);
+            float v = a[i];
+            if (!open) {
+                const uint32_t sn = (uint32_t)sx + (uint32_t)p.nx * ((uint32_t)sy + (uint32_t)p.ny * (uint32_t)sz);
+                const uint32_t sid = boundary_id(p.bnd, p.bits, sn);
+                const int inv = opp(i);
+                const float Tw = __ldg(p.objects + 3u * sid).w;
+                v = __fadd_rn(-b[inv], __fmul_rn(2.f * TL::w(inv), Tw));
+            }
+            p.th_tgt[(uint64_t)i * S + n] = v;
+        }
+    }
+}
+
 // THERMAL (FP32 and 16-bit storage; FORCED set with it): the buoyancy and
 // the thermal collision of the boundary-aware kernel, for cells whose
 // sources are all plain.  GUARD: the cell's mask is loaded beside its
@@ -637,7 +691,11 @@ __device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepP
         if (!(p.flags & F_MEASURE)) p.psi_tgt[n] = psi_self;
     }
     if constexpr (THERMAL && !F64) {
-        if (!(p.flags & F_MEASURE)) thermal_collide<Q>(p, n, m, temperature);
+        // plain cells: every thermal source and destination is a fluid cell in the domain
+        if (!(p.flags & F_MEASURE)) {
+            if (p.thermal_push) thermal_collide_push<Q>(p, n, x, y, z, 0u, m, temperature);
+            else thermal_collide<Q>(p, n, m, temperature);
+        }
     }
     if (p.flags & F_SAVE) {
         p.vel_den[n] = make_float4((float)m.ux, (float)m.uy, (float)m.uz, (float)m.rho);
@@ -981,7 +1039,10 @@ __device__ __forceinline__ CellSum masked_cell(const StepParams& p, int x, int y
         else if (m.out_ext) collide_fixed<Q, TRT, FRC, true, C::SHIFTED>(f, m, k, emit);
         else collide_fixed<Q, TRT, FRC, false, C::SHIFTED>(f, m, k, emit);
     }
-    if (THERMAL && !(flags & F_MEASURE)) thermal_collide<Q>(p, n, m, temperature);
+    if (THERMAL && !(flags & F_MEASURE)) {
+        if (p.thermal_push) thermal_collide_push<Q>(p, n, x, y, z, mask, m, temperature);
+        else thermal_collide<Q>(p, n, m, temperature);
+    }
     if (flags & F_SAVE) {
         p.vel_den[n] = make_float4(m.ux, m.uy, m.uz, m.rho);
         p.force_temp[n] = make_float4(m.Fx, m.Fy, m.Fz, temperature);

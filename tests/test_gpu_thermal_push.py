@@ -66,3 +66,33 @@ def test_thermal_push_equals_stream_pass(monkeypatch):
                     s.get_force_temperature_texture().copy()))
     for a, b in zip(out[0], out[1]):
         assert np.array_equal(a, b)
+
+
+def test_thermal_push_with_reductions_saves_and_snapshots(monkeypatch, tmp_path):
+    """Reductions (a measure pass reading the thermal state), save steps,
+    graph-sized batches and a snapshot round trip between pushed steps give
+    what the separate stream pass gives."""
+    res, ids, temp, u, f, objs = walls_case(19)
+    runs = []
+    for flag in ("1", "0"):
+        monkeypatch.setenv("BF_THERMAL_PUSH", flag)
+        s, _ = make_pair(res, 0.6, VS[19], ids=ids, objects=objs, force=f, temperature=temp, velocity=u,
+                         periodic=(False, True, True), boundary_mode=1, thermal_init_equilibrium=True,
+                         tau_t=0.8, beta=0.5)
+        rec = []
+        s.iterate_time(steps=5, save=False)
+        rec.append(s.reduce().copy())
+        s.iterate_time(steps=3, save=True)
+        rec.append(s.get_force_temperature_texture().copy())
+        p = tmp_path / f"snap{flag}.bin"
+        s.save_current_tick_mesoscropic(p)
+        s.iterate_time(steps=20, save=True)  # includes a 16-step graph batch
+        rec.append(s.get_thermal_populations().copy())
+        s.load_tick_mesoscropic(p)
+        s.iterate_time(steps=20, save=True)
+        rec.append(s.get_thermal_populations().copy())
+        rec.append(s.reduce().copy())
+        runs.append(rec)
+    for a, b in zip(runs[0], runs[1]):
+        assert np.array_equal(a, b)
+    assert np.array_equal(runs[0][2], runs[0][3])  # the snapshot replays the same steps

@@ -96,3 +96,17 @@ def test_thermal_push_with_reductions_saves_and_snapshots(monkeypatch, tmp_path)
     for a, b in zip(runs[0], runs[1]):
         assert np.array_equal(a, b)
     assert np.array_equal(runs[0][2], runs[0][3])  # the snapshot replays the same steps
+
+
+@pytest.mark.parametrize("storage", [bf.FloatingPointAccuracy.fp16s, bf.FloatingPointAccuracy.fp16c])
+def test_thermal_push_with_16bit_flow_storage(storage):
+    """The thermal lattice (FP32) beside a 16-bit flow lattice in the split step."""
+    res, ids, temp, u, f, objs = walls_case(19)
+    s, o = make_pair(res, 0.6, VS[19], ids=ids, objects=objs, force=f, temperature=temp, velocity=u,
+                     periodic=(False, True, True), boundary_mode=1, thermal_init_equilibrium=True,
+                     tau_t=0.8, beta=0.5, storage=storage)
+    fluid = ids == 0
+    step_and_compare(s, o, [1, 2, 9], mask=fluid, check_temperature=True)
+    mine = s.get_thermal_populations()
+    ref = o.thermal_lattice().reshape(-1, 7).T
+    assert np.array_equal(mine[:, fluid], ref[:, fluid])

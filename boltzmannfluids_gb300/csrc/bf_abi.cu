@@ -40,6 +40,11 @@ int fail(int code, const std::string& msg) {
 constexpr int kMaxObjects = 256;  // ids 0..255 (LBM.h:29)
 constexpr int kGraphSteps = 16;   // steps per captured graph (even: the AA state has period 2)
 
+// host-side fault injection (bf_debug_fail_allocation_after): the number of
+// further device allocations that succeed before one fails as out of
+// memory; negative = off
+int g_alloc_failure_countdown = -1;
+
 struct DeviceBuf {
     void* p = nullptr;
     size_t bytes = 0;
@@ -52,6 +57,11 @@ struct DeviceBuf {
     cudaError_t alloc(size_t n) {
         release();
         if (n == 0) return cudaSuccess;
+        if (g_alloc_failure_countdown == 0) {
+            g_alloc_failure_countdown = -1;
+            return cudaErrorMemoryAllocation;
+        }
+        if (g_alloc_failure_countdown > 0) g_alloc_failure_countdown--;
         cudaError_t e = cudaMalloc(&p, n);
         if (e == cudaSuccess) bytes = n; else p = nullptr;
         return e;
@@ -653,6 +663,11 @@ int bf_pack_boundries(const uint32_t* ids, size_t cells, int32_t bits, uint32_t*
 }
 int bf_abi_version(void) { return BF_ABI_VERSION; }
 
+int bf_debug_fail_allocation_after(int32_t n) {
+    g_alloc_failure_countdown = n < 0 ? -1 : n;
+    return BF_OK;
+}
+
 int bf_create(bf_solver** out) {
     if (!out) return fail(BF_ERR_INVALID_ARGUMENT, "bf_create: out is NULL");
     int count = 0;
@@ -928,7 +943,7 @@ int bf_initialize_fields(bf_solver* s, const bf_init_desc* d, const float* densi
     case 19: e = launch_init<19>(ip, d->storage, s->stream); break;
     default: e = launch_init<27>(ip, d->storage, s->stream); break;
     }
-    if (e != cudaSuccess) return fail(BF_ERR_CUDA, std::string("init kernel: ") + cudaGetErrorString(e));
+    if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? BF_ERR_OUT_OF_MEMORY : BF_ERR_CUDA, std::string("init kernel: ") + cudaGetErrorString(e));
     if (s->thermal) {
         BF_CUDA(s->th[0].alloc((size_t)N * s->QT * 4));
         BF_CUDA(s->th[1].alloc((size_t)N * s->QT * 4));
@@ -948,7 +963,7 @@ int bf_initialize_fields(bf_solver* s, const bf_init_desc* d, const float* densi
             tp.T = d_Tb.as<float>();
             tp.stride = N;
             e = s->QT == 5 ? launch_init_thermal<5>(tp, s->stream) : launch_init_thermal<7>(tp, s->stream);
-            if (e != cudaSuccess) return fail(BF_ERR_CUDA, std::string("thermal init kernel: ") + cudaGetErrorString(e));
+            if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? BF_ERR_OUT_OF_MEMORY : BF_ERR_CUDA, std::string("thermal init kernel: ") + cudaGetErrorString(e));
             // both buffers start alike: slots nothing writes (solid cells) then
             // read the same whichever buffer holds the current state
             BF_CUDA(cudaMemcpyAsync(th_tgt(s), th_src(s), (size_t)N * s->QT * 4, cudaMemcpyDeviceToDevice, s->stream));
@@ -973,14 +988,14 @@ int bf_initialize_fields(bf_solver* s, const bf_init_desc* d, const float* densi
         case 19: e = launch_build_mask<19>(mp, s->nmask.as<uint32_t>(), s->stream); break;
         default: e = launch_build_mask<27>(mp, s->nmask.as<uint32_t>(), s->stream); break;
         }
-        if (e != cudaSuccess) return fail(BF_ERR_CUDA, std::string("mask kernel: ") + cudaGetErrorString(e));
+        if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? BF_ERR_OUT_OF_MEMORY : BF_ERR_CUDA, std::string("mask kernel: ") + cudaGetErrorString(e));
         e = build_special_list(s, (uint64_t)N);
         if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? BF_ERR_OUT_OF_MEMORY : BF_ERR_CUDA,
                                           std::string("special-cell list: ") + cudaGetErrorString(e));
     }
     // LBM.cpp:502: _iterate_time(true, false)
     e = iterate_once(s, true, false, false);
-    if (e != cudaSuccess) return fail(BF_ERR_CUDA, std::string("first pass: ") + cudaGetErrorString(e));
+    if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? BF_ERR_OUT_OF_MEMORY : BF_ERR_CUDA, std::string("first pass: ") + cudaGetErrorString(e));
     BF_CUDA(cudaStreamSynchronize(s->stream));
     s->last_saved = true;
     s->initialized = true;
@@ -1209,8 +1224,11 @@ int bf_save_snapshot(bf_solver* s, const char* path) {
     if (!s || !path) return fail(BF_ERR_INVALID_ARGUMENT, "NULL argument");
     if (!s->initialized) return fail(BF_ERR_NOT_INITIALIZED, "save_snapshot(): initialize_fields has not run");
     BF_CUDA(cudaStreamSynchronize(s->stream));
-    FILE* fp = std::fopen(path, "wb");
-    if (!fp) return fail(BF_ERR_IO, std::string("save_snapshot(): cannot open ") + path);
+    // written to a temporary file beside the target and renamed over it only
+    // once complete: an interrupted or failed save leaves no partial snapshot
+    const std::string tmp = std::string(path) + ".partial";
+    FILE* fp = std::fopen(tmp.c_str(), "wb");
+    if (!fp) return fail(BF_ERR_IO, std::string("save_snapshot(): cannot open ") + tmp);
     bool ok = true;
     auto put = [&](const void* p, size_t n) { if (ok && std::fwrite(p, 1, n, fp) != n) ok = false; };
     put(kMagic, 8);
@@ -1230,7 +1248,12 @@ int bf_save_snapshot(bf_solver* s, const char* path) {
     dump(s->lat[0]); dump(s->lat[1]); dump(s->th[0]); dump(s->th[1]); dump(s->psi[0]); dump(s->psi[1]);
     dump(s->vel_den); dump(s->force_temp);
     if (std::fclose(fp) != 0) ok = false;
-    return ok ? BF_OK : fail(BF_ERR_IO, std::string("save_snapshot(): write failed for ") + path);
+    if (ok && std::rename(tmp.c_str(), path) != 0) ok = false;
+    if (!ok) {
+        std::remove(tmp.c_str());
+        return fail(BF_ERR_IO, std::string("save_snapshot(): write failed for ") + path);
+    }
+    return BF_OK;
 }
 
 int bf_load_snapshot(bf_solver* s, const char* path) {
@@ -1257,6 +1280,19 @@ int bf_load_snapshot(bf_solver* s, const char* path) {
     }
     std::vector<char> h;
     DeviceBuf* bufs[] = {&s->lat[0], &s->lat[1], &s->th[0], &s->th[1], &s->psi[0], &s->psi[1], &s->vel_den, &s->force_temp};
+    // the file must be exactly this solver's snapshot size before any device
+    // buffer is touched: a truncated or foreign file leaves the state as it was
+    {
+        uint64_t expect = 8 + sizeof(d) + sizeof(ticks) + sizeof(st);
+        for (DeviceBuf* b : bufs) expect += 8 + b->bytes;
+        const long here = std::ftell(fp);
+        const bool sized = here >= 0 && std::fseek(fp, 0, SEEK_END) == 0;
+        const long end = sized ? std::ftell(fp) : -1;
+        if (!sized || end < 0 || (uint64_t)end != expect || std::fseek(fp, here, SEEK_SET) != 0) {
+            std::fclose(fp);
+            return fail(BF_ERR_IO, "load_snapshot(): truncated or mismatched snapshot");
+        }
+    }
     for (DeviceBuf* b : bufs) {
         uint64_t n = 0;
         get(&n, 8);

@@ -122,6 +122,7 @@ ABI = {
     "bf_init_desc_default": (None, [C.POINTER(_InitDesc)]),
     "bf_last_error": (C.c_char_p, []),
     "bf_abi_version": (C.c_int, []),
+    "bf_debug_fail_allocation_after": (C.c_int, [C.c_int32]),
     "bf_create": (C.c_int, [C.POINTER(C.c_void_p)]),
     "bf_destroy": (C.c_int, [C.c_void_p]),
     "bf_set_boundry_properties": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(_Object)]),

@@ -159,6 +159,10 @@ int bf_destroy(bf_solver* s);
 /* message of the last failed call on this thread */
 const char* bf_last_error(void);
 int bf_abi_version(void);
+/* Host-side fault injection for tests: after `n` further successful device
+ * allocations of the solver's buffers the next one fails as out of memory
+ * (BF_ERR_OUT_OF_MEMORY from the call that made it); n < 0 turns it off. */
+int bf_debug_fail_allocation_after(int32_t n);
 
 /* ---- boundary objects (LBM.h:60-82) ------------------------------------ */
 /* LBM::set_boundry_properties (all three overloads, LBM.cpp:1015-1065). id in 1..255. */

@@ -7,7 +7,12 @@
 //    asserted, LBM.cpp:429-437);
 //  * the Texture3D getters return bf::Field, a headless device buffer
 //    (pointer + shape) instead of a GL texture; copy_to_host() reads it back;
-//  * render2d_*/render3d_* are not provided (no graphics stack).
+//  * render3d_* write into a headless RGBA float device image (no graphics
+//    stack); render2d_* are not provided.
+//
+// Beyond the reference: bf::Adjoint, the differentiable channel flow as a
+// forward/backward pair (gradients of a drag / velocity-mismatch objective
+// with respect to a per-cell solid fraction and the inlet profile).
 #pragma once
 
 #include <cstdint>
@@ -349,5 +354,67 @@ inline std::vector<uint8_t> rasterize_mesh(const std::vector<float>& triangle_ve
     if (code != BF_OK) throw LBMError(code, bf_last_error());
     return mask;
 }
+
+// The discrete adjoint of a channel flow (bf_adjoint_*): forward() runs the
+// T-step solve with checkpoints and returns the objective J; backward()
+// returns dJ/ds per cell and dJ/du_in per (y, z) row of the last forward, in
+// FP64.  Parameters and the target are host arrays, x fastest.
+struct AdjointDesc {
+    ivec3 resolution = ivec3(512, 256, 1);
+    float relaxation_time = 0.6f;
+    VelocitySet velocity_set = D2Q9;   // D2Q9 (resolution.z = 1) or D3Q19 (periodic z)
+    int32_t steps = 2000;              // T
+    int32_t checkpoint_interval = 100; // K
+    float drag_weight = 1.0f;
+    float mismatch_weight = 1.0f;
+};
+
+class Adjoint {
+public:
+    using Desc = AdjointDesc;
+    explicit Adjoint(const Desc& d = Desc()) : n_((size_t)d.resolution.x * d.resolution.y * d.resolution.z),
+                                               rows_((size_t)d.resolution.y * d.resolution.z) {
+        bf_adjoint_desc c;
+        bf_adjoint_desc_default(&c);
+        c.resolution[0] = d.resolution.x; c.resolution[1] = d.resolution.y; c.resolution[2] = d.resolution.z;
+        c.relaxation_time = d.relaxation_time;
+        c.velocity_set = (int32_t)d.velocity_set;
+        c.steps = d.steps;
+        c.checkpoint_interval = d.checkpoint_interval;
+        c.drag_weight = d.drag_weight;
+        c.mismatch_weight = d.mismatch_weight;
+        check(bf_adjoint_create(&a_, &c));
+    }
+    ~Adjoint() { bf_adjoint_destroy(a_); }
+    Adjoint(const Adjoint&) = delete;
+    Adjoint& operator=(const Adjoint&) = delete;
+
+    // solid fraction s[N] in [0, 1] and inlet profile u_in[ny*nz]; an empty vector keeps the current one
+    void set_parameters(const std::vector<float>& solid_fraction, const std::vector<float>& inlet_velocity) {
+        if (!solid_fraction.empty() && solid_fraction.size() != n_) throw LBMError(BF_ERR_INVALID_ARGUMENT, "solid_fraction size");
+        if (!inlet_velocity.empty() && inlet_velocity.size() != rows_) throw LBMError(BF_ERR_INVALID_ARGUMENT, "inlet_velocity size");
+        check(bf_adjoint_set_parameters(a_, solid_fraction.empty() ? nullptr : solid_fraction.data(),
+                                        inlet_velocity.empty() ? nullptr : inlet_velocity.data()));
+    }
+    // target velocity u*[3N]
+    void set_target(const std::vector<float>& u_target) {
+        if (u_target.size() != 3 * n_) throw LBMError(BF_ERR_INVALID_ARGUMENT, "u_target size");
+        check(bf_adjoint_set_target(a_, u_target.data()));
+    }
+    double forward() {
+        double j = 0.0;
+        check(bf_adjoint_forward(a_, &j));
+        return j;
+    }
+    void backward(std::vector<double>& grad_solid_fraction, std::vector<double>& grad_inlet_velocity) {
+        grad_solid_fraction.resize(n_);
+        grad_inlet_velocity.resize(rows_);
+        check(bf_adjoint_backward(a_, grad_solid_fraction.data(), grad_inlet_velocity.data()));
+    }
+
+private:
+    bf_adjoint* a_ = nullptr;
+    size_t n_, rows_;
+};
 
 }  // namespace bf

@@ -10,17 +10,17 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIBDIR = os.path.join(ROOT, "boltzmannfluids_gb300")
 
 
-def build_demo(tmp_path):
-    exe = str(tmp_path / "lid_cavity_demo")
+def build_demo(tmp_path, name="lid_cavity_demo"):
+    exe = str(tmp_path / name)
     subprocess.check_call(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"),
-                           os.path.join(ROOT, "tests", "cpp", "lid_cavity_demo.cpp"), "-L", LIBDIR,
+                           os.path.join(ROOT, "tests", "cpp", name + ".cpp"), "-L", LIBDIR,
                            "-lbfgb300", f"-Wl,-rpath,{LIBDIR}", "-o", exe])
     return exe
 
 
 def test_facade_compiles_and_links(product_lib, tmp_path):
-    exe = build_demo(tmp_path)
-    assert os.path.exists(exe)
+    for name in ("lid_cavity_demo", "adjoint_demo"):
+        assert os.path.exists(build_demo(tmp_path, name))
 
 
 def test_facade_reports_missing_device(product_lib, tmp_path):
@@ -55,3 +55,30 @@ def test_facade_matches_python_api(product_lib, tmp_path):
     s.iterate_time(steps=steps, save=True)
     ref = s.get_velocity_density_texture().reshape(n, n, 4)
     assert np.array_equal(got, ref)
+
+
+@pytest.mark.gpu
+def test_facade_adjoint_matches_python_api(product_lib, tmp_path):
+    """bf::Adjoint's forward/backward pair gives the Python AdjointChannel's
+    objective and gradients bit for bit (the same library underneath)."""
+    from boltzmannfluids_gb300.adjoint import AdjointChannel, channel_setup
+    import boltzmannfluids_gb300 as bf
+    res, steps, K = (64, 32, 1), 120, 40
+    s, u_in, tgt = channel_setup(res)
+    inp = tmp_path / "in.bin"
+    with open(inp, "wb") as f:
+        for a in (s, u_in, tgt):
+            np.ascontiguousarray(a, np.float32).tofile(f)
+    out = tmp_path / "out.bin"
+    exe = build_demo(tmp_path, "adjoint_demo")
+    r = subprocess.run([exe, *map(str, res), str(steps), str(K), str(inp), str(out)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got = np.fromfile(out, np.float64)
+    n, rows = res[0] * res[1] * res[2], res[1] * res[2]
+    g = AdjointChannel(res, 0.6, bf.VelocitySet.D2Q9, steps, K)
+    g.set_parameters(s, u_in)
+    g.set_target(tgt)
+    j = g.forward()
+    gs, gu = g.backward()
+    assert got[0] == j
+    assert np.array_equal(got[1:1 + n], gs) and np.array_equal(got[1 + n:1 + n + rows], gu)

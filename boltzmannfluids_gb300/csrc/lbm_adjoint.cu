@@ -582,8 +582,8 @@ int bf_adjoint_create(bf_adjoint** out, const bf_adjoint_desc* d) {
         return e;
     };
     const size_t state = (size_t)Q * a->n * sizeof(float);
-    // the adjoint sweep (critical path) runs at the highest stream priority,
-    // the overlapped recomputation at the lowest
+    // the adjoint's one stream (forward, and the backward's merged sweep and
+    // recomputation launches) runs at the highest stream priority
     int prio_low = 0, prio_high = 0;
     cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
     cudaError_t e = cudaStreamCreateWithPriority(&a->stream, cudaStreamNonBlocking, prio_high);

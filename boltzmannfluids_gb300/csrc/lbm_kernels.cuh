@@ -1,10 +1,20 @@
 // lbm_kernels.cuh -- sm_103a kernels of the lattice Boltzmann update.
 //
-// One thread per cell, threads of a block run along x, the DDF is one
-// structure-of-arrays buffer (population plane i at f + i*stride), so every
-// population load/store of a warp touches 32 consecutive elements.
+// Threads of a block run along x and the DDF is one structure-of-arrays
+// buffer (population plane i at f + i*stride), so every population
+// load/store of a warp touches consecutive elements.  The kernels:
+//   step_kernel          generic fused stream+collide, one thread per cell
+//   fast_step_kernel     periodic boxes, one thread per cell
+//   fast2_step_kernel    periodic boxes, 16-bit storage, two cells per thread
+//   masked_mixed_kernel  objects, open faces, thermal lattice: plain cells in
+//                        the fast cell update, listed special cells in
+//                        blocks of their own (masked_step_kernel: one pass)
+//   stream_kernel, stream_thermal_kernel, init_kernel, ... the reference's
+//                        other passes
+// All evaluate the same canonical expression tree (below), so they agree
+// with one another and with the oracle bit for bit.
 //
-// step_kernel is the fused stream+collide of the reference's esoteric-pull
+// The update is the fused stream+collide of the reference's esoteric-pull
 // mode (collide.comp main, :676-794).  The AA pattern follows
 // collide.comp:244-369: on an even step a cell reads population i from
 // (x - c_i, slot i) and writes its post-collision population i to

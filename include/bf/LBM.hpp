@@ -96,9 +96,13 @@ public:
     // call advances one tick (the reference's behaviour with tps <= 0)
     void iterate_time(float target_tick_per_second = 0) {
         (void)target_tick_per_second;
+        sync_knobs();
         check(bf_iterate_time(s_, 1, 1));
     }
-    void iterate_time_steps(int32_t steps, bool save_fields = true) { check(bf_iterate_time(s_, steps, save_fields)); }
+    void iterate_time_steps(int32_t steps, bool save_fields = true) {
+        sync_knobs();
+        check(bf_iterate_time(s_, steps, save_fields));
+    }
     int32_t get_total_ticks_elapsed() {
         int64_t t = 0;
         check(bf_get_total_ticks_elapsed(s_, &t));
@@ -135,6 +139,7 @@ public:
                     T[k] = p.temperature;
                     ids[k] = p.boundry_id;
                 }
+        thermal_relaxation_time = 2.0f;  // initialize_fields resets it (LBM.cpp:461)
         bf_init_desc d;
         bf_init_desc_default(&d);
         d.resolution[0] = resolution.x; d.resolution[1] = resolution.y; d.resolution[2] = resolution.z;
@@ -155,6 +160,7 @@ public:
         d.thermal_init_equilibrium = thermal_init_equilibrium;
         d.two_buffer_fixed = two_buffer_fixed;
         check(bf_initialize_fields(s_, &d, rho.data(), u.data(), f.data(), T.data(), ids.data()));
+        sent_ = {velocity_limit, velocity_limit_extreme, thermal_relaxation_time, thermal_expension_coeficient};
         velocity_set_ = velocity_set;
         fp_ = fp_accuracy;
         periodic_[0] = periodic_x; periodic_[1] = periodic_y; periodic_[2] = periodic_z;
@@ -286,6 +292,23 @@ public:
     bf_solver* handle() { return s_; }
 
 private:
+    // the public knobs are uniforms the reference sets at every dispatch
+    // (LBM.cpp:1590-1591, :1612-1613): changed values reach the solver
+    // before the next step
+    struct Knobs { float vlim, vext, tau_t, beta; };
+    Knobs sent_{0.25f, 0.30f, 2.0f, 0.5f};
+    void sync_knobs() {
+        if (velocity_limit != sent_.vlim || velocity_limit_extreme != sent_.vext) {
+            check(bf_set_velocity_limits(s_, velocity_limit, velocity_limit_extreme));
+            sent_.vlim = velocity_limit;
+            sent_.vext = velocity_limit_extreme;
+        }
+        if (thermal_relaxation_time != sent_.tau_t || thermal_expension_coeficient != sent_.beta) {
+            check(bf_set_thermal_parameters(s_, thermal_relaxation_time, thermal_expension_coeficient));
+            sent_.tau_t = thermal_relaxation_time;
+            sent_.beta = thermal_expension_coeficient;
+        }
+    }
     Field field(int kind) {
         Field f;
         f.owner = s_;

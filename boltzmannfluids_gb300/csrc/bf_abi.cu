@@ -121,6 +121,7 @@ struct bf_solver {
     // buffer roles (LBM.h:280-291)
     int lat0_src = 1, th0_src = 1, psi0_src = 1;
     int64_t ticks = 0;
+    int64_t fields_tick = 0;  // tick of the step whose fields vel_den / force_temp hold
     bool last_saved = false;
     // graphs keyed by the state that repeats every two steps
     std::map<int, cudaGraphExec_t> graphs;
@@ -575,6 +576,7 @@ int run_steps(bf_solver* s, int n, bool save_last) {
         if (e != cudaSuccess) return fail(BF_ERR_CUDA, std::string("step launch: ") + cudaGetErrorString(e));
         s->ticks++;
         s->last_saved = need_save_here;
+        if (need_save_here) s->fields_tick = s->ticks;
         remaining--;
     }
     return BF_OK;
@@ -998,6 +1000,7 @@ int bf_initialize_fields(bf_solver* s, const bf_init_desc* d, const float* densi
     if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? BF_ERR_OUT_OF_MEMORY : BF_ERR_CUDA, std::string("first pass: ") + cudaGetErrorString(e));
     BF_CUDA(cudaStreamSynchronize(s->stream));
     s->last_saved = true;
+    s->fields_tick = 0;
     s->initialized = true;
     return BF_OK;
 }
@@ -1008,6 +1011,12 @@ int bf_iterate_time(bf_solver* s, int32_t n_steps, int32_t save_fields) {
     if (n_steps < 0) return fail(BF_ERR_INVALID_ARGUMENT, "iterate_time(): negative step count");
     cudaSetDevice(s->device);
     return run_steps(s, n_steps, save_fields != 0);
+}
+
+int bf_get_stream(bf_solver* s, void** stream) {
+    if (!s || !stream) return fail(BF_ERR_INVALID_ARGUMENT, "NULL argument");
+    *stream = s->stream;
+    return BF_OK;
 }
 
 int bf_synchronize(bf_solver* s, int32_t timeout_ms) {
@@ -1139,6 +1148,9 @@ int bf_get_field(bf_solver* s, int32_t kind, bf_field* out) {
     case BF_FIELD_THERMAL_POPULATIONS:
         if (!s->thermal) return fail(BF_ERR_INVALID_ARGUMENT, "get_field(): the flow is not thermal");
         out->device_ptr = th_src(s); out->components = s->QT; out->bytes_per_component = 4; out->bytes = (size_t)s->N * s->QT * 4; break;
+    case BF_FIELD_PSEUDOPOTENTIAL:
+        if (!s->desc.multiphase) return fail(BF_ERR_INVALID_ARGUMENT, "get_field(): the flow is not multiphase");
+        out->device_ptr = psi_src(s); out->components = 1; out->bytes_per_component = 4; out->bytes = (size_t)s->N * 4; break;
     default:
         return fail(BF_ERR_INVALID_ARGUMENT, "get_field(): unknown field kind");
     }
@@ -1190,6 +1202,7 @@ int bf_reduce(bf_solver* s, double out[5]) {
     // moments of the current state, as the next step would read them
     cudaError_t e = collide(s, true, false, true, true);
     if (e != cudaSuccess) return fail(BF_ERR_CUDA, std::string("reduce pass: ") + cudaGetErrorString(e));
+    s->fields_tick = s->ticks;  // the pass saves the current state's fields
     e = launch_reduce_finish(s->partials.as<double>(), s->n_blocks, s->red_out.as<double>(), s->stream);
     if (e != cudaSuccess) return fail(BF_ERR_CUDA, std::string("reduce finish: ") + cudaGetErrorString(e));
     BF_CUDA(cudaMemcpyAsync(out, s->red_out.p, 5 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
@@ -1307,9 +1320,140 @@ int bf_load_snapshot(bf_solver* s, const char* path) {
     std::fclose(fp);
     if (!ok) return fail(BF_ERR_IO, "load_snapshot(): truncated or mismatched snapshot");
     s->ticks = ticks;
+    s->fields_tick = ticks;
     s->lat0_src = st[0]; s->th0_src = st[1]; s->psi0_src = st[2];
     s->desc.relaxation_time = d.relaxation_time;
     clear_graphs(s);
+    return BF_OK;
+}
+
+// ---- macroscopic fields ---------------------------------------------------
+static const char kMacroMagic[8] = {'B', 'F', 'G', 'B', '3', 'M', 'C', '1'};
+struct MacroHeader {
+    char magic[8];
+    int32_t resolution[3];
+    int32_t thermal;
+    int64_t tick;
+};
+
+__global__ void bytes_to_ids_kernel(const uint8_t* __restrict__ b, uint32_t n, uint32_t* __restrict__ ids) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) ids[i] = b[i];
+}
+
+int bf_save_macroscopic(bf_solver* s, const char* path) {
+    if (!s || !path) return fail(BF_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (!s->initialized) return fail(BF_ERR_NOT_INITIALIZED, "save_current_tick_macroscopic(): initialize_fields has not run");
+    BF_CUDA(cudaStreamSynchronize(s->stream));
+    MacroHeader h{};
+    std::memcpy(h.magic, kMacroMagic, 8);
+    std::memcpy(h.resolution, s->desc.resolution, sizeof(h.resolution));
+    h.thermal = s->thermal ? 1 : 0;
+    h.tick = s->fields_tick;
+    const std::string tmp = std::string(path) + ".partial";
+    FILE* fp = std::fopen(tmp.c_str(), "wb");
+    if (!fp) return fail(BF_ERR_IO, std::string("save_current_tick_macroscopic(): cannot open ") + tmp);
+    bool ok = std::fwrite(&h, sizeof(h), 1, fp) == 1;
+    std::vector<char> buf;
+    for (const DeviceBuf* b : {&s->vel_den, &s->force_temp, &s->bnd_tex}) {
+        if (!ok) break;
+        buf.resize(b->bytes);
+        ok = cudaMemcpy(buf.data(), b->p, b->bytes, cudaMemcpyDeviceToHost) == cudaSuccess &&
+             std::fwrite(buf.data(), 1, b->bytes, fp) == b->bytes;
+    }
+    if (std::fclose(fp) != 0) ok = false;
+    if (ok && std::rename(tmp.c_str(), path) != 0) ok = false;
+    if (!ok) {
+        std::remove(tmp.c_str());
+        return fail(BF_ERR_IO, std::string("save_current_tick_macroscopic(): write failed for ") + path);
+    }
+    return BF_OK;
+}
+
+int bf_load_macroscopic(bf_solver* s, const char* path, int32_t target_tick) {
+    if (!s || !path) return fail(BF_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (!s->initialized) return fail(BF_ERR_NOT_INITIALIZED, "load_tick_macroscopic(): initialize_fields must run first");
+    cudaSetDevice(s->device);
+    BF_CUDA(cudaStreamSynchronize(s->stream));
+    const uint32_t N = s->N;
+    FILE* fp = std::fopen(path, "rb");
+    if (!fp) return fail(BF_ERR_IO, std::string("load_tick_macroscopic(): cannot open ") + path);
+    MacroHeader h{};
+    const uint64_t expect = sizeof(h) + (uint64_t)N * (16 + 16 + 1);
+    bool ok = std::fread(&h, sizeof(h), 1, fp) == 1 && std::memcmp(h.magic, kMacroMagic, 8) == 0;
+    if (ok) {
+        const bool sized = std::fseek(fp, 0, SEEK_END) == 0;
+        const long end = sized ? std::ftell(fp) : -1;
+        ok = sized && end >= 0 && (uint64_t)end == expect && std::fseek(fp, (long)sizeof(h), SEEK_SET) == 0;
+    }
+    if (!ok || std::memcmp(h.resolution, s->desc.resolution, sizeof(h.resolution)) != 0) {
+        std::fclose(fp);
+        return fail(BF_ERR_IO, "load_tick_macroscopic(): not a macroscopic file of this solver's resolution");
+    }
+    if (target_tick >= 0 && (int64_t)target_tick != h.tick) {
+        std::fclose(fp);
+        return fail(BF_ERR_INVALID_ARGUMENT, "load_tick_macroscopic(): the file holds tick " + std::to_string(h.tick) +
+                                                 ", not " + std::to_string(target_tick));
+    }
+    std::vector<float4> vd(N), ft(N);
+    ok = std::fread(vd.data(), 16, N, fp) == N && std::fread(ft.data(), 16, N, fp) == N;
+    std::fclose(fp);
+    if (!ok) return fail(BF_ERR_IO, "load_tick_macroscopic(): read failed");
+    std::vector<float> rho(N), u(3 * (size_t)N), T(N);
+    for (uint32_t c = 0; c < N; c++) {
+        rho[c] = vd[c].w;
+        u[3 * (size_t)c] = vd[c].x; u[3 * (size_t)c + 1] = vd[c].y; u[3 * (size_t)c + 2] = vd[c].z;
+        T[c] = ft[c].w;
+    }
+    DeviceBuf d_rho, d_u, d_ids, d_T;
+    BF_CUDA(d_rho.alloc((size_t)N * 4));
+    BF_CUDA(d_u.alloc((size_t)N * 12));
+    BF_CUDA(d_ids.alloc((size_t)N * 4));
+    BF_CUDA(cudaMemcpy(d_rho.p, rho.data(), (size_t)N * 4, cudaMemcpyHostToDevice));
+    BF_CUDA(cudaMemcpy(d_u.p, u.data(), (size_t)N * 12, cudaMemcpyHostToDevice));
+    // the solver's own boundary ids (its geometry is kept)
+    bytes_to_ids_kernel<<<(unsigned)((N + 255u) / 256u), 256, 0, s->stream>>>(s->bnd_tex.as<uint8_t>(), N,
+                                                                             d_ids.as<uint32_t>());
+    BF_CUDA(cudaGetLastError());
+    clear_graphs(s);
+    s->ticks = h.tick;
+    InitParams ip{};
+    ip.f = lat_src(s);
+    ip.stride = N;
+    ip.n_cells = N;
+    ip.rho = d_rho.as<float>();
+    ip.u = d_u.as<float>();
+    ip.ids = d_ids.as<uint32_t>();
+    ip.obj_kind = s->kinds.as<uint8_t>();
+    // an odd tick of the esoteric-pull step: the equilibrium goes where the odd step reads it
+    ip.odd = (s->desc.esoteric && (s->ticks & 1)) ? 1 : 0;
+    ip.nx = s->desc.resolution[0]; ip.ny = s->desc.resolution[1]; ip.nz = s->desc.resolution[2];
+    ip.flags = base_flags(s);
+    cudaError_t e;
+    switch (s->Q) {
+    case 9: e = launch_init<9>(ip, s->desc.storage, s->stream); break;
+    case 15: e = launch_init<15>(ip, s->desc.storage, s->stream); break;
+    case 19: e = launch_init<19>(ip, s->desc.storage, s->stream); break;
+    default: e = launch_init<27>(ip, s->desc.storage, s->stream); break;
+    }
+    if (e != cudaSuccess) return fail(BF_ERR_CUDA, std::string("load_tick_macroscopic(): init kernel: ") + cudaGetErrorString(e));
+    if (s->thermal) {
+        BF_CUDA(d_T.alloc((size_t)N * 4));
+        BF_CUDA(cudaMemcpy(d_T.p, T.data(), (size_t)N * 4, cudaMemcpyHostToDevice));
+        InitParams tp = ip;
+        tp.th = th_src(s);
+        tp.T = d_T.as<float>();
+        BF_CUDA(cudaMemsetAsync(tp.th, 0, (size_t)N * s->QT * 4, s->stream));
+        e = s->QT == 5 ? launch_init_thermal<5>(tp, s->stream) : launch_init_thermal<7>(tp, s->stream);
+        if (e != cudaSuccess) return fail(BF_ERR_CUDA, std::string("load_tick_macroscopic(): thermal init: ") + cudaGetErrorString(e));
+        BF_CUDA(cudaMemcpyAsync(th_tgt(s), th_src(s), (size_t)N * s->QT * 4, cudaMemcpyDeviceToDevice, s->stream));
+    }
+    // the fields of the loaded state, as initialize_fields saves them (LBM.cpp:502)
+    e = iterate_once(s, true, false, false);
+    if (e != cudaSuccess) return fail(BF_ERR_CUDA, std::string("load_tick_macroscopic(): first pass: ") + cudaGetErrorString(e));
+    BF_CUDA(cudaStreamSynchronize(s->stream));
+    s->last_saved = true;
+    s->fields_tick = s->ticks;
     return BF_OK;
 }
 

@@ -10,6 +10,7 @@
 // pointer (BF_FIELD_VELOCITY_DENSITY layout) and a host array for the sums.
 #include <cuda_runtime.h>
 
+#include <cstdint>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -88,6 +89,10 @@ extern "C" int bf_reduce_field_noalloc(const void* vel_den_device, size_t n_cell
         return fail(BF_ERR_INVALID_ARGUMENT, "bf_reduce_field_noalloc: " + std::to_string(n_cells) +
                                                  " cells exceed the fixed scratch capacity of " +
                                                  std::to_string(kMaxCells) + " cells");
+    // the kernel reads whole float4 cells: a pointer off a 16-byte boundary
+    // (an offset into some other buffer) would fault the context
+    if (reinterpret_cast<uintptr_t>(vel_den_device) % 16u != 0u)
+        return fail(BF_ERR_INVALID_ARGUMENT, "bf_reduce_field_noalloc: field pointer is not 16-byte aligned");
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return fail(BF_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));

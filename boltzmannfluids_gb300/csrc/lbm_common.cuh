@@ -128,32 +128,26 @@ __host__ __device__ constexpr int opp(int i) { return i == 0 ? 0 : ((i & 1) ? i 
 // ---------------------------------------------------------------------------
 enum Storage { ST_FP32 = 0, ST_FP16 = 1, ST_FP16S = 2, ST_FP16C = 3, ST_FP64 = 4 };
 
-// custom 16-bit "c16": 1 sign, 4 exponent, 11 mantissa bits = the top 15
-// bits of an FP32 scaled by 2^-114 (normal 2^(e-13)*(1+m/2048), subnormal
-// 2^-12*m/2048).  Encode: scale |f| by 2^-114, round the bit pattern to
-// nearest even at bit 12, saturate at the largest code (also for NaN/inf).
-__device__ __forceinline__ uint16_t encode_c16(float f) {
-    const uint32_t sign = (__float_as_uint(f) >> 16) & 0x8000u;
-    uint32_t b = __float_as_uint(__fmul_rn(fabsf(f), 0x1p-114f));
-    b = b + 0x7ffu + ((b >> 12) & 1u);
-    const uint32_t q = min(b >> 12, 0x7fffu);
-    return (uint16_t)(sign | q);
-}
-__device__ __forceinline__ float decode_c16(uint16_t h) {
-    const float a = __uint_as_float((uint32_t)(h & 0x7fffu) << 12);
-    return __uint_as_float(__float_as_uint(__fmul_rn(a, 0x1p114f)) | ((uint32_t)(h & 0x8000u) << 16));
-}
-
 template <int ST> struct Codec;
 // T: the stored element type; R: the arithmetic type of the update.
 // SHIFTED codecs store the shifted population g = f - w_i and the update
 // works on g directly (dec/enc), which drops the two +-w per population and
 // keeps the arithmetic on the small deviations; dec_f/enc_f convert from and
 // to f itself (initialisation, read-back, snapshots).
+// SCALE: the stored value is g * SCALE (a power of two).  raw_dec/raw_enc
+// convert without the scale: kernels that run the update on G = g * SCALE
+// (every equilibrium and source weight taken times SCALE, the density as
+// fma(sum G, 1/SCALE, 1), the momentum times 1/SCALE) get the same bits as
+// the update on g, because scaling by a power of two is exact in every
+// rounded operation.
 template <> struct Codec<ST_FP32> {
     using T = float;
     using R = float;
     static constexpr bool SHIFTED = false;
+    static constexpr float SCALE = 1.0f;
+    static constexpr int SCALE_EXP = 0;
+    __device__ __forceinline__ static R raw_dec(T v) { return dec(v, R(0)); }
+    __device__ __forceinline__ static T raw_enc(R v) { return enc(v, R(0)); }
     __device__ __forceinline__ static float dec(T v, float) { return v; }
     __device__ __forceinline__ static T enc(float v, float) { return v; }
     __device__ __forceinline__ static float dec_f(T v, float) { return v; }
@@ -163,6 +157,10 @@ template <> struct Codec<ST_FP16> {  // R16F: IEEE half of f
     using T = __half;
     using R = float;
     static constexpr bool SHIFTED = false;
+    static constexpr float SCALE = 1.0f;
+    static constexpr int SCALE_EXP = 0;
+    __device__ __forceinline__ static R raw_dec(T v) { return dec(v, R(0)); }
+    __device__ __forceinline__ static T raw_enc(R v) { return enc(v, R(0)); }
     __device__ __forceinline__ static float dec(T v, float) { return __half2float(v); }
     __device__ __forceinline__ static T enc(float v, float) { return __float2half_rn(v); }
     __device__ __forceinline__ static float dec_f(T v, float) { return __half2float(v); }
@@ -172,30 +170,40 @@ template <> struct Codec<ST_FP16S> {  // IEEE half of g = f - w
     using T = __half;
     using R = float;
     static constexpr bool SHIFTED = true;
+    static constexpr float SCALE = 1.0f;
+    static constexpr int SCALE_EXP = 0;
+    __device__ __forceinline__ static R raw_dec(T v) { return dec(v, R(0)); }
+    __device__ __forceinline__ static T raw_enc(R v) { return enc(v, R(0)); }
     __device__ __forceinline__ static float dec(T v, float) { return __half2float(v); }
     __device__ __forceinline__ static T enc(float g, float) { return __float2half_rn(g); }
     __device__ __forceinline__ static float dec_f(T v, float w) { return __fadd_rn(__half2float(v), w); }
     __device__ __forceinline__ static T enc_f(float v, float w) { return __float2half_rn(__fsub_rn(v, w)); }
 };
-template <> struct Codec<ST_FP16C> {  // custom 16-bit of g/w = (f - w)/w
-    using T = uint16_t;
+template <> struct Codec<ST_FP16C> {  // custom-scaled: IEEE half of g * 2^12
+    // g = f - w times 2^12 before the conversion: the scaled populations stay
+    // in the half's normal range down to |g| = 2^-26 (IEEE half of g itself,
+    // fp16s, loses precision below 2^-14), and |g| < 16 fits; one hardware
+    // conversion each way, as fp16s
+    using T = __half;
     using R = float;
     static constexpr bool SHIFTED = true;
-    // = decode_c16(v) * w with one rounding: the 15 code bits and the sign
-    // placed in an FP32 pattern from the sign-extended code (shift, one AND),
-    // times the exact constant w * 2^114
-    __device__ __forceinline__ static float dec(T v, float w) {
-        const uint32_t a = ((uint32_t)(int32_t)(int16_t)v << 12) & 0x87fff000u;
-        return __fmul_rn(__uint_as_float(a), w * 0x1p114f);
-    }
-    __device__ __forceinline__ static T enc(float g, float w) { return encode_c16(__fmul_rn(g, 1.0f / w)); }
-    __device__ __forceinline__ static float dec_f(T v, float w) { return fmaf(decode_c16(v), w, w); }
-    __device__ __forceinline__ static T enc_f(float v, float w) { return encode_c16(__fmul_rn(__fsub_rn(v, w), 1.0f / w)); }
+    static constexpr int SCALE_EXP = 12;
+    static constexpr float SCALE = float(1 << SCALE_EXP);
+    __device__ __forceinline__ static float raw_dec(T v) { return __half2float(v); }
+    __device__ __forceinline__ static T raw_enc(float v) { return __float2half_rn(v); }
+    __device__ __forceinline__ static float dec(T v, float) { return __fmul_rn(__half2float(v), 1.0f / SCALE); }
+    __device__ __forceinline__ static T enc(float g, float) { return __float2half_rn(__fmul_rn(g, SCALE)); }
+    __device__ __forceinline__ static float dec_f(T v, float w) { return __fmaf_rn(__half2float(v), 1.0f / SCALE, w); }
+    __device__ __forceinline__ static T enc_f(float v, float w) { return __float2half_rn(__fmul_rn(__fsub_rn(v, w), SCALE)); }
 };
 template <> struct Codec<ST_FP64> {  // FP64 reference stepper: populations and arithmetic in double
     using T = double;
     using R = double;
     static constexpr bool SHIFTED = false;
+    static constexpr float SCALE = 1.0f;
+    static constexpr int SCALE_EXP = 0;
+    __device__ __forceinline__ static R raw_dec(T v) { return dec(v, R(0)); }
+    __device__ __forceinline__ static T raw_enc(R v) { return enc(v, R(0)); }
     __device__ __forceinline__ static double dec(T v, double) { return v; }
     __device__ __forceinline__ static T enc(double v, double) { return v; }
     __device__ __forceinline__ static double dec_f(T v, double) { return v; }
@@ -350,6 +358,15 @@ struct InitParams {
     // thermal
     float* th;
     const float* T;
+    // odd != 0: write the equilibrium state in the slots an odd esoteric-pull
+    // step reads (a state loaded at an odd tick): population i of cell n goes
+    // to slot opp(i) of n + c_i (dropped outside the domain), and a cell whose
+    // source n - c_i lies outside takes its own opp(i) population in slot
+    // opp(i), the value the reference's odd step finds there.  nx, ny, nz and
+    // flags (F_PERIODIC_*) give the geometry.
+    int odd;
+    int nx, ny, nz;
+    uint32_t flags;
 };
 
 __device__ __forceinline__ uint32_t boundary_id(const uint32_t* __restrict__ bnd, int bits, uint64_t cell) {

@@ -25,6 +25,7 @@
 #include "lbm_common.cuh"
 
 #include <algorithm>
+#include <type_traits>
 
 namespace bf {
 
@@ -180,7 +181,9 @@ __device__ __forceinline__ R density_of(const R (&f)[Q]) {
 // |u| > limit is tested on |u|^2 against thresholds t = the largest float
 // whose IEEE square root does not exceed the limit, which decides exactly as
 // sqrt(|u|^2) > limit does; the square root is taken only for limited cells.
-template <int Q>
+// SCE: the populations are held times 2^SCE (scaled shifted storage): the
+// momentum takes r * 2^-SCE (exact), the force term r itself.
+template <int Q, int SCE = 0>
 __device__ __forceinline__ void velocity_and_limit(const float (&f)[Q], Moments& m, bool forced, float vlim,
                                                    float t_lim, float t_ext) {
     using L = Lattice<Q>;
@@ -195,9 +198,10 @@ __device__ __forceinline__ void velocity_and_limit(const float (&f)[Q], Moments&
         if (c.z) { const float t = c.z > 0 ? d : -d; jz = fz ? t : FADD(jz, t); fz = false; }
     }
     const float r = __fdiv_rn(1.0f, m.rho);
-    m.ux = FMUL(jx, r);
-    m.uy = FMUL(jy, r);
-    m.uz = FMUL(jz, r);
+    const float rj = SCE ? FMUL(r, 1.0f / float(1 << SCE)) : r;
+    m.ux = FMUL(jx, rj);
+    m.uy = FMUL(jy, rj);
+    m.uz = FMUL(jz, rj);
     if (forced) {
         const float h = FMUL(r, 0.5f);
         m.ux = FFMA(m.Fx, h, m.ux);
@@ -333,10 +337,16 @@ __device__ __forceinline__ Coef<double> coef_of(const StepParams& p, double) {
 // branches once per cell on the rare extreme case instead of selecting per
 // population); R = float is the canonical FP32 evaluation, R = double the
 // FP64 reference stepper.
-template <int Q, bool TRT, bool SRC, bool EXT, bool SH, class R, class Emit>
+// SCE (shifted storage only): f holds G = g * 2^SCE and every weight of the
+// shifted arithmetic is taken times 2^SCE, so that the emitted values are the
+// g update's times 2^SCE exactly.
+template <int Q, bool TRT, bool SRC, bool EXT, bool SH, int SCE = 0, class R, class Emit>
 __device__ __forceinline__ void collide_fixed(const R (&f)[Q], const MomentsT<R>& m, const Coef<R>& k, Emit emit) {
     using L = Lattice<Q>;
-    using W = LatticeW<Q, R>;
+    struct W {
+        __device__ __forceinline__ static constexpr R w(int i) { return LatticeW<Q, R>::w(i) * R(1 << SCE); }
+    };
+    static_assert(SH || SCE == 0, "scaled populations are shifted");
     const R one_m = FSUB(R(1), FMUL(uu_of(m.ux, m.uy, m.uz), k.R2h));
     const R fuR2 = SRC ? FMUL(FFMA(m.Fz, m.uz, FFMA(m.Fy, m.uy, FMUL(m.Fx, m.ux))), k.R2) : R(0);
     if (!TRT) {
@@ -668,11 +678,13 @@ __device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepP
     const uint32_t guard_mask = GUARD ? __ldg(p.nmask + n) : 0u;
     R f[Q];
 #pragma unroll
-    for (int i = 0; i < Q; i++) f[i] = C::dec(load(i, ptr_of), W::w(i));
+    for (int i = 0; i < Q; i++) f[i] = C::raw_dec(load(i, ptr_of));
     if (GUARD && guard_mask != 0u) return cs;
+    // the update runs on the stored values times 1/SCALE implied: G = g * SCALE
+    constexpr int SCE = C::SCALE_EXP;
     MomentsT<R> m;
     m.rho = density_of<Q>(f);
-    if (C::SHIFTED) m.rho = FADD(R(1), m.rho);  // sum of g plus sum of w
+    if (C::SHIFTED) m.rho = SCE ? FFMA(m.rho, R(1.0f / C::SCALE), R(1)) : FADD(R(1), m.rho);  // sum of g plus sum of w
     if (!(m.rho == m.rho)) atomicOr(p.err, 1u);
     m.rho = m.rho < R(0.01) ? R(0.01) : m.rho;
     constexpr bool F64 = sizeof(R) == 8;
@@ -689,12 +701,12 @@ __device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepP
         temperature = thermal_buoyancy<Q>(p, n, m);
     }
     if constexpr (F64) velocity_and_limit<Q>(f, m, FORCED, p.k64.vlim, p.k64.vlim_ext);
-    else velocity_and_limit<Q>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
+    else velocity_and_limit<Q, SCE>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
     if (p.flags & F_UPDATE) {
         const Coef<R> k = coef_of(p, R(0));
-        auto emit = [&](int i, R v) { *ptr_st(opp(i)) = C::enc(v, W::w(i)); };
-        if (m.out_ext) collide_fixed<Q, TRT, FORCED, true, C::SHIFTED>(f, m, k, emit);
-        else collide_fixed<Q, TRT, FORCED, false, C::SHIFTED>(f, m, k, emit);
+        auto emit = [&](int i, R v) { *ptr_st(opp(i)) = C::raw_enc(v); };
+        if (m.out_ext) collide_fixed<Q, TRT, FORCED, true, C::SHIFTED, SCE>(f, m, k, emit);
+        else collide_fixed<Q, TRT, FORCED, false, C::SHIFTED, SCE>(f, m, k, emit);
     }
     if constexpr (MP && !F64) {
         // psi of this step's density for the next step (collide.comp:763-769)
@@ -817,19 +829,21 @@ __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, i
     };
     auto to16 = [](uint32_t v) -> T { const unsigned short u = (unsigned short)v; T t; memcpy(&t, &u, 2); return t; };
     auto bits16 = [](T t) -> uint32_t { unsigned short u; memcpy(&u, &t, 2); return u; };
-    // cell a's populations of the paired directions until cell b's are known:
-    // encoded (fp16c), or as floats that one cvt.rn.f16x2.f32 converts
-    // together with cell b's (fp16s; the same rounding as two conversions)
+    // cell a's populations of the paired directions until cell b's are known,
+    // as floats that one cvt.rn.f16x2.f32 converts together with cell b's
+    // (IEEE half storages; the same rounding as two conversions)
     uint32_t keep[Q];
     const Coef<float> k = coef_of(p, 0.0f);
+    // the update runs on the stored values: G = g * SCALE for scaled storage
+    constexpr int SCE = C::SCALE_EXP;
 #pragma unroll
     for (int half = 0; half < 2; half++) {
         float f[Q];
 #pragma unroll
-        for (int i = 0; i < Q; i++) f[i] = C::dec(to16(half ? (ld[i] >> 16) : ld[i]), L::w(i));
+        for (int i = 0; i < Q; i++) f[i] = C::raw_dec(to16(half ? (ld[i] >> 16) : ld[i]));
         Moments m;
         m.rho = density_of<Q>(f);
-        if (C::SHIFTED) m.rho = FADD(1.0f, m.rho);
+        if (C::SHIFTED) m.rho = SCE ? FFMA(m.rho, 1.0f / C::SCALE, 1.0f) : FADD(1.0f, m.rho);
         if (!(m.rho == m.rho)) atomicOr(p.err, 1u);
         m.rho = m.rho < 0.01f ? 0.01f : m.rho;
         m.Fx = FORCED ? p.fconst[0] : 0.f;
@@ -843,10 +857,10 @@ __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, i
             const int oxp = half ? (x + 2 == nx ? 1 - nx : 1) : 1;
             psi_self = sc_force<Q>(p, n + half, oxm, oxp, oym, oyp, ozm, ozp, m);
         }
-        velocity_and_limit<Q>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
+        velocity_and_limit<Q, SCE>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
         auto emit = [&](int i, float v) {
             const int o = opp(i);
-            if constexpr (ST == ST_FP16S) {
+            if constexpr (std::is_same<T, __half>::value) {
                 if (paired(o)) {
                     if (half == 0) {
                         keep[i] = __float_as_uint(v);
@@ -859,7 +873,7 @@ __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, i
                     return;
                 }
             }
-            const uint32_t e = bits16(C::enc(v, L::w(i)));
+            const uint32_t e = bits16(C::raw_enc(v));
             if (paired(o)) {
                 if (half == 0) keep[i] = e;
                 else *reinterpret_cast<unsigned int*>(dst_a(i)) = keep[i] | (e << 16);
@@ -867,8 +881,8 @@ __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, i
                 *reinterpret_cast<unsigned short*>(half ? dst_b(i) : dst_a(i)) = (unsigned short)e;
             }
         };
-        if (m.out_ext) collide_fixed<Q, TRT, FORCED, true, C::SHIFTED>(f, m, k, emit);
-        else collide_fixed<Q, TRT, FORCED, false, C::SHIFTED>(f, m, k, emit);
+        if (m.out_ext) collide_fixed<Q, TRT, FORCED, true, C::SHIFTED, SCE>(f, m, k, emit);
+        else collide_fixed<Q, TRT, FORCED, false, C::SHIFTED, SCE>(f, m, k, emit);
         if constexpr (MP) {
             // psi of this step's density for the next step (collide.comp:763-769)
             if (!(p.flags & F_MEASURE)) p.psi_tgt[n + half] = psi_self;
@@ -1448,12 +1462,42 @@ __global__ void init_kernel(const __grid_constant__ InitParams p) {
     // w*rho*(1 + 3*cu + 9*cu^2/2 - 3*uu/2) with the shader's literal constants
     // and operation order, rounded operations only (init runs once)
     const R uu = feq_init_dot(ux, uy, uz, ux, uy, uz);
+    if (!p.odd) {
+#pragma unroll
+        for (int i = 0; i < Q; i++) {
+            const Dir c = L::c(i);
+            const R w = LatticeW<Q, R>::w(i);
+            const R cu = feq_init_dot(R(c.x), R(c.y), R(c.z), ux, uy, uz);
+            F[i * p.stride + n] = C::enc_f(feq_init_literal(w, r, cu, uu), w);
+        }
+        return;
+    }
+    const int x = (int)(n % (uint64_t)p.nx), y = (int)((n / (uint64_t)p.nx) % (uint64_t)p.ny),
+              z = (int)(n / ((uint64_t)p.nx * (uint64_t)p.ny));
 #pragma unroll
     for (int i = 0; i < Q; i++) {
         const Dir c = L::c(i);
         const R w = LatticeW<Q, R>::w(i);
         const R cu = feq_init_dot(R(c.x), R(c.y), R(c.z), ux, uy, uz);
-        F[i * p.stride + n] = C::enc_f(feq_init_literal(w, r, cu, uu), w);
+        const T v = C::enc_f(feq_init_literal(w, r, cu, uu), w);
+        // destination n + c_i: read there as population i at the odd step
+        int dx = x + c.x, dy = y + c.y, dz = z + c.z;
+        bool dopen;
+        coords_wrap<Q>(dx, dy, dz, p.nx, p.ny, p.nz, dopen, p.flags);
+        if (!dopen)
+            F[(uint64_t)opp(i) * p.stride + (uint64_t)dx + (uint64_t)p.nx * ((uint64_t)dy + (uint64_t)p.ny * (uint64_t)dz)] = v;
+        int sx = x - c.x, sy = y - c.y, sz = z - c.z;
+        bool sopen;
+        coords_wrap<Q>(sx, sy, sz, p.nx, p.ny, p.nz, sopen, p.flags);
+        if (sopen) {
+            // slot opp(i) of n is read as population i, whose source n - c_i is
+            // outside: it holds the cell's own population opp(i)
+            const int o = opp(i);
+            const Dir co = L::c(o);
+            const R wo = LatticeW<Q, R>::w(o);
+            const R cuo = feq_init_dot(R(co.x), R(co.y), R(co.z), ux, uy, uz);
+            F[(uint64_t)o * p.stride + n] = C::enc_f(feq_init_literal(wo, r, cuo, uu), wo);
+        }
     }
 }
 

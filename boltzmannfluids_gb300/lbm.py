@@ -11,6 +11,7 @@ from __future__ import annotations
 import ctypes as C
 import enum
 import os
+import time
 from dataclasses import dataclass, field
 from typing import Callable, Optional, Sequence
 
@@ -31,7 +32,7 @@ class VelocitySet(enum.IntEnum):
 class FloatingPointAccuracy(enum.IntEnum):
     """DDF storage.  fp32/fp16 are the reference's FloatingPointAccuracy
     (FloatingPointAccuracy.h:6-9, fp16 = R16F lattice); fp16s (shifted IEEE
-    half) and fp16c (custom 1-4-11 format of (f-w)/w) are extensions; fp64 is
+    half of f-w) and fp16c (custom-scaled: IEEE half of (f-w)*2^12) are extensions; fp64 is
     the FP64 accuracy reference stepper (periodic boxes, no objects)."""
     fp32 = 0
     fp16 = 1
@@ -62,6 +63,7 @@ class Field(enum.IntEnum):
     force_temperature = 2
     populations = 3
     thermal_populations = 4
+    pseudopotential = 5
 
 
 class LBMError(RuntimeError):
@@ -130,6 +132,7 @@ ABI = {
     "bf_initialize_fields": (C.c_int, [C.c_void_p, C.POINTER(_InitDesc), C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p, C.c_void_p]),
     "bf_iterate_time": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "bf_get_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "bf_synchronize": (C.c_int, [C.c_void_p, C.c_int32]),
     "bf_get_total_ticks_elapsed": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
     "bf_get_resolution": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
@@ -149,6 +152,8 @@ ABI = {
     "bf_reduce": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "bf_save_snapshot": (C.c_int, [C.c_void_p, C.c_char_p]),
     "bf_load_snapshot": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "bf_save_macroscopic": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "bf_load_macroscopic": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int32]),
     "bf_benchmark_steps": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_float)]),
     "bf_get_velosity_vectors": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p, C.POINTER(C.c_int32)]),
     "bf_bits_per_boundry": (C.c_int, [C.c_int32, C.POINTER(C.c_int32)]),
@@ -272,6 +277,12 @@ class LBM:
         self.two_buffer_fixed = False
         self._res = (0, 0, 0)
         self._vs = VelocitySet.D2Q9
+        # knob values the solver holds (sent at initialisation, then when changed)
+        self._sent = None
+        # LBM::iterate_time's wall-clock state (LBM.cpp:220-240): epoch before the first call
+        self._first_iteration = True
+        self._simulation_begin = 0.0
+        self._last_visual_update = 0.0
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -384,15 +395,71 @@ class LBM:
 
         arrs = (prep(density, 1, np.float32), prep(velocity, 3, np.float32), prep(force, 3, np.float32),
                 prep(temperature, 1, np.float32), prep(boundry_id, 1, np.uint32))
+        # initialize_fields resets the thermal relaxation time to 2 (LBM.cpp:461);
+        # a value set afterwards reaches the solver before the next step
+        self.thermal_relaxation_time = 2.0
         d = self._desc((rx, ry, rz), relaxation_time, periodic, velocity_set, fp_accuracy, is_flow_multiphase)
         _check(self._lib.bf_initialize_fields(self._h, C.byref(d), *[_ptr(a) for a in arrs]))
         self._res = (rx, ry, rz)
         self._vs = VelocitySet(int(velocity_set))
+        self._sent = self._knobs()
+
+    def _knobs(self):
+        return (float(self.velocity_limit), float(self.velocity_limit_extreme), float(self.thermal_relaxation_time),
+                float(self.thermal_expansion_coefficient))
+
+    def _sync_knobs(self):
+        """The public knobs are uniforms the reference sets at every dispatch
+        (LBM.cpp:1590-1591, :1612-1613): changed values reach the solver
+        before the next step.  An invalid thermal relaxation time (<= 0.5)
+        raises here, and again at every later step until it is fixed."""
+        if self._sent is None:
+            return
+        k = self._knobs()
+        if k[:2] != self._sent[:2]:
+            _check(self._lib.bf_set_velocity_limits(self._h, k[0], k[1]))
+            self._sent = k[:2] + self._sent[2:]
+        if k[2:] != self._sent[2:]:
+            _check(self._lib.bf_set_thermal_parameters(self._h, k[2], k[3]))
+            self._sent = self._sent[:2] + k[2:]
 
     # ---- time (LBM.h:34-38) -------------------------------------------
-    def iterate_time(self, target_tick_per_second: float = 0, steps: int = 1, save: bool = True):
-        """One (or `steps`) LBM::iterate_time ticks; `save` writes the macroscopic fields on the last."""
-        _check(self._lib.bf_iterate_time(self._h, int(steps), int(bool(save))))
+    def iterate_time(self, target_tick_per_second: float = 0, steps: Optional[int] = None,
+                     save: Optional[bool] = None):
+        """LBM::iterate_time (LBM.cpp:220-240) when called without `steps` and
+        `save`: one tick, unless a positive target_tick_per_second is already
+        met by the ticks run since the first call; the macroscopic fields are
+        saved on the first tick and then only when more than 1000/60 ms (whole
+        milliseconds) have passed since the last save.  With `steps` and/or
+        `save`: that many ticks (default 1) at once, saving the fields on the
+        last one when `save` (default True)."""
+        self._sync_knobs()
+        if steps is None and save is None:
+            now = time.time()
+            if self._first_iteration:
+                self._simulation_begin = now
+                self._last_visual_update = now
+            targeted = int(target_tick_per_second * self.get_total_time_elapsed() / 1000.0)
+            if target_tick_per_second <= 0 or self.get_total_ticks_elapsed() < targeted or self._first_iteration:
+                since_ms = int((time.time() - self._last_visual_update) * 1000.0)
+                do_save = self._first_iteration or since_ms > 1000.0 / 60
+                if do_save:
+                    self._last_visual_update = time.time()
+                _check(self._lib.bf_iterate_time(self._h, 1, int(do_save)))
+            self._first_iteration = False
+            return
+        _check(self._lib.bf_iterate_time(self._h, int(1 if steps is None else steps),
+                                         int(True if save is None else bool(save))))
+
+    def get_total_time_elapsed(self) -> float:
+        """Milliseconds since the first LBM-style iterate_time call (LBM.cpp:247-250)."""
+        return (time.time() - self._simulation_begin) * 1000.0
+
+    def get_stream(self) -> int:
+        """The solver's CUDA stream handle (a cudaStream_t as an integer)."""
+        v = C.c_void_p()
+        _check(self._lib.bf_get_stream(self._h, C.byref(v)))
+        return v.value or 0
 
     def synchronize(self, timeout_ms: int = 0):
         _check(self._lib.bf_synchronize(self._h, int(timeout_ms)))
@@ -494,6 +561,11 @@ class LBM:
         q = self.get_velocity_set_vector_count()
         return self._copy(Field.populations, np.float32, q).reshape(q, -1)
 
+    def get_pseudopotential(self) -> np.ndarray:
+        """(nz, ny, nx) float32 psi = 1 - exp(-rho_eff) that the next Shan-Chen step reads."""
+        rx, ry, rz = self._res
+        return self._copy(Field.pseudopotential, np.float32, 1).reshape(rz, ry, rx)
+
     def get_thermal_populations(self) -> np.ndarray:
         q = 5 if self._vs == VelocitySet.D2Q9 else 7
         return self._copy(Field.thermal_populations, np.float32, q).reshape(q, -1)
@@ -525,9 +597,20 @@ class LBM:
     def load_tick_mesoscropic(self, path, target_tick: int = -1):
         _check(self._lib.bf_load_snapshot(self._h, os.fsencode(str(path))))
 
+    def save_current_tick_macroscopic(self, path):
+        """u/rho, F/T and boundary ids of the last saved tick, with that tick (bf_save_macroscopic)."""
+        _check(self._lib.bf_save_macroscopic(self._h, os.fsencode(str(path))))
+
+    def load_tick_macroscopic(self, path, target_tick: int = -1):
+        """Restarts from a macroscopic file: equilibrium populations of its
+        fields, the tick counter at its tick (bf_load_macroscopic)."""
+        self._sync_knobs()
+        _check(self._lib.bf_load_macroscopic(self._h, os.fsencode(str(path)), int(target_tick)))
+
     def benchmark_steps(self, steps: int) -> float:
         """Runs `steps` steps bracketed by CUDA events on the solver's stream; returns milliseconds."""
         ms = C.c_float()
+        self._sync_knobs()
         _check(self._lib.bf_benchmark_steps(self._h, int(steps), C.byref(ms)))
         return ms.value
 

@@ -65,7 +65,6 @@ def rayleigh_benard(res, ra=1e5, pr=0.71, kappa=0.008, beta=0.5, seed=5, storage
     s.is_collide_esoteric = True
     s.boundary_mode = bf.BoundaryMode.bounce_back
     s.collision = bf.Collision.trt
-    s.thermal_relaxation_time = tau_t
     s.thermal_expansion_coefficient = beta
     s.thermal_init_equilibrium = True
     s.set_boundry_properties(1, velocity_translational=(0, 0, 0), temperature=1.0)
@@ -73,6 +72,9 @@ def rayleigh_benard(res, ra=1e5, pr=0.71, kappa=0.008, beta=0.5, seed=5, storage
     s.initialize_fields_from_arrays(res, tau, force=force, temperature=temp, boundry_id=ids,
                                     periodic=(True, True, False), velocity_set=bf.VelocitySet.D3Q19,
                                     fp_accuracy=storage)
+    # initialisation resets the thermal relaxation time to 2 (LBM.cpp:461);
+    # the flow's value takes effect from the first step
+    s.thermal_relaxation_time = tau_t
     return s, kappa, h
 
 

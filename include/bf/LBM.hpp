@@ -15,6 +15,7 @@
 // with respect to a per-cell solid fraction and the inlet profile).
 #pragma once
 
+#include <chrono>
 #include <cstdint>
 #include <functional>
 #include <stdexcept>
@@ -92,12 +93,27 @@ public:
     LBM& operator=(const LBM&) = delete;
 
     // ---- simulation controls (LBM.h:34-38) ----
-    // target_tick_per_second is accepted for signature compatibility; every
-    // call advances one tick (the reference's behaviour with tps <= 0)
+    // LBM::iterate_time (LBM.cpp:220-240): advances one tick unless a
+    // positive target_tick_per_second is already met by the ticks run since
+    // the first call; saves the macroscopic fields on the first tick and then
+    // only when more than 1000/60 ms (whole milliseconds) have passed since
+    // the last save, as the reference's visual update does
     void iterate_time(float target_tick_per_second = 0) {
-        (void)target_tick_per_second;
-        sync_knobs();
-        check(bf_iterate_time(s_, 1, 1));
+        const auto now = std::chrono::system_clock::now();
+        if (first_iteration_) {
+            simulation_begin_ = now;
+            last_visual_update_ = now;
+        }
+        const size_t targeted_tick_count = (size_t)(target_tick_per_second * get_total_time_elapsed().count() / 1000.0f);
+        if (target_tick_per_second <= 0 || (size_t)get_total_ticks_elapsed() < targeted_tick_count || first_iteration_) {
+            const auto since = std::chrono::system_clock::now() - last_visual_update_;
+            const bool save = first_iteration_ ||
+                              std::chrono::duration_cast<std::chrono::milliseconds>(since).count() > 1000.0 / 60;
+            if (save) last_visual_update_ = std::chrono::system_clock::now();
+            sync_knobs();
+            check(bf_iterate_time(s_, 1, save ? 1 : 0));
+        }
+        first_iteration_ = false;
     }
     void iterate_time_steps(int32_t steps, bool save_fields = true) {
         sync_knobs();
@@ -107,6 +123,12 @@ public:
         int64_t t = 0;
         check(bf_get_total_ticks_elapsed(s_, &t));
         return (int32_t)t;
+    }
+    // wall-clock time since the first iterate_time call (LBM.cpp:247-250;
+    // measured from the clock's epoch before that call, as the reference's
+    // default-constructed time point does)
+    std::chrono::duration<double, std::milli> get_total_time_elapsed() {
+        return std::chrono::system_clock::now() - simulation_begin_;
     }
     ivec3 get_resolution() {
         int32_t r[3];
@@ -241,6 +263,14 @@ public:
         (void)target_tick;
         check(bf_load_snapshot(s_, path.c_str()));
     }
+    // the macroscopic fields (u/rho, F/T, boundary ids) of the last saved tick
+    void save_current_tick_macroscopic(const std::string& path) { check(bf_save_macroscopic(s_, path.c_str())); }
+    // restart from a macroscopic file: equilibrium populations of its fields,
+    // the tick counter set to its tick (target_tick >= 0 must match it)
+    void load_tick_macroscopic(const std::string& path, int32_t target_tick = -1) {
+        sync_knobs();
+        check(bf_load_macroscopic(s_, path.c_str(), target_tick));
+    }
 
     // FP64 {mass, momentum x, y, z, kinetic energy} of the current state (extension)
     std::vector<double> reduce() {
@@ -303,6 +333,8 @@ private:
             sent_.vlim = velocity_limit;
             sent_.vext = velocity_limit_extreme;
         }
+        // an invalid value (tau_T <= 0.5) throws here, and again at every
+        // later step until the knob holds a valid value
         if (thermal_relaxation_time != sent_.tau_t || thermal_expension_coeficient != sent_.beta) {
             check(bf_set_thermal_parameters(s_, thermal_relaxation_time, thermal_expension_coeficient));
             sent_.tau_t = thermal_relaxation_time;
@@ -321,6 +353,9 @@ private:
         return fl;
     }
     bf_solver* s_ = nullptr;
+    bool first_iteration_ = true;
+    std::chrono::system_clock::time_point simulation_begin_{};
+    std::chrono::system_clock::time_point last_visual_update_{};
     VelocitySet velocity_set_ = D2Q9;
     FloatingPointAccuracy fp_ = fp32;
     bool periodic_[3] = {true, true, true};

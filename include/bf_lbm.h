@@ -46,8 +46,11 @@ typedef enum { BF_D2Q9 = 2, BF_D3Q15 = 3, BF_D3Q19 = 4, BF_D3Q27 = 5 } bf_veloci
 /* DDF storage.  BF_STORE_FP16 is the reference's FloatingPointAccuracy::fp16
  * (an R16F lattice: IEEE half of f itself, LBM.cpp:446-449);
  * BF_STORE_FP16S stores IEEE half of the shifted population f_i - w_i;
- * BF_STORE_FP16C stores (f_i - w_i)/w_i in a custom 1-4-11 16-bit float
- * (exponent range 2^-12..2^2, subnormals to 2^-23, saturating).
+ * BF_STORE_FP16C ("custom-scaled") stores the IEEE half of (f_i - w_i) * 2^12:
+ * the shifted populations keep the half's 11-bit relative precision down to
+ * |f_i - w_i| = 2^-26 (fp16s turns subnormal below 2^-14); |f_i - w_i| must
+ * stay below 16 (beyond it the half overflows and the step reports
+ * BF_ERR_UNSTABLE).
  * Arithmetic is FP32 in these four modes.
  * BF_STORE_FP64 (no counterpart in the reference) is the accuracy reference
  * stepper: FP64 populations and FP64 arithmetic in the same operation order
@@ -84,7 +87,10 @@ typedef enum {
     BF_FIELD_BOUNDARY = 1,         /* uint8 boundary id per cell: get_boundry_texture, LBM.h:98 */
     BF_FIELD_FORCE_TEMPERATURE = 2,/* float4 (F.xyz, T) per cell: get_force_temperature_texture, LBM.h:99 */
     BF_FIELD_POPULATIONS = 3,      /* float per (population, cell), SoA i*N+cell, decoded to FP32 */
-    BF_FIELD_THERMAL_POPULATIONS = 4 /* float per (population, cell), SoA */
+    BF_FIELD_THERMAL_POPULATIONS = 4, /* float per (population, cell), SoA */
+    BF_FIELD_PSEUDOPOTENTIAL = 5   /* float psi = 1 - exp(-rho_eff) per cell, the Shan-Chen field the
+                                      next step reads (the reference's multiphase density texture,
+                                      LBM.cpp:848-866, holds rho_eff) */
 } bf_field_kind;
 
 typedef struct bf_solver bf_solver;
@@ -193,6 +199,9 @@ int bf_initialize_fields(bf_solver* s, const bf_init_desc* desc,
  * launched from a captured CUDA graph per batch; the call returns once the
  * work is queued (use bf_synchronize to wait). */
 int bf_iterate_time(bf_solver* s, int32_t n_steps, int32_t save_fields);
+/* the handle's CUDA stream (a cudaStream_t, created non-blocking): work a
+ * caller enqueues on it runs after the solver's queued steps */
+int bf_get_stream(bf_solver* s, void** stream);
 /* waits for the handle's stream; gives up with BF_ERR_TIMEOUT after timeout_ms
  * (<= 0: wait without limit), and returns BF_ERR_UNSTABLE if a step saw NaN. */
 int bf_synchronize(bf_solver* s, int32_t timeout_ms);
@@ -237,8 +246,23 @@ int bf_reduce(bf_solver* s, double out[5]);
 int bf_benchmark_steps(bf_solver* s, int32_t n_steps, float* ms);
 
 /* ---- snapshots (LBM.h:123-126, declared but never defined upstream) ------ */
+/* mesoscopic (LBM::save_current_tick_mesoscropic / load_tick_mesoscropic,
+ * LBM.h:124, :126): the whole state -- populations, thermal and
+ * pseudopotential buffers, the tick -- restored exactly */
 int bf_save_snapshot(bf_solver* s, const char* path);
 int bf_load_snapshot(bf_solver* s, const char* path);
+/* macroscopic (LBM::save_current_tick_macroscopic, LBM.h:123): the fields of
+ * the last saved step -- u/rho, F/T and the boundary ids per cell -- and
+ * that step's tick, written through a temporary file renamed when complete */
+int bf_save_macroscopic(bf_solver* s, const char* path);
+/* LBM::load_tick_macroscopic (LBM.h:125): the solver (initialised with the
+ * file's resolution; geometry, objects and knobs are kept) restarts from the
+ * file's fields: every cell's populations become the equilibrium of its
+ * saved (rho, u), a thermal lattice the equilibrium of its saved T, the tick
+ * counter the file's tick, and the fields are saved as at initialisation.
+ * target_tick >= 0 must equal the file's tick (else BF_ERR_INVALID_ARGUMENT);
+ * -1 takes the file's.  A file of another size leaves the state as it was. */
+int bf_load_macroscopic(bf_solver* s, const char* path, int32_t target_tick);
 
 /* ---- differentiable channel flow and its discrete adjoint ---------------- */
 /* No counterpart in the reference (it has no adjoint).  A forward/backward
@@ -361,8 +385,11 @@ int bf_render3d(bf_solver* s, int32_t mode, const float view[16], const float pr
  * Its scratch is one fixed 327,744-byte device array that every GPU loading
  * the library keeps until the process exits; that limits a call to
  * 134,217,728 cells (512^3), and larger counts return
- * BF_ERR_INVALID_ARGUMENT.  The work runs on `stream` (NULL: the legacy
- * default stream) and the call returns once it is done.  The first call on
+ * BF_ERR_INVALID_ARGUMENT, as does a field pointer off a 16-byte boundary.
+ * The work runs on `stream` and the call returns once it is done.  NULL
+ * selects the legacy default stream, which is NOT ordered after a solver's
+ * own stream (created non-blocking): to reduce a solver's field, pass the
+ * solver's stream (bf_get_stream) or call bf_synchronize first.  The first call on
  * a device looks up the array's device address (cudaGetSymbolAddress);
  * make that first call before any stream capture.  All calls share the
  * array and every call overwrites what it reads, so calls that overlap on

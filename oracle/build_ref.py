@@ -29,8 +29,17 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-REFERENCE = os.environ.get("REFERENCE", "/root/reference")
-SHADER_DIR = os.path.join(REFERENCE, "BoltzmannFluids", "Source", "GLSL", "LBM")
+
+
+def reference_root(reference=None):
+    """The reference checkout: the argument, else the REFERENCE environment
+    variable; None when neither names one (nothing is built then)."""
+    return reference or os.environ.get("REFERENCE") or None
+
+
+def shader_dir(root):
+    return os.path.join(root, "BoltzmannFluids", "Source", "GLSL", "LBM")
+
 # (namespace, shader file, per-variant macros): collide is compiled three times
 # like LBM::_compile_shaders does (LBM.cpp:17-38)
 UNITS = [
@@ -117,22 +126,22 @@ def lower(text):
     return t
 
 
-def velocity_tables():
+def velocity_tables(root):
     """The (c, w) tables of VelocitySet.cpp, parsed from the reference's text
     (the same parser that makes tests/golden/velocity_sets.json)."""
     sys.path.insert(0, os.path.join(HERE, "..", "tests", "golden"))
     import make_golden
-    text = open(os.path.join(REFERENCE, "BoltzmannFluids", "Source", "LBMConstants", "VelocitySet.cpp")).read()
+    text = open(os.path.join(root, "BoltzmannFluids", "Source", "LBMConstants", "VelocitySet.cpp")).read()
     return make_golden.parse_velocity_sets(text)
 
 
-def unit_source(cfg, tables):
+def unit_source(cfg, tables, root):
     macros = dict(BASE)
     macros.update(cfg)
     parts = ["// generated by oracle/build_ref.py from the reference's shader sources -- do not edit",
              '#include "ref_shim.hpp"']
     for ns, shader, extra in UNITS:
-        src = open(os.path.join(SHADER_DIR, shader + ".comp")).read()
+        src = open(os.path.join(shader_dir(root), shader + ".comp")).read()
         low = lower(src)
         defined = sorted(set(re.findall(r"#define\s+(\w+)", src)) | set(INJECTED))
         m = dict(macros)
@@ -166,14 +175,17 @@ def unit_source(cfg, tables):
     return "\n".join(parts) + "\n"
 
 
-def build(verbose=False):
-    """Builds every configuration; returns {name: path}.  Empty when the reference is absent."""
-    if not os.path.isdir(SHADER_DIR):
+def build(verbose=False, reference=None):
+    """Builds every configuration from the reference checkout at `reference`
+    (else $REFERENCE); returns {name: path}.  Empty when no checkout is given
+    or it lacks the shaders."""
+    root = reference_root(reference)
+    if not root or not os.path.isdir(shader_dir(root)):
         return {}
     os.makedirs(OUT, exist_ok=True)
     deps = [os.path.join(HERE, f) for f in ("ref_shim.hpp", "ref_driver.inc", "build_ref.py")]
-    deps += [os.path.join(SHADER_DIR, s + ".comp") for s in SHADERS]
-    tables = velocity_tables()
+    deps += [os.path.join(shader_dir(root), s + ".comp") for s in SHADERS]
+    tables = velocity_tables(root)
     stamp = hashlib.sha1("".join(open(d).read() for d in deps).encode()).hexdigest()[:12]
     built = {}
     procs = []
@@ -185,7 +197,7 @@ def build(verbose=False):
             continue
         cpp = os.path.join(OUT, f"ref_{name}.cpp")
         with open(cpp, "w") as f:
-            f.write(unit_source(cfg, tables))
+            f.write(unit_source(cfg, tables, root))
         cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math", "-w",
                "-I", HERE, cpp, "-o", so]
         procs.append((subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True), tag, name))
@@ -201,4 +213,5 @@ def build(verbose=False):
 
 
 if __name__ == "__main__":
-    print(build(verbose=True))
+    # python oracle/build_ref.py [reference checkout]  (default: $REFERENCE)
+    print(build(verbose=True, reference=sys.argv[1] if len(sys.argv) > 1 else None))

@@ -111,31 +111,11 @@ static float f16_to_f32(uint16_t h) {
     else x = sign | ((e + 112u) << 23) | (m << 13);
     float f; memcpy(&f, &x, 4); return f;
 }
-/* custom 16-bit "c16": 1 sign, 4 exponent, 11 mantissa bits; magnitude
- * 2^(e-13)*(1+m/2048) for e=1..15 and 2^-12*(m/2048) for e=0, i.e. the top
- * 15 bits of an FP32 scaled by 2^-114.  Encoding: scale |f| by 2^-114 in
- * FP32 (exact for |f| >= 2^-12, rounded into FP32 subnormals below), round
- * the bit pattern to nearest even at bit 12, saturate at the largest code
- * (2^2*(2-2^-11)); NaN saturates too.  Decoding scales back by 2^114 (exact). */
-static uint16_t f32_to_c16(float f) {
-    uint32_t x; memcpy(&x, &f, 4);
-    uint32_t sign = (x >> 16) & 0x8000u;
-    float a = fabsf(f) * 0x1p-114f;
-    uint32_t b; memcpy(&b, &a, 4);
-    b = b + 0x7ffu + ((b >> 12) & 1u);
-    uint32_t q = b >> 12;
-    if (q > 0x7fffu) q = 0x7fffu;
-    return (uint16_t)(sign | q);
-}
-static float c16_to_f32(uint16_t h) {
-    uint32_t b = (uint32_t)(h & 0x7fffu) << 12;
-    float a; memcpy(&a, &b, 4);
-    float v = a * 0x1p114f;
-    uint32_t vb; memcpy(&vb, &v, 4);
-    vb |= (uint32_t)(h & 0x8000u) << 16;
-    memcpy(&v, &vb, 4);
-    return v;
-}
+/* custom-scaled 16-bit (fp16c): the IEEE half of g * 2^12, g = f - w.  The
+ * scale keeps shifted populations in the half's normal range down to
+ * |g| = 2^-26; decoding multiplies by 2^-12 (exact). */
+#define C16_SCALE 4096.0f
+static float c16_round(float g) { return f16_to_f32(f32_to_f16_rne(g * C16_SCALE)) * (1.0f / C16_SCALE); }
 
 /* ------------------------------------------------------------------------ */
 /* solver state                                                              */
@@ -189,16 +169,15 @@ static REAL dot3(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 
 /* DDF storage emulation.  The lattice array holds what the device stores,
  * decoded to a float: f itself for fp32 and fp16 (rounded to half);
- * the shifted population g = f - w (rounded to half) for fp16s; the custom
- * 16-bit value a of (f - w)/w for fp16c.  The shifted storages run the
- * update on g (see collide), as the kernels do. */
+ * the shifted population g = f - w (rounded to half) for fp16s; g rounded
+ * through the scaled half for fp16c.  The shifted storages run the update
+ * on g (see collide), as the kernels do. */
 static int shifted(const orc_t* s) {
     return IS_F32 && (s->d.storage == ORC_STORE_FP16S || s->d.storage == ORC_STORE_FP16C);
 }
-static float c16_round(float v) { return c16_to_f32(f32_to_c16(v)); }
 /* stored value of slot i -> the value the update works on (g when shifted) */
 static REAL lat_load(const orc_t* s, REAL raw, int i) {
-    if (IS_F32 && s->d.storage == ORC_STORE_FP16C) return (REAL)((float)raw * (float)s->V[i].w);
+    (void)s; (void)i;
     return raw;
 }
 /* value the update produced -> stored value */
@@ -207,7 +186,7 @@ static REAL lat_store(const orc_t* s, REAL v, int i) {
     switch (s->d.storage) {
     case ORC_STORE_FP16:
     case ORC_STORE_FP16S: return (REAL)f16_to_f32(f32_to_f16_rne((float)v));
-    case ORC_STORE_FP16C: return (REAL)c16_round((float)v * (1.0f / (float)s->V[i].w));
+    case ORC_STORE_FP16C: return (REAL)c16_round((float)v);
     default: return v;
     }
 }
@@ -216,7 +195,7 @@ static REAL lat_from_f(const orc_t* s, REAL f, int i) {
     if (shifted(s)) {
         float w = (float)s->V[i].w;
         if (s->d.storage == ORC_STORE_FP16S) return (REAL)f16_to_f32(f32_to_f16_rne((float)f - w));
-        return (REAL)c16_round(((float)f - w) * (1.0f / w));
+        return (REAL)c16_round((float)f - w);
     }
     return lat_store(s, f, i);
 }
@@ -224,8 +203,7 @@ static REAL lat_from_f(const orc_t* s, REAL f, int i) {
 static REAL lat_to_f(const orc_t* s, REAL raw, int i) {
     if (!shifted(s)) return raw;
     float w = (float)s->V[i].w;
-    if (s->d.storage == ORC_STORE_FP16S) return (REAL)((float)raw + w);
-    return (REAL)fmaf((float)raw, w, w);
+    return (REAL)((float)raw + w);
 }
 
 static int opp(int i) { /* collide.comp:219-222 */
@@ -829,6 +807,13 @@ void ORC(iterate)(orc_t* s, int n, int save_last) {
     }
 }
 
+/* the thermal knobs between steps (the reference sets them as uniforms at
+ * every dispatch, LBM.cpp:1612-1613) */
+void ORC(set_thermal)(orc_t* s, float tau_t, float beta) {
+    s->d.tau_t = tau_t;
+    s->d.beta = beta;
+    s->Rtau_t = (REAL)1 / (REAL)tau_t;
+}
 long ORC(ticks)(orc_t* s) { return s->ticks; }
 int ORC(thermal)(orc_t* s) { return s->thermal; }
 int ORC(forcing)(orc_t* s) { return s->forcing; }
@@ -876,5 +861,7 @@ void ORC(reduce)(orc_t* s, double out[5]) {
 }
 uint16_t ORC(f32_to_f16)(float f) { return f32_to_f16_rne(f); }
 float ORC(f16_to_f32)(uint16_t h) { return f16_to_f32(h); }
-uint16_t ORC(f32_to_c16)(float f) { return f32_to_c16(f); }
-float ORC(c16_to_f32)(uint16_t h) { return c16_to_f32(h); }
+/* the hand-written exp of the pseudopotential (FP32 build) */
+float ORC(exp_f32)(float x) { return exp_f32(x); }
+/* the fp16c round trip of a shifted population g (encode, then decode) */
+float ORC(fp16c_round)(float g) { return c16_round(g); }

@@ -46,6 +46,7 @@ def load():
         getattr(lib, p + "get_thermal").argtypes = [C.c_void_p, C.c_void_p]
         getattr(lib, p + "get_boundries").argtypes = [C.c_void_p, C.c_void_p, C.c_size_t]
         getattr(lib, p + "reduce").argtypes = [C.c_void_p, C.c_void_p]
+        getattr(lib, p + "set_thermal").argtypes = [C.c_void_p, C.c_float, C.c_float]
         for n in ("thermal", "forcing", "constant_force", "bits", "q"):
             getattr(lib, p + n).argtypes = [C.c_void_p]
             getattr(lib, p + n).restype = C.c_int
@@ -67,10 +68,10 @@ def load():
     lib.orc32_f32_to_f16.restype = C.c_uint16
     lib.orc32_f16_to_f32.argtypes = [C.c_uint16]
     lib.orc32_f16_to_f32.restype = C.c_float
-    lib.orc32_f32_to_c16.argtypes = [C.c_float]
-    lib.orc32_f32_to_c16.restype = C.c_uint16
-    lib.orc32_c16_to_f32.argtypes = [C.c_uint16]
-    lib.orc32_c16_to_f32.restype = C.c_float
+    lib.orc32_exp_f32.argtypes = [C.c_float]
+    lib.orc32_exp_f32.restype = C.c_float
+    lib.orc32_fp16c_round.argtypes = [C.c_float]
+    lib.orc32_fp16c_round.restype = C.c_float
     _lib = lib
     return lib
 
@@ -111,7 +112,11 @@ class Oracle:
         d.velocity_limit = float(velocity_limit)
         d.velocity_limit_extreme = float(velocity_limit_extreme)
         d.G = float(G)
-        d.tau_t = float(tau_t)
+        # initialize_fields resets the thermal relaxation time to 2
+        # (LBM.cpp:461): the initial pass runs with 2, the given value applies
+        # from the first step on (set after initialisation, as a caller of the
+        # reference must)
+        d.tau_t = 2.0
         d.beta = float(beta)
         d.thermal_init_equilibrium = int(bool(thermal_init_equilibrium))
         d.two_buffer_fixed = int(bool(two_buffer_fixed))
@@ -147,6 +152,8 @@ class Oracle:
                                                      nobj, ptrs[5], ptrs[6])
         if not self.h:
             raise ValueError("oracle: bad description")
+        if float(tau_t) != 2.0:
+            self.set_thermal(tau_t, beta)
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -155,6 +162,9 @@ class Oracle:
 
     def _f(self, name):
         return getattr(self.lib, self.p + name)
+
+    def set_thermal(self, tau_t, beta):
+        self._f("set_thermal")(self.h, C.c_float(float(tau_t)), C.c_float(float(beta)))
 
     def iterate(self, n=1, save=True):
         self._f("iterate")(self.h, int(n), int(bool(save)))

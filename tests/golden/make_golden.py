@@ -1,8 +1,8 @@
 """Generates the golden fixtures in this folder from the reference's source text.
 
-Run in a checkout that has the reference at REFERENCE (default
-/root/reference); the outputs are committed so the tests never need the
-reference at run time.
+Run with the environment variable REFERENCE naming a checkout of the
+reference; the outputs are committed so the tests never need the reference
+at run time.
 
   velocity_sets.json  -- the (c, w) tables of
                          BoltzmannFluids/Source/LBMConstants/VelocitySet.cpp,
@@ -18,7 +18,7 @@ import re
 import sys
 from fractions import Fraction
 
-REFERENCE = os.environ.get("REFERENCE", "/root/reference")
+REFERENCE = os.environ.get("REFERENCE")
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
@@ -56,6 +56,8 @@ def parse_defaults(h_text, cpp_text):
 
 
 def main():
+    if not REFERENCE:
+        sys.exit("set REFERENCE to a checkout of the reference")
     src = os.path.join(REFERENCE, "BoltzmannFluids", "Source")
     vs_text = open(os.path.join(src, "LBMConstants", "VelocitySet.cpp")).read()
     sets = parse_velocity_sets(vs_text)

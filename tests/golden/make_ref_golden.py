@@ -4,8 +4,9 @@ sources) for the seeded cases of tests/ref_cases.py, so that tests on a
 machine without the reference sources can compare against them.
 
 For each case: the u/rho field (float4) and force/temperature field (float4)
-saved at each step of ref_cases.STEPS.  Run from the repository root where
-the reference is present:  python tests/golden/make_ref_golden.py
+saved at each step of ref_cases.STEPS.  Run from the repository root with
+REFERENCE naming a checkout of the reference:
+    REFERENCE=<checkout> python tests/golden/make_ref_golden.py
 """
 import os
 import sys

@@ -34,7 +34,6 @@ def make_pair(res, tau, vs, *, density=None, velocity=None, force=None, temperat
     s.collision = collision
     s.trt_magic = trt_magic
     s.intermolecular_interaction_strength = G
-    s.thermal_relaxation_time = tau_t
     s.thermal_expansion_coefficient = beta
     s.thermal_init_equilibrium = thermal_init_equilibrium
     s.two_buffer_fixed = two_buffer_fixed
@@ -49,6 +48,9 @@ def make_pair(res, tau, vs, *, density=None, velocity=None, force=None, temperat
     s.initialize_fields_from_arrays(res, tau, density=density, velocity=velocity, force=force,
                                     temperature=temperature, boundry_id=ids, periodic=periodic,
                                     velocity_set=vs, fp_accuracy=storage, is_flow_multiphase=multiphase)
+    # initialisation resets it to 2 (LBM.cpp:461); set afterwards, it takes
+    # effect at the next step
+    s.thermal_relaxation_time = tau_t
     o = Oracle(res, tau, density=density, velocity=velocity, force=force, temperature=temperature,
                boundry_id=ids, periodic=periodic, velocity_set=int(vs), storage=int(storage),
                multiphase=multiphase, esoteric=esoteric, boundary_mode=int(boundary_mode), collision=int(collision),

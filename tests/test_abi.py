@@ -65,3 +65,7 @@ def test_null_and_invalid_arguments(product_lib):
     assert lib.bf_get_velosity_vectors(7, 0, None, C.byref(n)) == -1
     w = C.c_size_t()
     assert lib.bf_pack_boundries(None, 10, 3, None, 0, C.byref(w)) == -1
+    # the allocation-free reduction refuses a misaligned field before touching the device
+    out = (C.c_double * 5)()
+    assert lib.bf_reduce_field_noalloc(C.c_void_p(8), 1024, None, out) == -1
+    assert b"aligned" in lib.bf_last_error()

@@ -192,7 +192,7 @@ def test_shan_chen(q):
 @pytest.mark.parametrize("storage", [1, 2, 3])
 def test_16bit_storage_matches_emulation(storage):
     """16-bit storage: the oracle emulates the same codecs (IEEE half RNE of
-    f or of f - w, and the custom c16 format of (f - w)/w); with FP32
+    f or of f - w, and the half of (f - w) * 2^12); with FP32
     arithmetic identical on both sides the stored lattices agree bit for bit."""
     res = (20, 14, 12)
     rho, u = seeded_fields(res, seed=31)
@@ -322,3 +322,31 @@ def test_lambda_initialisation_matches_arrays():
     a.iterate_time(steps=5)
     b.iterate_time(steps=5)
     assert np.array_equal(a.get_velocity_density_texture(), b.get_velocity_density_texture())
+
+
+def test_pseudopotential_exp_against_cuda_expf():
+    """The kernels' hand-written exp in psi = 1 - exp(-rho): bit-exact with the
+    oracle's, and within a few ulp of CUDA's expf (through torch) over the
+    densities of a Shan-Chen flow, rho in [0.01, 10]."""
+    import torch
+    import boltzmannfluids_gb300 as bf
+    from oracle import oracle as orc
+    res = (256, 40, 1)
+    n = res[0] * res[1]
+    rho = np.linspace(0.01, 10.0, n).astype(np.float32)
+    s = bf.LBM()
+    s.is_collide_esoteric = True
+    s.intermolecular_interaction_strength = -5.0
+    s.initialize_fields_from_arrays(res, 1.0, density=rho, velocity_set=bf.VelocitySet.D2Q9, is_flow_multiphase=True)
+    d = s.get_velocity_density_texture().reshape(-1, 4)[:, 3]  # the densities psi was formed from
+    psi = s.get_pseudopotential().reshape(-1)
+    lib = orc.load()
+    e_orc = np.array([lib.orc32_exp_f32(float(-r)) for r in d], np.float32)
+    assert np.array_equal(psi, (np.float32(1.0) - e_orc).astype(np.float32))
+    dt = torch.from_numpy(d.copy()).cuda()
+    e_cuda = torch.exp(-dt)
+    psi_cuda = (1.0 - e_cuda).cpu().numpy()
+    e_cuda = e_cuda.cpu().numpy()
+    bound = 4 * np.spacing(e_cuda) + 2 * np.spacing(psi_cuda)
+    assert (np.abs(psi - psi_cuda) <= bound).all()
+    assert (np.abs(e_orc - e_cuda) <= 2 * np.spacing(e_cuda)).all()

@@ -51,3 +51,11 @@ def test_noalloc_reduction_rejects_oversize(product_lib):
     rc = lib.bf_reduce_field_noalloc(C.c_void_p(1), MAX_CELLS + 1, None, out)
     assert rc == -1 and b"capacity" in lib.bf_last_error()
     assert lib.bf_reduce_field_noalloc(None, 0, None, out) == 0 and list(out) == [0.0] * 5
+
+
+def test_noalloc_reduction_rejects_misaligned_field(product_lib):
+    """A field pointer off a 16-byte boundary is refused before any launch."""
+    lib = product_lib
+    out = (C.c_double * 5)()
+    rc = lib.bf_reduce_field_noalloc(C.c_void_p(8), 1024, None, out)
+    assert rc == -1 and b"aligned" in lib.bf_last_error()

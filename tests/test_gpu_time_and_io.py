@@ -118,35 +118,40 @@ def test_macroscopic_load_restarts_as_initialisation(tmp_path, vs, res, storage,
         assert np.array_equal(a.get_velocity_density_texture(), b.get_velocity_density_texture())
 
 
-def test_macroscopic_load_keeps_geometry_and_rejects_other_files(tmp_path):
-    nx, ny = 40, 24
-    y, x = np.mgrid[0:ny, 0:nx]
-    ids = np.zeros((ny, nx), np.uint32)
-    ids[(x - 12) ** 2 + (y - 12) ** 2 < 20] = 1
+def cylinder_solver(nx, ny, ids, rho=None, u=None):
     s = bf.LBM()
     s.is_collide_esoteric = True
     s.boundary_mode = bf.BoundaryMode.bounce_back
     s.set_boundry_properties(1, velocity_translational=(0, 0, 0))
+    s.initialize_fields_from_arrays((nx, ny, 1), 0.6, density=rho, velocity=u, boundry_id=ids,
+                                    periodic=(True, True, True), velocity_set=bf.VelocitySet.D2Q9)
+    return s
+
+
+def test_macroscopic_load_keeps_geometry_and_rejects_other_files(tmp_path):
+    """A restart at an odd tick with a solid cylinder under bounce-back: the
+    geometry is kept, and the steps after it agree bit for bit with a fresh
+    solver of the same geometry initialised from the saved fields."""
+    nx, ny = 40, 24
+    y, x = np.mgrid[0:ny, 0:nx]
+    ids = np.zeros((ny, nx), np.uint32)
+    ids[(x - 12) ** 2 + (y - 12) ** 2 < 20] = 1
     u = np.zeros((nx * ny, 3), np.float32)
     u[:, 0] = 0.04
-    s.initialize_fields_from_arrays((nx, ny, 1), 0.6, velocity=u, boundry_id=ids, periodic=(True, True, True),
-                                    velocity_set=bf.VelocitySet.D2Q9)
+    s = cylinder_solver(nx, ny, ids, u=u)
     s.iterate_time(steps=51, save=True)
     path = tmp_path / "m.bin"
     s.save_current_tick_macroscopic(path)
-    before = s.get_velocity_density_texture().copy()
+    saved = s.get_velocity_density_texture().reshape(-1, 4).copy()
     s.iterate_time(steps=20, save=True)
     s.load_tick_macroscopic(path)
-    after = s.get_velocity_density_texture()
-    fluid = ids == 0
-    # the restarted state's fields are the moments of the saved fields'
-    # equilibrium as the first step reads it (streamed from the neighbours,
-    # as after initialize_fields): close to the saved fields, not equal
-    assert np.abs(after[0][fluid] - before[0][fluid]).max() < 5e-3
-    assert np.abs(after[0][fluid][:, 0] - before[0][fluid][:, 0]).mean() < 5e-4
     assert np.array_equal(s.get_boundry_texture()[0], ids.astype(np.uint8))
-    s.iterate_time(steps=10, save=True)
-    assert np.isfinite(s.get_velocity_density_texture()).all()
+    fresh = cylinder_solver(nx, ny, ids, rho=saved[:, 3].copy(), u=saved[:, :3].copy())
+    assert np.array_equal(s.get_velocity_density_texture(), fresh.get_velocity_density_texture())
+    for k in (1, 10):
+        s.iterate_time(steps=k, save=True)
+        fresh.iterate_time(steps=k, save=True)
+        assert np.array_equal(s.get_velocity_density_texture(), fresh.get_velocity_density_texture())
     # a file of another resolution or kind leaves the solver as it was
     other = bf.LBM()
     other.initialize_fields_from_arrays((32, 32, 1), 0.6, velocity_set=bf.VelocitySet.D2Q9)
@@ -154,5 +159,10 @@ def test_macroscopic_load_keeps_geometry_and_rejects_other_files(tmp_path):
         other.load_tick_macroscopic(path)
     junk = tmp_path / "junk.bin"
     junk.write_bytes(b"\0" * 100)
+    before = s.get_velocity_density_texture().copy()
     with pytest.raises(bf.LBMError):
         s.load_tick_macroscopic(junk)
+    s.iterate_time(steps=1, save=True)
+    fresh.iterate_time(steps=1, save=True)
+    assert np.array_equal(s.get_velocity_density_texture(), fresh.get_velocity_density_texture())
+    assert not np.array_equal(before, s.get_velocity_density_texture())

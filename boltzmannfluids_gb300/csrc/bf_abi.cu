@@ -84,6 +84,9 @@ int q_of(int vs) {
     return 0;
 }
 size_t storage_bytes(int st) { return st == BF_STORE_FP64 ? 8 : (st == BF_STORE_FP32 ? 4 : 2); }
+// element size of the thermal lattice and the pseudopotential field (double
+// for the FP64 stepper, float otherwise)
+size_t aux_bytes(int st) { return st == BF_STORE_FP64 ? 8 : 4; }
 
 // LBM.cpp:569 / :606: bits per id = exp2(ceil(log2(ceil(log2(count))))), 0 for one object
 int bits_per_boundry(int count) {
@@ -160,6 +163,11 @@ __global__ void copy16_kernel(const uint4* __restrict__ src, uint4* __restrict__
 __global__ void ids_to_bytes_kernel(const uint32_t* __restrict__ ids, uint32_t n, uint8_t* __restrict__ out) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) out[i] = (uint8_t)ids[i];
+}
+
+__global__ void d2f_kernel(const double* __restrict__ a, uint64_t n, float* __restrict__ out) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (float)a[i];
 }
 
 __global__ void fill_f32_kernel(float* __restrict__ p, uint32_t n, float v) {
@@ -300,6 +308,10 @@ float* th_src(bf_solver* s) { return s->th[s->th0_src ? 0 : 1].as<float>(); }
 float* th_tgt(bf_solver* s) { return s->th[s->th0_src ? 1 : 0].as<float>(); }
 float* psi_src(bf_solver* s) { return s->psi[s->psi0_src ? 0 : 1].as<float>(); }
 float* psi_tgt(bf_solver* s) { return s->psi[s->psi0_src ? 1 : 0].as<float>(); }
+void* th_src_v(bf_solver* s) { return s->th[s->th0_src ? 0 : 1].p; }
+void* th_tgt_v(bf_solver* s) { return s->th[s->th0_src ? 1 : 0].p; }
+void* psi_src_v(bf_solver* s) { return s->psi[s->psi0_src ? 0 : 1].p; }
+void* psi_tgt_v(bf_solver* s) { return s->psi[s->psi0_src ? 1 : 0].p; }
 
 cudaError_t dispatch_step(bf_solver* s, const StepParams& p, int mode, int path) {
     switch (s->Q) {
@@ -347,6 +359,10 @@ void fill_constants(bf_solver* s, StepParams& p) {
     const float tau = s->desc.relaxation_time;
     p.R2 = 1.0f / cs2;
     p.R4 = 1.0f / cs4;
+    p.cs2 = cs2;
+    p.cs4 = cs4;
+    p.tau = tau;
+    p.tau_t = s->desc.thermal_relaxation_time;
     p.R2h = p.R2 * 0.5f;
     p.R4h = p.R4 * 0.5f;
     p.Rtau = 1.0f / tau;
@@ -369,6 +385,12 @@ void fill_constants(bf_solver* s, StepParams& p) {
     const double tau_d = (double)tau;
     p.k64.R2 = 1.0 / cs2_d;
     p.k64.R4 = 1.0 / cs4_d;
+    p.k64.cs2 = cs2_d;
+    p.k64.cs4 = cs4_d;
+    p.k64.tau = tau_d;
+    p.k64.tau_t = (double)s->desc.thermal_relaxation_time;
+    p.k64.beta = (double)s->desc.thermal_expansion_coefficient;
+    p.k64.G = (double)s->desc.intermolecular_interaction_strength;
     p.k64.R2h = p.k64.R2 * 0.5;
     p.k64.R4h = p.k64.R4 * 0.5;
     p.k64.Rtau = 1.0 / tau_d;
@@ -416,8 +438,15 @@ cudaError_t collide(bf_solver* s, bool save, bool update, bool reduce, bool meas
     p.objects = s->objs.as<float4>();
     p.obj_kind = s->kinds.as<uint8_t>();
     p.bvals = s->bvals.as<float4>();
-    if (s->thermal) { p.th_src = th_src(s); p.th_tgt = th_tgt(s); }
-    if (s->desc.multiphase) { p.psi_src = psi_src(s); p.psi_tgt = psi_tgt(s); }
+    const bool f64 = s->desc.storage == BF_STORE_FP64;
+    if (s->thermal) {
+        if (f64) { p.th_src64 = static_cast<const double*>(th_src_v(s)); p.th_tgt64 = static_cast<double*>(th_tgt_v(s)); }
+        else { p.th_src = th_src(s); p.th_tgt = th_tgt(s); }
+    }
+    if (s->desc.multiphase) {
+        if (f64) { p.psi_src64 = static_cast<const double*>(psi_src_v(s)); p.psi_tgt64 = static_cast<double*>(psi_tgt_v(s)); }
+        else { p.psi_src = psi_src(s); p.psi_tgt = psi_tgt(s); }
+    }
     p.vel_den = s->vel_den.as<float4>();
     p.force_temp = s->force_temp.as<float4>();
     p.bnd_tex = nullptr;  // the boundary-id field is written once at initialisation
@@ -432,7 +461,9 @@ cudaError_t collide(bf_solver* s, bool save, bool update, bool reduce, bool meas
                               (F_PERIODIC_X | F_PERIODIC_Y | F_PERIODIC_Z);
     // the fast kernel indexes every slot with 32 bits off the first plane
     const bool idx32 = (uint64_t)s->N * (uint64_t)s->Q < (1ull << 32);
-    const bool generic = mode == AA_LOCAL || (p.flags & heavy) || !all_periodic || !idx32;
+    // the FP64 stepper's multiphase flow runs the generic kernel
+    const bool generic = mode == AA_LOCAL || (p.flags & heavy) || !all_periodic || !idx32 ||
+                         (f64 && (p.flags & F_MULTIPHASE));
     // objects and open faces (thermal flow included) without force-field or
     // multiphase flow: the boundary-aware fast kernel, with its masks
     const uint32_t masked_excl = F_FORCE_FIELD | F_MULTIPHASE;
@@ -505,8 +536,13 @@ cudaError_t stream(bf_solver* s) {
 // LBM::_stream_thermal (LBM.cpp:1728-1773)
 cudaError_t stream_thermal(bf_solver* s) {
     ThermalStreamParams p{};
-    p.src = th_src(s);
-    p.dst = th_tgt(s);
+    if (s->desc.storage == BF_STORE_FP64) {
+        p.src64 = static_cast<const double*>(th_src_v(s));
+        p.dst64 = static_cast<double*>(th_tgt_v(s));
+    } else {
+        p.src = th_src(s);
+        p.dst = th_tgt(s);
+    }
     p.stride = s->N;
     p.nx = s->desc.resolution[0]; p.ny = s->desc.resolution[1]; p.nz = s->desc.resolution[2];
     p.flags = base_flags(s);
@@ -758,10 +794,8 @@ int bf_initialize_fields(bf_solver* s, const bf_init_desc* d, const float* densi
     if (N64 >= (1ull << 32) || ry > 65535 || rz > 65535)
         return fail(BF_ERR_INVALID_ARGUMENT, "initialize_fields(): at most 2^32-1 cells and 65535 cells along y and z");
     if (d->storage < BF_STORE_FP32 || d->storage > BF_STORE_FP64) return fail(BF_ERR_INVALID_ARGUMENT, "initialize_fields(): unknown storage");
-    if (d->storage == BF_STORE_FP64 &&
-        (!d->esoteric || !d->periodic[0] || !d->periodic[1] || !d->periodic[2] || d->multiphase ||
-         N64 * (uint64_t)Q >= (1ull << 32)))
-        return fail(BF_ERR_INVALID_ARGUMENT, "initialize_fields(): FP64 storage (the accuracy reference stepper) covers fully periodic esoteric-pull boxes only");
+    if (d->storage == BF_STORE_FP64 && !d->esoteric)
+        return fail(BF_ERR_INVALID_ARGUMENT, "initialize_fields(): FP64 storage (the accuracy reference stepper) runs the esoteric-pull step only");
     if (!(d->relaxation_time > 0.5f)) return fail(BF_ERR_INVALID_ARGUMENT, "initialize_fields(): relaxation_time must exceed 0.5");
     if (d->collision == BF_COLLISION_TRT && !(d->trt_magic > 0.f)) return fail(BF_ERR_INVALID_ARGUMENT, "initialize_fields(): TRT magic parameter must be positive");
 
@@ -822,8 +856,6 @@ int bf_initialize_fields(bf_solver* s, const bf_init_desc* d, const float* densi
     if (s->bits > 8) return fail(BF_ERR_INVALID_ARGUMENT, "too many objects are defined, maximum of 255 bits are possible but number of objets were: " + std::to_string(nobj));
     s->has_eq_objects = false;
     for (int k = 1; k < nobj; k++) if (s->objects[k].kind != BF_OBJECT_SOLID) s->has_eq_objects = true;
-    if (d->storage == BF_STORE_FP64 && (s->boundaries || s->thermal || !s->constant_force))
-        return fail(BF_ERR_INVALID_ARGUMENT, "initialize_fields(): FP64 storage (the accuracy reference stepper) takes no boundary objects, temperature field or force field");
 
     const size_t sb = storage_bytes(d->storage);
     const size_t lat_bytes = (size_t)N * Q * sb;
@@ -910,10 +942,11 @@ int bf_initialize_fields(bf_solver* s, const bf_init_desc* d, const float* densi
     }
     // Shan-Chen pseudopotential textures (LBM.cpp:848-866), zero initial contents
     if (d->multiphase) {
-        BF_CUDA(s->psi[0].alloc((size_t)N * 4));
-        BF_CUDA(s->psi[1].alloc((size_t)N * 4));
-        BF_CUDA(cudaMemset(s->psi[0].p, 0, (size_t)N * 4));
-        BF_CUDA(cudaMemset(s->psi[1].p, 0, (size_t)N * 4));
+        const size_t pb = (size_t)N * aux_bytes(d->storage);
+        BF_CUDA(s->psi[0].alloc(pb));
+        BF_CUDA(s->psi[1].alloc(pb));
+        BF_CUDA(cudaMemset(s->psi[0].p, 0, pb));
+        BF_CUDA(cudaMemset(s->psi[1].p, 0, pb));
     }
     BF_CUDA(s->vel_den.alloc((size_t)N * 16));
     BF_CUDA(s->force_temp.alloc((size_t)N * 16));
@@ -947,10 +980,11 @@ int bf_initialize_fields(bf_solver* s, const bf_init_desc* d, const float* densi
     }
     if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? BF_ERR_OUT_OF_MEMORY : BF_ERR_CUDA, std::string("init kernel: ") + cudaGetErrorString(e));
     if (s->thermal) {
-        BF_CUDA(s->th[0].alloc((size_t)N * s->QT * 4));
-        BF_CUDA(s->th[1].alloc((size_t)N * s->QT * 4));
-        BF_CUDA(cudaMemsetAsync(s->th[0].p, 0, (size_t)N * s->QT * 4, s->stream));
-        BF_CUDA(cudaMemsetAsync(s->th[1].p, 0, (size_t)N * s->QT * 4, s->stream));
+        const size_t tb = (size_t)N * s->QT * aux_bytes(d->storage);
+        BF_CUDA(s->th[0].alloc(tb));
+        BF_CUDA(s->th[1].alloc(tb));
+        BF_CUDA(cudaMemsetAsync(s->th[0].p, 0, tb, s->stream));
+        BF_CUDA(cudaMemsetAsync(s->th[1].p, 0, tb, s->stream));
         if (d->thermal_init_equilibrium) {
             DeviceBuf d_Tb;
             BF_CUDA(d_Tb.alloc((size_t)N * 4));
@@ -961,14 +995,15 @@ int bf_initialize_fields(bf_solver* s, const bf_init_desc* d, const float* densi
                 BF_CUDA(cudaGetLastError());
             }
             InitParams tp = ip;
-            tp.th = th_src(s);
+            if (d->storage == BF_STORE_FP64) tp.th64 = s->th[s->th0_src ? 0 : 1].as<double>();
+            else tp.th = th_src(s);
             tp.T = d_Tb.as<float>();
             tp.stride = N;
             e = s->QT == 5 ? launch_init_thermal<5>(tp, s->stream) : launch_init_thermal<7>(tp, s->stream);
             if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? BF_ERR_OUT_OF_MEMORY : BF_ERR_CUDA, std::string("thermal init kernel: ") + cudaGetErrorString(e));
             // both buffers start alike: slots nothing writes (solid cells) then
             // read the same whichever buffer holds the current state
-            BF_CUDA(cudaMemcpyAsync(th_tgt(s), th_src(s), (size_t)N * s->QT * 4, cudaMemcpyDeviceToDevice, s->stream));
+            BF_CUDA(cudaMemcpyAsync(th_tgt(s), th_src(s), tb, cudaMemcpyDeviceToDevice, s->stream));
             BF_CUDA(cudaStreamSynchronize(s->stream));
         }
         // As the reference reads it, set_equilibrium_populations_thermal.comp:101-107
@@ -1146,11 +1181,23 @@ int bf_get_field(bf_solver* s, int32_t kind, bf_field* out) {
         break;
     }
     case BF_FIELD_THERMAL_POPULATIONS:
-        if (!s->thermal) return fail(BF_ERR_INVALID_ARGUMENT, "get_field(): the flow is not thermal");
-        out->device_ptr = th_src(s); out->components = s->QT; out->bytes_per_component = 4; out->bytes = (size_t)s->N * s->QT * 4; break;
-    case BF_FIELD_PSEUDOPOTENTIAL:
-        if (!s->desc.multiphase) return fail(BF_ERR_INVALID_ARGUMENT, "get_field(): the flow is not multiphase");
-        out->device_ptr = psi_src(s); out->components = 1; out->bytes_per_component = 4; out->bytes = (size_t)s->N * 4; break;
+    case BF_FIELD_PSEUDOPOTENTIAL: {
+        const bool th = kind == BF_FIELD_THERMAL_POPULATIONS;
+        if (th && !s->thermal) return fail(BF_ERR_INVALID_ARGUMENT, "get_field(): the flow is not thermal");
+        if (!th && !s->desc.multiphase) return fail(BF_ERR_INVALID_ARGUMENT, "get_field(): the flow is not multiphase");
+        const int comps = th ? s->QT : 1;
+        const size_t count = (size_t)s->N * comps;
+        out->components = comps; out->bytes_per_component = 4; out->bytes = count * 4;
+        void* src = th ? th_src_v(s) : psi_src_v(s);
+        if (s->desc.storage != BF_STORE_FP64) { out->device_ptr = src; break; }
+        // the FP64 stepper's double values, rounded to float
+        if (s->decode_tmp.bytes < count * 4) BF_CUDA(s->decode_tmp.alloc(count * 4));
+        d2f_kernel<<<(unsigned)((count + 255) / 256), 256, 0, s->stream>>>(static_cast<const double*>(src), count,
+                                                                          s->decode_tmp.as<float>());
+        BF_CUDA(cudaGetLastError());
+        out->device_ptr = s->decode_tmp.p;
+        break;
+    }
     default:
         return fail(BF_ERR_INVALID_ARGUMENT, "get_field(): unknown field kind");
     }
@@ -1441,12 +1488,14 @@ int bf_load_macroscopic(bf_solver* s, const char* path, int32_t target_tick) {
         BF_CUDA(d_T.alloc((size_t)N * 4));
         BF_CUDA(cudaMemcpy(d_T.p, T.data(), (size_t)N * 4, cudaMemcpyHostToDevice));
         InitParams tp = ip;
-        tp.th = th_src(s);
+        const size_t tb = (size_t)N * s->QT * aux_bytes(s->desc.storage);
+        if (s->desc.storage == BF_STORE_FP64) tp.th64 = static_cast<double*>(th_src_v(s));
+        else tp.th = th_src(s);
         tp.T = d_T.as<float>();
-        BF_CUDA(cudaMemsetAsync(tp.th, 0, (size_t)N * s->QT * 4, s->stream));
+        BF_CUDA(cudaMemsetAsync(th_src_v(s), 0, tb, s->stream));
         e = s->QT == 5 ? launch_init_thermal<5>(tp, s->stream) : launch_init_thermal<7>(tp, s->stream);
         if (e != cudaSuccess) return fail(BF_ERR_CUDA, std::string("load_tick_macroscopic(): thermal init: ") + cudaGetErrorString(e));
-        BF_CUDA(cudaMemcpyAsync(th_tgt(s), th_src(s), (size_t)N * s->QT * 4, cudaMemcpyDeviceToDevice, s->stream));
+        BF_CUDA(cudaMemcpyAsync(th_tgt_v(s), th_src_v(s), tb, cudaMemcpyDeviceToDevice, s->stream));
     }
     // the fields of the loaded state, as initialize_fields saves them (LBM.cpp:502)
     e = iterate_once(s, true, false, false);

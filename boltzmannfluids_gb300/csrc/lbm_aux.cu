@@ -4,17 +4,21 @@
 
 namespace bf {
 
+// the FP64 stepper's thermal lattice is double (src64 / th64 set), every
+// other storage's FP32
 template <int QT>
 cudaError_t launch_stream_thermal(const ThermalStreamParams& p, cudaStream_t st) {
     int block;
     dim3 grid = cell_grid(p.nx, p.ny, p.nz, block);
-    stream_thermal_kernel<QT><<<grid, block, 0, st>>>(p);
+    if (p.src64) stream_thermal_kernel<QT, double><<<grid, block, 0, st>>>(p);
+    else stream_thermal_kernel<QT, float><<<grid, block, 0, st>>>(p);
     return cudaGetLastError();
 }
 template <int QT>
 cudaError_t launch_init_thermal(const InitParams& p, cudaStream_t st) {
     const unsigned blocks = (unsigned)((p.n_cells + 255u) / 256u);
-    init_thermal_kernel<QT><<<blocks, 256, 0, st>>>(p);
+    if (p.th64) init_thermal_kernel<QT, double><<<blocks, 256, 0, st>>>(p);
+    else init_thermal_kernel<QT, float><<<blocks, 256, 0, st>>>(p);
     return cudaGetLastError();
 }
 template cudaError_t launch_stream_thermal<5>(const ThermalStreamParams&, cudaStream_t);

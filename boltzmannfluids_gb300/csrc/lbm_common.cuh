@@ -86,6 +86,7 @@ template <> struct ThermalLattice<5> {
         return t[i];
     }
     __host__ __device__ static constexpr float w(int i) { return i == 0 ? float(1.0 / 3) : float(1.0 / 6); }
+    __host__ __device__ static constexpr double wd(int i) { return i == 0 ? 1.0 / 3 : 1.0 / 6; }
 };
 template <> struct ThermalLattice<7> {
     __host__ __device__ static constexpr Dir c(int i) {
@@ -93,6 +94,15 @@ template <> struct ThermalLattice<7> {
         return t[i];
     }
     __host__ __device__ static constexpr float w(int i) { return i == 0 ? float(1.0 / 4) : float(1.0 / 8); }
+    __host__ __device__ static constexpr double wd(int i) { return i == 0 ? 1.0 / 4 : 1.0 / 8; }
+};
+// thermal weight in the arithmetic type R
+template <int QT, class R> struct ThermalW;
+template <int QT> struct ThermalW<QT, float> {
+    __host__ __device__ static constexpr float w(int i) { return ThermalLattice<QT>::w(i); }
+};
+template <int QT> struct ThermalW<QT, double> {
+    __host__ __device__ static constexpr double w(int i) { return ThermalLattice<QT>::wd(i); }
 };
 
 // the thermal set's directions are the velocity set's first QT directions,
@@ -284,7 +294,17 @@ struct alignas(16) StepParams {
     // FP64 oracle does (cs = 1/sqrt(3), tau and the limits from the FP32 inputs)
     struct {
         double R2, R4, R2h, R4h, Rtau, P, Wm, Pp, Pm, vlim, vlim_ext, fconst[3];
+        double cs2, cs4, tau, tau_t, beta, G;
     } k64;
+    // the FP64 stepper's thermal lattice and pseudopotential (double; the
+    // FP32 pointers below serve every other storage)
+    const double* th_src64;
+    double* th_tgt64;
+    const double* psi_src64;
+    double* psi_tgt64;
+    // the literal evaluation's divisors: cs^2 = cs*cs, cs^4 = cs^2*cs^2 (the
+    // shim of pow(cs, 2) / pow(cs, 4)), tau, tau_T
+    float cs2, cs4, tau, tau_t;
     // launch constants, FP32, computed on the host exactly as the oracle
     // does: cs = float(1/sqrt(3)), cs2 = cs*cs, cs4 = cs2*cs2
     float R2;                 // 1/cs2
@@ -334,6 +354,9 @@ struct StreamParams {
 struct ThermalStreamParams {
     const float* src;
     float* dst;
+    // FP64 stepper: the thermal lattice in double (src/dst unused)
+    const double* src64;
+    double* dst64;
     uint64_t stride;
     int nx, ny, nz;
     uint32_t flags;
@@ -355,8 +378,9 @@ struct InitParams {
     const float* u;        // 3N
     const uint32_t* ids;   // N (may be null)
     const uint8_t* obj_kind;
-    // thermal
+    // thermal (th64: the FP64 stepper's thermal lattice)
     float* th;
+    double* th64;
     const float* T;
     // odd != 0: write the equilibrium state in the slots an odd esoteric-pull
     // step reads (a state loaded at an odd tick): population i of cell n goes

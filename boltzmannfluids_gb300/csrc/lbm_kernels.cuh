@@ -11,8 +11,8 @@
 //                        blocks of their own (masked_step_kernel: one pass)
 //   stream_kernel, stream_thermal_kernel, init_kernel, ... the reference's
 //                        other passes
-// All evaluate the same canonical expression tree (below), so they agree
-// with one another and with the oracle bit for bit.
+// All evaluate the same expression trees (below), so they agree with one
+// another and with the oracle bit for bit.
 //
 // The update is the fused stream+collide of the reference's esoteric-pull
 // mode (collide.comp main, :676-794).  The AA pattern follows
@@ -32,14 +32,20 @@ namespace bf {
 template <class R> struct CellSumT { R m, px, py, pz, ke; };
 using CellSum = CellSumT<float>;
 
-// Rounded, never-contracted FP32 operations: the kernels evaluate the same
-// expression tree as the oracle's canonical FP32 restatement, so FP32
-// results agree bit for bit.  That tree: divisions by launch uniforms become
-// multiplications by once-rounded reciprocals (a /2 folds in exactly),
-// u = j * (1/rho) with one IEEE division, opposite populations are summed
-// pairwise (s = f_i + f_opp, d = f_i - f_opp), and the multiply-adds marked
-// FFMA are single-rounding fused operations (C's fmaf on the host side).
-// The same operations in double drive the FP64 reference stepper.
+// Rounded, never-contracted operations: the kernels evaluate the same
+// expression trees as the oracle, so results agree bit for bit.  Two trees:
+//  * literal (FP32 and FP16 storage of f, and the FP64 reference stepper):
+//    the reference's expressions (collide.comp:383-395, :512-629, :702-782)
+//    in their written order, one IEEE operation per operator, divisions as
+//    correctly rounded divisions (FDIV), no fused multiply-adds; products
+//    with a lattice component (0, +-1) are exact and their zero terms are
+//    left out, which changes nothing but the sign of a zero;
+//  * shifted (fp16s / fp16c, extensions): the update on g = f - w with
+//    divisions by launch uniforms as multiplications by once-rounded
+//    reciprocals, u = j * (1/rho) with one IEEE division, opposite
+//    populations summed pairwise (s = f_i + f_opp, d = f_i - f_opp), and the
+//    multiply-adds marked FFMA single-rounding fused operations.  TRT (an
+//    extension) uses this fixed order with every storage.
 __device__ __forceinline__ float r_mul(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float r_add(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float r_sub(float a, float b) { return __fsub_rn(a, b); }
@@ -53,6 +59,7 @@ __device__ __forceinline__ double r_div(double a, double b) { return __ddiv_rn(a
 #define FMUL r_mul
 #define FADD r_add
 #define FSUB r_sub
+#define FDIV r_div
 
 // exp for the pseudopotential psi = 1 - exp(-rho), the same operations as the
 // oracle's exp_f32: Cody-Waite reduction x = k ln2 + r (ln2 split in a 15-bit
@@ -73,6 +80,35 @@ __device__ __forceinline__ float exp_f32(float x) {
     q = FADD(FMUL(q, r), 1.0f);
     return FMUL(q, __uint_as_float((uint32_t)((int)kf + 127) << 23));
 }
+
+// exp for the FP64 pseudopotential, the same operations as the oracle's
+// exp_f64: Cody-Waite reduction (ln2 split in a head with 21 zero low bits
+// and a tail), degree-13 Taylor polynomial in Horner form (|r| <= ln2/2,
+// truncation < 5e-18 relative), exact scaling by 2^k.  Valid for x in
+// [-708, 709]; within 1.1 ulp of the exact exponential.
+__device__ __forceinline__ double exp_f64(double x) {
+    const double L2E = 0x1.71547652b82fep+0, LN2_HI = 0x1.62e42fee00000p-1, LN2_LO = 0x1.a39ef35793c76p-33;
+    const double kf = rint(FMUL(x, L2E));
+    const double r = FSUB(FSUB(x, FMUL(kf, LN2_HI)), FMUL(kf, LN2_LO));
+    double q = 0x1.6124613a86d09p-33;  // 1/13!
+    q = FADD(FMUL(q, r), 0x1.1eed8eff8d898p-29);
+    q = FADD(FMUL(q, r), 0x1.ae64567f544e4p-26);
+    q = FADD(FMUL(q, r), 0x1.27e4fb7789f5cp-22);
+    q = FADD(FMUL(q, r), 0x1.71de3a556c734p-19);
+    q = FADD(FMUL(q, r), 0x1.a01a01a01a01ap-16);
+    q = FADD(FMUL(q, r), 0x1.a01a01a01a01ap-13);
+    q = FADD(FMUL(q, r), 0x1.6c16c16c16c17p-10);
+    q = FADD(FMUL(q, r), 0x1.1111111111111p-7);
+    q = FADD(FMUL(q, r), 0x1.5555555555555p-5);
+    q = FADD(FMUL(q, r), 0x1.5555555555555p-3);
+    q = FADD(FMUL(q, r), 0x1p-1);
+    q = FADD(FMUL(q, r), 1.0);
+    q = FADD(FMUL(q, r), 1.0);
+    return FMUL(q, __longlong_as_double((long long)((int64_t)kf + 1023) << 52));
+}
+// psi = 1 - exp(-rho) (collide.comp:512-516, rho0 = 1) in the arithmetic type
+__device__ __forceinline__ float psi_of(float rho) { return FSUB(1.0f, exp_f32(-rho)); }
+__device__ __forceinline__ double psi_of(double rho) { return FSUB(1.0, exp_f64(-rho)); }
 
 // c . v for a lattice direction with components in {-1, 0, 1}: the dot
 // product's x, y, z sum with the zero terms dropped (they add +-0 only)
@@ -104,6 +140,22 @@ __device__ __forceinline__ R uu_of(R ux, R uy, R uz) {
 template <class R>
 __device__ __forceinline__ R bracket(R cu, R one_m, R R2, R R4h) {
     return FFMA(FMUL(cu, cu), R4h, FFMA(cu, R2, one_m));
+}
+
+// GLSL's dot(a, b) as written: a.x*b.x + a.y*b.y + a.z*b.z
+template <class R>
+__device__ __forceinline__ R dot_lit(R ax, R ay, R az, R bx, R by, R bz) {
+    return FADD(FADD(FMUL(ax, bx), FMUL(ay, by)), FMUL(az, bz));
+}
+// collide.comp:589-604 (and the thermal :634-651) as written:
+// (w p) (((1 + cu/cs2) + cu^2/2/cs4) - uuh), uuh = (u.u/2)/cs2 of the cell
+template <class R>
+__device__ __forceinline__ R feq_lit(R wp, R cu, R cs2, R cs4, R uuh) {
+    return FMUL(wp, FSUB(FADD(FADD(R(1), FDIV(cu, cs2)), FDIV(FMUL(FMUL(cu, cu), R(0.5)), cs4)), uuh));
+}
+template <class R>
+__device__ __forceinline__ R uuh_of(R ux, R uy, R uz, R cs2) {
+    return FDIV(FMUL(dot_lit(ux, uy, uz, ux, uy, uz), R(0.5)), cs2);
 }
 
 template <int Q>
@@ -167,17 +219,32 @@ __device__ __forceinline__ R pair_sum(const R (&f)[Q], int i) { return FADD(f[i]
 template <int Q, class R>
 __device__ __forceinline__ R pair_diff(const R (&f)[Q], int i) { return FSUB(f[i], f[i + 1]); }
 
-// rho = f_0 + s_1 + s_2 + ...  (collide.comp:383-388, pairwise order)
-template <int Q, class R>
-__device__ __forceinline__ R density_of(const R (&f)[Q]) {
+// shifted storage: rho = 1 + (g_0 + s_1 + s_2 + ...) (pairwise order), the
+// populations held times 2^SCE: rho = fma(sum, 2^-SCE, 1)
+template <int Q, int SCE, class R>
+__device__ __forceinline__ R density_shifted(const R (&f)[Q]) {
     R rho = f[0];
 #pragma unroll
     for (int i = 1; i < Q; i += 2) rho = FADD(rho, pair_sum<Q>(f, i));
+    return SCE ? FFMA(rho, R(1.0 / (double)(1 << SCE)), R(1)) : FADD(R(1), rho);
+}
+// compute_density (collide.comp:383-388): the populations in order
+template <int Q, class R>
+__device__ __forceinline__ R density_lit(const R (&f)[Q]) {
+    R rho = f[0];
+#pragma unroll
+    for (int i = 1; i < Q; i++) rho = FADD(rho, f[i]);
     return rho;
 }
+template <int Q, bool SH, int SCE, class R>
+__device__ __forceinline__ R density_of(const R (&f)[Q]) {
+    if constexpr (SH) return density_shifted<Q, SCE>(f);
+    else return density_lit<Q>(f);
+}
 
-// u = j/rho (+ F/(2 rho)) and the velocity limiter (collide.comp:722-725):
-// j from the pair differences, r = 1/rho once, u = j r, u = fma(F, r/2, u).
+// shifted storage: u = j/rho (+ F/(2 rho)) and the velocity limiter
+// (collide.comp:722-725): j from the pair differences, r = 1/rho once,
+// u = j r, u = fma(F, r/2, u).
 // |u| > limit is tested on |u|^2 against thresholds t = the largest float
 // whose IEEE square root does not exceed the limit, which decides exactly as
 // sqrt(|u|^2) > limit does; the square root is taken only for limited cells.
@@ -218,39 +285,52 @@ __device__ __forceinline__ void velocity_and_limit(const float (&f)[Q], Moments&
     }
 }
 
-// FP64 reference stepper: the same moments in double; the limiter compares
-// sqrt(|u|^2) with the limits directly, as the FP64 oracle does.
-template <int Q>
-__device__ __forceinline__ void velocity_and_limit(const double (&f)[Q], MomentsT<double>& m, bool forced,
-                                                   double vlim, double vlim_ext) {
+// compute_velocity (collide.comp:390-395) and the limiter (:722-725) as
+// written: j = the populations times their lattice vectors summed in order,
+// u = j/rho, + F/(2 rho) (each a correctly rounded division); |u| > limit
+// decided on the literal u.u (float: against the square-root thresholds,
+// which decides exactly as sqrt(u.u) > limit; double: on the square root);
+// a limited u becomes (u/|u|) * limit.  Forced: the force term is compiled in
+// (adding F/(2 rho) = +0 would change nothing but the sign of a zero).
+template <int Q, class R>
+__device__ __forceinline__ void velocity_literal(const R (&f)[Q], MomentsT<R>& m, bool forced, R vlim, R t_lim,
+                                                 R t_ext) {
     using L = Lattice<Q>;
-    double jx = 0.0, jy = 0.0, jz = 0.0;
+    R jx = R(0), jy = R(0), jz = R(0);
     bool fx = true, fy = true, fz = true;
 #pragma unroll
-    for (int i = 1; i < Q; i += 2) {
+    for (int i = 1; i < Q; i++) {
         const Dir c = L::c(i);
-        const double d = pair_diff<Q>(f, i);
-        if (c.x) { const double t = c.x > 0 ? d : -d; jx = fx ? t : FADD(jx, t); fx = false; }
-        if (c.y) { const double t = c.y > 0 ? d : -d; jy = fy ? t : FADD(jy, t); fy = false; }
-        if (c.z) { const double t = c.z > 0 ? d : -d; jz = fz ? t : FADD(jz, t); fz = false; }
+        const R d = f[i];
+        if (c.x) { const R t = c.x > 0 ? d : -d; jx = fx ? t : FADD(jx, t); fx = false; }
+        if (c.y) { const R t = c.y > 0 ? d : -d; jy = fy ? t : FADD(jy, t); fy = false; }
+        if (c.z) { const R t = c.z > 0 ? d : -d; jz = fz ? t : FADD(jz, t); fz = false; }
     }
-    const double r = __ddiv_rn(1.0, m.rho);
-    m.ux = FMUL(jx, r);
-    m.uy = FMUL(jy, r);
-    m.uz = FMUL(jz, r);
+    m.ux = FDIV(jx, m.rho);
+    m.uy = FDIV(jy, m.rho);
+    m.uz = FDIV(jz, m.rho);
     if (forced) {
-        const double h = FMUL(r, 0.5);
-        m.ux = FFMA(m.Fx, h, m.ux);
-        m.uy = FFMA(m.Fy, h, m.uy);
-        m.uz = FFMA(m.Fz, h, m.uz);
+        const R d2 = FMUL(R(2), m.rho);
+        m.ux = FADD(m.ux, FDIV(m.Fx, d2));
+        m.uy = FADD(m.uy, FDIV(m.Fy, d2));
+        m.uz = FADD(m.uz, FDIV(m.Fz, d2));
     }
-    const double len = __dsqrt_rn(uu_of(m.ux, m.uy, m.uz));
-    m.out_ext = len > vlim_ext;
-    if (len > vlim) {
-        const double q = __ddiv_rn(vlim, len);
-        m.ux = FMUL(m.ux, q);
-        m.uy = FMUL(m.uy, q);
-        m.uz = FMUL(m.uz, q);
+    const R uu = dot_lit(m.ux, m.uy, m.uz, m.ux, m.uy, m.uz);
+    bool lim;
+    R len = R(0);
+    if constexpr (sizeof(R) == 4) {
+        m.out_ext = uu > t_ext;
+        lim = uu > t_lim;
+        if (lim) len = sqrtf(uu);
+    } else {
+        len = __dsqrt_rn(uu);
+        m.out_ext = len > t_ext;
+        lim = len > vlim;
+    }
+    if (lim) {
+        m.ux = FMUL(FDIV(m.ux, len), vlim);
+        m.uy = FMUL(FDIV(m.uy, len), vlim);
+        m.uz = FMUL(FDIV(m.uz, len), vlim);
     }
 }
 
@@ -267,54 +347,84 @@ __device__ __forceinline__ void velocity_and_limit(const double (&f)[Q], Moments
 // populations become the equilibrium (BGK: feq, TRT: e+ +- e-).
 // SH (shifted storage): f holds g = f - w and every equilibrium is formed
 // as g_eq = fma(w rho, bracket, -w); the rest of the update is unchanged.
-template <int Q, bool SH, class Emit>
-__device__ __forceinline__ void collide_emit(const float (&f)[Q], const Moments& m, const StepParams& p, bool trt,
+// launch constants of the collision in the arithmetic type
+template <class R> struct Coef { R R2, R4, R2h, R4h, Rtau, P, Wm, Pp, Pm, cs2, cs4, tau; };
+__device__ __forceinline__ Coef<float> coef_of(const StepParams& p, float) {
+    return Coef<float>{p.R2, p.R4, p.R2h, p.R4h, p.Rtau, p.P, p.Wm, p.Pp, p.Pm, p.cs2, p.cs4, p.tau};
+}
+__device__ __forceinline__ Coef<double> coef_of(const StepParams& p, double) {
+    return Coef<double>{p.k64.R2, p.k64.R4, p.k64.R2h, p.k64.R4h, p.k64.Rtau, p.k64.P, p.k64.Wm, p.k64.Pp,
+                        p.k64.Pm, p.k64.cs2, p.k64.cs4, p.k64.tau};
+}
+
+template <int Q, bool SH, class R, class Emit>
+__device__ __forceinline__ void collide_emit(const R (&f)[Q], const MomentsT<R>& m, const Coef<R>& k, bool trt,
                                              bool src, bool to_equilibrium, Emit emit) {
     using L = Lattice<Q>;
-    const float one_m = FSUB(1.0f, FMUL(uu_of(m.ux, m.uy, m.uz), p.R2h));
-    const float fuR2 = FMUL(FFMA(m.Fz, m.uz, FFMA(m.Fy, m.uy, FMUL(m.Fx, m.ux))), p.R2);
+    using W = LatticeW<Q, R>;
+    if (!SH && (to_equilibrium || !trt)) {
+        // collide.comp:727-745 with :589-629 as written: f + (-(f - feq)/tau) + source
+        const R uuh = uuh_of(m.ux, m.uy, m.uz, k.cs2);
+        const R fuc = src ? FDIV(dot_lit(m.Fx, m.Fy, m.Fz, m.ux, m.uy, m.uz), k.cs2) : R(0);
+#pragma unroll
+        for (int i = 0; i < Q; i++) {
+            const Dir c = L::c(i);
+            const R w = W::w(i);
+            const R cu = cdot_rt(c, m.ux, m.uy, m.uz);
+            const R fe = feq_lit(FMUL(w, m.rho), cu, k.cs2, k.cs4, uuh);
+            R v = FSUB(f[i], FDIV(FSUB(f[i], fe), k.tau));
+            if (src) {
+                const R fc = cdot_rt(c, m.Fx, m.Fy, m.Fz);
+                v = FADD(v, FMUL(FMUL(k.P, w), FADD(FDIV(fc, k.cs2), FSUB(FDIV(FMUL(fc, cu), k.cs4), fuc))));
+            }
+            emit(i, (to_equilibrium || m.out_ext) ? fe : v);
+        }
+        return;
+    }
+    const R one_m = FSUB(R(1), FMUL(uu_of(m.ux, m.uy, m.uz), k.R2h));
+    const R fuR2 = FMUL(FFMA(m.Fz, m.uz, FFMA(m.Fy, m.uy, FMUL(m.Fx, m.ux))), k.R2);
     if (to_equilibrium || !trt) {
 #pragma unroll
         for (int i = 0; i < Q; i++) {
             const Dir c = L::c(i);
-            const float w = L::w(i);
-            const float cu = cdot_rt(c, m.ux, m.uy, m.uz);
-            const float br = bracket(cu, one_m, p.R2, p.R4h);
-            const float fe = SH ? FFMA(FMUL(w, m.rho), br, -w) : FMUL(FMUL(w, m.rho), br);
-            float v = FFMA(FSUB(fe, f[i]), p.Rtau, f[i]);  // old + (-(old - feq)/tau)
+            const R w = W::w(i);
+            const R cu = cdot_rt(c, m.ux, m.uy, m.uz);
+            const R br = bracket(cu, one_m, k.R2, k.R4h);
+            const R fe = SH ? FFMA(FMUL(w, m.rho), br, -w) : FMUL(FMUL(w, m.rho), br);
+            R v = FFMA(FSUB(fe, f[i]), k.Rtau, f[i]);  // old + (-(old - feq)/tau)
             if (src) {
-                const float fc = cdot_rt(c, m.Fx, m.Fy, m.Fz);
-                v = FFMA(FMUL(p.P, w), FFMA(fc, p.R2, FFMA(FMUL(fc, cu), p.R4, -fuR2)), v);
+                const R fc = cdot_rt(c, m.Fx, m.Fy, m.Fz);
+                v = FFMA(FMUL(k.P, w), FFMA(fc, k.R2, FFMA(FMUL(fc, cu), k.R4, -fuR2)), v);
             }
             emit(i, (to_equilibrium || m.out_ext) ? fe : v);
         }
         return;
     }
     {
-        const float w0 = L::w(0);
-        const float fe0 = SH ? FFMA(FMUL(w0, m.rho), one_m, -w0) : FMUL(FMUL(w0, m.rho), one_m);
-        float v = FFMA(FSUB(fe0, f[0]), p.Rtau, f[0]);
-        if (src) v = FFMA(FMUL(p.Pp, w0), -fuR2, v);
+        const R w0 = W::w(0);
+        const R fe0 = SH ? FFMA(FMUL(w0, m.rho), one_m, -w0) : FMUL(FMUL(w0, m.rho), one_m);
+        R v = FFMA(FSUB(fe0, f[0]), k.Rtau, f[0]);
+        if (src) v = FFMA(FMUL(k.Pp, w0), -fuR2, v);
         emit(0, m.out_ext ? fe0 : v);
     }
 #pragma unroll
     for (int i = 1; i < Q; i += 2) {
         const int j = i + 1;
         const Dir c = L::c(i);
-        const float w = L::w(i);
-        const float cu = cdot_rt(c, m.ux, m.uy, m.uz);
-        const float wr = FMUL(w, m.rho);
-        const float be = FFMA(FMUL(cu, cu), p.R4h, one_m);
-        const float ep = SH ? FFMA(wr, be, -w) : FMUL(wr, be);
-        const float em = FMUL(FMUL(wr, p.R2), cu);
-        const float Pd = FFMA(pair_sum<Q>(f, i), 0.5f, -ep);
-        const float Md = FFMA(pair_diff<Q>(f, i), 0.5f, -em);
-        float vi = FFMA(-Md, p.Wm, FFMA(-Pd, p.Rtau, f[i]));
-        float vj = FFMA(Md, p.Wm, FFMA(-Pd, p.Rtau, f[j]));
+        const R w = W::w(i);
+        const R cu = cdot_rt(c, m.ux, m.uy, m.uz);
+        const R wr = FMUL(w, m.rho);
+        const R be = FFMA(FMUL(cu, cu), k.R4h, one_m);
+        const R ep = SH ? FFMA(wr, be, -w) : FMUL(wr, be);
+        const R em = FMUL(FMUL(wr, k.R2), cu);
+        const R Pd = FFMA(pair_sum<Q>(f, i), R(0.5), -ep);
+        const R Md = FFMA(pair_diff<Q>(f, i), R(0.5), -em);
+        R vi = FFMA(-Md, k.Wm, FFMA(-Pd, k.Rtau, f[i]));
+        R vj = FFMA(Md, k.Wm, FFMA(-Pd, k.Rtau, f[j]));
         if (src) {
-            const float fc = cdot_rt(c, m.Fx, m.Fy, m.Fz);
-            const float Sp = FMUL(FMUL(p.Pp, w), FFMA(FMUL(fc, cu), p.R4, -fuR2));
-            const float Sm = FMUL(FMUL(p.Pm, w), FMUL(fc, p.R2));
+            const R fc = cdot_rt(c, m.Fx, m.Fy, m.Fz);
+            const R Sp = FMUL(FMUL(k.Pp, w), FFMA(FMUL(fc, cu), k.R4, -fuR2));
+            const R Sm = FMUL(FMUL(k.Pm, w), FMUL(fc, k.R2));
             vi = FADD(vi, FADD(Sp, Sm));
             vj = FADD(vj, FSUB(Sp, Sm));
         }
@@ -323,20 +433,11 @@ __device__ __forceinline__ void collide_emit(const float (&f)[Q], const Moments&
     }
 }
 
-// launch constants of the collision in the arithmetic type
-template <class R> struct Coef { R R2, R4, R2h, R4h, Rtau, P, Wm, Pp, Pm; };
-__device__ __forceinline__ Coef<float> coef_of(const StepParams& p, float) {
-    return Coef<float>{p.R2, p.R4, p.R2h, p.R4h, p.Rtau, p.P, p.Wm, p.Pp, p.Pm};
-}
-__device__ __forceinline__ Coef<double> coef_of(const StepParams& p, double) {
-    return Coef<double>{p.k64.R2, p.k64.R4, p.k64.R2h, p.k64.R4h, p.k64.Rtau, p.k64.P, p.k64.Wm, p.k64.Pp, p.k64.Pm};
-}
-
 // The same arithmetic as collide_emit with the collision model, the source
 // term and the extreme-velocity case fixed at compile time (the fast kernel
 // branches once per cell on the rare extreme case instead of selecting per
-// population); R = float is the canonical FP32 evaluation, R = double the
-// FP64 reference stepper.
+// population); R = float is the FP32 evaluation, R = double the FP64
+// reference stepper (the literal tree in double).
 // SCE (shifted storage only): f holds G = g * 2^SCE and every weight of the
 // shifted arithmetic is taken times 2^SCE, so that the emitted values are the
 // g update's times 2^SCE exactly.
@@ -347,6 +448,26 @@ __device__ __forceinline__ void collide_fixed(const R (&f)[Q], const MomentsT<R>
         __device__ __forceinline__ static constexpr R w(int i) { return LatticeW<Q, R>::w(i) * R(1 << SCE); }
     };
     static_assert(SH || SCE == 0, "scaled populations are shifted");
+    if (!SH && !TRT) {
+        // collide.comp:727-745 with :589-629 as written: f + (-(f - feq)/tau) + source
+        const R uuh = uuh_of(m.ux, m.uy, m.uz, k.cs2);
+        const R fuc = SRC ? FDIV(dot_lit(m.Fx, m.Fy, m.Fz, m.ux, m.uy, m.uz), k.cs2) : R(0);
+#pragma unroll
+        for (int i = 0; i < Q; i++) {
+            const Dir c = L::c(i);
+            const R w = W::w(i);
+            const R cu = cdot_rt(c, m.ux, m.uy, m.uz);
+            const R fe = feq_lit(FMUL(w, m.rho), cu, k.cs2, k.cs4, uuh);
+            if (EXT) { emit(i, fe); continue; }
+            R v = FSUB(f[i], FDIV(FSUB(f[i], fe), k.tau));
+            if (SRC) {
+                const R fc = cdot_rt(c, m.Fx, m.Fy, m.Fz);
+                v = FADD(v, FMUL(FMUL(k.P, w), FADD(FDIV(fc, k.cs2), FSUB(FDIV(FMUL(fc, cu), k.cs4), fuc))));
+            }
+            emit(i, v);
+        }
+        return;
+    }
     const R one_m = FSUB(R(1), FMUL(uu_of(m.ux, m.uy, m.uz), k.R2h));
     const R fuR2 = SRC ? FMUL(FFMA(m.Fz, m.uz, FFMA(m.Fy, m.uy, FMUL(m.Fx, m.ux))), k.R2) : R(0);
     if (!TRT) {
@@ -511,8 +632,9 @@ __device__ __forceinline__ float sc_force(const StepParams& p, uint32_t n, int o
         if (c.y) sy = FADD(sy, c.y > 0 ? wp : -wp);
         if (c.z) sz = FADD(sz, c.z > 0 ? wp : -wp);
     }
+    // interaction_force *= -self_psi * G; force += interaction_force (:580-583, :718-720)
     const float k = FMUL(-self_psi, p.G);
-    m.Fx = FFMA(sx, k, m.Fx); m.Fy = FFMA(sy, k, m.Fy); m.Fz = FFMA(sz, k, m.Fz);
+    m.Fx = FADD(m.Fx, FMUL(sx, k)); m.Fy = FADD(m.Fy, FMUL(sy, k)); m.Fz = FADD(m.Fz, FMUL(sz, k));
     return self_psi;
 }
 
@@ -525,24 +647,68 @@ __device__ __forceinline__ float thermal_buoyancy(const StepParams& p, uint32_t 
     float temperature = 0.f;
 #pragma unroll
     for (int i = 0; i < QT; i++) temperature = FADD(temperature, __ldg(p.th_src + (uint64_t)i * p.stride + n));
+    // buoyancy = -beta (T - 1) force; force += buoyancy
     const float k = FMUL(-p.beta, FSUB(temperature, 1.0f));
-    m.Fx = FFMA(k, m.Fx, m.Fx); m.Fy = FFMA(k, m.Fy, m.Fy); m.Fz = FFMA(k, m.Fz, m.Fz);
+    m.Fx = FADD(m.Fx, FMUL(k, m.Fx)); m.Fy = FADD(m.Fy, FMUL(k, m.Fy)); m.Fz = FADD(m.Fz, FMUL(k, m.Fz));
     return temperature;
 }
 
-// thermal BGK towards g_eq(T, u) (collide.comp:771-782)
+// thermal BGK towards g_eq(T, u) as written (collide.comp:771-782, :634-651,
+// :668-670): g + (-(g - g_eq)/tau_T)
+__device__ __forceinline__ float thermal_relax(const StepParams& p, float g, float geq) {
+    return FSUB(g, FDIV(FSUB(g, geq), p.tau_t));
+}
 template <int Q>
 __device__ __forceinline__ void thermal_collide(const StepParams& p, uint32_t n, const Moments& m, float temperature) {
     constexpr int QT = Lattice<Q>::D == 2 ? 5 : 7;
-    const float one_m = FSUB(1.0f, FMUL(uu_of(m.ux, m.uy, m.uz), p.R2h));
+    const float uuh = uuh_of(m.ux, m.uy, m.uz, p.cs2);
 #pragma unroll
     for (int i = 0; i < QT; i++) {
         const Dir c = ThermalLattice<QT>::c(i);
         const float w = ThermalLattice<QT>::w(i);
         const float cu = cdot_rt(c, m.ux, m.uy, m.uz);
-        const float geq = FMUL(FMUL(w, temperature), bracket(cu, one_m, p.R2, p.R4h));
+        const float geq = feq_lit(FMUL(w, temperature), cu, p.cs2, p.cs4, uuh);
         const float g = __ldg(p.th_src + (uint64_t)i * p.stride + n);
-        p.th_tgt[(uint64_t)i * p.stride + n] = FFMA(FSUB(geq, g), p.Rtau_t, g);
+        p.th_tgt[(uint64_t)i * p.stride + n] = thermal_relax(p, g, geq);
+    }
+}
+
+// the generic step's thermal lattice, pseudopotential and launch constants
+// in the arithmetic type R (float: the FP32 buffers; double: the FP64
+// stepper's)
+__device__ __forceinline__ const float* th_src_of(const StepParams& p, float) { return p.th_src; }
+__device__ __forceinline__ float* th_tgt_of(const StepParams& p, float) { return p.th_tgt; }
+__device__ __forceinline__ const float* psi_src_of(const StepParams& p, float) { return p.psi_src; }
+__device__ __forceinline__ float* psi_tgt_of(const StepParams& p, float) { return p.psi_tgt; }
+__device__ __forceinline__ const double* th_src_of(const StepParams& p, double) { return p.th_src64; }
+__device__ __forceinline__ double* th_tgt_of(const StepParams& p, double) { return p.th_tgt64; }
+__device__ __forceinline__ const double* psi_src_of(const StepParams& p, double) { return p.psi_src64; }
+__device__ __forceinline__ double* psi_tgt_of(const StepParams& p, double) { return p.psi_tgt64; }
+template <class R> struct Knobs { R tau_t, beta, G, vlim, t_lim, t_ext, fx, fy, fz; };
+__device__ __forceinline__ Knobs<float> knobs_of(const StepParams& p, float) {
+    return Knobs<float>{p.tau_t, p.beta, p.G, p.vlim, p.t_lim, p.t_ext, p.fconst[0], p.fconst[1], p.fconst[2]};
+}
+// double: the limiter compares the square root itself (t_lim = vlim, t_ext = the extreme limit)
+__device__ __forceinline__ Knobs<double> knobs_of(const StepParams& p, double) {
+    return Knobs<double>{p.k64.tau_t, p.k64.beta, p.k64.G, p.k64.vlim, p.k64.vlim, p.k64.vlim_ext,
+                         p.k64.fconst[0], p.k64.fconst[1], p.k64.fconst[2]};
+}
+// the thermal collision of the generic step in the arithmetic type R
+template <int Q, class R>
+__device__ __forceinline__ void thermal_collide_r(const StepParams& p, uint32_t n, const MomentsT<R>& m, R temperature,
+                                                  const Coef<R>& k, R tau_t) {
+    constexpr int QT = Lattice<Q>::D == 2 ? 5 : 7;
+    const R uuh = uuh_of(m.ux, m.uy, m.uz, k.cs2);
+    const R* src = th_src_of(p, R(0));
+    R* tgt = th_tgt_of(p, R(0));
+#pragma unroll
+    for (int i = 0; i < QT; i++) {
+        const Dir c = ThermalLattice<QT>::c(i);
+        const R w = ThermalW<QT, R>::w(i);
+        const R cu = cdot_rt(c, m.ux, m.uy, m.uz);
+        const R geq = feq_lit(FMUL(w, temperature), cu, k.cs2, k.cs4, uuh);
+        const R g = __ldg(src + (uint64_t)i * p.stride + n);
+        tgt[(uint64_t)i * p.stride + n] = FSUB(g, FDIV(FSUB(g, geq), tau_t));
     }
 }
 
@@ -562,16 +728,16 @@ __device__ __forceinline__ void thermal_collide_push(const StepParams& p, uint32
     constexpr int QT = Lattice<Q>::D == 2 ? 5 : 7;
     using TL = ThermalLattice<QT>;
     const uint64_t S = p.stride;
-    const float one_m = FSUB(1.0f, FMUL(uu_of(m.ux, m.uy, m.uz), p.R2h));
+    const float uuh = uuh_of(m.ux, m.uy, m.uz, p.cs2);
     float a[QT], b[QT];
 #pragma unroll
     for (int i = 0; i < QT; i++) {
         const Dir c = TL::c(i);
         const float w = TL::w(i);
         const float cu = cdot_rt(c, m.ux, m.uy, m.uz);
-        const float geq = FMUL(FMUL(w, temperature), bracket(cu, one_m, p.R2, p.R4h));
+        const float geq = feq_lit(FMUL(w, temperature), cu, p.cs2, p.cs4, uuh);
         a[i] = __ldg(p.th_src + (uint64_t)i * S + n);
-        b[i] = FFMA(FSUB(geq, a[i]), p.Rtau_t, a[i]);
+        b[i] = thermal_relax(p, a[i], geq);
     }
     p.th_tgt[n] = b[0];
 #pragma unroll
@@ -683,8 +849,7 @@ __device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepP
     // the update runs on the stored values times 1/SCALE implied: G = g * SCALE
     constexpr int SCE = C::SCALE_EXP;
     MomentsT<R> m;
-    m.rho = density_of<Q>(f);
-    if (C::SHIFTED) m.rho = SCE ? FFMA(m.rho, R(1.0f / C::SCALE), R(1)) : FADD(R(1), m.rho);  // sum of g plus sum of w
+    m.rho = density_of<Q, C::SHIFTED, SCE>(f);
     if (!(m.rho == m.rho)) atomicOr(p.err, 1u);
     m.rho = m.rho < R(0.01) ? R(0.01) : m.rho;
     constexpr bool F64 = sizeof(R) == 8;
@@ -700,8 +865,9 @@ __device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepP
         static_assert(FORCED, "thermal flow runs with the source term on");
         temperature = thermal_buoyancy<Q>(p, n, m);
     }
-    if constexpr (F64) velocity_and_limit<Q>(f, m, FORCED, p.k64.vlim, p.k64.vlim_ext);
-    else velocity_and_limit<Q, SCE>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
+    if constexpr (F64) velocity_literal<Q>(f, m, FORCED, p.k64.vlim, p.k64.vlim, p.k64.vlim_ext);
+    else if constexpr (C::SHIFTED) velocity_and_limit<Q, SCE>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
+    else velocity_literal<Q>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
     if (p.flags & F_UPDATE) {
         const Coef<R> k = coef_of(p, R(0));
         auto emit = [&](int i, R v) { *ptr_st(opp(i)) = C::raw_enc(v); };
@@ -842,8 +1008,7 @@ __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, i
 #pragma unroll
         for (int i = 0; i < Q; i++) f[i] = C::raw_dec(to16(half ? (ld[i] >> 16) : ld[i]));
         Moments m;
-        m.rho = density_of<Q>(f);
-        if (C::SHIFTED) m.rho = SCE ? FFMA(m.rho, 1.0f / C::SCALE, 1.0f) : FADD(1.0f, m.rho);
+        m.rho = density_of<Q, C::SHIFTED, SCE>(f);
         if (!(m.rho == m.rho)) atomicOr(p.err, 1u);
         m.rho = m.rho < 0.01f ? 0.01f : m.rho;
         m.Fx = FORCED ? p.fconst[0] : 0.f;
@@ -857,7 +1022,8 @@ __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, i
             const int oxp = half ? (x + 2 == nx ? 1 - nx : 1) : 1;
             psi_self = sc_force<Q>(p, n + half, oxm, oxp, oym, oyp, ozm, ozp, m);
         }
-        velocity_and_limit<Q, SCE>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
+        if constexpr (C::SHIFTED) velocity_and_limit<Q, SCE>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
+        else velocity_literal<Q>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
         auto emit = [&](int i, float v) {
             const int o = opp(i);
             if constexpr (std::is_same<T, __half>::value) {
@@ -1029,8 +1195,7 @@ __device__ __forceinline__ CellSum masked_cell(const StepParams& p, int x, int y
     asm volatile("" : "+r"(n_st), "+r"(oxm_st), "+r"(oxp_st));
 
     Moments m;
-    m.rho = density_of<Q>(f);
-    if (C::SHIFTED) m.rho = FADD(1.0f, m.rho);
+    m.rho = density_of<Q, C::SHIFTED, 0>(f);
     if (!(m.rho == m.rho)) atomicOr(p.err, 1u);
     m.rho = m.rho < 0.01f ? 0.01f : m.rho;
     m.Fx = FORCED ? p.fconst[0] : 0.f;
@@ -1040,7 +1205,8 @@ __device__ __forceinline__ CellSum masked_cell(const StepParams& p, int x, int y
     if (THERMAL) temperature = thermal_buoyancy<Q>(p, n, m);  // the generic kernel's buoyancy
     // thermal flow is forced with the source term on, as in the generic kernel
     constexpr bool FRC = FORCED || THERMAL;
-    velocity_and_limit<Q>(f, m, FRC, p.vlim, p.t_lim, p.t_ext);
+    if constexpr (C::SHIFTED) velocity_and_limit<Q>(f, m, FRC, p.vlim, p.t_lim, p.t_ext);
+    else velocity_literal<Q>(f, m, FRC, p.vlim, p.t_lim, p.t_ext);
     if (eqb) {
         const int kind = __ldg(p.obj_kind + bid);
         if (kind == 1) { m.ux = bv.y; m.uy = bv.z; m.uz = bv.w; } else { m.rho = bv.x; }
@@ -1175,15 +1341,19 @@ __global__ void __launch_bounds__(kStepBlock, BF_MIXED_MIN_BLOCKS) masked_mixed_
 // lattice, Shan-Chen pseudopotential, field saving and reductions
 // ---------------------------------------------------------------------------
 template <int Q, int ST, int MODE>
-__device__ __forceinline__ CellSum cell_update(const StepParams& p, int x, int y, int z) {
+__device__ __forceinline__ CellSumT<typename Codec<ST>::R> cell_update(const StepParams& p, int x, int y, int z) {
     using L = Lattice<Q>;
     using C = Codec<ST>;
     using T = typename C::T;
+    using R = typename C::R;
+    using W = LatticeW<Q, R>;
     const int nx = p.nx, ny = p.ny, nz = p.nz;
     const uint32_t flags = p.flags;
     const uint32_t n = (uint32_t)x + (uint32_t)nx * ((uint32_t)y + (uint32_t)ny * (uint32_t)z);
     auto plane = [&](int i) -> T* { return static_cast<T*>(p.plane[i]); };
-    CellSum out = {0.f, 0.f, 0.f, 0.f, 0.f};
+    CellSumT<R> out = {R(0), R(0), R(0), R(0), R(0)};
+    const Coef<R> k = coef_of(p, R(0));
+    const Knobs<R> kn = knobs_of(p, R(0));
 
     uint32_t bid = 0;
     if (flags & F_BOUNDARIES) {
@@ -1202,11 +1372,11 @@ __device__ __forceinline__ CellSum cell_update(const StepParams& p, int x, int y
     if (eqb && p.bvals) bv = __ldg(p.bvals + n);
 
     // ---- load (AA read, collide.comp:244-305) ----
-    float f[Q];
+    R f[Q];
 #pragma unroll
     for (int i = 0; i < Q; i++) {
         const Dir c = L::c(i);
-        const float w = L::w(i);
+        const R w = W::w(i);
         int sx = x - c.x, sy = y - c.y, sz = z - c.z;
         bool sopen;
         coords_wrap<Q>(sx, sy, sz, nx, ny, nz, sopen, flags);
@@ -1215,10 +1385,11 @@ __device__ __forceinline__ CellSum cell_update(const StepParams& p, int x, int y
         if (MODE != AA_LOCAL && (eqb || (flags & F_BOUNCE_BACK)) && i != 0) {
             if (eqb && sopen) {
                 // population entering from outside the domain: f_eq(rho_b, u_b)
-                const float cu = cdot_rt(c, bv.y, bv.z, bv.w);
-                const float one_mb = FSUB(1.0f, FMUL(uu_of(bv.y, bv.z, bv.w), p.R2h));
-                const float br = bracket(cu, one_mb, p.R2, p.R4h);
-                f[i] = C::SHIFTED ? FFMA(FMUL(w, bv.x), br, -w) : FMUL(FMUL(w, bv.x), br);
+                const R bx = R(bv.y), by = R(bv.z), bz = R(bv.w);
+                const R cu = cdot_rt(c, bx, by, bz);
+                const R one_mb = FSUB(R(1), FMUL(uu_of(bx, by, bz), k.R2h));
+                const R br = bracket(cu, one_mb, k.R2, k.R4h);
+                f[i] = C::SHIFTED ? FFMA(FMUL(w, R(bv.x)), br, -w) : FMUL(FMUL(w, R(bv.x)), br);
                 done = true;
             } else if ((flags & F_BOUNCE_BACK) && !sopen && (flags & F_BOUNDARIES)) {
                 const uint32_t sid = boundary_id(p.bnd, p.bits, sn);
@@ -1228,8 +1399,9 @@ __device__ __forceinline__ CellSum cell_update(const StepParams& p, int x, int y
                     // stream.comp:487-496 with rho_wall = 1
                     const float4 uw = __ldg(p.objects + 3u * sid);
                     const Dir co = L::c(opp(i));
-                    const float wall = FMUL(FMUL(-2.f * w, co.x * uw.x + co.y * uw.y + co.z * uw.z), 3.f);
-                    const float v = (MODE == AA_EVEN) ? C::dec(plane(opp(i))[n], w) : C::dec(plane(i)[sn], w);
+                    const R dw = FADD(FADD(FMUL(R(co.x), R(uw.x)), FMUL(R(co.y), R(uw.y))), FMUL(R(co.z), R(uw.z)));
+                    const R wall = FMUL(FMUL(R(-2) * w, dw), R(3));
+                    const R v = (MODE == AA_EVEN) ? C::dec(plane(opp(i))[n], w) : C::dec(plane(i)[sn], w);
                     f[i] = FADD(v, wall);
                     done = true;
                 }
@@ -1237,61 +1409,63 @@ __device__ __forceinline__ CellSum cell_update(const StepParams& p, int x, int y
         }
         if (!done) {
             // out-of-domain reads give 0.01 (collide.comp:278-298), g = 0.01 - w when shifted
-            if (MODE == AA_EVEN) f[i] = sopen ? (C::SHIFTED ? FSUB(0.01f, w) : 0.01f) : C::dec(plane(i)[sn], w);
+            if (MODE == AA_EVEN) f[i] = sopen ? (C::SHIFTED ? FSUB(R(0.01), w) : R(0.01)) : C::dec(plane(i)[sn], w);
             else if (MODE == AA_ODD) f[i] = C::dec(plane(opp(i))[n], w);
             else f[i] = C::dec(plane(i)[n], w);
         }
     }
 
     // ---- moments and forces (collide.comp:702-725) ----
-    Moments m;
-    m.rho = density_of<Q>(f);
-    if (C::SHIFTED) m.rho = FADD(1.0f, m.rho);  // sum of g plus sum of w
+    MomentsT<R> m;
+    m.rho = density_of<Q, C::SHIFTED, 0>(f);
     if (!(m.rho == m.rho)) atomicOr(p.err, 1u);
-    m.rho = m.rho < 0.01f ? 0.01f : m.rho;  // max(density, 0.01), NaN kept
-    m.Fx = m.Fy = m.Fz = 0.f;
-    if (flags & F_FORCE_CONST) { m.Fx = p.fconst[0]; m.Fy = p.fconst[1]; m.Fz = p.fconst[2]; }
-    if (flags & F_FORCE_FIELD) { const float4 fv = __ldg(p.force + n); m.Fx = fv.x; m.Fy = fv.y; m.Fz = fv.z; }
-    float temperature = 0.f;
+    m.rho = m.rho < R(0.01) ? R(0.01) : m.rho;  // max(density, 0.01), NaN kept
+    m.Fx = m.Fy = m.Fz = R(0);
+    if (flags & F_FORCE_CONST) { m.Fx = kn.fx; m.Fy = kn.fy; m.Fz = kn.fz; }
+    if (flags & F_FORCE_FIELD) { const float4 fv = __ldg(p.force + n); m.Fx = R(fv.x); m.Fy = R(fv.y); m.Fz = R(fv.z); }
+    R temperature = R(0);
     constexpr int QT = L::D == 2 ? 5 : 7;
     if (flags & F_THERMAL) {
+        const R* th = th_src_of(p, R(0));
 #pragma unroll
-        for (int i = 0; i < QT; i++) temperature = FADD(temperature, __ldg(p.th_src + (uint64_t)i * p.stride + n));
-        const float k = FMUL(-p.beta, FSUB(temperature, 1.0f));
-        m.Fx = FFMA(k, m.Fx, m.Fx); m.Fy = FFMA(k, m.Fy, m.Fy); m.Fz = FFMA(k, m.Fz, m.Fz);
+        for (int i = 0; i < QT; i++) temperature = FADD(temperature, __ldg(th + (uint64_t)i * p.stride + n));
+        const R kb = FMUL(-kn.beta, FSUB(temperature, R(1)));  // buoyancy (collide.comp:709-716)
+        m.Fx = FADD(m.Fx, FMUL(kb, m.Fx)); m.Fy = FADD(m.Fy, FMUL(kb, m.Fy)); m.Fz = FADD(m.Fz, FMUL(kb, m.Fz));
     }
     if (flags & F_MULTIPHASE) {  // collide.comp:534-584
-        const float self_psi = FSUB(1.0f, exp_f32(-m.rho));
-        float sx = 0.f, sy = 0.f, sz = 0.f;
+        const R self_psi = psi_of(m.rho);
+        const R* ps_src = psi_src_of(p, R(0));
+        R sx = R(0), sy = R(0), sz = R(0);
 #pragma unroll
         for (int i = 1; i < Q; i++) {
             const Dir c = L::c(i);
             int ax = x + c.x, ay = y + c.y, az = z + c.z;
             bool aopen;
             coords_wrap<Q>(ax, ay, az, nx, ny, nz, aopen, flags);
-            const float ps = aopen ? self_psi
-                                   : __ldg(p.psi_src + (uint32_t)ax + (uint32_t)nx * ((uint32_t)ay + (uint32_t)ny * (uint32_t)az));
-            const float wp = FMUL(L::w(i), ps);
+            const R ps = aopen ? self_psi
+                               : __ldg(ps_src + (uint32_t)ax + (uint32_t)nx * ((uint32_t)ay + (uint32_t)ny * (uint32_t)az));
+            const R wp = FMUL(W::w(i), ps);
             if (c.x) sx = FADD(sx, c.x > 0 ? wp : -wp);
             if (c.y) sy = FADD(sy, c.y > 0 ? wp : -wp);
             if (c.z) sz = FADD(sz, c.z > 0 ? wp : -wp);
         }
-        const float k = FMUL(-self_psi, p.G);
-        m.Fx = FFMA(sx, k, m.Fx); m.Fy = FFMA(sy, k, m.Fy); m.Fz = FFMA(sz, k, m.Fz);
+        const R ks = FMUL(-self_psi, kn.G);
+        m.Fx = FADD(m.Fx, FMUL(sx, ks)); m.Fy = FADD(m.Fy, FMUL(sy, ks)); m.Fz = FADD(m.Fz, FMUL(sz, ks));
     }
-    velocity_and_limit<Q>(f, m, (flags & (F_FORCE_CONST | F_FORCE_FIELD | F_THERMAL | F_MULTIPHASE)) != 0, p.vlim,
-                          p.t_lim, p.t_ext);
+    const bool forced = (flags & (F_FORCE_CONST | F_FORCE_FIELD | F_THERMAL | F_MULTIPHASE)) != 0;
+    if constexpr (C::SHIFTED) velocity_and_limit<Q>(f, m, forced, p.vlim, p.t_lim, p.t_ext);
+    else velocity_literal<Q>(f, m, forced, kn.vlim, kn.t_lim, kn.t_ext);
     if (eqb) {
         const int kind = __ldg(p.obj_kind + bid);
-        if (kind == 1) { m.ux = bv.y; m.uy = bv.z; m.uz = bv.w; } else { m.rho = bv.x; }
-        m.Fx = m.Fy = m.Fz = 0.f;
+        if (kind == 1) { m.ux = R(bv.y); m.uy = R(bv.z); m.uz = R(bv.w); } else { m.rho = R(bv.x); }
+        m.Fx = m.Fy = m.Fz = R(0);
     }
 
     // ---- collision + AA store (collide.comp:727-760) ----
     if (flags & F_UPDATE) {
-        collide_emit<Q, C::SHIFTED>(f, m, p, (flags & F_TRT) != 0, (flags & F_SOURCE) != 0, eqb, [&](int i, float v) {
+        collide_emit<Q, C::SHIFTED>(f, m, k, (flags & F_TRT) != 0, (flags & F_SOURCE) != 0, eqb, [&](int i, R v) {
             const Dir c = L::c(i);
-            const float w = L::w(i);
+            const R w = W::w(i);
             if (MODE == AA_EVEN) {
                 int dx = x + c.x, dy = y + c.y, dz = z + c.z;
                 bool dopen;
@@ -1305,39 +1479,29 @@ __device__ __forceinline__ CellSum cell_update(const StepParams& p, int x, int y
     }
 
     if ((flags & F_MULTIPHASE) && !(flags & F_MEASURE)) {  // collide.comp:763-769, psi of the effective density
-        float eff = m.rho;
-        if (bid != 0u) eff = __ldg(p.objects + 3u * bid + 2u).w;
-        p.psi_tgt[n] = FSUB(1.0f, exp_f32(-eff));
+        R eff = m.rho;
+        if (bid != 0u) eff = R(__ldg(p.objects + 3u * bid + 2u).w);
+        psi_tgt_of(p, R(0))[n] = psi_of(eff);
     }
-    if ((flags & F_THERMAL) && !(flags & F_MEASURE)) {  // collide.comp:771-782
-        const float one_m = FSUB(1.0f, FMUL(uu_of(m.ux, m.uy, m.uz), p.R2h));
-#pragma unroll
-        for (int i = 0; i < QT; i++) {
-            const Dir c = ThermalLattice<QT>::c(i);
-            const float w = ThermalLattice<QT>::w(i);
-            const float cu = cdot_rt(c, m.ux, m.uy, m.uz);
-            const float geq = FMUL(FMUL(w, temperature), bracket(cu, one_m, p.R2, p.R4h));
-            const float g = __ldg(p.th_src + (uint64_t)i * p.stride + n);
-            p.th_tgt[(uint64_t)i * p.stride + n] = FFMA(FSUB(geq, g), p.Rtau_t, g);  // g + (-(g - geq)/tau_T)
-        }
-    }
+    if ((flags & F_THERMAL) && !(flags & F_MEASURE)) thermal_collide_r<Q>(p, n, m, temperature, k, kn.tau_t);  // :771-782
     if (flags & F_SAVE) {  // collide.comp:784-792
-        p.vel_den[n] = make_float4(m.ux, m.uy, m.uz, m.rho);
-        p.force_temp[n] = make_float4(m.Fx, m.Fy, m.Fz, temperature);
+        p.vel_den[n] = make_float4((float)m.ux, (float)m.uy, (float)m.uz, (float)m.rho);
+        p.force_temp[n] = make_float4((float)m.Fx, (float)m.Fy, (float)m.Fz, (float)temperature);
         if (p.bnd_tex) p.bnd_tex[n] = (uint8_t)bid;
     }
     if (flags & F_REDUCE) {
-        const float uu = uu_of(m.ux, m.uy, m.uz);
+        const R uu = uu_of(m.ux, m.uy, m.uz);
         out.m = m.rho; out.px = m.rho * m.ux; out.py = m.rho * m.uy; out.pz = m.rho * m.uz;
-        out.ke = 0.5f * m.rho * uu;
+        out.ke = R(0.5f) * m.rho * uu;
     }
     return out;
 }
 
 template <int Q, int ST, int MODE>
 __global__ void __launch_bounds__(kStepBlock) step_kernel(const __grid_constant__ StepParams p) {
+    using R = typename Codec<ST>::R;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    CellSum cs = {0.f, 0.f, 0.f, 0.f, 0.f};
+    CellSumT<R> cs = {R(0), R(0), R(0), R(0), R(0)};
     if (x < p.nx) cs = cell_update<Q, ST, MODE>(p, x, blockIdx.y, blockIdx.z);
     if (p.flags & F_REDUCE) block_reduce_store(cs, p.red_partials);
 }
@@ -1384,9 +1548,12 @@ __global__ void __launch_bounds__(kStepBlock) stream_kernel(const __grid_constan
 // ---------------------------------------------------------------------------
 // thermal pull streaming (stream_thermal.comp main, :457-526), SoA layout
 // ---------------------------------------------------------------------------
-template <int QT>
+template <int QT, class R>
 __global__ void __launch_bounds__(kStepBlock) stream_thermal_kernel(const __grid_constant__ ThermalStreamParams p) {
     using TL = ThermalLattice<QT>;
+    // the thermal lattice in the arithmetic type (double: the FP64 stepper)
+    const R* __restrict__ src = sizeof(R) == 8 ? reinterpret_cast<const R*>(p.src64) : reinterpret_cast<const R*>(p.src);
+    R* __restrict__ dst = sizeof(R) == 8 ? reinterpret_cast<R*>(p.dst64) : reinterpret_cast<R*>(p.dst);
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
     if (x >= p.nx) return;
     const uint64_t S = p.stride;
@@ -1404,7 +1571,7 @@ __global__ void __launch_bounds__(kStepBlock) stream_thermal_kernel(const __grid
                 bool open;
                 coords_wrap<QT>(sx, sy, sz, p.nx, p.ny, p.nz, open, p.flags);
                 const uint32_t sn = (uint32_t)sx + (uint32_t)p.nx * ((uint32_t)sy + (uint32_t)p.ny * (uint32_t)sz);
-                p.dst[(uint64_t)i * S + n] = __ldg(p.src + (uint64_t)i * S + sn);
+                dst[(uint64_t)i * S + n] = __ldg(src + (uint64_t)i * S + sn);
             }
             return;
         }
@@ -1422,10 +1589,11 @@ __global__ void __launch_bounds__(kStepBlock) stream_thermal_kernel(const __grid
         uint32_t sid = (p.flags & F_BOUNDARIES) ? boundary_id(p.bnd, p.bits, sn) : 0u;
         if (sid != 0u && solid_id(p.obj_kind, sid)) {
             const int inv = (i == 0) ? 0 : ((i & 1) ? i + 1 : i - 1);
-            const float Tw = __ldg(p.objects + 3u * sid).w;
-            p.dst[(uint64_t)i * S + n] = __fadd_rn(-__ldg(p.src + (uint64_t)inv * S + n), __fmul_rn(2.f * TL::w(inv), Tw));
+            const R Tw = R(__ldg(p.objects + 3u * sid).w);
+            // -g_opp + 2 w_opp T_wall (stream_thermal.comp:440-447, :520-522)
+            dst[(uint64_t)i * S + n] = FADD(-__ldg(src + (uint64_t)inv * S + n), FMUL(R(2) * ThermalW<QT, R>::w(inv), Tw));
         } else {
-            p.dst[(uint64_t)i * S + n] = __ldg(p.src + (uint64_t)i * S + sn);
+            dst[(uint64_t)i * S + n] = __ldg(src + (uint64_t)i * S + sn);
         }
     }
 }
@@ -1501,23 +1669,24 @@ __global__ void init_kernel(const __grid_constant__ InitParams p) {
     }
 }
 
-template <int QT>
+template <int QT, class R>
 __global__ void init_thermal_kernel(const __grid_constant__ InitParams p) {
     using TL = ThermalLattice<QT>;
     const uint64_t n = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (n >= p.n_cells) return;
-    const float t = p.T ? p.T[n] : 1.0f;
-    if (t == 0.0f) return;  // set_equilibrium_populations_thermal.comp:171-172
-    float ux = 0.f, uy = 0.f, uz = 0.f;
+    const R t = p.T ? R(p.T[n]) : R(1);
+    if (t == R(0)) return;  // set_equilibrium_populations_thermal.comp:171-172
+    R ux = R(0), uy = R(0), uz = R(0);
     const uint32_t id = p.ids ? p.ids[n] : 0u;
     const bool solid = id != 0u && p.obj_kind[id] == 0;
-    if (p.u && !solid) { ux = p.u[3 * n]; uy = p.u[3 * n + 1]; uz = p.u[3 * n + 2]; }
-    const float uu = feq_init_dot(ux, uy, uz, ux, uy, uz);
+    if (p.u && !solid) { ux = R(p.u[3 * n]); uy = R(p.u[3 * n + 1]); uz = R(p.u[3 * n + 2]); }
+    const R uu = feq_init_dot(ux, uy, uz, ux, uy, uz);
+    R* th = sizeof(R) == 8 ? reinterpret_cast<R*>(p.th64) : reinterpret_cast<R*>(p.th);
 #pragma unroll
     for (int i = 0; i < QT; i++) {
         const Dir c = TL::c(i);
-        const float cu = feq_init_dot((float)c.x, (float)c.y, (float)c.z, ux, uy, uz);
-        p.th[i * p.stride + n] = feq_init_literal(TL::w(i), t, cu, uu);
+        const R cu = feq_init_dot(R(c.x), R(c.y), R(c.z), ux, uy, uz);
+        th[i * p.stride + n] = feq_init_literal(ThermalW<QT, R>::w(i), t, cu, uu);
     }
 }
 
@@ -1651,8 +1820,9 @@ cudaError_t launch_step_st(const StepParams& p, int mode, int path, cudaStream_t
         const bool forced = (p.flags & F_FORCE_CONST) != 0 || mp;
         auto go = [&](auto kernel) { kernel<<<grid, block, 0, st>>>(p); };
 #define BF_FAST(MODE_, TRT_, F_, MP_) go(fast_step_kernel<Q, ST, MODE_, TRT_, F_, MP_>)
-        if (ST == ST_FP64 && mp) return cudaErrorInvalidValue;  // rejected at initialisation
-        constexpr bool MPX = ST != ST_FP64;  // no multiphase variants of the FP64 stepper
+        // the FP64 stepper's multiphase flow runs the generic kernel (path set by the host)
+        if (ST == ST_FP64 && mp) return cudaErrorInvalidValue;
+        constexpr bool MPX = ST != ST_FP64;  // no multiphase variants of the FP64 fast kernel
         if (mode == AA_EVEN) {
             if (mp) { if (trt) BF_FAST(AA_EVEN, true, true, MPX); else BF_FAST(AA_EVEN, false, true, MPX); }
             else if (trt) { if (forced) BF_FAST(AA_EVEN, true, true, false); else BF_FAST(AA_EVEN, true, false, false); }
@@ -1664,11 +1834,11 @@ cudaError_t launch_step_st(const StepParams& p, int mode, int path, cudaStream_t
         }
 #undef BF_FAST
     } else {
-        // the FP64 reference stepper covers the fast path only
-        if constexpr (ST == ST_FP64) return cudaErrorInvalidValue;
-        else if (mode == AA_EVEN) step_kernel<Q, ST, AA_EVEN><<<grid, block, 0, st>>>(p);
+        // the FP64 reference stepper runs the esoteric-pull modes only
+        if (ST == ST_FP64 && mode == AA_LOCAL) return cudaErrorInvalidValue;  // rejected at initialisation
+        if (mode == AA_EVEN) step_kernel<Q, ST, AA_EVEN><<<grid, block, 0, st>>>(p);
         else if (mode == AA_ODD) step_kernel<Q, ST, AA_ODD><<<grid, block, 0, st>>>(p);
-        else step_kernel<Q, ST, AA_LOCAL><<<grid, block, 0, st>>>(p);
+        else if constexpr (ST != ST_FP64) step_kernel<Q, ST, AA_LOCAL><<<grid, block, 0, st>>>(p);
     }
     return cudaGetLastError();
 }

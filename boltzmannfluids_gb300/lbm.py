@@ -33,7 +33,7 @@ class FloatingPointAccuracy(enum.IntEnum):
     """DDF storage.  fp32/fp16 are the reference's FloatingPointAccuracy
     (FloatingPointAccuracy.h:6-9, fp16 = R16F lattice); fp16s (shifted IEEE
     half of f-w) and fp16c (custom-scaled: IEEE half of (f-w)*2^12) are extensions; fp64 is
-    the FP64 accuracy reference stepper (periodic boxes, no objects)."""
+    the FP64 accuracy reference stepper (every esoteric-pull configuration)."""
     fp32 = 0
     fp16 = 1
     fp16s = 2

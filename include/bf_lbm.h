@@ -53,10 +53,11 @@ typedef enum { BF_D2Q9 = 2, BF_D3Q15 = 3, BF_D3Q19 = 4, BF_D3Q27 = 5 } bf_veloci
  * BF_ERR_UNSTABLE).
  * Arithmetic is FP32 in these four modes.
  * BF_STORE_FP64 (no counterpart in the reference) is the accuracy reference
- * stepper: FP64 populations and FP64 arithmetic in the same operation order
- * as the FP32 path, for fully periodic esoteric-pull boxes without boundary
- * objects, temperature or force fields, or multiphase flow (other
- * configurations fail with BF_ERR_INVALID_ARGUMENT); fields read back as FP32. */
+ * stepper: FP64 populations, thermal lattice and pseudopotential, and FP64
+ * arithmetic in the same operation order as the FP32 path, for every
+ * esoteric-pull configuration (boundary objects, open faces, force fields,
+ * thermal and multiphase flow; the two-buffer mode fails with
+ * BF_ERR_INVALID_ARGUMENT); fields read back as FP32. */
 typedef enum {
     BF_STORE_FP32 = 0,
     BF_STORE_FP16 = 1,

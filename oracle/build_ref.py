@@ -81,6 +81,11 @@ CONFIGS = {
     "d2q9_two_buffer": dict(boundry_count=3, bits_per_boundry=2, periodic_x=0, periodic_y=0, esoteric_pull=0),
     "d2q9_fp16_texture": dict(floating_point_accuracy="fp16", lattice_is_texutre3d=1,
                               lattice_texture3d_internal_format="r16f"),
+    # long runs on the reference's own AA path (skip mode)
+    "d2q9_cavity_skip": dict(boundry_count=3, bits_per_boundry=2, periodic_x=0, periodic_y=0, forcing_scheme=1),
+    "d3q19_sphere_skip": dict(velocity_set="D3Q19", velocity_set_thermal="D3Q7", boundry_count=2, bits_per_boundry=1),
+    "d2q9_von_karman": dict(boundry_count=2, bits_per_boundry=1),
+    "d3q19_droplets_limiter": dict(velocity_set="D3Q19", velocity_set_thermal="D3Q7", multiphase_flow=1),
 }
 
 

@@ -13,9 +13,11 @@
  *     succeeds; tests/test_oracle_vs_ref.py compares the two.
  * Without the second item the restatement is "parity unpinned".
  *
- * The file is compiled twice: REAL=float gives the "ref-literal" FP32
- * stepper (same operation order as the GLSL, no FMA contraction), REAL=double
- * gives the FP64 accuracy oracle (orc64_* symbols).
+ * The file is compiled twice: REAL=float gives the FP32 stepper (the
+ * shaders' expressions in their written order, no FMA contraction: bit for
+ * bit the reference's shader code as the reference-built checker runs it),
+ * REAL=double the FP64 accuracy oracle (orc64_* symbols, the same order in
+ * double).
  *
  * Memory-level restatement: the DDF lives in one buffer with the reference's
  * SoA address  i*N + cell  (collide.comp:196-200), and every read/write goes
@@ -138,10 +140,11 @@ typedef struct {
     const orc_dir* V;
     const orc_dir* Vt;
     REAL cs;
-    /* launch constants, computed once per launch as the host does:
-     * divisions by these uniforms are evaluated as multiplications by their
-     * correctly rounded reciprocals (see the canonical-order note below). */
+    /* launch constants, computed once per launch as the host does: the
+     * shifted tree multiplies by the correctly rounded reciprocals, the
+     * literal tree divides by cs2, cs4, tau, tau_t (see the note below). */
     REAL R2, R4, R2h, R4h, Rtau, P, Rtau_t, Wm, Pp, Pm;
+    REAL cs2, cs4, tau, tau_t;  /* the literal evaluation divides by these */
     int forced; /* force term in u: forcing, thermal or multiphase */
     REAL* lat[2];
     int lat0_src;
@@ -274,15 +277,22 @@ static int aa_write_addr(orc_t* s, int x, int y, int z, int i, int odd, size_t* 
 /* physics (collide.comp:512-629, :634-673)                                  */
 /* ------------------------------------------------------------------------ */
 /*
- * Canonical FP32 evaluation, shared bit for bit with the CUDA kernels.
- * The reference's formulas (collide.comp:589-629, :634-651, :722-745) are
- * evaluated in one fixed order: divisions by launch uniforms (cs^2, cs^4,
- * tau) become multiplications by their once-rounded reciprocals (/2 folds
- * into them exactly), u = j * (1/rho) with one IEEE division, and the sums
- * marked FMA below are single-rounding fused multiply-adds.  Everything else
- * is one rounded operation at a time (the file is compiled without FMA
- * contraction).  GLSL leaves both reassociation and contraction to the
- * driver, so this is one admissible evaluation of the same expressions.
+ * Two evaluations, each shared bit for bit with the CUDA kernels.
+ *
+ * Literal (FP32 and FP16 storage of f itself, and the FP64 oracle): the
+ * reference's expressions (collide.comp:383-395, :512-629, :634-673,
+ * :702-782) in the order they are written, one IEEE operation per operator,
+ * divisions as correctly rounded divisions, no contraction (the file is
+ * compiled with -ffp-contract=off).  Products with a lattice component
+ * (0 or +-1) are exact and the zero terms of such dot products are left
+ * out (cdot below), which changes nothing but the sign of a zero.
+ *
+ * Shifted (fp16s / fp16c, extensions with no counterpart in the reference):
+ * the update on g = f - w in a fixed order where divisions by launch
+ * uniforms (cs^2, cs^4, tau) are multiplications by their once-rounded
+ * reciprocals, u = j * (1/rho) with one IEEE division, and the sums marked
+ * FMA are single-rounding fused multiply-adds.  The TRT collision (an
+ * extension) uses the same fixed order with either storage.
  */
 #define FMA(a, b, c) (IS_F32 ? (REAL)fmaf((float)(a), (float)(b), (float)(c)) : (REAL)fma((double)(a), (double)(b), (double)(c)))
 /* u.u = fma(uz, uz, fma(uy, uy, ux*ux)) */
@@ -297,6 +307,11 @@ static REAL cdot(int cx, int cy, int cz, v3 v) {
 }
 /* (1 + cu/cs2 + cu^2/2/cs4 - uu/2/cs2) = fma(cu^2, R4/2, fma(cu, R2, 1 - uu R2/2)) */
 static REAL bracket(const orc_t* s, REAL cu, REAL one_m) { return FMA(cu * cu, s->R4h, FMA(cu, s->R2, one_m)); }
+/* collide.comp:589-604 as written: (w p)(((1 + cu/cs2) + cu^2/2/cs4) - uu/2/cs2),
+ * uuh = (u.u/2)/cs2 of the cell; the thermal form (:634-651) is the same with T */
+static REAL feq_lit(const orc_t* s, REAL wp, REAL cu, REAL uuh) {
+    return wp * ((((REAL)1 + cu / s->cs2) + (cu * cu / (REAL)2) / s->cs4) - uuh);
+}
 static REAL feq_init(const orc_t* s, REAL rho, v3 u, int i) { /* set_equilibrium_populations.comp:179-196 */
     REAL w = (REAL)s->V[i].w;
     v3 c = mk3((REAL)s->V[i].cx, (REAL)s->V[i].cy, (REAL)s->V[i].cz);
@@ -334,9 +349,30 @@ static float exp_f32(float x) {
     float sc; memcpy(&sc, &sb, 4);
     return q * sc;
 }
+/* exp for the FP64 pseudopotential, identical to the CUDA kernels' copy:
+ * Cody-Waite reduction with ln2 split in a head whose low 21 bits are zero
+ * (exact products for |k| < 2^21) and a tail, exp(r) by the degree-13
+ * Taylor polynomial in Horner form (|r| <= ln2/2, truncation < 5e-18
+ * relative), exact scaling by 2^k.  Valid for x in [-708, 709]. */
+static double exp_f64(double x) {
+    const double L2E = 0x1.71547652b82fep+0, LN2_HI = 0x1.62e42fee00000p-1, LN2_LO = 0x1.a39ef35793c76p-33;
+    static const double C[12] = {0x1.6124613a86d09p-33, 0x1.1eed8eff8d898p-29, 0x1.ae64567f544e4p-26,
+                                 0x1.27e4fb7789f5cp-22, 0x1.71de3a556c734p-19, 0x1.a01a01a01a01ap-16,
+                                 0x1.a01a01a01a01ap-13, 0x1.6c16c16c16c17p-10, 0x1.1111111111111p-7,
+                                 0x1.5555555555555p-5, 0x1.5555555555555p-3, 0x1p-1}; /* 1/13! .. 1/2! */
+    double kf = rint(x * L2E);
+    double r = (x - kf * LN2_HI) - kf * LN2_LO;
+    double q = C[0];
+    for (int i = 1; i < 12; i++) q = q * r + C[i];
+    q = q * r + 1.0;
+    q = q * r + 1.0;
+    uint64_t sb = (uint64_t)((int64_t)kf + 1023) << 52;
+    double sc; memcpy(&sc, &sb, 8);
+    return q * sc;
+}
 static REAL psi(REAL rho) { /* collide.comp:512-516, rho0 = 1 */
     REAL rho0 = 1;
-    return rho0 * ((REAL)1 - (IS_F32 ? (REAL)exp_f32((float)(-rho / rho0)) : (REAL)exp((double)(-rho / rho0))));
+    return rho0 * ((REAL)1 - (IS_F32 ? (REAL)exp_f32((float)(-rho / rho0)) : (REAL)exp_f64((double)(-rho / rho0))));
 }
 
 /* Shan-Chen interaction force sum (collide.comp:534-584): acc = sum over
@@ -420,55 +456,86 @@ static void collide(orc_t* s, int save, int update) {
             /* out-of-domain reads give 0.01 (collide.comp:278-298); g = 0.01 - w when shifted */
             f[i] = open ? (sh ? (REAL)0.01 - (REAL)s->V[i].w : (REAL)0.01) : lat_load(s, L[(size_t)rs * N + rc], rs);
         }
-        /* ---- canonical FP32 evaluation (shared with the CUDA kernels) ----
-         * opposite populations pair as (i, i+1), i odd:  s = f_i + f_i+1,
-         * d = f_i - f_i+1; rho and the momentum are summed pairwise in order. */
+        /* opposite populations pair as (i, i+1), i odd:  s = f_i + f_i+1,
+         * d = f_i - f_i+1 (the shifted density and momentum, and TRT) */
         REAL sp[QMAX / 2 + 1], dp_[QMAX / 2 + 1];
         for (int i = 1; i < Q; i += 2) { sp[i / 2] = f[i] + f[i + 1]; dp_[i / 2] = f[i] - f[i + 1]; }
-        REAL density = f[0];
-        for (int i = 1; i < Q; i += 2) density = density + sp[i / 2];
-        if (sh) density = (REAL)1 + density; /* sum of g plus sum of w */
+        REAL density;
+        if (sh) { /* pairwise, plus the sum of w */
+            density = f[0];
+            for (int i = 1; i < Q; i += 2) density = density + sp[i / 2];
+            density = (REAL)1 + density;
+        } else { /* compute_density (collide.comp:383-388): in population order */
+            density = f[0];
+            for (int i = 1; i < Q; i++) density = density + f[i];
+        }
         if (density < (REAL)0.01) density = (REAL)0.01; /* max(density, 0.01) */
         v3 force = get_force(s, cell);
         REAL temperature = 0;
-        if (s->thermal) {
+        if (s->thermal) { /* collide.comp:709-716 */
             REAL* TS = TSRC(s);
             for (int i = 0; i < s->Qt; i++) temperature += TS[cell * s->Qt + i];
             REAL k = -(REAL)s->d.beta * (temperature - (REAL)1);
-            force.x = FMA(k, force.x, force.x);
-            force.y = FMA(k, force.y, force.y);
-            force.z = FMA(k, force.z, force.z);
+            force.x = force.x + k * force.x;
+            force.y = force.y + k * force.y;
+            force.z = force.z + k * force.z;
         }
-        if (s->d.multiphase) {
+        if (s->d.multiphase) { /* collide.comp:580-583, :718-720 */
             v3 sc = sc_force_acc(s, x, y, z, density);
             REAL k = -psi(density) * (REAL)s->d.G;
-            force.x = FMA(sc.x, k, force.x);
-            force.y = FMA(sc.y, k, force.y);
-            force.z = FMA(sc.z, k, force.z);
+            force.x = force.x + sc.x * k;
+            force.y = force.y + sc.y * k;
+            force.z = force.z + sc.z * k;
         }
         REAL jx = 0, jy = 0, jz = 0;
         int fx = 1, fy = 1, fz = 1;
-        for (int i = 1; i < Q; i += 2) {
-            REAL d = dp_[i / 2];
-            if (s->V[i].cx) { REAL t = s->V[i].cx > 0 ? d : -d; jx = fx ? t : jx + t; fx = 0; }
-            if (s->V[i].cy) { REAL t = s->V[i].cy > 0 ? d : -d; jy = fy ? t : jy + t; fy = 0; }
-            if (s->V[i].cz) { REAL t = s->V[i].cz > 0 ? d : -d; jz = fz ? t : jz + t; fz = 0; }
+        v3 vel;
+        if (sh) {
+            for (int i = 1; i < Q; i += 2) {
+                REAL d = dp_[i / 2];
+                if (s->V[i].cx) { REAL t = s->V[i].cx > 0 ? d : -d; jx = fx ? t : jx + t; fx = 0; }
+                if (s->V[i].cy) { REAL t = s->V[i].cy > 0 ? d : -d; jy = fy ? t : jy + t; fy = 0; }
+                if (s->V[i].cz) { REAL t = s->V[i].cz > 0 ? d : -d; jz = fz ? t : jz + t; fz = 0; }
+            }
+            REAL r = (REAL)1 / density;
+            vel = mk3(jx * r, jy * r, jz * r);
+            if (s->forced) {
+                REAL h = r * (REAL)0.5;
+                vel.x = FMA(force.x, h, vel.x);
+                vel.y = FMA(force.y, h, vel.y);
+                vel.z = FMA(force.z, h, vel.z);
+            }
+        } else {
+            /* compute_velocity (collide.comp:390-395): the populations times
+             * their lattice vectors summed in order, divided by the density;
+             * plus force/(2 density) (:722) */
+            for (int i = 0; i < Q; i++) {
+                REAL d = f[i];
+                if (s->V[i].cx) { REAL t = s->V[i].cx > 0 ? d : -d; jx = fx ? t : jx + t; fx = 0; }
+                if (s->V[i].cy) { REAL t = s->V[i].cy > 0 ? d : -d; jy = fy ? t : jy + t; fy = 0; }
+                if (s->V[i].cz) { REAL t = s->V[i].cz > 0 ? d : -d; jz = fz ? t : jz + t; fz = 0; }
+            }
+            vel = mk3(jx / density, jy / density, jz / density);
+            if (s->forced) {
+                REAL d2 = (REAL)2 * density;
+                vel.x = vel.x + force.x / d2;
+                vel.y = vel.y + force.y / d2;
+                vel.z = vel.z + force.z / d2;
+            }
         }
-        REAL r = (REAL)1 / density;
-        v3 vel = mk3(jx * r, jy * r, jz * r);
-        if (s->forced) {
-            REAL h = r * (REAL)0.5;
-            vel.x = FMA(force.x, h, vel.x);
-            vel.y = FMA(force.y, h, vel.y);
-            vel.z = FMA(force.z, h, vel.z);
-        }
-        REAL uu = uu_of(vel);
+        REAL uu = sh ? uu_of(vel) : dot3(vel, vel);
         REAL len = IS_F32 ? (REAL)sqrtf((float)uu) : (REAL)sqrt((double)uu);
         int out_lim = len > (REAL)s->d.velocity_limit;
         int out_ext = len > (REAL)s->d.velocity_limit_extreme;
         if (out_lim) { /* normalize(u) * limit */
-            REAL q = (REAL)s->d.velocity_limit / len;
-            vel.x = vel.x * q; vel.y = vel.y * q; vel.z = vel.z * q;
+            if (sh) {
+                REAL q = (REAL)s->d.velocity_limit / len;
+                vel.x = vel.x * q; vel.y = vel.y * q; vel.z = vel.z * q;
+            } else {
+                vel.x = (vel.x / len) * (REAL)s->d.velocity_limit;
+                vel.y = (vel.y / len) * (REAL)s->d.velocity_limit;
+                vel.z = (vel.z / len) * (REAL)s->d.velocity_limit;
+            }
         }
         if (eqb) {
             /* equilibrium boundary cell (extension): velocity kind keeps the
@@ -481,10 +548,26 @@ static void collide(orc_t* s, int save, int update) {
             force = mk3(0, 0, 0);
         }
         const REAL one_m = (REAL)1 - uu_of(vel) * s->R2h;
+        /* (u.u/2)/cs2 of the (limited) velocity: the literal equilibria's last term */
+        const REAL uuh = (dot3(vel, vel) / (REAL)2) / s->cs2;
         if (update) {
             REAL fn[QMAX];
             const REAL fuR2 = FMA(force.z, vel.z, FMA(force.y, vel.y, force.x * vel.x)) * s->R2;
-            if (eqb || s->d.collision != ORC_TRT) {
+            if (!sh && (eqb || s->d.collision != ORC_TRT)) {
+                /* collide.comp:727-745 with :589-629: f + (-(f - feq)/tau) + source */
+                const REAL fuc = dot3(force, vel) / s->cs2;
+                for (int i = 0; i < Q; i++) {
+                    REAL w = (REAL)s->V[i].w;
+                    REAL cu = cdot(s->V[i].cx, s->V[i].cy, s->V[i].cz, vel);
+                    REAL fe = feq_lit(s, w * density, cu, uuh);
+                    REAL v = f[i] + -((f[i] - fe) / s->tau);
+                    if (s->src_on) {
+                        REAL fc = cdot(s->V[i].cx, s->V[i].cy, s->V[i].cz, force);
+                        v = v + (s->P * w) * (fc / s->cs2 + ((fc * cu) / s->cs4 - fuc));
+                    }
+                    fn[i] = (eqb || out_ext) ? fe : v;
+                }
+            } else if (eqb || s->d.collision != ORC_TRT) {
                 for (int i = 0; i < Q; i++) {
                     REAL w = (REAL)s->V[i].w;
                     REAL cu = cdot(s->V[i].cx, s->V[i].cy, s->V[i].cz, vel);
@@ -553,11 +636,11 @@ static void collide(orc_t* s, int save, int update) {
         }
         if (s->thermal) {
             REAL* TS = TSRC(s); REAL* TT = TTGT(s);
-            for (int i = 0; i < s->Qt; i++) {
+            for (int i = 0; i < s->Qt; i++) { /* collide.comp:771-782, :634-651, :668-670 */
                 REAL cu = cdot(s->Vt[i].cx, s->Vt[i].cy, s->Vt[i].cz, vel);
-                REAL ge = ((REAL)s->Vt[i].w * temperature) * bracket(s, cu, one_m);
+                REAL ge = feq_lit(s, (REAL)s->Vt[i].w * temperature, cu, uuh);
                 REAL g = TS[cell * s->Qt + i];
-                TT[cell * s->Qt + i] = FMA(ge - g, s->Rtau_t, g); /* g + (-(g - geq)/tau_T) */
+                TT[cell * s->Qt + i] = g + -((g - ge) / s->tau_t);
             }
         }
         if (save) {
@@ -698,6 +781,10 @@ orc_t* ORC(create)(const orc_desc* d, const float* rho, const float* u, const fl
         s->Rtau = (REAL)1 / tau;
         s->P = (REAL)1 - (REAL)1 / ((REAL)2 * tau);
         s->Rtau_t = (REAL)1 / (REAL)d->tau_t;
+        s->cs2 = cs2;
+        s->cs4 = cs4;
+        s->tau = tau;
+        s->tau_t = (REAL)d->tau_t;
         REAL taum = (REAL)d->trt_magic / (tau - (REAL)0.5) + (REAL)0.5;
         s->Wm = (REAL)1 / taum;
         s->Pp = (REAL)1 - s->Rtau * (REAL)0.5;
@@ -813,6 +900,7 @@ void ORC(set_thermal)(orc_t* s, float tau_t, float beta) {
     s->d.tau_t = tau_t;
     s->d.beta = beta;
     s->Rtau_t = (REAL)1 / (REAL)tau_t;
+    s->tau_t = (REAL)tau_t;
 }
 long ORC(ticks)(orc_t* s) { return s->ticks; }
 int ORC(thermal)(orc_t* s) { return s->thermal; }
@@ -861,7 +949,8 @@ void ORC(reduce)(orc_t* s, double out[5]) {
 }
 uint16_t ORC(f32_to_f16)(float f) { return f32_to_f16_rne(f); }
 float ORC(f16_to_f32)(uint16_t h) { return f16_to_f32(h); }
-/* the hand-written exp of the pseudopotential (FP32 build) */
+/* the hand-written exps of the pseudopotential */
 float ORC(exp_f32)(float x) { return exp_f32(x); }
+double ORC(exp_f64)(double x) { return exp_f64(x); }
 /* the fp16c round trip of a shifted population g (encode, then decode) */
 float ORC(fp16c_round)(float g) { return c16_round(g); }

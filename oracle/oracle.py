@@ -70,6 +70,8 @@ def load():
     lib.orc32_f16_to_f32.restype = C.c_float
     lib.orc32_exp_f32.argtypes = [C.c_float]
     lib.orc32_exp_f32.restype = C.c_float
+    lib.orc64_exp_f64.argtypes = [C.c_double]
+    lib.orc64_exp_f64.restype = C.c_double
     lib.orc32_fp16c_round.argtypes = [C.c_float]
     lib.orc32_fp16c_round.restype = C.c_float
     _lib = lib

@@ -79,8 +79,8 @@ def step_and_compare(s, o, checkpoints, rtol=RTOL, mask=None, check_temperature=
     """Steps both to each checkpoint (saving fields there) and compares.
 
     The bar is RTOL; with exact=True the fields must also agree bit for bit:
-    the kernels and the FP32 oracle evaluate the same canonical expression
-    tree with individually rounded operations."""
+    the kernels and the oracle evaluate the same expression trees with
+    individually rounded operations."""
     done = 0
     worst = (0.0, 0.0)
     for k in checkpoints:

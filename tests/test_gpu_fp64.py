@@ -55,20 +55,100 @@ def test_fp64_stepper_matches_fp64_oracle(vs, res, collision, forced, product_li
     assert np.array_equal(s.get_populations(), o.lattice().astype(np.float32))
 
 
-def test_fp64_storage_rejects_unsupported_configurations(product_lib):
+def test_fp64_storage_rejects_the_two_buffer_mode(product_lib):
+    s = bf.LBM()
+    s.is_collide_esoteric = False
+    with pytest.raises(bf.LBMError):
+        s.initialize_fields_from_arrays((16, 16, 1), 0.6, velocity_set=bf.VelocitySet.D2Q9,
+                                        fp_accuracy=bf.FloatingPointAccuracy.fp64)
+
+
+def generic_fp64_case(name):
+    """Bounded configurations of the generic (boundary-aware) step: inputs
+    for LBM.initialize_fields_from_arrays and the oracle."""
+    d = dict(objects=None, ids=None, force=None, temperature=None, density=None, velocity=None,
+             periodic=(True, True, True), multiphase=False, boundary_mode=0, collision=0, tau=0.6, G=-6.0,
+             tau_t=2.0, thermal_init_equilibrium=False)
+    if name == "d2q9_cavity_bounce_back":
+        n = 48
+        y, x = np.mgrid[0:n, 0:n]
+        ids = np.zeros((n, n), np.uint32)
+        ids[(x == 0) | (x == n - 1) | (y == 0)] = 1
+        ids[y == n - 1] = 2
+        d.update(res=(n, n, 1), vs=bf.VelocitySet.D2Q9, periodic=(False, False, True), boundary_mode=1,
+                 ids=ids.reshape(-1), objects={1: dict(velocity=(0, 0, 0)), 2: dict(velocity=(0.1, 0, 0))})
+    elif name == "d3q19_sphere_channel_trt":
+        from boltzmannfluids_gb300.workloads import sphere_channel
+        res = (32, 16, 12)
+        rho, u, ids, objs = sphere_channel(res, radius=3.0, center=(10.0, 8.0, 6.0))
+        d.update(res=res, vs=bf.VelocitySet.D3Q19, periodic=(False, True, True), boundary_mode=1, collision=1,
+                 tau=0.55, ids=ids, objects=objs, density=rho, velocity=u)
+    elif name == "d2q9_thermal_walls":
+        res = (32, 24, 1)
+        y = np.repeat(np.arange(24), 32)
+        ids = np.zeros(32 * 24, np.uint32)
+        ids[y == 0] = 1
+        ids[y == 23] = 2
+        f = np.zeros((32 * 24, 3), np.float32)
+        f[:, 1] = -1e-4
+        t = (1.0 + 0.01 * np.sin(np.arange(32 * 24))).astype(np.float32)
+        d.update(res=res, vs=bf.VelocitySet.D2Q9, periodic=(True, False, True), boundary_mode=1, ids=ids,
+                 objects={1: dict(temperature=1.5), 2: dict(temperature=0.5)}, force=f, temperature=t,
+                 tau_t=0.8, thermal_init_equilibrium=True)
+    elif name == "d3q19_shan_chen":
+        res = (16, 16, 16)
+        rng = np.random.default_rng(4)
+        d.update(res=res, vs=bf.VelocitySet.D3Q19, multiphase=True, G=-5.0, tau=1.0,
+                 density=(0.69 + 0.01 * rng.uniform(-1, 1, 16 ** 3)).astype(np.float32))
+    elif name == "d2q9_open_force_field":
+        res = (40, 20, 1)
+        rho, u = seeded_fields(res, 9, dims=2)
+        f = np.zeros((40 * 20, 3), np.float32)
+        f[:, 0] = (1e-5 * np.cos(np.arange(800) * 0.1)).astype(np.float32)
+        d.update(res=res, vs=bf.VelocitySet.D2Q9, periodic=(False, True, True), density=rho, velocity=u, force=f)
+    return d
+
+
+@pytest.mark.parametrize("name", ["d2q9_cavity_bounce_back", "d3q19_sphere_channel_trt", "d2q9_thermal_walls",
+                                  "d3q19_shan_chen", "d2q9_open_force_field"])
+def test_fp64_generic_step_matches_fp64_oracle(name, product_lib):
+    """The FP64 stepper on the boundary-aware configurations (objects with
+    bounce-back and moving walls, equilibrium inlet/outlet, open faces, force
+    fields, the thermal lattice, Shan-Chen) is bit-exact with the oracle's
+    FP64 restatement."""
+    d = generic_fp64_case(name)
     s = bf.LBM()
     s.is_collide_esoteric = True
-    with pytest.raises(bf.LBMError):
-        s.initialize_fields_from_arrays((16, 16, 1), 0.6, periodic=(False, True, True),
-                                        velocity_set=bf.VelocitySet.D2Q9, fp_accuracy=bf.FloatingPointAccuracy.fp64)
-    ids = np.zeros(16 * 16, np.uint32)
-    ids[:16] = 1
-    s2 = bf.LBM()
-    s2.is_collide_esoteric = True
-    s2.set_boundry_properties(1, velocity_translational=(0, 0, 0))
-    with pytest.raises(bf.LBMError):
-        s2.initialize_fields_from_arrays((16, 16, 1), 0.6, boundry_id=ids, velocity_set=bf.VelocitySet.D2Q9,
-                                         fp_accuracy=bf.FloatingPointAccuracy.fp64)
+    s.boundary_mode = d["boundary_mode"]
+    s.collision = d["collision"]
+    s.intermolecular_interaction_strength = d["G"]
+    s.thermal_init_equilibrium = d["thermal_init_equilibrium"]
+    s.clear_boundry_properties()
+    for k, o in (d["objects"] or {}).items():
+        s.set_boundry_properties(k, velocity_translational=o.get("velocity", (0, 0, 0)),
+                                 temperature=o.get("temperature", 1.0), kind=o.get("kind", 0))
+    s.initialize_fields_from_arrays(d["res"], d["tau"], density=d["density"], velocity=d["velocity"],
+                                    force=d["force"], temperature=d["temperature"], boundry_id=d["ids"],
+                                    periodic=d["periodic"], velocity_set=d["vs"], is_flow_multiphase=d["multiphase"],
+                                    fp_accuracy=bf.FloatingPointAccuracy.fp64)
+    s.thermal_relaxation_time = d["tau_t"]
+    o = Oracle(d["res"], f32(d["tau"]), density=d["density"], velocity=d["velocity"], force=d["force"],
+               temperature=d["temperature"], boundry_id=d["ids"], objects=d["objects"], periodic=d["periodic"],
+               velocity_set=int(d["vs"]), esoteric=True, boundary_mode=d["boundary_mode"],
+               collision=d["collision"], multiphase=d["multiphase"], G=d["G"], tau_t=d["tau_t"],
+               thermal_init_equilibrium=d["thermal_init_equilibrium"], velocity_limit=f32(0.25),
+               velocity_limit_extreme=f32(0.30), precision=64)
+    done = 0
+    for k in (1, 2, 9, 40):
+        s.iterate_time(steps=k - done, save=True)
+        o.iterate(k - done, True)
+        done = k
+        vd = s.get_velocity_density_texture().reshape(-1, 4)
+        ft = s.get_force_temperature_texture().reshape(-1, 4)
+        vr, fr = o.fields()
+        assert np.array_equal(vd, vr.astype(np.float32)), (name, k)
+        assert np.array_equal(ft, fr.astype(np.float32)), (name, k)
+    assert np.array_equal(s.get_populations(), o.lattice().astype(np.float32))
 
 
 def run_tg(res, storage, steps, every):

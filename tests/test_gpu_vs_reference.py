@@ -1,17 +1,18 @@
 """The GPU kernels against outputs of the reference's own shader code
 (tests/golden/ref_fields.npz, written by tests/golden/make_ref_golden.py from
-the reference-built checker), on the seeded cases of tests/ref_cases.py,
-with the criteria of tests/test_oracle_vs_ref.py."""
-import os
-
+the reference-built checker) on the seeded cases of tests/ref_cases.py: the
+u/rho and force/temperature fields at every stated step -- 1, 100 and 10,000
+steps of the 256^2 cavity on the reference's AA path; 1, 100 and 1,000 of the
+D3Q19 sphere, the periodic von Karman street and the droplet collision that
+drives the velocity limiter, its extreme branch and the density floor --
+are bit-identical (SHA-256), and within 1e-5 where the field is stored."""
 import numpy as np
 import pytest
 
-from ref_cases import NAMES, STEPS, case
-from test_oracle_vs_ref import FP16_LATE_RTOL, RTOL, assert_close
+from ref_cases import NAMES, case, steps_of
+from test_oracle_vs_ref import GOLD, check_against_gold
 
 pytestmark = pytest.mark.gpu
-GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_fields.npz")
 
 
 @pytest.mark.parametrize("name", NAMES)
@@ -24,6 +25,8 @@ def test_gpu_matches_reference_shader_outputs(name, product_lib):
     s.boundary_mode = bf.BoundaryMode.skip
     s.two_buffer_fixed = False
     s.intermolecular_interaction_strength = d["G"]
+    s.velocity_limit = d["velocity_limit"]
+    s.velocity_limit_extreme = d["velocity_limit_extreme"]
     s.clear_boundry_properties()
     for k, o in (d["objects"] or {}).items():
         s.set_boundry_properties(k, velocity_translational=o.get("velocity", (0, 0, 0)),
@@ -36,12 +39,9 @@ def test_gpu_matches_reference_shader_outputs(name, product_lib):
     n = d["res"][0] * d["res"][1] * d["res"][2]
     fluid = np.ones(n, bool) if d["ids"] is None else (np.asarray(d["ids"]) == 0)
     done = 0
-    for k in STEPS:
+    for k in steps_of(name):
         s.iterate_time(steps=k - done, save=True)
         done = k
-        vo = s.get_velocity_density_texture().reshape(-1, 4).astype(np.float64)[fluid]
-        fo = s.get_force_temperature_texture().reshape(-1, 4).astype(np.float64)[fluid]
-        vr = gold[f"{name}/vd/{k}"].astype(np.float64)[fluid]
-        fr = gold[f"{name}/ft/{k}"].astype(np.float64)[fluid]
-        tol = FP16_LATE_RTOL if (d["storage"] != 0 and k > 5) else RTOL
-        assert_close(vo, fo, vr, fr, tol, k)
+        vo = s.get_velocity_density_texture().reshape(-1, 4)
+        fo = s.get_force_temperature_texture().reshape(-1, 4)
+        check_against_gold(gold, name, k, vo, fo, fluid)

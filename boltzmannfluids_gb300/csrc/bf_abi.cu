@@ -10,6 +10,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
@@ -352,6 +353,35 @@ float sqrt_threshold(float lim) {
     return y;
 }
 
+// Whether x / y == fma(fma(-q, y, x), r, q) with q = x * r, r = RN(1/y), for
+// every significand of x (so for every x whose quotient and remainder stay
+// normal): the fast kernels then divide by the launch-uniform y in three
+// operations.  Results are kept per divisor (the knobs change rarely).
+bool division_checked(float y) {
+    static std::mutex mu;
+    static std::map<uint32_t, bool> seen;
+    uint32_t key;
+    std::memcpy(&key, &y, 4);
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        auto it = seen.find(key);
+        if (it != seen.end()) return it->second;
+    }
+    bool ok = std::isfinite(y) && y != 0.0f;
+    const float r = 1.0f / y;
+    for (uint32_t m = 0; ok && m < (1u << 23); m++) {
+        const uint32_t xb = 0x3f800000u | m;
+        float x;
+        std::memcpy(&x, &xb, 4);
+        const float q = x * r;
+        const float e = std::fma(-q, y, x);
+        ok = std::fma(e, r, q) == x / y;
+    }
+    std::lock_guard<std::mutex> lock(mu);
+    seen[key] = ok;
+    return ok;
+}
+
 void fill_constants(bf_solver* s, StepParams& p) {
     // the reference's FP32 constants: cs = float(1/sqrt(3)) (LBM.cpp:1587)
     const float cs = (float)(1.0 / std::sqrt(3.0));
@@ -363,6 +393,8 @@ void fill_constants(bf_solver* s, StepParams& p) {
     p.cs4 = cs4;
     p.tau = tau;
     p.tau_t = s->desc.thermal_relaxation_time;
+    p.div_ok = (division_checked(cs2) ? 1u : 0u) | (division_checked(cs4) ? 2u : 0u) |
+               (division_checked(tau) ? 4u : 0u) | (division_checked(p.tau_t) ? 8u : 0u);
     p.R2h = p.R2 * 0.5f;
     p.R4h = p.R4 * 0.5f;
     p.Rtau = 1.0f / tau;
@@ -467,8 +499,13 @@ cudaError_t collide(bf_solver* s, bool save, bool update, bool reduce, bool meas
     // objects and open faces (thermal flow included) without force-field or
     // multiphase flow: the boundary-aware fast kernel, with its masks
     const uint32_t masked_excl = F_FORCE_FIELD | F_MULTIPHASE;
-    int path = generic ? PATH_GENERIC : PATH_FAST;
-    if (generic && mode != AA_LOCAL && idx32 && !(p.flags & masked_excl) && s->nmask.p &&
+    // the fast and boundary-aware kernels divide by the launch's divisors in
+    // three operations, which the host has checked for every divisor
+    // (fill_constants); a divisor that failed the check sends the step to the
+    // generic kernel, which divides by it in full
+    const bool div_checked = f64 || p.div_ok == 0xFu;
+    int path = (generic || !div_checked) ? PATH_GENERIC : PATH_FAST;
+    if (generic && div_checked && mode != AA_LOCAL && idx32 && !(p.flags & masked_excl) && s->nmask.p &&
         s->desc.storage != BF_STORE_FP64 && s->masked_step)
         path = PATH_MASKED;
     p.nmask = s->nmask.as<uint32_t>();

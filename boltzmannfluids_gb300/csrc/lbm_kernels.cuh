@@ -142,6 +142,31 @@ __device__ __forceinline__ R bracket(R cu, R one_m, R R2, R R4h) {
     return FFMA(FMUL(cu, cu), R4h, FFMA(cu, R2, one_m));
 }
 
+// x / y for a launch-uniform divisor y with r = RN(1/y): q = RN(x r), the
+// exact remainder e = fma(-q, y, x), then q + e r with one rounding
+// (Markstein's correction) -- the correctly rounded quotient, three
+// operations.  The host checks the sequence against IEEE division for every
+// significand of x with each launch divisor (StepParams::div_ok); the fast
+// and boundary-aware kernels use it only when every check passed (div_m),
+// the generic kernel per divisor (div_u).  Double: the full division.
+__device__ __forceinline__ float div_m(float x, float y, float r) {
+    const float q = __fmul_rn(x, r);
+    return __fmaf_rn(__fmaf_rn(-q, y, x), r, q);
+}
+__device__ __forceinline__ double div_m(double x, double y, double) { return __ddiv_rn(x, y); }
+__device__ __forceinline__ float div_u(float x, float y, float r, bool ok) {
+    return ok ? div_m(x, y, r) : __fdiv_rn(x, y);
+}
+__device__ __forceinline__ double div_u(double x, double y, double, bool) { return __ddiv_rn(x, y); }
+template <bool MK, class R>
+__device__ __forceinline__ R div_k(R x, R y, R r, bool ok) {
+    if constexpr (MK) return div_m(x, y, r);
+    else return div_u(x, y, r, ok);
+}
+// the divisors cs^2 and cs^4 of the literal evaluation, their reciprocals
+// and checks
+template <class R> struct Div { R cs2, rcs2, cs4, rcs4; bool ok2, ok4; };
+
 // GLSL's dot(a, b) as written: a.x*b.x + a.y*b.y + a.z*b.z
 template <class R>
 __device__ __forceinline__ R dot_lit(R ax, R ay, R az, R bx, R by, R bz) {
@@ -149,13 +174,15 @@ __device__ __forceinline__ R dot_lit(R ax, R ay, R az, R bx, R by, R bz) {
 }
 // collide.comp:589-604 (and the thermal :634-651) as written:
 // (w p) (((1 + cu/cs2) + cu^2/2/cs4) - uuh), uuh = (u.u/2)/cs2 of the cell
-template <class R>
-__device__ __forceinline__ R feq_lit(R wp, R cu, R cs2, R cs4, R uuh) {
-    return FMUL(wp, FSUB(FADD(FADD(R(1), FDIV(cu, cs2)), FDIV(FMUL(FMUL(cu, cu), R(0.5)), cs4)), uuh));
+template <bool MK, class R>
+__device__ __forceinline__ R feq_lit(R wp, R cu, const Div<R>& d, R uuh) {
+    return FMUL(wp, FSUB(FADD(FADD(R(1), div_k<MK>(cu, d.cs2, d.rcs2, d.ok2)),
+                              div_k<MK>(FMUL(FMUL(cu, cu), R(0.5)), d.cs4, d.rcs4, d.ok4)),
+                         uuh));
 }
-template <class R>
-__device__ __forceinline__ R uuh_of(R ux, R uy, R uz, R cs2) {
-    return FDIV(FMUL(dot_lit(ux, uy, uz, ux, uy, uz), R(0.5)), cs2);
+template <bool MK, class R>
+__device__ __forceinline__ R uuh_of(R ux, R uy, R uz, const Div<R>& d) {
+    return div_k<MK>(FMUL(dot_lit(ux, uy, uz, ux, uy, uz), R(0.5)), d.cs2, d.rcs2, d.ok2);
 }
 
 template <int Q>
@@ -335,7 +362,9 @@ __device__ __forceinline__ void velocity_literal(const R (&f)[Q], MomentsT<R>& m
 }
 
 // Post-collision populations, handed to emit(i, value) as soon as each is
-// known.  BGK follows collide.comp:589-629/727-745:
+// known.  BGK with unshifted storage is collide.comp:589-629/727-745 as
+// written (feq_lit, f + (-(f - feq)/tau) + (P w)(F.c/cs2 + ((F.c)(u.c)/cs4 -
+// F.u/cs2))); with shifted storage (SH) the fixed order
 //   feq = (w rho) bracket(cu),  f <- fma(feq - f, 1/tau, f)
 //   + fma(P w, fma(F.c, R2, fma((F.c) cu, R4, -(F.u) R2)), .)   [Guo]
 // TRT is an extension, evaluated over the pair (i, opp i):
@@ -348,13 +377,21 @@ __device__ __forceinline__ void velocity_literal(const R (&f)[Q], MomentsT<R>& m
 // SH (shifted storage): f holds g = f - w and every equilibrium is formed
 // as g_eq = fma(w rho, bracket, -w); the rest of the update is unchanged.
 // launch constants of the collision in the arithmetic type
-template <class R> struct Coef { R R2, R4, R2h, R4h, Rtau, P, Wm, Pp, Pm, cs2, cs4, tau; };
+template <class R> struct Coef {
+    R R2, R4, R2h, R4h, Rtau, P, Wm, Pp, Pm;
+    Div<R> d;
+    R tau;
+    bool ok_tau;
+};
 __device__ __forceinline__ Coef<float> coef_of(const StepParams& p, float) {
-    return Coef<float>{p.R2, p.R4, p.R2h, p.R4h, p.Rtau, p.P, p.Wm, p.Pp, p.Pm, p.cs2, p.cs4, p.tau};
+    return Coef<float>{p.R2, p.R4, p.R2h, p.R4h, p.Rtau, p.P, p.Wm, p.Pp, p.Pm,
+                       Div<float>{p.cs2, p.R2, p.cs4, p.R4, (p.div_ok & 1u) != 0, (p.div_ok & 2u) != 0},
+                       p.tau, (p.div_ok & 4u) != 0};
 }
 __device__ __forceinline__ Coef<double> coef_of(const StepParams& p, double) {
     return Coef<double>{p.k64.R2, p.k64.R4, p.k64.R2h, p.k64.R4h, p.k64.Rtau, p.k64.P, p.k64.Wm, p.k64.Pp,
-                        p.k64.Pm, p.k64.cs2, p.k64.cs4, p.k64.tau};
+                        p.k64.Pm, Div<double>{p.k64.cs2, p.k64.R2, p.k64.cs4, p.k64.R4, false, false},
+                        p.k64.tau, false};
 }
 
 template <int Q, bool SH, class R, class Emit>
@@ -364,18 +401,20 @@ __device__ __forceinline__ void collide_emit(const R (&f)[Q], const MomentsT<R>&
     using W = LatticeW<Q, R>;
     if (!SH && (to_equilibrium || !trt)) {
         // collide.comp:727-745 with :589-629 as written: f + (-(f - feq)/tau) + source
-        const R uuh = uuh_of(m.ux, m.uy, m.uz, k.cs2);
-        const R fuc = src ? FDIV(dot_lit(m.Fx, m.Fy, m.Fz, m.ux, m.uy, m.uz), k.cs2) : R(0);
+        const Div<R>& d = k.d;
+        const R uuh = uuh_of<false>(m.ux, m.uy, m.uz, d);
+        const R fuc = src ? div_u(dot_lit(m.Fx, m.Fy, m.Fz, m.ux, m.uy, m.uz), d.cs2, d.rcs2, d.ok2) : R(0);
 #pragma unroll
         for (int i = 0; i < Q; i++) {
             const Dir c = L::c(i);
             const R w = W::w(i);
             const R cu = cdot_rt(c, m.ux, m.uy, m.uz);
-            const R fe = feq_lit(FMUL(w, m.rho), cu, k.cs2, k.cs4, uuh);
-            R v = FSUB(f[i], FDIV(FSUB(f[i], fe), k.tau));
+            const R fe = feq_lit<false>(FMUL(w, m.rho), cu, d, uuh);
+            R v = FSUB(f[i], div_u(FSUB(f[i], fe), k.tau, k.Rtau, k.ok_tau));
             if (src) {
                 const R fc = cdot_rt(c, m.Fx, m.Fy, m.Fz);
-                v = FADD(v, FMUL(FMUL(k.P, w), FADD(FDIV(fc, k.cs2), FSUB(FDIV(FMUL(fc, cu), k.cs4), fuc))));
+                v = FADD(v, FMUL(FMUL(k.P, w), FADD(div_u(fc, d.cs2, d.rcs2, d.ok2),
+                                                    FSUB(div_u(FMUL(fc, cu), d.cs4, d.rcs4, d.ok4), fuc))));
             }
             emit(i, (to_equilibrium || m.out_ext) ? fe : v);
         }
@@ -450,19 +489,21 @@ __device__ __forceinline__ void collide_fixed(const R (&f)[Q], const MomentsT<R>
     static_assert(SH || SCE == 0, "scaled populations are shifted");
     if (!SH && !TRT) {
         // collide.comp:727-745 with :589-629 as written: f + (-(f - feq)/tau) + source
-        const R uuh = uuh_of(m.ux, m.uy, m.uz, k.cs2);
-        const R fuc = SRC ? FDIV(dot_lit(m.Fx, m.Fy, m.Fz, m.ux, m.uy, m.uz), k.cs2) : R(0);
+        const Div<R>& d = k.d;
+        const R uuh = uuh_of<true>(m.ux, m.uy, m.uz, d);
+        const R fuc = SRC ? div_m(dot_lit(m.Fx, m.Fy, m.Fz, m.ux, m.uy, m.uz), d.cs2, d.rcs2) : R(0);
 #pragma unroll
         for (int i = 0; i < Q; i++) {
             const Dir c = L::c(i);
             const R w = W::w(i);
             const R cu = cdot_rt(c, m.ux, m.uy, m.uz);
-            const R fe = feq_lit(FMUL(w, m.rho), cu, k.cs2, k.cs4, uuh);
+            const R fe = feq_lit<true>(FMUL(w, m.rho), cu, d, uuh);
             if (EXT) { emit(i, fe); continue; }
-            R v = FSUB(f[i], FDIV(FSUB(f[i], fe), k.tau));
+            R v = FSUB(f[i], div_m(FSUB(f[i], fe), k.tau, k.Rtau));
             if (SRC) {
                 const R fc = cdot_rt(c, m.Fx, m.Fy, m.Fz);
-                v = FADD(v, FMUL(FMUL(k.P, w), FADD(FDIV(fc, k.cs2), FSUB(FDIV(FMUL(fc, cu), k.cs4), fuc))));
+                v = FADD(v, FMUL(FMUL(k.P, w), FADD(div_m(fc, d.cs2, d.rcs2),
+                                                    FSUB(div_m(FMUL(fc, cu), d.cs4, d.rcs4), fuc))));
             }
             emit(i, v);
         }
@@ -656,18 +697,22 @@ __device__ __forceinline__ float thermal_buoyancy(const StepParams& p, uint32_t 
 // thermal BGK towards g_eq(T, u) as written (collide.comp:771-782, :634-651,
 // :668-670): g + (-(g - g_eq)/tau_T)
 __device__ __forceinline__ float thermal_relax(const StepParams& p, float g, float geq) {
-    return FSUB(g, FDIV(FSUB(g, geq), p.tau_t));
+    return FSUB(g, div_m(FSUB(g, geq), p.tau_t, p.Rtau_t));
+}
+__device__ __forceinline__ Div<float> div_of(const StepParams& p) {
+    return Div<float>{p.cs2, p.R2, p.cs4, p.R4, (p.div_ok & 1u) != 0, (p.div_ok & 2u) != 0};
 }
 template <int Q>
 __device__ __forceinline__ void thermal_collide(const StepParams& p, uint32_t n, const Moments& m, float temperature) {
     constexpr int QT = Lattice<Q>::D == 2 ? 5 : 7;
-    const float uuh = uuh_of(m.ux, m.uy, m.uz, p.cs2);
+    const Div<float> d = div_of(p);
+    const float uuh = uuh_of<true>(m.ux, m.uy, m.uz, d);
 #pragma unroll
     for (int i = 0; i < QT; i++) {
         const Dir c = ThermalLattice<QT>::c(i);
         const float w = ThermalLattice<QT>::w(i);
         const float cu = cdot_rt(c, m.ux, m.uy, m.uz);
-        const float geq = feq_lit(FMUL(w, temperature), cu, p.cs2, p.cs4, uuh);
+        const float geq = feq_lit<true>(FMUL(w, temperature), cu, d, uuh);
         const float g = __ldg(p.th_src + (uint64_t)i * p.stride + n);
         p.th_tgt[(uint64_t)i * p.stride + n] = thermal_relax(p, g, geq);
     }
@@ -698,17 +743,19 @@ template <int Q, class R>
 __device__ __forceinline__ void thermal_collide_r(const StepParams& p, uint32_t n, const MomentsT<R>& m, R temperature,
                                                   const Coef<R>& k, R tau_t) {
     constexpr int QT = Lattice<Q>::D == 2 ? 5 : 7;
-    const R uuh = uuh_of(m.ux, m.uy, m.uz, k.cs2);
+    const R uuh = uuh_of<false>(m.ux, m.uy, m.uz, k.d);
     const R* src = th_src_of(p, R(0));
     R* tgt = th_tgt_of(p, R(0));
+    const R rtau_t = sizeof(R) == 4 ? R(p.Rtau_t) : R(0);
+    const bool ok_t = sizeof(R) == 4 && (p.div_ok & 8u) != 0;
 #pragma unroll
     for (int i = 0; i < QT; i++) {
         const Dir c = ThermalLattice<QT>::c(i);
         const R w = ThermalW<QT, R>::w(i);
         const R cu = cdot_rt(c, m.ux, m.uy, m.uz);
-        const R geq = feq_lit(FMUL(w, temperature), cu, k.cs2, k.cs4, uuh);
+        const R geq = feq_lit<false>(FMUL(w, temperature), cu, k.d, uuh);
         const R g = __ldg(src + (uint64_t)i * p.stride + n);
-        tgt[(uint64_t)i * p.stride + n] = FSUB(g, FDIV(FSUB(g, geq), tau_t));
+        tgt[(uint64_t)i * p.stride + n] = FSUB(g, div_u(FSUB(g, geq), tau_t, rtau_t, ok_t));
     }
 }
 
@@ -728,14 +775,15 @@ __device__ __forceinline__ void thermal_collide_push(const StepParams& p, uint32
     constexpr int QT = Lattice<Q>::D == 2 ? 5 : 7;
     using TL = ThermalLattice<QT>;
     const uint64_t S = p.stride;
-    const float uuh = uuh_of(m.ux, m.uy, m.uz, p.cs2);
+    const Div<float> d = div_of(p);
+    const float uuh = uuh_of<true>(m.ux, m.uy, m.uz, d);
     float a[QT], b[QT];
 #pragma unroll
     for (int i = 0; i < QT; i++) {
         const Dir c = TL::c(i);
         const float w = TL::w(i);
         const float cu = cdot_rt(c, m.ux, m.uy, m.uz);
-        const float geq = feq_lit(FMUL(w, temperature), cu, p.cs2, p.cs4, uuh);
+        const float geq = feq_lit<true>(FMUL(w, temperature), cu, d, uuh);
         a[i] = __ldg(p.th_src + (uint64_t)i * S + n);
         b[i] = thermal_relax(p, a[i], geq);
     }

@@ -918,7 +918,21 @@ __device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepP
     else velocity_literal<Q>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
     if (p.flags & F_UPDATE) {
         const Coef<R> k = coef_of(p, R(0));
-        auto emit = [&](int i, R v) { *ptr_st(opp(i)) = C::raw_enc(v); };
+        // 16-bit multiphase flow: mass-conserving rounding -- each population
+        // is stored with the rounding error of the ones emitted before it
+        // (population order) added first, so that the cell's stored
+        // populations sum to its computed ones up to the last rounding
+        R carry = R(0);
+        auto emit = [&](int i, R v) {
+            if constexpr (MP && C::SHIFTED) {
+                const R vv = FADD(v, carry);
+                const T h = C::raw_enc(vv);
+                carry = FSUB(vv, C::raw_dec(h));
+                *ptr_st(opp(i)) = h;
+            } else {
+                *ptr_st(opp(i)) = C::raw_enc(v);
+            }
+        };
         if (m.out_ext) collide_fixed<Q, TRT, FORCED, true, C::SHIFTED, SCE>(f, m, k, emit);
         else collide_fixed<Q, TRT, FORCED, false, C::SHIFTED, SCE>(f, m, k, emit);
     }
@@ -1072,8 +1086,15 @@ __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, i
         }
         if constexpr (C::SHIFTED) velocity_and_limit<Q, SCE>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
         else velocity_literal<Q>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
+        // multiphase: the mass-conserving rounding of the one-cell kernel
+        // (each population carries the rounding error of the ones before it)
+        float carry = 0.f;
         auto emit = [&](int i, float v) {
             const int o = opp(i);
+            if constexpr (MP && C::SHIFTED) {
+                v = FADD(v, carry);
+                carry = FSUB(v, C::raw_dec(C::raw_enc(v)));
+            }
             if constexpr (std::is_same<T, __half>::value) {
                 if (paired(o)) {
                     if (half == 0) {
@@ -1511,17 +1532,29 @@ __device__ __forceinline__ CellSumT<typename Codec<ST>::R> cell_update(const Ste
 
     // ---- collision + AA store (collide.comp:727-760) ----
     if (flags & F_UPDATE) {
+        // 16-bit multiphase flow: the mass-conserving rounding (each population
+        // carries the rounding error of the ones before it, written or not)
+        const bool carry_on = C::SHIFTED && (flags & F_MULTIPHASE);
+        R carry = R(0);
         collide_emit<Q, C::SHIFTED>(f, m, k, (flags & F_TRT) != 0, (flags & F_SOURCE) != 0, eqb, [&](int i, R v) {
             const Dir c = L::c(i);
             const R w = W::w(i);
+            T h;
+            if (carry_on) {
+                const R vv = FADD(v, carry);
+                h = C::enc(vv, w);
+                carry = FSUB(vv, C::dec(h, w));
+            } else {
+                h = C::enc(v, w);
+            }
             if (MODE == AA_EVEN) {
                 int dx = x + c.x, dy = y + c.y, dz = z + c.z;
                 bool dopen;
                 coords_wrap<Q>(dx, dy, dz, nx, ny, nz, dopen, flags);
                 if (!dopen)
-                    plane(opp(i))[(uint32_t)dx + (uint32_t)nx * ((uint32_t)dy + (uint32_t)ny * (uint32_t)dz)] = C::enc(v, w);
+                    plane(opp(i))[(uint32_t)dx + (uint32_t)nx * ((uint32_t)dy + (uint32_t)ny * (uint32_t)dz)] = h;
             } else {
-                plane(i)[n] = C::enc(v, w);
+                plane(i)[n] = h;
             }
         });
     }

@@ -620,6 +620,21 @@ static void collide(orc_t* s, int save, int update) {
                     fn[j] = out_ext ? ep - em : vj;
                 }
             }
+            if (sh && s->d.multiphase) {
+                /* 16-bit storage of multiphase flow: mass-conserving rounding.
+                 * Each population is rounded with the rounding error of the
+                 * ones before it (in population order) added first, so the
+                 * stored populations of a cell sum to the computed ones up to
+                 * the last rounding (an error diffusion; Shan-Chen interfaces
+                 * otherwise gain mass at ~1e-5 per step from rounding). */
+                REAL carry = 0;
+                for (int i = 0; i < Q; i++) {
+                    const REAL v = fn[i] + carry;
+                    const REAL h = lat_store(s, v, i);
+                    carry = v - h;
+                    fn[i] = h;
+                }
+            }
             for (int i = 0; i < Q; i++) {
                 size_t wc; int ws;
                 if (aa_write_addr(s, x, y, z, i, odd, &wc, &ws)) continue;

@@ -23,12 +23,13 @@ def spinodal_solver(res, storage, seed=4):
 
 # Mass drift over 4000 steps at 128^3 (FP64 sums of the densities).  FP64
 # arithmetic conserves mass to 1e-13 (the FP64 oracle); the FP32 update (the
-# reference's unshifted arithmetic) gains ~1.5e-8 of the mass per step here;
-# 16-bit storage rounds every population each step and the rounding of the
-# interface's forced populations does not cancel: fp16s and fp16c (the same
-# half rounding, scaled) drift by a few percent.
-SC_DRIFT_BOUND = {bf.FloatingPointAccuracy.fp32: 2e-4, bf.FloatingPointAccuracy.fp16s: 0.1,
-                  bf.FloatingPointAccuracy.fp16c: 0.1}
+# reference's unshifted arithmetic) gains ~1.5e-8 of the mass per step here.
+# 16-bit storage rounds every population each step; rounded independently,
+# the errors of a phase-separated flow add up (+1.8e-2 over 2000 steps at
+# 48^3 in the oracle), so multiphase flow stores each population with the
+# rounding error of the ones before it added (-1.1e-4 over the same run).
+SC_DRIFT_BOUND = {bf.FloatingPointAccuracy.fp32: 2e-4, bf.FloatingPointAccuracy.fp16s: 1e-3,
+                  bf.FloatingPointAccuracy.fp16c: 1e-3}
 
 
 @pytest.mark.parametrize("storage", list(SC_DRIFT_BOUND))

@@ -302,73 +302,167 @@ def run_precision_leg(bf, size, steps, every=100):
     return out
 
 
-def run_multiphysics_leg(bf, full=False):
-    """Multiphysics configuration: Shan-Chen spinodal decomposition (D3Q19,
-    psi = 1 - exp(-rho), G = -5, rho = 0.69 + 0.01 U(-1,1) seeded) in FP32,
-    FP16S and FP16C storage with the FP64 mass drift; Rayleigh-Benard
-    convection (D3Q19 flow + D3Q7 temperature, hot bottom / cold top walls,
-    Ra 1e5, Pr 0.71, T noise 1e-3 seeded) with its Nusselt number and mass
-    drift.  Reduced sizes by default (128^3 x 2000 steps, 64x64x34 x 20000);
-    full=True runs the configuration's 256^3 x 20000 and 256x256x130 x 50000."""
+def spinodal_solver(bf, res, storage, rho):
+    s = bf.LBM()
+    s.is_collide_esoteric = True
+    s.intermolecular_interaction_strength = -5.0
+    s.initialize_fields_from_arrays(res, 1.0, density=rho, velocity_set=bf.VelocitySet.D3Q19, fp_accuracy=storage,
+                                    is_flow_multiphase=True)
+    return s
+
+
+def run_multiphysics_leg(bf, sc_res=(256, 256, 256), sc_steps=20000, rb_res=(256, 256, 130), rb_steps=50000,
+                         ref_sc_res=(64, 64, 64), ref_sc_steps=2000, ref_rb_res=(64, 64, 34), ref_rb_steps=50000):
+    """Multiphysics configuration at its own sizes: Shan-Chen spinodal
+    decomposition (D3Q19, psi = 1 - exp(-rho), G = -5, rho = 0.69 +
+    0.01 U(-1,1) seeded) 256^3 x 20000 steps in FP32, FP16S and FP16C with the
+    mass drift (FP64 sums); Rayleigh-Benard convection (D3Q19 flow + D3Q7
+    temperature, hot bottom / cold top walls, Ra 1e5, Pr 0.71, T noise 1e-3
+    seeded) 256x256x130 x 50000 steps with its Nusselt number and mass drift.
+    Against the FP64 stepper (bit-exact with the FP64 oracle), at reduced sizes:
+    the Shan-Chen mass drift and liquid fraction at 64^3 x 2000 steps and the
+    Rayleigh-Benard Nusselt number at 64x64x34 x 50000 steps."""
     import numpy as np
     from boltzmannfluids_gb300.workloads import nusselt, rayleigh_benard, spinodal
     out = {}
-    res, steps = ((256, 256, 256), 20000) if full else ((128, 128, 128), 2000)
-    n = res[0] * res[1] * res[2]
-    sc = {"workload": f"Shan-Chen spinodal decomposition D3Q19, G -5, {res[0]}^3 periodic, {steps} steps"}
-    rho = spinodal(res, 0.69, 0.01, 4)
+    n = sc_res[0] * sc_res[1] * sc_res[2]
+    sc = {"workload": f"Shan-Chen spinodal decomposition D3Q19, G -5, {sc_res[0]}^3 periodic, {sc_steps} steps"}
+    rho = spinodal(sc_res, 0.69, 0.01, 4)
     for name in ("fp32", "fp16s", "fp16c"):
-        s = bf.LBM()
-        s.is_collide_esoteric = True
-        s.intermolecular_interaction_strength = -5.0
-        s.initialize_fields_from_arrays(res, 1.0, density=rho, velocity_set=bf.VelocitySet.D3Q19,
-                                        fp_accuracy=getattr(bf.FloatingPointAccuracy, name), is_flow_multiphase=True)
+        s = spinodal_solver(bf, sc_res, getattr(bf.FloatingPointAccuracy, name), rho)
         m0 = s.reduce()[0]
-        ms = s.benchmark_steps(steps)
+        ms = s.benchmark_steps(sc_steps)
         m1 = s.reduce()[0]
         d = s.get_velocity_density_texture().reshape(-1, 4)[:, 3]
         sc[name] = {"mass_rel_drift": float((m1 - m0) / m0), "rho_min": float(d.min()), "rho_max": float(d.max()),
-                    "mlups": round(n * steps / (ms * 1e-3) / 1e6, 1)}
+                    "liquid_fraction": float((d > 0.69).mean()), "mlups": round(n * sc_steps / (ms * 1e-3) / 1e6, 1)}
         del s
-    sc["note"] = "FP64 arithmetic conserves this flow's mass to 1e-13 (the FP64 oracle on a 32^3 case)"
+    # against FP64 at a reduced size: the mass FP64 arithmetic conserves and the phase split
+    rn_ = ref_sc_res[0] * ref_sc_res[1] * ref_sc_res[2]
+    rrho = spinodal(ref_sc_res, 0.69, 0.01, 4)
+    ref = {}
+    for name in ("fp64", "fp32", "fp16s", "fp16c"):
+        s = spinodal_solver(bf, ref_sc_res, getattr(bf.FloatingPointAccuracy, name), rrho)
+        m0 = s.reduce()[0]
+        ms = s.benchmark_steps(ref_sc_steps)
+        m1 = s.reduce()[0]
+        d = s.get_velocity_density_texture().reshape(-1, 4)[:, 3]
+        ref[name] = {"mass_rel_drift": float((m1 - m0) / m0), "liquid_fraction": float((d > 0.69).mean()),
+                     "mlups": round(rn_ * ref_sc_steps / (ms * 1e-3) / 1e6, 1)}
+        del s
+    sc["vs_fp64"] = {"workload": f"{ref_sc_res[0]}^3 x {ref_sc_steps} steps", **ref}
     out["shan_chen"] = sc
-    rres, rsteps = ((256, 256, 130), 50000) if full else ((64, 64, 34), 20000)
-    s, kappa, h = rayleigh_benard(rres, kappa=0.02 if full else 0.008)
+    s, kappa, h = rayleigh_benard(rb_res, kappa=0.02)
     m0 = s.reduce()[0]
-    ms = s.benchmark_steps(rsteps)
+    ms = s.benchmark_steps(rb_steps)
     s.reduce()
     nu_num = nusselt(s, kappa, h)
     m1 = s.reduce()[0]
-    rn = rres[0] * rres[1] * rres[2]
-    out["rayleigh_benard"] = {
-        "workload": f"Rayleigh-Benard D3Q19+D3Q7 TRT, {rres[0]}x{rres[1]}x{rres[2]} (walls at z = 0, {rres[2] - 1}), "
-                    f"Ra 1e5, Pr 0.71, {rsteps} steps, FP32",
-        "nusselt": float(nu_num), "mass_rel_drift": float((m1 - m0) / m0),
-        "mlups": round(rn * rsteps / (ms * 1e-3) / 1e6, 1)}
+    rn = rb_res[0] * rb_res[1] * rb_res[2]
+    rb = {"workload": f"Rayleigh-Benard D3Q19+D3Q7 TRT, {rb_res[0]}x{rb_res[1]}x{rb_res[2]} (walls at z = 0, "
+                      f"{rb_res[2] - 1}), Ra 1e5, Pr 0.71, {rb_steps} steps, FP32",
+          "nusselt": float(nu_num), "mass_rel_drift": float((m1 - m0) / m0),
+          "mlups": round(rn * rb_steps / (ms * 1e-3) / 1e6, 1)}
     del s
-    if not full:
-        out["throughput_full_size"] = multiphysics_throughput(bf)
+    ref = {}
+    for name in ("fp64", "fp32"):
+        s, kappa, h = rayleigh_benard(ref_rb_res, kappa=0.008, storage=getattr(bf.FloatingPointAccuracy, name))
+        m0 = s.reduce()[0]
+        ms = s.benchmark_steps(ref_rb_steps)
+        s.reduce()
+        nu_num = nusselt(s, kappa, h)
+        m1 = s.reduce()[0]
+        ref[name] = {"nusselt": float(nu_num), "mass_rel_drift": float((m1 - m0) / m0),
+                     "mlups": round(ref_rb_res[0] * ref_rb_res[1] * ref_rb_res[2] * ref_rb_steps / (ms * 1e-3) / 1e6, 1)}
+        del s
+    ref["nusselt_rel_err_fp32"] = abs(ref["fp32"]["nusselt"] - ref["fp64"]["nusselt"]) / ref["fp64"]["nusselt"]
+    rb["vs_fp64"] = {"workload": f"{ref_rb_res[0]}x{ref_rb_res[1]}x{ref_rb_res[2]} x {ref_rb_steps} steps", **ref}
+    out["rayleigh_benard"] = rb
+    out["throughput_full_size"] = multiphysics_throughput(bf)
+    return out
+
+
+def run_fp64_error_leg(bf, cavity_steps=10000, sphere_res=(128, 64, 64), sphere_steps=2000):
+    """Every storage's error against the FP64 stepper on the plain-method
+    configurations: the D2Q9 BGK lid-driven cavity 256^2 (tau 0.6, lid u 0.1
+    as a moving wall under halfway bounce-back, the other walls at rest) after
+    10000 steps, and D3Q19 TRT flow past a sphere (velocity inlet 0.05,
+    density outlet, periodic y/z) at half the configuration's size, 2000 steps.
+    Error = max |u - u64| / max |u64| and max |rho - rho64| over fluid cells."""
+    import numpy as np
+    from boltzmannfluids_gb300.workloads import sphere_channel
+    out = {}
+    n = 256
+    y, x = np.mgrid[0:n, 0:n]
+    ids = np.zeros((n, n), np.uint32)
+    ids[(x == 0) | (x == n - 1) | (y == 0)] = 1
+    ids[y == n - 1] = 2
+    fields = {}
+    for name in ("fp64", "fp32", "fp16s", "fp16c"):
+        s = bf.LBM()
+        s.is_collide_esoteric = True
+        s.boundary_mode = bf.BoundaryMode.bounce_back
+        s.set_boundry_properties(1, velocity_translational=(0, 0, 0))
+        s.set_boundry_properties(2, velocity_translational=(0.1, 0, 0))
+        s.initialize_fields_from_arrays((n, n, 1), 0.6, boundry_id=ids.reshape(-1), periodic=(False, False, True),
+                                        velocity_set=bf.VelocitySet.D2Q9,
+                                        fp_accuracy=getattr(bf.FloatingPointAccuracy, name))
+        s.iterate_time(steps=cavity_steps, save=True)
+        fields[name] = s.get_velocity_density_texture().reshape(-1, 4).astype(np.float64)
+        del s
+    fluid = ids.reshape(-1) == 0
+    ref = fields["fp64"][fluid]
+    scale = np.abs(ref[:, :3]).max()
+    out["cavity"] = {"workload": f"D2Q9 BGK lid-driven cavity 256^2, tau 0.6, lid 0.1, {cavity_steps} steps"}
+    for name in ("fp32", "fp16s", "fp16c"):
+        f = fields[name][fluid]
+        out["cavity"][name] = {"u_err_max_over_umax": float(np.abs(f[:, :3] - ref[:, :3]).max() / scale),
+                               "rho_err_max": float(np.abs(f[:, 3] - ref[:, 3]).max())}
+    rho, u, ids3, objs = sphere_channel(sphere_res, radius=8.0, center=(32.0, 32.0, 32.0))
+    fields = {}
+    for name in ("fp64", "fp32", "fp16s", "fp16c"):
+        s = bf.LBM()
+        s.is_collide_esoteric = True
+        s.collision = bf.Collision.trt
+        s.boundary_mode = bf.BoundaryMode.bounce_back
+        for k, o in objs.items():
+            s.set_boundry_properties(k, velocity_translational=(0, 0, 0), kind=o["kind"])
+        s.initialize_fields_from_arrays(sphere_res, 0.55, density=rho, velocity=u, boundry_id=ids3,
+                                        periodic=(False, True, True), velocity_set=bf.VelocitySet.D3Q19,
+                                        fp_accuracy=getattr(bf.FloatingPointAccuracy, name))
+        s.iterate_time(steps=sphere_steps, save=True)
+        fields[name] = s.get_velocity_density_texture().reshape(-1, 4).astype(np.float64)
+        del s
+    fluid = ids3 == 0
+    ref = fields["fp64"][fluid]
+    scale = np.abs(ref[:, :3]).max()
+    out["sphere"] = {"workload": f"D3Q19 TRT flow past a sphere r8, {sphere_res[0]}x{sphere_res[1]}x{sphere_res[2]}, "
+                                 f"inlet 0.05, {sphere_steps} steps"}
+    for name in ("fp32", "fp16s", "fp16c"):
+        f = fields[name][fluid]
+        out["sphere"][name] = {"u_err_max_over_umax": float(np.abs(f[:, :3] - ref[:, :3]).max() / scale),
+                               "rho_err_max": float(np.abs(f[:, 3] - ref[:, 3]).max())}
     return out
 
 
 def multiphysics_throughput(bf, steps=300):
     """MLUPs of the multiphysics configuration's step at its own sizes
-    (Shan-Chen 256^3 in each storage, Rayleigh-Benard 256x256x130), a few
-    hundred timed steps each after the start-up steps."""
+    (Shan-Chen 256^3 in each storage -- fp16s also with the psi stencil staged
+    in shared memory -- and Rayleigh-Benard 256x256x130), a few hundred timed
+    steps each after the start-up steps."""
     from boltzmannfluids_gb300.workloads import rayleigh_benard, spinodal
     res = (256, 256, 256)
     n = res[0] * res[1] * res[2]
     out = {"steps_timed": steps}
     rho = spinodal(res, 0.69, 0.01, 4)
-    for name in ("fp32", "fp16s", "fp16c"):
-        s = bf.LBM()
-        s.is_collide_esoteric = True
-        s.intermolecular_interaction_strength = -5.0
-        s.initialize_fields_from_arrays(res, 1.0, density=rho, velocity_set=bf.VelocitySet.D3Q19,
-                                        fp_accuracy=getattr(bf.FloatingPointAccuracy, name), is_flow_multiphase=True)
+    for name, tile in (("fp32", "0"), ("fp16s", "0"), ("fp16c", "0"), ("fp16s", "1"), ("fp16c", "1")):
+        os.environ["BF_PSI_TILE"] = tile
+        s = spinodal_solver(bf, res, getattr(bf.FloatingPointAccuracy, name), rho)
+        os.environ.pop("BF_PSI_TILE")
         s.iterate_time(steps=4, save=False)
         ms = s.benchmark_steps(steps)
-        out[f"shan_chen_256^3_{name}_mlups"] = round(n * steps / (ms * 1e-3) / 1e6, 1)
+        key = f"shan_chen_256^3_{name}" + ("_psi_tile" if tile == "1" else "") + "_mlups"
+        out[key] = round(n * steps / (ms * 1e-3) / 1e6, 1)
         del s
     rres = (256, 256, 130)
     s, _, _ = rayleigh_benard(rres, kappa=0.02)
@@ -408,7 +502,7 @@ def run_sphere_leg(bf, steps=1000):
     return out
 
 
-def compact_summary(sweep, adj, prec, multi, sphere, peak):
+def compact_summary(sweep, adj, prec, multi, sphere, fp64err):
     """The headline figures of every leg in a few hundred characters (the
     end of the line, which short log tails keep)."""
     out = {}
@@ -423,7 +517,13 @@ def compact_summary(sweep, adj, prec, multi, sphere, peak):
         out["sc_mass_drift"] = {k: float(f"{multi['shan_chen'][k]['mass_rel_drift']:.2e}")
                                 for k in ("fp32", "fp16s", "fp16c")}
     if multi and "rayleigh_benard" in multi:
-        out["rb_nusselt"] = round(multi["rayleigh_benard"]["nusselt"], 4)
+        rb = multi["rayleigh_benard"]
+        out["rb_nusselt"] = round(rb["nusselt"], 4)
+        if "vs_fp64" in rb:
+            out["rb_nusselt_err_vs_fp64"] = float(f"{rb['vs_fp64']['nusselt_rel_err_fp32']:.2e}")
+    if fp64err:
+        out["u_err_vs_fp64"] = {case: {k: float(f"{v[k]['u_err_max_over_umax']:.2e}") for k in ("fp32", "fp16s", "fp16c")}
+                                for case, v in fp64err.items()}
     if sphere:
         out["sphere_mlups"] = sphere["mlups"]
     return out
@@ -498,7 +598,10 @@ def run_gpu(args):
     if args.multiphysics_throughput_steps:
         multi = {"throughput_full_size": multiphysics_throughput(bf, args.multiphysics_throughput_steps)}
     elif not args.no_multiphysics:
-        multi = run_multiphysics_leg(bf, args.multiphysics_full)
+        multi = run_multiphysics_leg(bf)
+    fp64err = None
+    if not args.no_fp64_errors:
+        fp64err = run_fp64_error_leg(bf)
     sphere = None
     if not args.no_sphere:
         sphere = run_sphere_leg(bf, args.sphere_steps)
@@ -527,11 +630,12 @@ def run_gpu(args):
             "conservation_fp64": {"mass": red[0], "momentum": list(red[1:4]), "kinetic_energy": red[4]},
             "precision": prec,
             "multiphysics": multi,
+            "fp64_errors": fp64err,
             "sphere": sphere,
             "adjoint": adj,
             "e2e": e2e,
             "storage_sweep": sweep,
-            "summary": compact_summary(sweep, adj, prec, multi, sphere, peak),
+            "summary": compact_summary(sweep, adj, prec, multi, sphere, fp64err),
             "gpu_launches": args.steps,
             "clocks": clock_info,
         }
@@ -560,7 +664,7 @@ def main():
     ap.add_argument("--precision-size", type=int, default=128, help="cube edge of the Taylor-Green precision leg")
     ap.add_argument("--precision-steps", type=int, default=2000)
     ap.add_argument("--no-multiphysics", action="store_true", help="skip the Shan-Chen / Rayleigh-Benard leg")
-    ap.add_argument("--multiphysics-full", action="store_true", help="run the multiphysics configurations at full size")
+    ap.add_argument("--no-fp64-errors", action="store_true", help="skip the cavity / sphere errors against FP64")
     ap.add_argument("--multiphysics-throughput-steps", type=int, default=0,
                     help="instead of the multiphysics leg, only its full-size throughput part with this many timed steps")
     ap.add_argument("--no-sphere", action="store_true", help="skip the flow-past-a-sphere leg")

@@ -261,6 +261,9 @@ struct alignas(16) StepParams {
     uint32_t tma;
     // 1: 16-bit update steps may run two cells per thread (fast2_step_kernel)
     uint32_t two_cell;
+    // 1: the two-cell Shan-Chen step stages the psi rows of its block in
+    // shared memory (otherwise each neighbour is a cached global load)
+    uint32_t psi_tile;
     // 1: the thermal collision pushes each post-collision thermal population
     // to the slot the thermal pull stream would fill with it (th_tgt becomes
     // the next step's pre-collision state; no stream pass).  Set by the host

@@ -657,26 +657,43 @@ constexpr int kFastMinBlocks16 = BF_FAST_MIN_BLOCKS_16;
 // x + c_i (offsets ox*/oy*/oz* from cell n to x -+ 1, y -+ 1, z -+ 1),
 // summed as w_i psi c_i in direction order, times -G psi(rho) of the cell;
 // returns psi(rho), which is also this step's psi field value of the cell
-template <int Q>
-__device__ __forceinline__ float sc_force(const StepParams& p, uint32_t n, int oxm, int oxp, int oym, int oyp, int ozm,
-                                          int ozp, Moments& m) {
+// nb(c) returns psi at x + c
+template <int Q, class NB>
+__device__ __forceinline__ float sc_force_nb(float G, Moments& m, NB nb) {
     using L = Lattice<Q>;
     const float self_psi = FSUB(1.0f, exp_f32(-m.rho));
     float sx = 0.f, sy = 0.f, sz = 0.f;
 #pragma unroll
     for (int i = 1; i < Q; i++) {
         const Dir c = L::c(i);
-        const uint32_t a = n + (uint32_t)((c.x > 0 ? oxp : (c.x < 0 ? oxm : 0)) + (c.y > 0 ? oyp : (c.y < 0 ? oym : 0)) +
-                                          (c.z > 0 ? ozp : (c.z < 0 ? ozm : 0)));
-        const float wp = FMUL(L::w(i), __ldg(p.psi_src + a));
+        const float wp = FMUL(L::w(i), nb(c));
         if (c.x) sx = FADD(sx, c.x > 0 ? wp : -wp);
         if (c.y) sy = FADD(sy, c.y > 0 ? wp : -wp);
         if (c.z) sz = FADD(sz, c.z > 0 ? wp : -wp);
     }
     // interaction_force *= -self_psi * G; force += interaction_force (:580-583, :718-720)
-    const float k = FMUL(-self_psi, p.G);
+    const float k = FMUL(-self_psi, G);
     m.Fx = FADD(m.Fx, FMUL(sx, k)); m.Fy = FADD(m.Fy, FMUL(sy, k)); m.Fz = FADD(m.Fz, FMUL(sz, k));
     return self_psi;
+}
+template <int Q>
+__device__ __forceinline__ float sc_force(const StepParams& p, uint32_t n, int oxm, int oxp, int oym, int oyp, int ozm,
+                                          int ozp, Moments& m) {
+    return sc_force_nb<Q>(p.G, m, [&](const Dir c) {
+        const uint32_t a = n + (uint32_t)((c.x > 0 ? oxp : (c.x < 0 ? oxm : 0)) + (c.y > 0 ? oyp : (c.y < 0 ? oym : 0)) +
+                                          (c.z > 0 ? ozp : (c.z < 0 ? ozm : 0)));
+        return __ldg(p.psi_src + a);
+    });
+}
+// The same force with psi read from a shared-memory tile of the block's
+// rows: row (c_y + 1) * 3 + (c_z + 1) (3D; c_y + 1 in 2D) of `pitch` floats,
+// column lx + 1 + c_x for the cell at tile column lx (one halo cell each side)
+template <int Q>
+__device__ __forceinline__ float sc_force_tile(float G, const float* tile, int pitch, int lx, Moments& m) {
+    return sc_force_nb<Q>(G, m, [&](const Dir c) {
+        const int row = Lattice<Q>::D == 2 ? c.y + 1 : (c.y + 1) * 3 + (c.z + 1);
+        return tile[row * pitch + lx + 1 + c.x];
+    });
 }
 
 // Boussinesq buoyancy of the thermal lattice (collide.comp:709-716): the
@@ -992,7 +1009,8 @@ __global__ void __launch_bounds__(kStepBlock,
 // one-cell kernel's (fast_cell), so results agree bit for bit.
 // ---------------------------------------------------------------------------
 template <int Q, int ST, int MODE, bool TRT, bool FORCED, bool MP, bool EDGE>
-__device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, int z) {
+__device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, int z, const float* tile = nullptr,
+                                            int pitch = 0, int lx = 0) {
     using L = Lattice<Q>;
     using C = Codec<ST>;
     using T = typename C::T;
@@ -1082,7 +1100,8 @@ __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, i
             // of the first and x + 2 of the second can wrap (x even, nx even)
             const int oxm = half ? -1 : (x == 0 ? nx - 1 : -1);
             const int oxp = half ? (x + 2 == nx ? 1 - nx : 1) : 1;
-            psi_self = sc_force<Q>(p, n + half, oxm, oxp, oym, oyp, ozm, ozp, m);
+            if (tile) psi_self = sc_force_tile<Q>(p.G, tile, pitch, lx + half, m);
+            else psi_self = sc_force<Q>(p, n + half, oxm, oxp, oym, oyp, ozm, ozp, m);
         }
         if constexpr (C::SHIFTED) velocity_and_limit<Q, SCE>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
         else velocity_literal<Q>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
@@ -1147,10 +1166,41 @@ __global__ void __launch_bounds__(kStepBlock, MP ? BF_FAST2_MP_MIN_BLOCKS : BF_F
     }
     const int x = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
     const int y = blockIdx.y, z = blockIdx.z;
+    const float* tile = nullptr;
+    constexpr int kPitch = 2 * kStepBlock + 2;
+    if constexpr (MP) {
+        // p.psi_tile: the block stages the psi rows its cells' stencils read
+        // -- (y + dy, z + dz) for dy, dz in {-1, 0, 1} (dz = 0 in 2D) over its
+        // x range plus one halo cell each side, wrapped -- in shared memory
+        // with plain loads, and the force reads them from there
+        // (dynamic shared memory, sized by the launch only when tiling, so the
+        // cached-load variant keeps its L1 share)
+        constexpr int ROWS = Lattice<Q>::D == 2 ? 3 : 9;
+        extern __shared__ float s_psi[];
+        if (p.psi_tile) {
+            const int nx = p.nx, ny = p.ny, nz = p.nz;
+            const int x0 = 2 * (int)(blockIdx.x * blockDim.x);
+            const int span = min(2 * (int)blockDim.x, nx - x0) + 2;
+            for (int r = 0; r < ROWS; r++) {
+                const int dy = Lattice<Q>::D == 2 ? r - 1 : r / 3 - 1, dz = Lattice<Q>::D == 2 ? 0 : r % 3 - 1;
+                const int yy = y + dy < 0 ? y + dy + ny : (y + dy >= ny ? y + dy - ny : y + dy);
+                const int zz = z + dz < 0 ? z + dz + nz : (z + dz >= nz ? z + dz - nz : z + dz);
+                const float* row = p.psi_src + (size_t)nx * ((size_t)yy + (size_t)ny * (size_t)zz);
+                for (int t = threadIdx.x; t < span; t += blockDim.x) {
+                    int xx = x0 - 1 + t;
+                    xx = xx < 0 ? xx + nx : (xx >= nx ? xx - nx : xx);
+                    s_psi[r * kPitch + t] = __ldg(row + xx);
+                }
+            }
+            __syncthreads();
+            tile = s_psi;
+        }
+    }
     if (x >= p.nx) return;
+    const int lx = x - 2 * (int)(blockIdx.x * blockDim.x);
     const bool edge = MODE == AA_EVEN && (y == 0 || y == p.ny - 1 || (Lattice<Q>::D == 3 && (z == 0 || z == p.nz - 1)));
-    if (edge) fast2_cells<Q, ST, MODE, TRT, FORCED, MP, true>(p, x, y, z);
-    else fast2_cells<Q, ST, MODE, TRT, FORCED, MP, false>(p, x, y, z);
+    if (edge) fast2_cells<Q, ST, MODE, TRT, FORCED, MP, true>(p, x, y, z, tile, kPitch, lx);
+    else fast2_cells<Q, ST, MODE, TRT, FORCED, MP, false>(p, x, y, z, tile, kPitch, lx);
 }
 
 // ---------------------------------------------------------------------------
@@ -1883,7 +1933,10 @@ cudaError_t launch_step_st(const StepParams& p, int mode, int path, cudaStream_t
             // multiphase flow is forced (the pseudopotential) with the source term on
             const bool trt = (p.flags & F_TRT) != 0, mp = (p.flags & F_MULTIPHASE) != 0;
             const bool forced = (p.flags & F_FORCE_CONST) != 0 || mp;
-#define BF_FAST2(MODE_, TRT_, F_, MP_) fast2_step_kernel<Q, ST, MODE_, TRT_, F_, MP_><<<g2, threads, 0, st>>>(p)
+            // the Shan-Chen variant's psi tile (p.psi_tile): ROWS x (2 x block + 2) floats
+            const size_t tile_bytes =
+                (mp && p.psi_tile) ? (size_t)(Lattice<Q>::D == 2 ? 3 : 9) * (2 * kStepBlock + 2) * sizeof(float) : 0;
+#define BF_FAST2(MODE_, TRT_, F_, MP_) fast2_step_kernel<Q, ST, MODE_, TRT_, F_, MP_><<<g2, threads, tile_bytes, st>>>(p)
 #define BF_FAST2_MODE(MODE_)                                                                                  \
     if (mp) { if (trt) BF_FAST2(MODE_, true, true, true); else BF_FAST2(MODE_, false, true, true); }          \
     else if (trt) { if (forced) BF_FAST2(MODE_, true, true, false); else BF_FAST2(MODE_, true, false, false); } \

@@ -79,3 +79,22 @@ def test_two_cell_shan_chen_equals_one_cell(monkeypatch, product_lib):
         out.append((s.get_populations(), s.get_velocity_density_texture().copy()))
     assert np.array_equal(out[0][0], out[1][0])
     assert np.array_equal(out[0][1], out[1][1])
+
+
+@pytest.mark.parametrize("vs,res,storage", [
+    (bf.VelocitySet.D3Q19, (24, 20, 16), bf.FloatingPointAccuracy.fp16s),
+    (bf.VelocitySet.D3Q19, (600, 3, 4), bf.FloatingPointAccuracy.fp16c),
+    (bf.VelocitySet.D3Q15, (34, 6, 4), bf.FloatingPointAccuracy.fp16s),
+    (bf.VelocitySet.D2Q9, (40, 24, 1), bf.FloatingPointAccuracy.fp16s),
+])
+def test_two_cell_shan_chen_psi_tile_matches_oracle(vs, res, storage, monkeypatch, product_lib):
+    """The Shan-Chen step with psi staged in a shared-memory tile of the
+    block's rows (BF_PSI_TILE=1; x wrap through the halo, rows of several
+    blocks with a partly filled last one) against the oracle, bit for bit."""
+    monkeypatch.setenv("BF_PSI_TILE", "1")
+    n = res[0] * res[1] * res[2]
+    rng = np.random.default_rng(33)
+    rho = (0.69 + 0.01 * rng.uniform(-1, 1, n)).astype(np.float32)
+    s, o = make_pair(res, 1.0, vs, density=rho, storage=storage, multiphase=True, G=-5.0, esoteric=True)
+    step_and_compare(s, o, [1, 2, 3, 8, 17])
+    assert np.array_equal(s.get_populations(), o.lattice().astype(np.float32))

@@ -237,26 +237,31 @@ def run_adjoint_leg(bf):
     Poiseuille inlet u_max 0.05, partial-bounce-back obstacle in the central
     64x64 box, T = 2000 steps, checkpoints every 100 steps; ms per gradient
     (forward + backward) against the forward solve, device time by CUDA events."""
-    from boltzmannfluids_gb300.adjoint import AdjointChannel, channel_setup
+    from boltzmannfluids_gb300.adjoint import RESIDENT_AUTO, AdjointChannel, channel_setup
 
-    def timed(res, vs, K, reps):
+    def timed(res, vs, K, reps, resident=0):
         s, u_in, tgt = channel_setup(res)
-        g = AdjointChannel(res, 0.6, vs, 2000, K)
+        g = AdjointChannel(res, 0.6, vs, 2000, K, resident_states=resident)
         g.set_parameters(s, u_in)
         g.set_target(tgt)
         g.forward()
         g.backward()
         f_ms, b_ms = g.time(reps)
+        r = g.resident_states
         del g
-        return {"forward_ms": round(f_ms, 3), "backward_ms": round(b_ms, 3),
+        return {"resident_states": r, "forward_ms": round(f_ms, 3), "backward_ms": round(b_ms, 3),
                 "ms_per_gradient": round(f_ms + b_ms, 3), "gradient_over_forward": round((f_ms + b_ms) / f_ms, 3)}
 
     out = {"workload": "D2Q9 BGK channel 512x256, PSM obstacle, T=2000"}
     for K, key in ((100, "checkpoint_every_100"), (2000, "all_states_stored")):
         out[key] = timed((512, 256, 1), bf.VelocitySet.D2Q9, K, 5)
-    # the configuration's 3D case: D3Q19 channel 128^3 (periodic z), checkpoints every 100 steps
-    out["d3q19_128"] = {"workload": "D3Q19 BGK channel 128x128x128 (periodic z), PSM obstacle, T=2000, K=100",
-                        **timed((128, 128, 128), bf.VelocitySet.D3Q19, 100, 2)}
+    # the configuration's 3D case: D3Q19 channel 128^3 (periodic z), checkpoints every 100 steps;
+    # the forward's last states kept in device memory (as many as fit), the rest recomputed
+    w3 = "D3Q19 BGK channel 128x128x128 (periodic z), PSM obstacle, T=2000, K=100"
+    out["d3q19_128"] = {"workload": w3 + ", resident pool (auto)",
+                        **timed((128, 128, 128), bf.VelocitySet.D3Q19, 100, 2, RESIDENT_AUTO)}
+    out["d3q19_128_segments"] = {"workload": w3 + ", two segment buffers",
+                                 **timed((128, 128, 128), bf.VelocitySet.D3Q19, 100, 2)}
     return out
 
 
@@ -510,7 +515,8 @@ def compact_summary(sweep, adj, prec, multi, sphere, fp64err):
         out[name] = {"x_fp32": v["x_fp32"], "frac": v["frac"]}
     if adj:
         out["adjoint_grad_over_fwd"] = {"d2q9_512x256": adj["checkpoint_every_100"]["gradient_over_forward"],
-                                        "d3q19_128": adj["d3q19_128"]["gradient_over_forward"]}
+                                        "d3q19_128": adj["d3q19_128"]["gradient_over_forward"],
+                                        "d3q19_128_segments": adj["d3q19_128_segments"]["gradient_over_forward"]}
     if prec:
         out["tg_ke_err_vs_fp64"] = {k: float(f"{prec[k]['ke_rel_err_max']:.2e}") for k in ("fp32", "fp16s", "fp16c")}
     if multi and "shan_chen" in multi:

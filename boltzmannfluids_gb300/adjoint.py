@@ -18,15 +18,26 @@ class AdjointDesc(C.Structure):
         ("checkpoint_interval", C.c_int32),
         ("drag_weight", C.c_float),
         ("mismatch_weight", C.c_float),
-        ("reserved", C.c_int32 * 8),
+        ("resident_states", C.c_int32),
+        ("reserved", C.c_int32 * 7),
     ]
 
 
+# resident_states: let the library keep as many forward states in device
+# memory as fit (bf_lbm.h, BF_ADJOINT_RESIDENT_AUTO)
+RESIDENT_AUTO = -1
+
+
 class AdjointChannel:
-    """J(s, u_in) and its gradient.  Arrays are x-fastest: s (N,), u_in (ny*nz,), u_target (N, 3)."""
+    """J(s, u_in) and its gradient.  Arrays are x-fastest: s (N,), u_in (ny*nz,), u_target (N, 3).
+
+    resident_states: 0 for two segment buffers of checkpoint_interval states,
+    R > 0 for a pool of R states kept from the forward (at least
+    checkpoint_interval - 1), RESIDENT_AUTO for as many as device memory holds.
+    The gradients do not depend on it."""
 
     def __init__(self, resolution=(512, 256, 1), relaxation_time=0.6, velocity_set=VelocitySet.D2Q9, steps=2000,
-                 checkpoint_interval=100, drag_weight=1.0, mismatch_weight=1.0):
+                 checkpoint_interval=100, drag_weight=1.0, mismatch_weight=1.0, resident_states=0):
         self._lib = load_library()
         d = AdjointDesc()
         self._lib.bf_adjoint_desc_default(C.byref(d))
@@ -37,6 +48,7 @@ class AdjointChannel:
         d.checkpoint_interval = int(checkpoint_interval)
         d.drag_weight = float(drag_weight)
         d.mismatch_weight = float(mismatch_weight)
+        d.resident_states = int(resident_states)
         h = C.c_void_p()
         _check(self._lib.bf_adjoint_create(C.byref(h), C.byref(d)))
         self._h = h
@@ -70,6 +82,13 @@ class AdjointChannel:
         gu = np.zeros(self.rows, np.float64)
         _check(self._lib.bf_adjoint_backward(self._h, gs.ctypes.data_as(C.c_void_p), gu.ctypes.data_as(C.c_void_p)))
         return gs, gu
+
+    @property
+    def resident_states(self) -> int:
+        """The schedule in use: 0 (segment buffers) or the pool's state count."""
+        r = C.c_int32()
+        _check(self._lib.bf_adjoint_get_resident_states(self._h, C.byref(r)))
+        return r.value
 
     def time(self, repeats=3):
         f, b = C.c_float(), C.c_float()

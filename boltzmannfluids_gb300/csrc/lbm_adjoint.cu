@@ -19,13 +19,20 @@
 //   mu_i = (1-w)(1-s) L_i + w (A0 + (c_i - u).V) + s L_opp(i),
 //   A0 = sum_k (1-s) L_k w_k B_k,  V = sum_k (1-s) L_k w_k (3 c_k + 9 (c_k.u) c_k - 3 u),
 // with w = 1/tau and B_k = feq_k/(w_k rho).  Parameter gradients accumulate in
-// FP64 (per-cell terms are summed in FP32 first).  The forward trajectory is
-// checkpointed every K steps; the forward leaves the last segment's states in
-// a segment buffer and every earlier segment is recomputed from its
-// checkpoint.  Two segment buffers alternate: while the adjoint sweeps
-// segment k, segment k-1 is recomputed into the other buffer, each adjoint
-// step sharing one launch with one recomputation step, so the recomputation
-// runs beside the latency-bound sweep.
+// FP64: dJ/ds per cell in FP32 over at most kGradFold steps, then folded into
+// FP64 (the fold steps are fixed by t, so every schedule sums alike).  The forward trajectory is
+// checkpointed every K steps, under one of two schedules:
+//  - segment buffers: the forward leaves the last segment's states in a
+//    segment buffer and every earlier segment is recomputed from its
+//    checkpoint.  Two segment buffers alternate: while the adjoint sweeps
+//    segment k, segment k-1 is recomputed into the other buffer (for D2Q9
+//    each adjoint step shares one launch with one recomputation step, so the
+//    recomputation runs beside the latency-bound sweep);
+//  - a resident pool of R state slots: the forward leaves its last R states
+//    there, so the sweep over them recomputes nothing, and the earlier states
+//    are recomputed from the checkpoints in chunks of up to R states into the
+//    slots the sweep has finished with.  A 128^3 D3Q19 state is 159 MB, so
+//    device memory holds most of a 2000-step trajectory.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -41,6 +48,10 @@ namespace bf {
 namespace {
 
 constexpr int kAdjBlock = 256;
+// dJ/ds: the adjoint step t adds its term to an FP32 partial and folds the
+// partial into the FP64 gradient when (t - 1) % kGradFold == 0 (t = 1, the
+// sweep's last step, always folds)
+constexpr int kGradFold = 64;
 
 struct AdjParams {
     int nx, ny, nz;
@@ -54,6 +65,7 @@ struct AdjParams {
     const float* lam_in;    // adjoint of f^t
     float* lam_out;         // adjoint of f^(t-1)
     double* grad_s;         // n
+    float* grad_acc;        // n: dJ/ds of the steps since the last fold into grad_s
     double* grad_in;        // ny*nz, from the x = 0 cells
     double* grad_out;       // ny*nz, from the x = nx-1 cells
     double* partials;       // one per block (objective)
@@ -115,6 +127,65 @@ __device__ __forceinline__ void adj_pull(const AdjParams& p, int x, int y, int z
     }
 }
 
+// A row (y, z) off the walls (0 < y < ny - 1): population i of cell x comes
+// from cell x - c_i of plane i, z periodic, except where x - c_i leaves the
+// domain in x (the equilibrium inlet and outlet).  A block covers part of one
+// row, so the source's offset from the cell is the same for all its threads
+// and a source index costs one integer add.
+struct RowGeom {
+    uint32_t n;          // the thread's cell
+    uint32_t nx;
+    uint32_t zup, zdn;   // index shift to the source plane z - c_z for c_z = +1 / -1 (periodic)
+    bool xlo, xhi;       // x = 0, x = nx - 1
+};
+__device__ __forceinline__ RowGeom row_geom(const AdjParams& p, int x, int y, int z) {
+    RowGeom r;
+    const uint32_t nx = (uint32_t)p.nx, nxny = nx * (uint32_t)p.ny, last = (uint32_t)(p.nz - 1) * nxny;
+    r.n = (uint32_t)x + nx * ((uint32_t)y + (uint32_t)p.ny * (uint32_t)z);
+    r.nx = nx;
+    r.zup = z == 0 ? last : 0u - nxny;
+    r.zdn = z == p.nz - 1 ? 0u - last : nxny;
+    r.xlo = x == 0;
+    r.xhi = x == p.nx - 1;
+    return r;
+}
+// index of cell x - c_i (in [0, n) for a row off the walls and a source inside in x)
+template <int Q>
+__device__ __forceinline__ uint32_t row_src(const RowGeom& r, int i) {
+    const Dir c = Lattice<Q>::c(i);
+    uint32_t d = 0u - (uint32_t)c.x;
+    if (c.y > 0) d -= r.nx;
+    else if (c.y < 0) d += r.nx;
+    if (c.z > 0) d += r.zup;
+    else if (c.z < 0) d += r.zdn;
+    return r.n + d;
+}
+// the source of population i lies outside in x (equilibrium inlet/outlet)
+template <int Q>
+__device__ __forceinline__ bool row_outside(const RowGeom& r, int i) {
+    const Dir c = Lattice<Q>::c(i);
+    return (c.x > 0 && r.xlo) || (c.x < 0 && r.xhi);
+}
+template <int Q>
+__device__ __forceinline__ void adj_pull_row(const AdjParams& p, const RowGeom& r, float ui, float (&g)[Q]) {
+#pragma unroll
+    for (int i = 0; i < Q; i++) {
+        if (row_outside<Q>(r, i)) g[i] = feq_plain<Q>(i, 1.0f, ui, 0.f, 0.f);
+        else g[i] = p.f_prev[(uint64_t)i * p.n + row_src<Q>(r, i)];
+    }
+}
+// density and momentum of the pulled populations (zero lattice components left out)
+template <int Q>
+__device__ __forceinline__ void adj_moments(const float (&g)[Q], float& rho, float& jx, float& jy, float& jz) {
+    rho = 0.f; jx = 0.f; jy = 0.f; jz = 0.f;
+#pragma unroll
+    for (int i = 0; i < Q; i++) {
+        const Dir c = Lattice<Q>::c(i);
+        rho += g[i];
+        lattice_axpy(c.x, g[i], jx); lattice_axpy(c.y, g[i], jy); lattice_axpy(c.z, g[i], jz);
+    }
+}
+
 __device__ __forceinline__ void block_sum_store(double v, double* out) {
     __shared__ double sm[kAdjBlock / 32];
 #pragma unroll
@@ -148,13 +219,10 @@ __device__ __forceinline__ double adj_forward_cell(const AdjParams& p, int x, in
     {
         const uint32_t n = adj_cell(p, x, y, z);
         float g[Q];
-        adj_pull<Q>(p, x, y, z, n, g);
-        float rho = 0.f, jx = 0.f, jy = 0.f, jz = 0.f;
-#pragma unroll
-        for (int i = 0; i < Q; i++) {
-            const Dir c = L::c(i);
-            rho += g[i]; jx += c.x * g[i]; jy += c.y * g[i]; jz += c.z * g[i];
-        }
+        if (y > 0 && y < p.ny - 1) adj_pull_row<Q>(p, row_geom(p, x, y, z), p.uin[(uint32_t)z * p.ny + y], g);
+        else adj_pull<Q>(p, x, y, z, n, g);
+        float rho, jx, jy, jz;
+        adj_moments<Q>(g, rho, jx, jy, jz);
         const float rr = 1.0f / rho;
         const float ux = jx * rr, uy = jy * rr, uz = jz * rr;
         const float s = p.s[n];
@@ -182,32 +250,35 @@ __global__ void __launch_bounds__(kAdjBlock) adj_forward_kernel(AdjParams p) {
     if (FINAL) block_sum_store(contrib, p.partials);
 }
 
-template <int Q, bool FINAL>
+// ROW: a row off the walls (the sources at block-uniform offsets); else the
+// general pull and push of the wall rows
+template <int Q, bool FINAL, bool FOLD, bool ROW>
 __device__ __forceinline__ void adj_backward_cell(const AdjParams& p, int x, int y, int z) {
     using L = Lattice<Q>;
     const uint32_t n = adj_cell(p, x, y, z);
+    constexpr bool off_walls = ROW;
+    const RowGeom r = row_geom(p, x, y, z);
+    const uint32_t row = (uint32_t)z * p.ny + y;
+    const float ui = p.uin[row];
     // every load of the step is issued before any arithmetic, so the step
     // waits on memory once: the pulled state, the incoming adjoint, the
     // solid fraction and the running parameter gradient
     float g[Q], lam[Q];
-    adj_pull<Q>(p, x, y, z, n, g);
+    if constexpr (off_walls) adj_pull_row<Q>(p, r, ui, g);
+    else adj_pull<Q>(p, x, y, z, n, g);
     if (!FINAL) {
 #pragma unroll
         for (int k = 0; k < Q; k++) lam[k] = p.lam_in[(uint64_t)k * p.n + n];
     }
     const float s = p.s[n];
-    const double gs_prev = p.grad_s[n];
-    float rho = 0.f, jx = 0.f, jy = 0.f, jz = 0.f;
-#pragma unroll
-    for (int i = 0; i < Q; i++) {
-        const Dir c = L::c(i);
-        rho += g[i]; jx += c.x * g[i]; jy += c.y * g[i]; jz += c.z * g[i];
-    }
+    const float gs_acc = p.grad_acc[n];
+    float rho, jx, jy, jz;
+    adj_moments<Q>(g, rho, jx, jy, jz);
     const float rr = 1.0f / rho;
     const float ux = jx * rr, uy = jy * rr, uz = jz * rr;
     // the cell's transposed Jacobian as a few scalars; mu_i is formed where
     // it is stored (no array of Q adjoint populations held in registers)
-    double gs;
+    float gs;
     float fdx = 0.f, fdy = 0.f, fdz = 0.f;        // final step
     float a0 = 0.f, a1 = 0.f;                     // other steps
     const float om = p.omega;
@@ -217,7 +288,7 @@ __device__ __forceinline__ void adj_backward_cell(const AdjParams& p, int x, int
         fdx = 2.0f * p.wm * (ux - p.ustar[3 * (uint64_t)n]) * rr;
         fdy = 2.0f * p.wm * (uy - p.ustar[3 * (uint64_t)n + 1]) * rr;
         fdz = 2.0f * p.wm * (uz - p.ustar[3 * (uint64_t)n + 2]) * rr;
-        gs = (double)p.wd * 2.0 * (double)jx;
+        gs = 2.0f * p.wd * jx;
     } else {
         // The lattice components are -1, 0 or 1 and known per unrolled
         // direction: terms with a zero component are left out and the others
@@ -243,7 +314,7 @@ __device__ __forceinline__ void adj_backward_cell(const AdjParams& p, int x, int
             gsf += lam[k] * (g[opp(k)] - gck);
         }
         Vx = fmaf(-3.0f * ux, Lsum, Vx); Vy = fmaf(-3.0f * uy, Lsum, Vy); Vz = fmaf(-3.0f * uz, Lsum, Vz);
-        gs = (double)gsf;  // per-cell sum in FP32, accumulated over steps in FP64
+        gs = gsf;
         // mu_i = (1 - om)(1 - s) lam_i + om (A0 + (c_i - u).V) + s lam_opp(i)
         a1 = (1.0f - om) * oms;
         a0 = om * (A0 - (ux * Vx + uy * Vy + uz * Vz));
@@ -258,43 +329,73 @@ __device__ __forceinline__ void adj_backward_cell(const AdjParams& p, int x, int
             return fmaf(a1, lam[i], fmaf(om, cv, a0)) + s * lam[opp(i)];
         }
     };
-    p.grad_s[n] = gs_prev + gs;
-    // transpose of the pull; cells off the walls and the inlet/outlet layers
-    // push every adjoint population to an interior neighbour (z periodic)
-    if (x > 0 && x < p.nx - 1 && y > 0 && y < p.ny - 1) {
-        const int zm = z == 0 ? p.nz - 1 : z - 1, zp = z == p.nz - 1 ? 0 : z + 1;
+    if (FOLD) {
+        p.grad_s[n] += (double)(gs_acc + gs);
+        p.grad_acc[n] = 0.0f;
+    } else {
+        p.grad_acc[n] = gs_acc + gs;
+    }
+    // transpose of the pull: mu_i goes where g_i came from; the part sent to
+    // an equilibrium source becomes dJ/du of the inlet/outlet row
+    if constexpr (off_walls) {
+        // the push indices are the pull's; recomputing them (one add each)
+        // from a copy of the cell index the compiler cannot match keeps 19
+        // indices from staying live across the step
+        RowGeom rs = r;
+        asm volatile("mov.b32 %0, %1;" : "=r"(rs.n) : "r"(r.n));
+        float guf = 0.f;
 #pragma unroll
         for (int i = 0; i < Q; i++) {
-            const Dir c = L::c(i);
-            const int Z = c.z > 0 ? zm : (c.z < 0 ? zp : z);
-            p.lam_out[(uint64_t)i * p.n + adj_cell(p, x - c.x, y - c.y, Z)] = mu_of(i);
+            const float mi = mu_of(i);
+            if (!row_outside<Q>(rs, i)) p.lam_out[(uint64_t)i * p.n + row_src<Q>(rs, i)] = mi;
+            else guf += mi * dfeq_du<Q>(i, ui);
         }
-        return;
-    }
-    const float ui = p.uin[(uint32_t)z * p.ny + y];
-    float guf = 0.f;
-    bool eq_source = false;
+        if (r.xlo || r.xhi) {
+            // populations of f^(t-1) that leave through the inlet or outlet feed nothing
 #pragma unroll
-    for (int i = 0; i < Q; i++) {
-        int X, Y, Z;
-        const int kind = adj_source<Q>(p, x, y, z, i, X, Y, Z);
-        const float mi = mu_of(i);
-        if (kind == 0) p.lam_out[(uint64_t)i * p.n + adj_cell(p, X, Y, Z)] = mi;
-        else if (kind == 1) p.lam_out[(uint64_t)opp(i) * p.n + n] = mi;
-        else { guf += mi * dfeq_du<Q>(i, ui); eq_source = true; }
-    }
-    // populations of f^(t-1) that leave through the inlet or outlet feed nothing
+            for (int j = 0; j < Q; j++) {
+                const Dir c = L::c(j);
+                if ((c.x < 0 && r.xlo) || (c.x > 0 && r.xhi)) p.lam_out[(uint64_t)j * p.n + n] = 0.0f;
+            }
+            if (r.xlo) p.grad_in[row] += (double)guf;
+            else p.grad_out[row] += (double)guf;
+        }
+    } else {
+        float guf = 0.f;
+        bool eq_source = false;
 #pragma unroll
-    for (int j = 0; j < Q; j++) {
-        const Dir c = L::c(j);
-        const int X = x + c.x, Y = y + c.y;
-        if (Y >= 0 && Y < p.ny && (X < 0 || X >= p.nx)) p.lam_out[(uint64_t)j * p.n + n] = 0.0f;
+        for (int i = 0; i < Q; i++) {
+            int X, Y, Z;
+            const int kind = adj_source<Q>(p, x, y, z, i, X, Y, Z);
+            const float mi = mu_of(i);
+            if (kind == 0) p.lam_out[(uint64_t)i * p.n + adj_cell(p, X, Y, Z)] = mi;
+            else if (kind == 1) p.lam_out[(uint64_t)opp(i) * p.n + n] = mi;
+            else { guf += mi * dfeq_du<Q>(i, ui); eq_source = true; }
+        }
+        // populations of f^(t-1) that leave through the inlet or outlet feed nothing
+#pragma unroll
+        for (int j = 0; j < Q; j++) {
+            const Dir c = L::c(j);
+            const int X = x + c.x, Y = y + c.y;
+            if (Y >= 0 && Y < p.ny && (X < 0 || X >= p.nx)) p.lam_out[(uint64_t)j * p.n + n] = 0.0f;
+        }
+        if (eq_source) {
+            if (x == 0) p.grad_in[row] += (double)guf;
+            else p.grad_out[row] += (double)guf;
+        }
     }
-    if (eq_source) {
-        const uint32_t row = (uint32_t)z * p.ny + y;
-        if (x == 0) p.grad_in[row] += (double)guf;
-        else p.grad_out[row] += (double)guf;
-    }
+}
+
+// the wall rows' step as a call of its own, so that its registers do not
+// weigh on the rows off the walls (the kernel's common case)
+template <int Q, bool FINAL, bool FOLD>
+__device__ __noinline__ void adj_backward_wall_row(const AdjParams p, int x, int y, int z) {
+    adj_backward_cell<Q, FINAL, FOLD, false>(p, x, y, z);
+}
+template <int Q, bool FINAL, bool FOLD>
+__device__ __forceinline__ void adj_backward_any(const AdjParams& p, int x, int y, int z) {
+    if (y > 0 && y < p.ny - 1) adj_backward_cell<Q, FINAL, FOLD, true>(p, x, y, z);
+    else adj_backward_wall_row<Q, FINAL, FOLD>(p, x, y, z);
 }
 
 // blocks per SM of the adjoint step: D2Q9 5 (48 registers; the 512x256
@@ -310,21 +411,21 @@ __device__ __forceinline__ void adj_backward_cell(const AdjParams& p, int x, int
 template <int Q>
 constexpr int adj_min_blocks() { return Q == 9 ? BF_ADJ_MIN_BLOCKS_Q9 : BF_ADJ_MIN_BLOCKS_Q19; }
 
-template <int Q, bool FINAL>
+template <int Q, bool FINAL, bool FOLD>
 __global__ void __launch_bounds__(kAdjBlock, adj_min_blocks<Q>()) adj_backward_kernel(AdjParams p) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
-    if (x < p.nx) adj_backward_cell<Q, FINAL>(p, x, y, z);
+    if (x < p.nx) adj_backward_any<Q, FINAL, FOLD>(p, x, y, z);
 }
 
 // One adjoint step (blocks z < nz, first in launch order: the longer of the
 // two) and one step of the recomputation of the previous segment (blocks
 // z >= nz) in one launch.  The two read and write disjoint buffers, so their
 // blocks run side by side; stream order keeps each chain in sequence.
-template <int Q>
+template <int Q, bool FOLD>
 __global__ void __launch_bounds__(kAdjBlock, adj_min_blocks<Q>()) adj_sweep_recompute_kernel(AdjParams pb, AdjParams pf) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
     if (x >= pb.nx) return;
-    if (z < pb.nz) adj_backward_cell<Q, false>(pb, x, y, z);
+    if (z < pb.nz) adj_backward_any<Q, false, FOLD>(pb, x, y, z);
     else adj_forward_cell<Q, false>(pf, x, y, z - pb.nz);
 }
 
@@ -373,12 +474,16 @@ struct bf_adjoint {
     int Q = 0;
     uint32_t n = 0, rows = 0, nblocks = 0;
     int nseg = 0;
+    int resident = 0;             // R: 0 for the segment buffers, else the pool's slot count
     cudaStream_t stream = nullptr;
     std::vector<void*> allocs;
     float *s = nullptr, *uin = nullptr, *ustar = nullptr;
     std::vector<float*> ckpt, seg[2];
+    float* pool = nullptr;        // R states, slot j at pool + j Q n
+    float* slot(int j) const { return pool + (size_t)j * Q * n; }
     float *pp[2] = {nullptr, nullptr}, *lam[2] = {nullptr, nullptr};
     double *grad_s = nullptr, *grad_in = nullptr, *grad_out = nullptr, *partials = nullptr, *J = nullptr;
+    float* grad_acc = nullptr;
     cudaGraphExec_t fwd_graph = nullptr, bwd_graph = nullptr;
     bool forward_done = false;
 };
@@ -406,6 +511,7 @@ AdjParams base_params(bf_adjoint* a) {
     p.wm = a->d.mismatch_weight;
     p.s = a->s; p.uin = a->uin; p.ustar = a->ustar;
     p.grad_s = a->grad_s; p.grad_in = a->grad_in; p.grad_out = a->grad_out; p.partials = a->partials;
+    p.grad_acc = a->grad_acc;
     return p;
 }
 
@@ -414,6 +520,22 @@ dim3 adj_grid(const bf_adjoint* a, int& block) {
     block = nx >= kAdjBlock ? kAdjBlock : ((nx + 31) / 32) * 32;
     return dim3((unsigned)((nx + block - 1) / block), (unsigned)a->d.resolution[1], (unsigned)a->d.resolution[2]);
 }
+
+bool grad_fold(int t) { return (t - 1) % kGradFold == 0; }
+
+// the adjoint step t (the last step T seeds the adjoint from dJ/dg)
+template <int Q>
+void launch_adjoint_step(bf_adjoint* a, const AdjParams& p, int t, dim3 grid, int block) {
+    const bool fin = t == a->d.steps, fold = grad_fold(t);
+    if (fin && fold) adj_backward_kernel<Q, true, true><<<grid, block, 0, a->stream>>>(p);
+    else if (fin) adj_backward_kernel<Q, true, false><<<grid, block, 0, a->stream>>>(p);
+    else if (fold) adj_backward_kernel<Q, false, true><<<grid, block, 0, a->stream>>>(p);
+    else adj_backward_kernel<Q, false, false><<<grid, block, 0, a->stream>>>(p);
+}
+
+// first state of the resident tail under the pool schedule: f^P .. f^(T-1)
+// stay in slots 0 .. R-1 (P = T when nothing is resident, T = 1)
+int pool_tail_start(const bf_adjoint* a) { return a->d.steps - std::min(a->resident, a->d.steps - 1); }
 
 template <int Q>
 cudaError_t enqueue_forward(bf_adjoint* a) {
@@ -424,11 +546,14 @@ cudaError_t enqueue_forward(bf_adjoint* a) {
     p.f_next = a->ckpt[0];
     adj_init_kernel<Q><<<grid, block, 0, a->stream>>>(p);
     const float* cur = a->ckpt[0];
-    // states of the last segment go straight to the segment buffer, where the
-    // backward sweep starts, so that segment needs no recomputation
+    // states of the last segment (or the resident tail) go straight to the
+    // buffer where the backward sweep starts, so they need no recomputation
     const int t_last = (a->nseg - 1) * K;
+    const int P = a->resident ? pool_tail_start(a) : T;
     for (int t = 1; t < T; t++) {
-        float* dst = (t % K == 0) ? a->ckpt[t / K] : (t > t_last ? a->seg[(a->nseg - 1) & 1][t - t_last] : a->pp[t & 1]);
+        float* dst;
+        if (a->resident) dst = t >= P ? a->slot(t - P) : (t % K == 0 ? a->ckpt[t / K] : a->pp[t & 1]);
+        else dst = (t % K == 0) ? a->ckpt[t / K] : (t > t_last ? a->seg[(a->nseg - 1) & 1][t - t_last] : a->pp[t & 1]);
         p.f_prev = cur;
         p.f_next = dst;
         adj_forward_kernel<Q, false><<<grid, block, 0, a->stream>>>(p);
@@ -451,6 +576,46 @@ cudaError_t enqueue_forward(bf_adjoint* a) {
 template <int Q>
 constexpr bool kMergeRecompute = Q == 9 || BF_ADJ_MERGE_Q19;
 
+// The pool schedule's backward: adjoint steps t = T .. P+1 over the resident
+// tail, then the states below P in chunks from the top.  A chunk starts at
+// the checkpoint `start` that leaves at most R states start+1 .. top above it
+// (start <= top because R >= K - 1); they are recomputed into slots 0 ..
+// top-start-1, which the sweep has finished with, and swept.
+template <int Q>
+cudaError_t enqueue_backward_pool(bf_adjoint* a) {
+    int block;
+    const dim3 grid = adj_grid(a, block);
+    const int T = a->d.steps, K = a->d.checkpoint_interval, R = a->resident;
+    const int P = pool_tail_start(a);
+    AdjParams p = base_params(a);
+    int cur = -1;
+    auto sweep = [&](int t, const float* f_prev) {
+        const int out = cur == 0 ? 1 : 0;
+        p.f_prev = f_prev;
+        p.lam_out = a->lam[out];
+        p.lam_in = t == T ? nullptr : a->lam[cur];
+        launch_adjoint_step<Q>(a, p, t, grid, block);
+        cur = out;
+    };
+    for (int t = T; t > P; t--) sweep(t, a->slot(t - 1 - P));
+    AdjParams q = p;
+    for (int top = P - 1; top >= 0;) {
+        const int start = top > R ? K * ((top - R + K - 1) / K) : 0;
+        const float* prev = a->ckpt[start / K];
+        for (int j = start + 1; j <= top; j++) {
+            q.f_prev = prev;
+            q.f_next = a->slot(j - start - 1);
+            adj_forward_kernel<Q, false><<<grid, block, 0, a->stream>>>(q);
+            prev = q.f_next;
+        }
+        for (int t = top + 1; t > start; t--) sweep(t, t - 1 == start ? a->ckpt[start / K] : a->slot(t - 2 - start));
+        top = start - 1;
+    }
+    p.lam_in = a->lam[cur];
+    adj_init_grad_kernel<Q><<<dim3((unsigned)a->d.resolution[1], (unsigned)a->d.resolution[2]), kAdjBlock, 0, a->stream>>>(p);
+    return cudaGetLastError();
+}
+
 template <int Q>
 cudaError_t enqueue_backward(bf_adjoint* a) {
     int block;
@@ -458,8 +623,10 @@ cudaError_t enqueue_backward(bf_adjoint* a) {
     const int T = a->d.steps, K = a->d.checkpoint_interval, nseg = a->nseg;
     AdjParams p = base_params(a);
     cudaMemsetAsync(a->grad_s, 0, (size_t)a->n * sizeof(double), a->stream);
+    cudaMemsetAsync(a->grad_acc, 0, (size_t)a->n * sizeof(float), a->stream);
     cudaMemsetAsync(a->grad_in, 0, (size_t)a->rows * sizeof(double), a->stream);
     cudaMemsetAsync(a->grad_out, 0, (size_t)a->rows * sizeof(double), a->stream);
+    if (a->resident) return enqueue_backward_pool<Q>(a);
     // one stream: adjoint step i of segment k together with step i + 1
     // of the recomputation of segment k - 1 (into the other segment
     // buffer, which the sweep of segment k + 1 has finished with)
@@ -480,13 +647,12 @@ cudaError_t enqueue_backward(bf_adjoint* a) {
             if (kMergeRecompute<Q> && t != T && j <= r_steps) {
                 q.f_prev = rprev;
                 q.f_next = a->seg[r & 1][j];
-                adj_sweep_recompute_kernel<Q><<<grid2, block, 0, a->stream>>>(p, q);
+                if (grad_fold(t)) adj_sweep_recompute_kernel<Q, true><<<grid2, block, 0, a->stream>>>(p, q);
+                else adj_sweep_recompute_kernel<Q, false><<<grid2, block, 0, a->stream>>>(p, q);
                 rprev = q.f_next;
                 j++;
-            } else if (t == T) {
-                adj_backward_kernel<Q, true><<<grid, block, 0, a->stream>>>(p);
             } else {
-                adj_backward_kernel<Q, false><<<grid, block, 0, a->stream>>>(p);
+                launch_adjoint_step<Q>(a, p, t, grid, block);
             }
             cur = out;
         }
@@ -558,6 +724,12 @@ int bf_adjoint_create(bf_adjoint** out, const bf_adjoint_desc* d) {
     if (nx <= 0 || ny <= 0 || nz <= 0 || (Q == 9 && nz != 1) || ny > 65535 || nz > 65535)
         return afail(BF_ERR_INVALID_ARGUMENT, "bf_adjoint_create: bad resolution");
     if (d->steps < 1 || d->checkpoint_interval < 1) return afail(BF_ERR_INVALID_ARGUMENT, "bf_adjoint_create: steps and checkpoint_interval must be positive");
+    if (d->resident_states < BF_ADJOINT_RESIDENT_AUTO)
+        return afail(BF_ERR_INVALID_ARGUMENT, "bf_adjoint_create: resident_states must be 0, positive or BF_ADJOINT_RESIDENT_AUTO");
+    // a pool below K - 1 slots could not hold the states between two checkpoints
+    const int min_resident = std::min(d->checkpoint_interval - 1, d->steps - 1);
+    if (d->resident_states > 0 && d->resident_states < min_resident)
+        return afail(BF_ERR_INVALID_ARGUMENT, "bf_adjoint_create: resident_states must be at least checkpoint_interval - 1");
     if (!(d->relaxation_time > 0.5f)) return afail(BF_ERR_INVALID_ARGUMENT, "bf_adjoint_create: relaxation_time must exceed 0.5");
     const uint64_t n64 = (uint64_t)nx * ny * nz;
     if (n64 * Q >= (1ull << 40)) return afail(BF_ERR_INVALID_ARGUMENT, "bf_adjoint_create: domain too large");
@@ -590,19 +762,38 @@ int bf_adjoint_create(bf_adjoint** out, const bf_adjoint_desc* d) {
     if (e == cudaSuccess) e = alloc((size_t)a->n * 4, (void**)&a->s);
     if (e == cudaSuccess) e = alloc((size_t)a->rows * 4, (void**)&a->uin);
     if (e == cudaSuccess) e = alloc((size_t)a->n * 12, (void**)&a->ustar);
-    a->ckpt.assign(a->nseg, nullptr);
-    for (int k = 0; k < a->nseg && e == cudaSuccess; k++) e = alloc(state, (void**)&a->ckpt[k]);
-    for (int b = 0; b < (a->nseg >= 2 ? 2 : 1); b++) {
-        a->seg[b].assign(d->checkpoint_interval, nullptr);
-        for (int j = 1; j < d->checkpoint_interval && e == cudaSuccess; j++) e = alloc(state, (void**)&a->seg[b][j]);
-    }
     for (int k = 0; k < 2 && e == cudaSuccess; k++) e = alloc(state, (void**)&a->pp[k]);
     for (int k = 0; k < 2 && e == cudaSuccess; k++) e = alloc(state, (void**)&a->lam[k]);
     if (e == cudaSuccess) e = alloc((size_t)a->n * 8, (void**)&a->grad_s);
+    if (e == cudaSuccess) e = alloc((size_t)a->n * 4, (void**)&a->grad_acc);
     if (e == cudaSuccess) e = alloc((size_t)a->rows * 8, (void**)&a->grad_in);
     if (e == cudaSuccess) e = alloc((size_t)a->rows * 8, (void**)&a->grad_out);
     if (e == cudaSuccess) e = alloc((size_t)a->nblocks * 8, (void**)&a->partials);
     if (e == cudaSuccess) e = alloc(8, (void**)&a->J);
+    int64_t R = d->resident_states;
+    if (e == cudaSuccess && R == BF_ADJOINT_RESIDENT_AUTO) {
+        // what is free now, less the reserve and the checkpoints' upper bound
+        size_t free_b = 0, total_b = 0;
+        e = cudaMemGetInfo(&free_b, &total_b);
+        const uint64_t reserve = std::max<uint64_t>(8ull << 30, total_b / 20);
+        const uint64_t ckpts = (uint64_t)a->nseg * state;
+        R = free_b > reserve + ckpts ? (int64_t)((free_b - reserve - ckpts) / state) : 0;
+        R = std::max<int64_t>(R, min_resident);
+    }
+    R = std::min<int64_t>(R, d->steps - 1);
+    a->resident = (int)R;
+    if (a->resident) {
+        // the pool, and checkpoints at the multiples of K below the resident tail
+        if (e == cudaSuccess) e = alloc((size_t)a->resident * state, (void**)&a->pool);
+        a->ckpt.assign((d->steps - a->resident - 1) / d->checkpoint_interval + 1, nullptr);
+    } else {
+        a->ckpt.assign(a->nseg, nullptr);
+        for (int b = 0; b < (a->nseg >= 2 ? 2 : 1); b++) {
+            a->seg[b].assign(d->checkpoint_interval, nullptr);
+            for (int j = 1; j < d->checkpoint_interval && e == cudaSuccess; j++) e = alloc(state, (void**)&a->seg[b][j]);
+        }
+    }
+    for (size_t k = 0; k < a->ckpt.size() && e == cudaSuccess; k++) e = alloc(state, (void**)&a->ckpt[k]);
     if (e == cudaSuccess) e = cudaMemset(a->s, 0, (size_t)a->n * 4);
     if (e == cudaSuccess) e = cudaMemset(a->uin, 0, (size_t)a->rows * 4);
     if (e == cudaSuccess) e = cudaMemset(a->ustar, 0, (size_t)a->n * 12);
@@ -694,6 +885,12 @@ int bf_adjoint_time(bf_adjoint* a, int32_t repeats, float* forward_ms, float* ba
     if (r != BF_OK) return r;
     if (forward_ms) *forward_ms = fsum / repeats;
     if (backward_ms) *backward_ms = bsum / repeats;
+    return BF_OK;
+}
+
+int bf_adjoint_get_resident_states(const bf_adjoint* a, int32_t* resident_states) {
+    if (!a || !resident_states) return afail(BF_ERR_INVALID_ARGUMENT, "NULL argument");
+    *resident_states = a->resident;
     return BF_OK;
 }
 

@@ -168,6 +168,7 @@ ABI = {
     "bf_adjoint_forward": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "bf_adjoint_backward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "bf_adjoint_time": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "bf_adjoint_get_resident_states": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "bf_mc_create": (C.c_int, [C.POINTER(C.c_void_p)]),
     "bf_mc_destroy": (C.c_int, [C.c_void_p]),
     "bf_mc_compute": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_int32), C.c_float,

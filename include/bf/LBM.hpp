@@ -425,6 +425,7 @@ struct AdjointDesc {
     int32_t checkpoint_interval = 100; // K
     float drag_weight = 1.0f;
     float mismatch_weight = 1.0f;
+    int32_t resident_states = 0;       // 0, R >= K - 1, or BF_ADJOINT_RESIDENT_AUTO (bf_lbm.h)
 };
 
 class Adjoint {
@@ -441,6 +442,7 @@ public:
         c.checkpoint_interval = d.checkpoint_interval;
         c.drag_weight = d.drag_weight;
         c.mismatch_weight = d.mismatch_weight;
+        c.resident_states = d.resident_states;
         check(bf_adjoint_create(&a_, &c));
     }
     ~Adjoint() { bf_adjoint_destroy(a_); }
@@ -468,6 +470,12 @@ public:
         grad_solid_fraction.resize(n_);
         grad_inlet_velocity.resize(rows_);
         check(bf_adjoint_backward(a_, grad_solid_fraction.data(), grad_inlet_velocity.data()));
+    }
+    // the schedule in use: 0 (segment buffers) or the pool's state count
+    int32_t resident_states() const {
+        int32_t r = 0;
+        check(bf_adjoint_get_resident_states(a_, &r));
+        return r;
     }
 
 private:

@@ -275,9 +275,25 @@ int bf_load_macroscopic(bf_solver* s, const char* path, int32_t target_tick);
  *   f^0 = feq(1, (u_in,0,0)),  J = wd sum 2 s j_x + wm sum |u - u*|^2 at step T,
  * D2Q9 (resolution[2] = 1) or D3Q19.  bf_adjoint_forward runs T steps and
  * stores a checkpoint every checkpoint_interval steps; bf_adjoint_backward
- * recomputes each segment from its checkpoint and runs the hand-written
- * adjoint (transposed pull and transposed BGK/PSM Jacobian), accumulating
- * dJ/ds (per cell) and dJ/du_in (per (y,z) row) in FP64. */
+ * recomputes the states it needs from the checkpoints and runs the
+ * hand-written adjoint (transposed pull and transposed BGK/PSM Jacobian),
+ * accumulating dJ/ds (per cell) and dJ/du_in (per (y,z) row) in FP64.
+ *
+ * resident_states picks how much of the trajectory stays in device memory:
+ *   0   two segment buffers of K states: the forward leaves the last segment
+ *       in one, and the backward recomputes every earlier segment from its
+ *       checkpoint into the other while it sweeps (D2Q9 runs both in one
+ *       launch per step);
+ *   R>0 the forward leaves its last min(R, T-1) states in a pool of R state
+ *       slots; the backward sweeps them, then recomputes the earlier states
+ *       from the checkpoints in chunks of up to R states into the same pool
+ *       (R >= K - 1; with R >= T - 1 nothing is recomputed);
+ *   BF_ADJOINT_RESIDENT_AUTO  R as large as the device memory free at
+ *       bf_adjoint_create allows, less a reserve of max(8 GiB, 5% of the
+ *       device), between K - 1 and T - 1.
+ * Every schedule gives bit-identical gradients: the same adjoint steps on the
+ * same states in the same order. */
+#define BF_ADJOINT_RESIDENT_AUTO (-1)
 typedef struct bf_adjoint bf_adjoint;
 typedef struct {
     int32_t resolution[3];
@@ -287,9 +303,10 @@ typedef struct {
     int32_t checkpoint_interval;   /* K */
     float drag_weight;             /* wd */
     float mismatch_weight;         /* wm */
-    int32_t reserved[8];
+    int32_t resident_states;       /* 0, R > 0 or BF_ADJOINT_RESIDENT_AUTO (above) */
+    int32_t reserved[7];
 } bf_adjoint_desc;
-/* 512 x 256 x 1 D2Q9, tau 0.6, T 2000, K 100, wd = wm = 1 */
+/* 512 x 256 x 1 D2Q9, tau 0.6, T 2000, K 100, wd = wm = 1, resident_states 0 */
 void bf_adjoint_desc_default(bf_adjoint_desc* desc);
 int bf_adjoint_create(bf_adjoint** out, const bf_adjoint_desc* desc);
 int bf_adjoint_destroy(bf_adjoint* a);
@@ -303,6 +320,8 @@ int bf_adjoint_forward(bf_adjoint* a, double* objective);
 int bf_adjoint_backward(bf_adjoint* a, double* grad_solid_fraction, double* grad_inlet_velocity);
 /* mean device milliseconds of `repeats` forward and backward passes (CUDA events) */
 int bf_adjoint_time(bf_adjoint* a, int32_t repeats, float* forward_ms, float* backward_ms);
+/* the schedule's resident state count: 0 (two segment buffers) or the pool's R */
+int bf_adjoint_get_resident_states(const bf_adjoint* a, int32_t* resident_states);
 
 /* ---- marching cubes ------------------------------------------------------ */
 /* Replaces MarchingCubes::compute (BoltzmannFluids/Source/MarchingCubes/

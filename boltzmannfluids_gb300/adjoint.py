@@ -125,3 +125,39 @@ def channel_setup(resolution, u_max=0.05, box=64, seed_s=6, seed_t=7):
     if nz == 1:
         tgt[..., 2] = 0.0
     return s.reshape(-1).astype(np.float32), u_in, tgt.reshape(-1, 3).astype(np.float32)
+
+
+def main(argv=None):
+    """Command line: one gradient of the channel model and, with --repeats,
+    the device time of forward and backward.
+
+    python -m boltzmannfluids_gb300.adjoint --resolution 128 128 128 --steps 2000 --interval 100 --resident auto --repeats 2
+    """
+    import argparse
+    ap = argparse.ArgumentParser(description=main.__doc__.splitlines()[0])
+    ap.add_argument("--resolution", type=int, nargs=3, default=(512, 256, 1))
+    ap.add_argument("--relaxation-time", type=float, default=0.6)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--interval", type=int, default=100, help="checkpoint interval K")
+    ap.add_argument("--resident", default="0", help="0, a state count, or 'auto'")
+    ap.add_argument("--repeats", type=int, default=0)
+    a = ap.parse_args(argv)
+    res = tuple(a.resolution)
+    vs = VelocitySet.D2Q9 if res[2] == 1 else VelocitySet.D3Q19
+    resident = RESIDENT_AUTO if a.resident == "auto" else int(a.resident)
+    s, u_in, tgt = channel_setup(res)
+    g = AdjointChannel(res, a.relaxation_time, vs, a.steps, a.interval, resident_states=resident)
+    g.set_parameters(s, u_in)
+    g.set_target(tgt)
+    J = g.forward()
+    gs, gu = g.backward()
+    out = {"J": J, "grad_s_norm": float(np.linalg.norm(gs)), "grad_u_in_norm": float(np.linalg.norm(gu)),
+           "resident_states": g.resident_states}
+    if a.repeats > 0:
+        f, b = g.time(a.repeats)
+        out.update(forward_ms=f, backward_ms=b, gradient_over_forward=(f + b) / f)
+    print(out)
+
+
+if __name__ == "__main__":
+    main()

@@ -236,6 +236,7 @@ __device__ __forceinline__ void block_reduce_store(CellSumT<R> cs, double* __res
 // ---------------------------------------------------------------------------
 template <class R> struct MomentsT {
     R rho, ux, uy, uz, Fx, Fy, Fz;
+    R drho;  // shifted storage: rho - 1 as summed from the populations (before the +1), 0.01 - 1 when clamped
     bool out_ext;
 };
 using Moments = MomentsT<float>;
@@ -267,6 +268,27 @@ template <int Q, bool SH, int SCE, class R>
 __device__ __forceinline__ R density_of(const R (&f)[Q]) {
     if constexpr (SH) return density_shifted<Q, SCE>(f);
     else return density_lit<Q>(f);
+}
+// m.rho (and, shifted, m.drho = the population sum itself, times 2^-SCE)
+// clamped to max(rho, 0.01) with NaN kept; a clamped shifted cell takes
+// drho = 0.01 - 1.  Flags NaN densities in *err.
+template <int Q, bool SH, int SCE, class R>
+__device__ __forceinline__ void density_into(const R (&f)[Q], MomentsT<R>& m, uint32_t* err) {
+    if constexpr (SH) {
+        R sum = f[0];
+#pragma unroll
+        for (int i = 1; i < Q; i += 2) sum = FADD(sum, pair_sum<Q>(f, i));
+        m.rho = SCE ? FFMA(sum, R(1.0 / (double)(1 << SCE)), R(1)) : FADD(R(1), sum);
+        m.drho = SCE ? FMUL(sum, R(1.0 / (double)(1 << SCE))) : sum;
+    } else {
+        m.rho = density_lit<Q>(f);
+        m.drho = R(0);
+    }
+    if (!(m.rho == m.rho)) atomicOr(err, 1u);
+    if (m.rho < R(0.01)) {
+        m.rho = R(0.01);
+        m.drho = FSUB(R(0.01), R(1));
+    }
 }
 
 // shifted storage: u = j/rho (+ F/(2 rho)) and the velocity limiter
@@ -394,11 +416,73 @@ __device__ __forceinline__ Coef<double> coef_of(const StepParams& p, double) {
                         p.k64.tau, false};
 }
 
+// Shifted storage with a source term (Guo forcing, Shan-Chen, buoyancy): the
+// relaxation and the source folded into one polynomial per opposite pair.
+// With delta = rho - 1 (the population sum), omega+ = 1/tau and omega- (TRT;
+// BGK: both 1/tau), P+- = 1 - omega+-/2:
+//   A = fma(omega+, delta, -fma(omega+ rho, u.u R2/2, P+ (F.u) R2))
+//   V = R4 fma(omega+ rho / 2, u, P+ F)       (even part, times c.u)
+//   U = R2 fma(omega- rho, u, P- F)           (odd part)
+//   g_0 <- fma(w_0, A, (1 - omega+) g_0)
+//   E = fma(c.u, c.V, A)
+//   BGK: g_i   <- fma(w, E + c.U, (1 - omega) g_i),  g_opp <- fma(w, E - c.U, (1 - omega) g_opp)
+//   TRT: g_i   <- fma(w, E + c.U, fma(a, g_i, b g_opp)),  g_opp <- fma(w, E - c.U, fma(a, g_opp, b g_i))
+//        a = 1 - (omega+ + omega-)/2,  b = (omega- - omega+)/2
+// which is, term by term, g + omega+-(g_eq - g) + P+- w S+- of the update on
+// g = f - w (g_eq = w rho bracket - w) with the omega+ rho - omega+ of the
+// equilibrium taken as omega+ delta.  SCE: weights times 2^SCE (the
+// populations are held times 2^SCE; delta is unscaled).
+template <int Q, bool TRT, int SCE, class R, class Emit>
+__device__ __forceinline__ void shifted_source_collide(const R (&f)[Q], const MomentsT<R>& m, const Coef<R>& k,
+                                                       Emit emit) {
+    using L = Lattice<Q>;
+    struct W {
+        __device__ __forceinline__ static constexpr R w(int i) { return LatticeW<Q, R>::w(i) * R(1 << SCE); }
+    };
+    const R op = k.Rtau;
+    const R om = TRT ? k.Wm : k.Rtau;
+    const R pp = TRT ? k.Pp : k.P;
+    const R pm = TRT ? k.Pm : k.P;
+    const R fuR2 = FMUL(FFMA(m.Fz, m.uz, FFMA(m.Fy, m.uy, FMUL(m.Fx, m.ux))), k.R2);
+    const R wp = FMUL(op, m.rho), wm = FMUL(om, m.rho);
+    const R A = FFMA(op, m.drho, -FFMA(wp, FMUL(uu_of(m.ux, m.uy, m.uz), k.R2h), FMUL(pp, fuR2)));
+    const R wph = FMUL(wp, R(0.5));
+    const R Vx = FMUL(FFMA(wph, m.ux, FMUL(pp, m.Fx)), k.R4);
+    const R Vy = FMUL(FFMA(wph, m.uy, FMUL(pp, m.Fy)), k.R4);
+    const R Vz = FMUL(FFMA(wph, m.uz, FMUL(pp, m.Fz)), k.R4);
+    const R Ux = FMUL(FFMA(wm, m.ux, FMUL(pm, m.Fx)), k.R2);
+    const R Uy = FMUL(FFMA(wm, m.uy, FMUL(pm, m.Fy)), k.R2);
+    const R Uz = FMUL(FFMA(wm, m.uz, FMUL(pm, m.Fz)), k.R2);
+    const R keep = FSUB(R(1), op);
+    emit(0, FFMA(W::w(0), A, FMUL(keep, f[0])));
+    const R a = TRT ? FSUB(R(1), FMUL(FADD(op, om), R(0.5))) : keep;
+    const R b = TRT ? FMUL(FSUB(om, op), R(0.5)) : R(0);
+#pragma unroll
+    for (int i = 1; i < Q; i += 2) {
+        const int j = i + 1;
+        const Dir c = L::c(i);
+        const R w = W::w(i);
+        const R E = FFMA(cdot_rt(c, m.ux, m.uy, m.uz), cdot_rt(c, Vx, Vy, Vz), A);
+        const R cU = cdot_rt(c, Ux, Uy, Uz);
+        const R bi = TRT ? FFMA(a, f[i], FMUL(b, f[j])) : FMUL(a, f[i]);
+        const R bj = TRT ? FFMA(a, f[j], FMUL(b, f[i])) : FMUL(a, f[j]);
+        emit(i, FFMA(w, FADD(E, cU), bi));
+        emit(j, FFMA(w, FSUB(E, cU), bj));
+    }
+}
+
 template <int Q, bool SH, class R, class Emit>
 __device__ __forceinline__ void collide_emit(const R (&f)[Q], const MomentsT<R>& m, const Coef<R>& k, bool trt,
                                              bool src, bool to_equilibrium, Emit emit) {
     using L = Lattice<Q>;
     using W = LatticeW<Q, R>;
+    if constexpr (SH) {
+        if (src && !to_equilibrium && !m.out_ext) {
+            if (trt) shifted_source_collide<Q, true, 0>(f, m, k, emit);
+            else shifted_source_collide<Q, false, 0>(f, m, k, emit);
+            return;
+        }
+    }
     if (!SH && (to_equilibrium || !trt)) {
         // collide.comp:727-745 with :589-629 as written: f + (-(f - feq)/tau) + source
         const Div<R>& d = k.d;
@@ -487,6 +571,10 @@ __device__ __forceinline__ void collide_fixed(const R (&f)[Q], const MomentsT<R>
         __device__ __forceinline__ static constexpr R w(int i) { return LatticeW<Q, R>::w(i) * R(1 << SCE); }
     };
     static_assert(SH || SCE == 0, "scaled populations are shifted");
+    if constexpr (SH && SRC && !EXT) {
+        shifted_source_collide<Q, TRT, SCE>(f, m, k, emit);
+        return;
+    }
     if (!SH && !TRT) {
         // collide.comp:727-745 with :589-629 as written: f + (-(f - feq)/tau) + source
         const Div<R>& d = k.d;
@@ -658,23 +746,31 @@ constexpr int kFastMinBlocks16 = BF_FAST_MIN_BLOCKS_16;
 // summed as w_i psi c_i in direction order, times -G psi(rho) of the cell;
 // returns psi(rho), which is also this step's psi field value of the cell
 // nb(c) returns psi at x + c
+struct ScSum { float x, y, z; };
 template <int Q, class NB>
-__device__ __forceinline__ float sc_force_nb(float G, Moments& m, NB nb) {
+__device__ __forceinline__ ScSum sc_sums(NB nb) {
     using L = Lattice<Q>;
-    const float self_psi = FSUB(1.0f, exp_f32(-m.rho));
-    float sx = 0.f, sy = 0.f, sz = 0.f;
+    ScSum s = {0.f, 0.f, 0.f};
 #pragma unroll
     for (int i = 1; i < Q; i++) {
         const Dir c = L::c(i);
         const float wp = FMUL(L::w(i), nb(c));
-        if (c.x) sx = FADD(sx, c.x > 0 ? wp : -wp);
-        if (c.y) sy = FADD(sy, c.y > 0 ? wp : -wp);
-        if (c.z) sz = FADD(sz, c.z > 0 ? wp : -wp);
+        if (c.x) s.x = FADD(s.x, c.x > 0 ? wp : -wp);
+        if (c.y) s.y = FADD(s.y, c.y > 0 ? wp : -wp);
+        if (c.z) s.z = FADD(s.z, c.z > 0 ? wp : -wp);
     }
-    // interaction_force *= -self_psi * G; force += interaction_force (:580-583, :718-720)
+    return s;
+}
+// interaction_force *= -self_psi * G; force += interaction_force (:580-583, :718-720)
+__device__ __forceinline__ float sc_apply(float G, Moments& m, const ScSum& s) {
+    const float self_psi = FSUB(1.0f, exp_f32(-m.rho));
     const float k = FMUL(-self_psi, G);
-    m.Fx = FADD(m.Fx, FMUL(sx, k)); m.Fy = FADD(m.Fy, FMUL(sy, k)); m.Fz = FADD(m.Fz, FMUL(sz, k));
+    m.Fx = FADD(m.Fx, FMUL(s.x, k)); m.Fy = FADD(m.Fy, FMUL(s.y, k)); m.Fz = FADD(m.Fz, FMUL(s.z, k));
     return self_psi;
+}
+template <int Q, class NB>
+__device__ __forceinline__ float sc_force_nb(float G, Moments& m, NB nb) {
+    return sc_apply(G, m, sc_sums<Q>(nb));
 }
 template <int Q>
 __device__ __forceinline__ float sc_force(const StepParams& p, uint32_t n, int oxm, int oxp, int oym, int oyp, int ozm,
@@ -694,6 +790,45 @@ __device__ __forceinline__ float sc_force_tile(float G, const float* tile, int p
         const int row = Lattice<Q>::D == 2 ? c.y + 1 : (c.y + 1) * 3 + (c.z + 1);
         return tile[row * pitch + lx + 1 + c.x];
     });
+}
+
+// psi of a cell pair's stencil (cells x and x + 1, x even, nx even): the
+// row (y + dy, z + dz) of a direction with c = (., dy, dz) at x - 1, x, x + 1
+// and x + 2 (slots 0..3), x and x + 1 as one aligned float2, x - 1 and x + 2
+// (periodic) only where some direction of the row has c_x = -1 / +1.  Both
+// cells' forces then read registers: D3Q19 takes 19 loads per pair instead
+// of 36, the sums unchanged.
+template <int Q>
+__host__ __device__ constexpr int psi_row(Dir c) {
+    return Lattice<Q>::D == 2 ? c.y + 1 : (c.y + 1) * 3 + (c.z + 1);
+}
+template <int Q>
+__host__ __device__ constexpr uint32_t psi_row_xs(int r) {  // bit c_x + 1 for each direction i >= 1 of row r
+    uint32_t m = 0;
+    for (int i = 1; i < Q; i++)
+        if (psi_row<Q>(Lattice<Q>::c(i)) == r) m |= 1u << (Lattice<Q>::c(i).x + 1);
+    return m;
+}
+template <int Q> constexpr int kPsiRows = Lattice<Q>::D == 2 ? 3 : 9;
+template <int Q>
+__device__ __forceinline__ void psi_pair_load(const float* __restrict__ ps, uint32_t n, int x, int nx, int oym,
+                                              int oyp, int ozm, int ozp, float (&pv)[kPsiRows<Q>][4]) {
+    const int oxm = x == 0 ? nx - 1 : -1;          // x - 1 from x
+    const int oxq = x + 2 == nx ? 2 - nx : 2;      // x + 2 from x
+#pragma unroll
+    for (int r = 0; r < kPsiRows<Q>; r++) {
+        constexpr int D = Lattice<Q>::D;
+        const uint32_t xs = psi_row_xs<Q>(r);
+        if (xs == 0u) continue;
+        const int dy = D == 2 ? r - 1 : r / 3 - 1, dz = D == 2 ? 0 : r % 3 - 1;
+        const uint32_t rb = n + (uint32_t)((dy > 0 ? oyp : (dy < 0 ? oym : 0)) + (dz > 0 ? ozp : (dz < 0 ? ozm : 0)));
+        const float2 mid = __ldg(reinterpret_cast<const float2*>(ps + rb));
+        pv[r][1] = mid.x;
+        pv[r][2] = mid.y;
+        // element indices wrap in 32 bits before they meet the pointer
+        if (xs & 1u) pv[r][0] = __ldg(ps + (rb + (uint32_t)oxm));
+        if (xs & 4u) pv[r][3] = __ldg(ps + (rb + (uint32_t)oxq));
+    }
 }
 
 // Boussinesq buoyancy of the thermal lattice (collide.comp:709-716): the
@@ -914,9 +1049,7 @@ __device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepP
     // the update runs on the stored values times 1/SCALE implied: G = g * SCALE
     constexpr int SCE = C::SCALE_EXP;
     MomentsT<R> m;
-    m.rho = density_of<Q, C::SHIFTED, SCE>(f);
-    if (!(m.rho == m.rho)) atomicOr(p.err, 1u);
-    m.rho = m.rho < R(0.01) ? R(0.01) : m.rho;
+    density_into<Q, C::SHIFTED, SCE>(f, m, p.err);
     constexpr bool F64 = sizeof(R) == 8;
     m.Fx = FORCED ? (F64 ? R(p.k64.fconst[0]) : R(p.fconst[0])) : R(0);
     m.Fy = FORCED ? (F64 ? R(p.k64.fconst[1]) : R(p.fconst[1])) : R(0);
@@ -1057,6 +1190,18 @@ __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, i
             ld[i] = a | (b << 16);
         }
     }
+    // Shan-Chen (cached-load variant): the pair's psi stencil, loaded while
+    // the populations are in flight, and both cells' stencil sums, so that
+    // six sums stay live through the first cell's update instead of the stencil
+    ScSum sc_pair[2];
+    if constexpr (MP) {
+        if (!tile) {
+            float pv[kPsiRows<Q>][4];
+            psi_pair_load<Q>(p.psi_src, n, x, nx, oym, oyp, ozm, ozp, pv);
+            sc_pair[0] = sc_sums<Q>([&](const Dir c) { return pv[psi_row<Q>(c)][c.x + 1]; });
+            sc_pair[1] = sc_sums<Q>([&](const Dir c) { return pv[psi_row<Q>(c)][c.x + 2]; });
+        }
+    }
     // the stores recompute their addresses from opaque copies of the pointers
     char *c0s = c0, *cms = cm, *cqs = cq;
     asm volatile("" : "+l"(c0s), "+l"(cms), "+l"(cqs));
@@ -1088,20 +1233,14 @@ __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, i
 #pragma unroll
         for (int i = 0; i < Q; i++) f[i] = C::raw_dec(to16(half ? (ld[i] >> 16) : ld[i]));
         Moments m;
-        m.rho = density_of<Q, C::SHIFTED, SCE>(f);
-        if (!(m.rho == m.rho)) atomicOr(p.err, 1u);
-        m.rho = m.rho < 0.01f ? 0.01f : m.rho;
+        density_into<Q, C::SHIFTED, SCE>(f, m, p.err);
         m.Fx = FORCED ? p.fconst[0] : 0.f;
         m.Fy = FORCED ? p.fconst[1] : 0.f;
         m.Fz = FORCED ? p.fconst[2] : 0.f;
         float psi_self = 0.f;
         if constexpr (MP) {
-            // x neighbours of cell x (half 0) and x + 1 (half 1): only x - 1
-            // of the first and x + 2 of the second can wrap (x even, nx even)
-            const int oxm = half ? -1 : (x == 0 ? nx - 1 : -1);
-            const int oxp = half ? (x + 2 == nx ? 1 - nx : 1) : 1;
             if (tile) psi_self = sc_force_tile<Q>(p.G, tile, pitch, lx + half, m);
-            else psi_self = sc_force<Q>(p, n + half, oxm, oxp, oym, oyp, ozm, ozp, m);
+            else psi_self = sc_apply(p.G, m, sc_pair[half]);
         }
         if constexpr (C::SHIFTED) velocity_and_limit<Q, SCE>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
         else velocity_literal<Q>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
@@ -1314,9 +1453,7 @@ __device__ __forceinline__ CellSum masked_cell(const StepParams& p, int x, int y
     asm volatile("" : "+r"(n_st), "+r"(oxm_st), "+r"(oxp_st));
 
     Moments m;
-    m.rho = density_of<Q, C::SHIFTED, 0>(f);
-    if (!(m.rho == m.rho)) atomicOr(p.err, 1u);
-    m.rho = m.rho < 0.01f ? 0.01f : m.rho;
+    density_into<Q, C::SHIFTED, 0>(f, m, p.err);
     m.Fx = FORCED ? p.fconst[0] : 0.f;
     m.Fy = FORCED ? p.fconst[1] : 0.f;
     m.Fz = FORCED ? p.fconst[2] : 0.f;
@@ -1536,9 +1673,7 @@ __device__ __forceinline__ CellSumT<typename Codec<ST>::R> cell_update(const Ste
 
     // ---- moments and forces (collide.comp:702-725) ----
     MomentsT<R> m;
-    m.rho = density_of<Q, C::SHIFTED, 0>(f);
-    if (!(m.rho == m.rho)) atomicOr(p.err, 1u);
-    m.rho = m.rho < R(0.01) ? R(0.01) : m.rho;  // max(density, 0.01), NaN kept
+    density_into<Q, C::SHIFTED, 0>(f, m, p.err);  // max(density, 0.01), NaN kept
     m.Fx = m.Fy = m.Fz = R(0);
     if (flags & F_FORCE_CONST) { m.Fx = kn.fx; m.Fy = kn.fy; m.Fz = kn.fz; }
     if (flags & F_FORCE_FIELD) { const float4 fv = __ldg(p.force + n); m.Fx = R(fv.x); m.Fy = R(fv.y); m.Fz = R(fv.z); }

@@ -460,16 +460,20 @@ static void collide(orc_t* s, int save, int update) {
          * d = f_i - f_i+1 (the shifted density and momentum, and TRT) */
         REAL sp[QMAX / 2 + 1], dp_[QMAX / 2 + 1];
         for (int i = 1; i < Q; i += 2) { sp[i / 2] = f[i] + f[i + 1]; dp_[i / 2] = f[i] - f[i + 1]; }
-        REAL density;
+        REAL density, delta = 0; /* delta: shifted storage's rho - 1, the population sum itself */
         if (sh) { /* pairwise, plus the sum of w */
             density = f[0];
             for (int i = 1; i < Q; i += 2) density = density + sp[i / 2];
+            delta = density;
             density = (REAL)1 + density;
         } else { /* compute_density (collide.comp:383-388): in population order */
             density = f[0];
             for (int i = 1; i < Q; i++) density = density + f[i];
         }
-        if (density < (REAL)0.01) density = (REAL)0.01; /* max(density, 0.01) */
+        if (density < (REAL)0.01) { /* max(density, 0.01) */
+            density = (REAL)0.01;
+            delta = (REAL)0.01 - (REAL)1;
+        }
         v3 force = get_force(s, cell);
         REAL temperature = 0;
         if (s->thermal) { /* collide.comp:709-716 */
@@ -553,7 +557,42 @@ static void collide(orc_t* s, int save, int update) {
         if (update) {
             REAL fn[QMAX];
             const REAL fuR2 = FMA(force.z, vel.z, FMA(force.y, vel.y, force.x * vel.x)) * s->R2;
-            if (!sh && (eqb || s->d.collision != ORC_TRT)) {
+            if (sh && s->src_on && !eqb && !out_ext) {
+                /* shifted storage with a source term: relaxation and source
+                 * folded into one polynomial per opposite pair (extension):
+                 *   A = fma(w+, delta, -fma(w+ rho, u.u R2/2, P+ (F.u) R2))
+                 *   V = R4 fma(w+ rho/2, u, P+ F),  U = R2 fma(w- rho, u, P- F)
+                 *   g_0 <- fma(w_0, A, (1 - w+) g_0),  E = fma(c.u, c.V, A)
+                 *   BGK: g_i <- fma(w, E +- c.U, (1 - w) g_i)
+                 *   TRT: g_i <- fma(w, E +- c.U, fma(a, g_i, b g_opp)),
+                 *        a = 1 - (w+ + w-)/2, b = (w- - w+)/2
+                 * (w+- the relaxation rates, P+- = 1 - w+-/2; BGK: w- = w+) */
+                const int trt = s->d.collision == ORC_TRT;
+                const REAL op = s->Rtau, om = trt ? s->Wm : s->Rtau;
+                const REAL pp = trt ? s->Pp : s->P, pm = trt ? s->Pm : s->P;
+                const REAL wp = op * density, wm = om * density;
+                const REAL A = FMA(op, delta, -FMA(wp, uu_of(vel) * s->R2h, pp * fuR2));
+                const REAL wph = wp * (REAL)0.5;
+                const v3 V = mk3(FMA(wph, vel.x, pp * force.x) * s->R4, FMA(wph, vel.y, pp * force.y) * s->R4,
+                                 FMA(wph, vel.z, pp * force.z) * s->R4);
+                const v3 U = mk3(FMA(wm, vel.x, pm * force.x) * s->R2, FMA(wm, vel.y, pm * force.y) * s->R2,
+                                 FMA(wm, vel.z, pm * force.z) * s->R2);
+                const REAL keep = (REAL)1 - op;
+                fn[0] = FMA((REAL)s->V[0].w, A, keep * f[0]);
+                const REAL a = trt ? (REAL)1 - (op + om) * (REAL)0.5 : keep;
+                const REAL b = trt ? (om - op) * (REAL)0.5 : (REAL)0;
+                for (int i = 1; i < Q; i += 2) {
+                    const int j = i + 1;
+                    const int cx = s->V[i].cx, cy = s->V[i].cy, cz = s->V[i].cz;
+                    const REAL w = (REAL)s->V[i].w;
+                    const REAL E = FMA(cdot(cx, cy, cz, vel), cdot(cx, cy, cz, V), A);
+                    const REAL cU = cdot(cx, cy, cz, U);
+                    const REAL bi = trt ? FMA(a, f[i], b * f[j]) : a * f[i];
+                    const REAL bj = trt ? FMA(a, f[j], b * f[i]) : a * f[j];
+                    fn[i] = FMA(w, E + cU, bi);
+                    fn[j] = FMA(w, E - cU, bj);
+                }
+            } else if (!sh && (eqb || s->d.collision != ORC_TRT)) {
                 /* collide.comp:727-745 with :589-629: f + (-(f - feq)/tau) + source */
                 const REAL fuc = dot3(force, vel) / s->cs2;
                 for (int i = 0; i < Q; i++) {

@@ -711,6 +711,30 @@ __device__ __forceinline__ void prefetch_block_rows(const StepParams& p, uint32_
     if (hi > lo) l2_prefetch_bulk(reinterpret_cast<const void*>(lo), (uint32_t)(hi - lo));
 }
 
+// Thermal flow: lanes Q .. Q + QT - 1 of the calling warp prefetch into L2
+// thermal plane (lane - Q) over block b's row (the cell's own row: the
+// thermal populations are read at the cell and pushed at the write), with
+// the flow planes' alignment rule (thermal planes are FP32 and share their
+// plane stride, so they start and end on 16-byte boundaries too).
+template <int Q>
+__device__ __forceinline__ void prefetch_block_thermal_rows(const StepParams& p, uint32_t b, int lane, int tile,
+                                                            uint32_t gx, uint32_t gy) {
+    constexpr int QT = Lattice<Q>::D == 2 ? 5 : 7;
+    const int k = lane - Q;
+    if (k < 0 || k >= QT) return;
+    const uint32_t bx = b % gx, yz = b / gx;
+    const int x0 = (int)bx * tile;
+    const int xhi = min(x0 + tile, p.nx);
+    const uintptr_t plane_bytes = (uintptr_t)p.n_cells * sizeof(float);
+    const uintptr_t base = reinterpret_cast<uintptr_t>(p.th_src) + (uintptr_t)k * (uintptr_t)p.stride * sizeof(float);
+    const uintptr_t row = (uintptr_t)p.nx * (uintptr_t)yz;
+    const uintptr_t lo = (base + (row + (uintptr_t)x0) * sizeof(float)) & ~(uintptr_t)15;
+    uintptr_t hi = (base + (row + (uintptr_t)xhi) * sizeof(float) + 15) & ~(uintptr_t)15;
+    hi = min(hi, base + plane_bytes);
+    (void)gy;
+    if (hi > lo) l2_prefetch_bulk(reinterpret_cast<const void*>(lo), (uint32_t)(hi - lo));
+}
+
 // ---------------------------------------------------------------------------
 // fast AA step: fully periodic box, no objects, no thermal / Shan-Chen /
 // force field (constant force allowed; TRT and forcing fixed per launch).
@@ -835,15 +859,23 @@ __device__ __forceinline__ void psi_pair_load(const float* __restrict__ ps, uint
 // temperature T = sum of the cell's thermal populations scales the force by
 // 1 - beta (T - 1); returns T
 template <int Q>
-__device__ __forceinline__ float thermal_buoyancy(const StepParams& p, uint32_t n, Moments& m) {
+__device__ __forceinline__ float thermal_buoyancy_of(const float (&th)[Lattice<Q>::D == 2 ? 5 : 7], float beta, Moments& m) {
     constexpr int QT = Lattice<Q>::D == 2 ? 5 : 7;
     float temperature = 0.f;
 #pragma unroll
-    for (int i = 0; i < QT; i++) temperature = FADD(temperature, __ldg(p.th_src + (uint64_t)i * p.stride + n));
+    for (int i = 0; i < QT; i++) temperature = FADD(temperature, th[i]);
     // buoyancy = -beta (T - 1) force; force += buoyancy
-    const float k = FMUL(-p.beta, FSUB(temperature, 1.0f));
+    const float k = FMUL(-beta, FSUB(temperature, 1.0f));
     m.Fx = FADD(m.Fx, FMUL(k, m.Fx)); m.Fy = FADD(m.Fy, FMUL(k, m.Fy)); m.Fz = FADD(m.Fz, FMUL(k, m.Fz));
     return temperature;
+}
+template <int Q>
+__device__ __forceinline__ float thermal_buoyancy(const StepParams& p, uint32_t n, Moments& m) {
+    constexpr int QT = Lattice<Q>::D == 2 ? 5 : 7;
+    float th[QT];
+#pragma unroll
+    for (int i = 0; i < QT; i++) th[i] = __ldg(p.th_src + (uint64_t)i * p.stride + n);
+    return thermal_buoyancy_of<Q>(th, p.beta, m);
 }
 
 // thermal BGK towards g_eq(T, u) as written (collide.comp:771-782, :634-651,
@@ -1045,6 +1077,14 @@ __device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepP
     R f[Q];
 #pragma unroll
     for (int i = 0; i < Q; i++) f[i] = C::raw_dec(load(i, ptr_of));
+    // thermal flow: the cell's thermal populations (the buoyancy's
+    // temperature) are loaded with its flow populations, one round trip
+    constexpr int QT = Lattice<Q>::D == 2 ? 5 : 7;
+    float th[QT];
+    if constexpr (THERMAL && sizeof(R) == 4) {
+#pragma unroll
+        for (int i = 0; i < QT; i++) th[i] = __ldg(p.th_src + (uint64_t)i * p.stride + n);
+    }
     if (GUARD && guard_mask != 0u) return cs;
     // the update runs on the stored values times 1/SCALE implied: G = g * SCALE
     constexpr int SCE = C::SCALE_EXP;
@@ -1061,7 +1101,7 @@ __device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepP
     float temperature = 0.f;
     if constexpr (THERMAL && !F64) {
         static_assert(FORCED, "thermal flow runs with the source term on");
-        temperature = thermal_buoyancy<Q>(p, n, m);
+        temperature = thermal_buoyancy_of<Q>(th, p.beta, m);
     }
     if constexpr (F64) velocity_literal<Q>(f, m, FORCED, p.k64.vlim, p.k64.vlim, p.k64.vlim_ext);
     else if constexpr (C::SHIFTED) velocity_and_limit<Q, SCE>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
@@ -1560,7 +1600,11 @@ __global__ void __launch_bounds__(kStepBlock, BF_MIXED_MIN_BLOCKS) masked_mixed_
         // entries ahead in the schedule (one plane per lane)
         if (p.pf_blocks != 0u && threadIdx.x < 32 && blockIdx.x + p.pf_blocks < p.n_sched) {
             const uint32_t ahead = __ldg(p.sched + blockIdx.x + p.pf_blocks);
-            if (!(ahead >> 31)) prefetch_block_rows<Q, ST, MODE>(p, ahead, (int)threadIdx.x, (int)blockDim.x, gx, ny);
+            if (!(ahead >> 31)) {
+                prefetch_block_rows<Q, ST, MODE>(p, ahead, (int)threadIdx.x, (int)blockDim.x, gx, ny);
+                if (THERMAL && ST != ST_FP64 && p.th_src)
+                    prefetch_block_thermal_rows<Q>(p, ahead, (int)threadIdx.x, (int)blockDim.x, gx, ny);
+            }
         }
         const uint32_t mb = e;
         const uint32_t yz = mb / gx;

@@ -764,25 +764,70 @@ constexpr int kFastMinBlocks16 = BF_FAST_MIN_BLOCKS_16;
 // load(i, ptr_of) returns the stored element of direction i; ptr_of(k) is
 // the address of the slot read for direction k (the plain kernel loads
 // *ptr_of(i), the staged kernel reads shared memory and never calls it)
-// Shan-Chen pseudopotential force (collide.comp:534-584) with the generic
-// kernel's arithmetic: psi of the previous step at the periodic neighbours
-// x + c_i (offsets ox*/oy*/oz* from cell n to x -+ 1, y -+ 1, z -+ 1),
-// summed as w_i psi c_i in direction order, times -G psi(rho) of the cell;
-// returns psi(rho), which is also this step's psi field value of the cell
-// nb(c) returns psi at x + c
-struct ScSum { float x, y, z; };
-template <int Q, class NB>
-__device__ __forceinline__ ScSum sc_sums(NB nb) {
+// Shan-Chen pseudopotential force (collide.comp:534-584): psi of the
+// previous step at the periodic neighbours x + c_i (offsets ox*/oy*/oz* from
+// cell n to x -+ 1, y -+ 1, z -+ 1), summed, times -G psi(rho) of the cell;
+// returns psi(rho), which is also this step's psi field value of the cell.
+// nb(c) returns psi at x + c.
+// Sums (sc_sums_t): unshifted storage as written, w_i psi_i c_i in
+// direction order; shifted storage (GROUPED, an extension) over opposite
+// pairs, d_k = psi(c_i) - psi(-c_i) for i = 2k + 1, then per component the
+// signed d_k of each weight class summed in pair order and the classes
+// combined as fma(w, class sum, .) in class order -- the same sum in about
+// half the operations.
+template <int Q, bool GROUPED, class R, class NB>
+__device__ __forceinline__ void sc_sums_t(NB nb, R& sx, R& sy, R& sz) {
     using L = Lattice<Q>;
-    ScSum s = {0.f, 0.f, 0.f};
+    using W = LatticeW<Q, R>;
+    if constexpr (!GROUPED) {
+        sx = R(0); sy = R(0); sz = R(0);
 #pragma unroll
-    for (int i = 1; i < Q; i++) {
-        const Dir c = L::c(i);
-        const float wp = FMUL(L::w(i), nb(c));
-        if (c.x) s.x = FADD(s.x, c.x > 0 ? wp : -wp);
-        if (c.y) s.y = FADD(s.y, c.y > 0 ? wp : -wp);
-        if (c.z) s.z = FADD(s.z, c.z > 0 ? wp : -wp);
+        for (int i = 1; i < Q; i++) {
+            const Dir c = L::c(i);
+            const R wp = FMUL(W::w(i), nb(c));
+            if (c.x) sx = FADD(sx, c.x > 0 ? wp : -wp);
+            if (c.y) sy = FADD(sy, c.y > 0 ? wp : -wp);
+            if (c.z) sz = FADD(sz, c.z > 0 ? wp : -wp);
+        }
+    } else {
+        R d[Q / 2];
+#pragma unroll
+        for (int k = 0; k < Q / 2; k++) d[k] = FSUB(nb(L::c(2 * k + 1)), nb(L::c(2 * k + 2)));
+        R out[3];
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            R acc = R(0), cls = R(0), wc = R(0);
+            bool have = false, open = false;
+#pragma unroll
+            for (int k = 0; k < Q / 2; k++) {
+                const int i = 2 * k + 1;
+                if (open && W::w(i) != wc) {  // the class ends: fold its sum in
+                    acc = have ? FFMA(wc, cls, acc) : FMUL(wc, cls);
+                    have = true;
+                    open = false;
+                }
+                const Dir c = L::c(i);
+                const int comp = a == 0 ? c.x : (a == 1 ? c.y : c.z);
+                if (comp == 0) continue;
+                const R t = comp > 0 ? d[k] : -d[k];
+                cls = open ? FADD(cls, t) : t;
+                wc = W::w(i);
+                open = true;
+            }
+            if (open) {
+                acc = have ? FFMA(wc, cls, acc) : FMUL(wc, cls);
+                have = true;
+            }
+            out[a] = have ? acc : R(0);
+        }
+        sx = out[0]; sy = out[1]; sz = out[2];
     }
+}
+struct ScSum { float x, y, z; };
+template <int Q, bool GROUPED, class NB>
+__device__ __forceinline__ ScSum sc_sums(NB nb) {
+    ScSum s;
+    sc_sums_t<Q, GROUPED, float>(nb, s.x, s.y, s.z);
     return s;
 }
 // interaction_force *= -self_psi * G; force += interaction_force (:580-583, :718-720)
@@ -792,14 +837,14 @@ __device__ __forceinline__ float sc_apply(float G, Moments& m, const ScSum& s) {
     m.Fx = FADD(m.Fx, FMUL(s.x, k)); m.Fy = FADD(m.Fy, FMUL(s.y, k)); m.Fz = FADD(m.Fz, FMUL(s.z, k));
     return self_psi;
 }
-template <int Q, class NB>
+template <int Q, bool GROUPED, class NB>
 __device__ __forceinline__ float sc_force_nb(float G, Moments& m, NB nb) {
-    return sc_apply(G, m, sc_sums<Q>(nb));
+    return sc_apply(G, m, sc_sums<Q, GROUPED>(nb));
 }
-template <int Q>
+template <int Q, bool GROUPED>
 __device__ __forceinline__ float sc_force(const StepParams& p, uint32_t n, int oxm, int oxp, int oym, int oyp, int ozm,
                                           int ozp, Moments& m) {
-    return sc_force_nb<Q>(p.G, m, [&](const Dir c) {
+    return sc_force_nb<Q, GROUPED>(p.G, m, [&](const Dir c) {
         const uint32_t a = n + (uint32_t)((c.x > 0 ? oxp : (c.x < 0 ? oxm : 0)) + (c.y > 0 ? oyp : (c.y < 0 ? oym : 0)) +
                                           (c.z > 0 ? ozp : (c.z < 0 ? ozm : 0)));
         return __ldg(p.psi_src + a);
@@ -808,9 +853,9 @@ __device__ __forceinline__ float sc_force(const StepParams& p, uint32_t n, int o
 // The same force with psi read from a shared-memory tile of the block's
 // rows: row (c_y + 1) * 3 + (c_z + 1) (3D; c_y + 1 in 2D) of `pitch` floats,
 // column lx + 1 + c_x for the cell at tile column lx (one halo cell each side)
-template <int Q>
+template <int Q, bool GROUPED>
 __device__ __forceinline__ float sc_force_tile(float G, const float* tile, int pitch, int lx, Moments& m) {
-    return sc_force_nb<Q>(G, m, [&](const Dir c) {
+    return sc_force_nb<Q, GROUPED>(G, m, [&](const Dir c) {
         const int row = Lattice<Q>::D == 2 ? c.y + 1 : (c.y + 1) * 3 + (c.z + 1);
         return tile[row * pitch + lx + 1 + c.x];
     });
@@ -1097,7 +1142,7 @@ __device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepP
     // psi(rho) of the cell: the force's factor and, unchanged (rho is not
     // modified after it), this step's psi field value
     float psi_self = 0.f;
-    if constexpr (MP && !F64) psi_self = sc_force<Q>(p, n, oxm, oxp, oym, oyp, ozm, ozp, m);
+    if constexpr (MP && !F64) psi_self = sc_force<Q, C::SHIFTED>(p, n, oxm, oxp, oym, oyp, ozm, ozp, m);
     float temperature = 0.f;
     if constexpr (THERMAL && !F64) {
         static_assert(FORCED, "thermal flow runs with the source term on");
@@ -1238,8 +1283,8 @@ __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, i
         if (!tile) {
             float pv[kPsiRows<Q>][4];
             psi_pair_load<Q>(p.psi_src, n, x, nx, oym, oyp, ozm, ozp, pv);
-            sc_pair[0] = sc_sums<Q>([&](const Dir c) { return pv[psi_row<Q>(c)][c.x + 1]; });
-            sc_pair[1] = sc_sums<Q>([&](const Dir c) { return pv[psi_row<Q>(c)][c.x + 2]; });
+            sc_pair[0] = sc_sums<Q, C::SHIFTED>([&](const Dir c) { return pv[psi_row<Q>(c)][c.x + 1]; });
+            sc_pair[1] = sc_sums<Q, C::SHIFTED>([&](const Dir c) { return pv[psi_row<Q>(c)][c.x + 2]; });
         }
     }
     // the stores recompute their addresses from opaque copies of the pointers
@@ -1279,7 +1324,7 @@ __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, i
         m.Fz = FORCED ? p.fconst[2] : 0.f;
         float psi_self = 0.f;
         if constexpr (MP) {
-            if (tile) psi_self = sc_force_tile<Q>(p.G, tile, pitch, lx + half, m);
+            if (tile) psi_self = sc_force_tile<Q, C::SHIFTED>(p.G, tile, pitch, lx + half, m);
             else psi_self = sc_apply(p.G, m, sc_pair[half]);
         }
         if constexpr (C::SHIFTED) velocity_and_limit<Q, SCE>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
@@ -1733,20 +1778,14 @@ __device__ __forceinline__ CellSumT<typename Codec<ST>::R> cell_update(const Ste
     if (flags & F_MULTIPHASE) {  // collide.comp:534-584
         const R self_psi = psi_of(m.rho);
         const R* ps_src = psi_src_of(p, R(0));
-        R sx = R(0), sy = R(0), sz = R(0);
-#pragma unroll
-        for (int i = 1; i < Q; i++) {
-            const Dir c = L::c(i);
+        R sx, sy, sz;
+        sc_sums_t<Q, C::SHIFTED, R>([&](const Dir c) -> R {
             int ax = x + c.x, ay = y + c.y, az = z + c.z;
             bool aopen;
             coords_wrap<Q>(ax, ay, az, nx, ny, nz, aopen, flags);
-            const R ps = aopen ? self_psi
-                               : __ldg(ps_src + (uint32_t)ax + (uint32_t)nx * ((uint32_t)ay + (uint32_t)ny * (uint32_t)az));
-            const R wp = FMUL(W::w(i), ps);
-            if (c.x) sx = FADD(sx, c.x > 0 ? wp : -wp);
-            if (c.y) sy = FADD(sy, c.y > 0 ? wp : -wp);
-            if (c.z) sz = FADD(sz, c.z > 0 ? wp : -wp);
-        }
+            return aopen ? self_psi
+                         : __ldg(ps_src + (uint32_t)ax + (uint32_t)nx * ((uint32_t)ay + (uint32_t)ny * (uint32_t)az));
+        }, sx, sy, sz);
         const R ks = FMUL(-self_psi, kn.G);
         m.Fx = FADD(m.Fx, FMUL(sx, ks)); m.Fy = FADD(m.Fy, FMUL(sy, ks)); m.Fz = FADD(m.Fz, FMUL(sz, ks));
     }

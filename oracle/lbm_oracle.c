@@ -378,15 +378,51 @@ static REAL psi(REAL rho) { /* collide.comp:512-516, rho0 = 1 */
 /* Shan-Chen interaction force sum (collide.comp:534-584): acc = sum over
  * i >= 1 of w_i psi(rho(x + c_i)) c_i, the nonzero terms added in order; the
  * caller multiplies by -psi(rho_self) G.  Out-of-domain neighbours use rho_self. */
+#define QMAX 27
 static v3 sc_force_acc(orc_t* s, int x, int y, int z, REAL self_density) {
     v3 f = mk3(0, 0, 0);
     int fx = 1, fy = 1, fz = 1;
     REAL* src = MSRC(s);
+    REAL ps[QMAX];
     for (int i = 1; i < s->Q; i++) {
         int nx = x + s->V[i].cx, ny = y + s->V[i].cy, nz = z + s->V[i].cz;
         int open = wrap(s, &nx, &ny, &nz);
-        REAL p = open ? psi(self_density) : src[cid(s, nx, ny, nz)];
-        REAL wp = (REAL)s->V[i].w * p;
+        ps[i] = open ? psi(self_density) : src[cid(s, nx, ny, nz)];
+    }
+    if (shifted(s)) {
+        /* shifted storages (extension): over opposite pairs, d_k = psi(c_i) -
+         * psi(-c_i) for i = 2k + 1; per component the signed d_k of each
+         * weight class summed in pair order, the classes combined as
+         * fma(w, class sum, .) in class order */
+        REAL d[QMAX / 2], out[3];
+        for (int k = 0; k < s->Q / 2; k++) d[k] = ps[2 * k + 1] - ps[2 * k + 2];
+        for (int a = 0; a < 3; a++) {
+            REAL acc = 0, cls = 0, wc = 0;
+            int have = 0, open = 0;
+            for (int k = 0; k < s->Q / 2; k++) {
+                const int i = 2 * k + 1;
+                if (open && (REAL)s->V[i].w != wc) { /* the class ends: fold its sum in */
+                    acc = have ? FMA(wc, cls, acc) : wc * cls;
+                    have = 1;
+                    open = 0;
+                }
+                const int comp = a == 0 ? s->V[i].cx : (a == 1 ? s->V[i].cy : s->V[i].cz);
+                if (!comp) continue;
+                const REAL t = comp > 0 ? d[k] : -d[k];
+                cls = open ? cls + t : t;
+                wc = (REAL)s->V[i].w;
+                open = 1;
+            }
+            if (open) {
+                acc = have ? FMA(wc, cls, acc) : wc * cls;
+                have = 1;
+            }
+            out[a] = have ? acc : 0;
+        }
+        return mk3(out[0], out[1], out[2]);
+    }
+    for (int i = 1; i < s->Q; i++) {
+        REAL wp = (REAL)s->V[i].w * ps[i];
         if (s->V[i].cx) { REAL t = s->V[i].cx > 0 ? wp : -wp; f.x = fx ? t : f.x + t; fx = 0; }
         if (s->V[i].cy) { REAL t = s->V[i].cy > 0 ? wp : -wp; f.y = fy ? t : f.y + t; fy = 0; }
         if (s->V[i].cz) { REAL t = s->V[i].cz > 0 ? wp : -wp; f.z = fz ? t : f.z + t; fz = 0; }
@@ -403,7 +439,6 @@ static v3 get_force(orc_t* s, size_t cell) { /* collide.comp:451-463 */
 /* ------------------------------------------------------------------------ */
 /* collide.comp main (:676-794) over every cell                               */
 /* ------------------------------------------------------------------------ */
-#define QMAX 27
 static void collide(orc_t* s, int save, int update) {
     const int Q = s->Q;
     const int odd = (int)(s->ticks % 2 == 1);

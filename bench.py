@@ -387,12 +387,13 @@ def run_multiphysics_leg(bf, sc_res=(256, 256, 256), sc_steps=20000, rb_res=(256
                       f"{rb_steps // 5} steps, every {rb_steps // 100}",
           **rb_run(rb_res, rb_steps, 0.02, bf.FloatingPointAccuracy.fp32, rb_steps // 5, rb_steps // 100)}
     ref = {}
-    for name in ("fp64", "fp32"):
+    for name in ("fp64", "fp32", "fp16s", "fp16c"):
         ref[name] = rb_run(ref_rb_res, ref_rb_steps, 0.008, getattr(bf.FloatingPointAccuracy, name),
                            ref_rb_steps // 5, ref_rb_steps // 200)
     ref["nusselt_rel_err_fp32"] = abs(ref["fp32"]["nusselt"] - ref["fp64"]["nusselt"]) / ref["fp64"]["nusselt"]
-    ref["nusselt_mean_rel_err_fp32"] = (abs(ref["fp32"]["nusselt_mean"] - ref["fp64"]["nusselt_mean"]) /
-                                        ref["fp64"]["nusselt_mean"])
+    for name in ("fp32", "fp16s", "fp16c"):
+        ref[f"nusselt_mean_rel_err_{name}"] = (abs(ref[name]["nusselt_mean"] - ref["fp64"]["nusselt_mean"]) /
+                                               ref["fp64"]["nusselt_mean"])
     rb["vs_fp64"] = {"workload": f"{ref_rb_res[0]}x{ref_rb_res[1]}x{ref_rb_res[2]} x {ref_rb_steps} steps, "
                                  f"Nusselt mean over the last {ref_rb_steps // 5} steps, every {ref_rb_steps // 200}",
                      **ref}
@@ -546,8 +547,9 @@ def compact_summary(sweep, adj, prec, multi, sphere, fp64err):
                              "std": round(rb["nusselt_std"], 4)}
         if "vs_fp64" in rb:
             v = rb["vs_fp64"]
-            out["rb_nusselt_err_vs_fp64"] = {"mean": float(f"{v['nusselt_mean_rel_err_fp32']:.2e}"),
-                                             "last_step": float(f"{v['nusselt_rel_err_fp32']:.2e}"),
+            out["rb_nusselt_err_vs_fp64"] = {**{f"mean_{k}": float(f"{v[f'nusselt_mean_rel_err_{k}']:.2e}")
+                                                for k in ("fp32", "fp16s", "fp16c")},
+                                             "last_step_fp32": float(f"{v['nusselt_rel_err_fp32']:.2e}"),
                                              "fp64_std_over_mean": float(f"{v['fp64']['nusselt_std'] / v['fp64']['nusselt_mean']:.2e}")}
     if fp64err:
         out["u_err_vs_fp64"] = {case: {k: float(f"{v[k]['u_err_max_over_umax']:.2e}") for k in ("fp32", "fp16s", "fp16c")}

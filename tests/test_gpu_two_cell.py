@@ -49,18 +49,38 @@ def test_two_cell_equals_one_cell(monkeypatch, product_lib):
     assert np.array_equal(out[0], out[1])
 
 
-@pytest.mark.parametrize("vs,res,storage", [
-    (bf.VelocitySet.D3Q19, (24, 20, 16), bf.FloatingPointAccuracy.fp16s),
-    (bf.VelocitySet.D3Q19, (34, 6, 4), bf.FloatingPointAccuracy.fp16c),
-    (bf.VelocitySet.D2Q9, (40, 24, 1), bf.FloatingPointAccuracy.fp16s),
+@pytest.mark.parametrize("vs,res,storage,collision", [
+    (bf.VelocitySet.D3Q19, (24, 20, 16), bf.FloatingPointAccuracy.fp16s, 0),
+    (bf.VelocitySet.D3Q19, (34, 6, 4), bf.FloatingPointAccuracy.fp16c, 0),
+    (bf.VelocitySet.D2Q9, (40, 24, 1), bf.FloatingPointAccuracy.fp16s, 0),
+    # three weight classes in the grouped stencil sum; TRT with the folded source term
+    (bf.VelocitySet.D3Q27, (14, 8, 6), bf.FloatingPointAccuracy.fp16c, 0),
+    (bf.VelocitySet.D3Q15, (16, 10, 8), bf.FloatingPointAccuracy.fp16s, 1),
+    # rows of several blocks, the last one partly filled
+    (bf.VelocitySet.D3Q19, (600, 3, 4), bf.FloatingPointAccuracy.fp16s, 1),
 ])
-def test_two_cell_shan_chen_matches_oracle(vs, res, storage, product_lib):
+def test_two_cell_shan_chen_matches_oracle(vs, res, storage, collision, product_lib):
     """The pseudopotential force per cell of the pair: psi of the previous
-    step at the neighbours, with the x wrap of each cell."""
+    step at the neighbours, loaded once per pair, with the x wrap of each cell."""
     n = res[0] * res[1] * res[2]
     rng = np.random.default_rng(31)
     rho = (0.69 + 0.01 * rng.uniform(-1, 1, n)).astype(np.float32)
-    s, o = make_pair(res, 1.0, vs, density=rho, storage=storage, multiphase=True, G=-5.0, esoteric=True)
+    s, o = make_pair(res, 1.0, vs, density=rho, storage=storage, multiphase=True, G=-5.0, esoteric=True,
+                     collision=collision)
+    step_and_compare(s, o, [1, 2, 3, 8, 17])
+    assert np.array_equal(s.get_populations(), o.lattice().astype(np.float32))
+
+
+@pytest.mark.parametrize("storage,collision", [(bf.FloatingPointAccuracy.fp16s, 0), (bf.FloatingPointAccuracy.fp16c, 1)])
+def test_shan_chen_16bit_generic_step_matches_oracle(storage, collision, product_lib):
+    """16-bit Shan-Chen through the generic step (open y faces: out-of-domain
+    neighbours take the cell's own psi) against the oracle, bit for bit."""
+    res = (18, 12, 10)
+    n = res[0] * res[1] * res[2]
+    rng = np.random.default_rng(34)
+    rho = (0.69 + 0.01 * rng.uniform(-1, 1, n)).astype(np.float32)
+    s, o = make_pair(res, 1.0, bf.VelocitySet.D3Q19, density=rho, storage=storage, multiphase=True, G=-5.0,
+                     esoteric=True, collision=collision, periodic=(True, False, True))
     step_and_compare(s, o, [1, 2, 3, 8, 17])
     assert np.array_equal(s.get_populations(), o.lattice().astype(np.float32))
 

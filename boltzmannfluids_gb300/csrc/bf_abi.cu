@@ -121,6 +121,7 @@ struct bf_solver {
     DeviceBuf special;        // the cells with a nonzero mask, in index order
     DeviceBuf sched;          // launch schedule of the boundary-aware step (StepParams::sched)
     uint32_t n_special = 0, n_sched = 0, special_chunk = 0;
+    uint32_t sched_shy = 0, sched_shz = 0;  // bit positions of y and z in a plain schedule entry
     uint32_t n_blocks = 0;
     // buffer roles (LBM.h:280-291)
     int lat0_src = 1, th0_src = 1, psi0_src = 1;
@@ -263,23 +264,34 @@ cudaError_t build_special_list(bf_solver* s, uint64_t n) {
 #endif
             const uint32_t chunk = std::min<uint32_t>(BF_SPECIAL_CHUNK, block);
             const uint32_t chunks = (count + chunk - 1) / chunk;
+            // plain entries hold bx | y << shy | z << shz: the bit widths of
+            // grid_x, ny and nz must fit in 31 bits, else no schedule is built
+            // (the one-pass boundary-aware step runs instead)
+            auto bits = [](uint32_t v) { uint32_t b = 0; while ((1ull << b) < v) b++; return b; };
+            const uint32_t ny = (uint32_t)s->desc.resolution[1], nz = (uint32_t)s->desc.resolution[2];
+            const uint32_t shy = bits(grid_x), shz = shy + bits(ny);
+            const bool packable = shz + bits(nz) <= 31;
             std::vector<uint32_t> sched;
-            sched.reserve((size_t)n_blocks + chunks);
-            uint32_t c = 0;
-            for (uint32_t b = 0; b < n_blocks; b++) {
-                const uint32_t bx = b % grid_x;
-                const uint32_t width = std::min<uint32_t>(block, nx - bx * block);
-                if (ptr[b + 1] - ptr[b] < width) sched.push_back(b);
-                while (c < chunks && std::min<uint64_t>((uint64_t)(c + 1) * chunk, count) <= ptr[b + 1])
-                    sched.push_back(0x80000000u | c++);
+            if (packable) {
+                sched.reserve((size_t)n_blocks + chunks);
+                uint32_t c = 0;
+                for (uint32_t b = 0; b < n_blocks; b++) {
+                    const uint32_t bx = b % grid_x, yz = b / grid_x;
+                    const uint32_t width = std::min<uint32_t>(block, nx - bx * block);
+                    if (ptr[b + 1] - ptr[b] < width) sched.push_back(bx | (yz % ny) << shy | (yz / ny) << shz);
+                    while (c < chunks && std::min<uint64_t>((uint64_t)(c + 1) * chunk, count) <= ptr[b + 1])
+                        sched.push_back(0x80000000u | c++);
+                }
+                while (c < chunks) sched.push_back(0x80000000u | c++);
             }
-            while (c < chunks) sched.push_back(0x80000000u | c++);
-            e = s->sched.alloc(sched.size() * sizeof(uint32_t));
-            if (e == cudaSuccess)
+            if (!sched.empty()) e = s->sched.alloc(sched.size() * sizeof(uint32_t));
+            if (e == cudaSuccess && !sched.empty())
                 e = cudaMemcpy(s->sched.p, sched.data(), sched.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
-            if (e == cudaSuccess) {
+            if (e == cudaSuccess && !sched.empty()) {
                 s->n_sched = (uint32_t)sched.size();
                 s->special_chunk = chunk;
+                s->sched_shy = shy;
+                s->sched_shz = shz;
             }
         }
     }
@@ -516,6 +528,8 @@ cudaError_t collide(bf_solver* s, bool save, bool update, bool reduce, bool meas
         p.n_special = s->n_special;
         p.n_sched = s->n_sched;
         p.special_chunk = s->special_chunk;
+        p.sched_shy = s->sched_shy;
+        p.sched_shz = s->sched_shz;
     }
     // the split kernel (masked_mixed_kernel) runs the thermal collision as a
     // push when the masks mark every special thermal source: solid sources

@@ -277,14 +277,18 @@ struct alignas(16) StepParams {
     const uint32_t* nmask;
     // the cells whose mask is nonzero, in increasing index order
     // (n_special), and a launch schedule (n_sched entries, one per block of
-    // masked_mixed_kernel): entry e < 2^31 is block e of the cell grid,
-    // which updates its cells with an empty mask in the periodic kernel's
-    // cell update; entry 2^31 + k updates the listed cells
+    // masked_mixed_kernel): entry e < 2^31 is a block (x-block bx, row y, z)
+    // of the cell grid, packed as below, which updates its cells with an
+    // empty mask in the periodic kernel's cell update; entry 2^31 + k updates the listed cells
     // special[k * special_chunk ..] (special_chunk of them, one per thread).
     // When set, the boundary-aware step runs this way.
     const uint32_t* special;
     const uint32_t* sched;
     uint32_t n_special, n_sched, special_chunk;
+    // a plain entry of the schedule packs its block as bx | y << sched_shy |
+    // z << sched_shz (bit fields of the grid's x-block count, ny and nz), so
+    // that the kernel decodes it with shifts and masks
+    uint32_t sched_shy, sched_shz;
     // fast kernel, even step, rows off the y/z faces: element offset of the
     // slot read for direction i relative to the cell, without its x part:
     // i * stride - (c_y nx + c_z nx ny), modulo 2^32

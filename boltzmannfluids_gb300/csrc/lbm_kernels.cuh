@@ -685,12 +685,9 @@ __host__ __device__ constexpr uint64_t packed_axis(int axis) {
 // inside the plane because planes start and end on 16-byte boundaries
 // whenever pf_blocks is set.  Planes lie `stride` elements apart.
 template <int Q, int ST, int MODE>
-__device__ __forceinline__ void prefetch_block_rows(const StepParams& p, uint32_t b, int lane, int tile,
-                                                    uint32_t gx = gridDim.x, uint32_t gy = gridDim.y) {
+__device__ __forceinline__ void prefetch_rows_at(const StepParams& p, uint32_t bx, int ys, int zs, int lane, int tile) {
     using T = typename Codec<ST>::T;
     if (lane >= Q) return;
-    const uint32_t bx = b % gx, yz = b / gx;
-    int ys = (int)(yz % gy), zs = (int)(yz / gy);
     const int nx = p.nx, ny = p.ny, nz = p.nz;
     const int x0 = (int)bx * tile;
     const int xlo = MODE == AA_EVEN ? max(x0 - 8, 0) : x0;
@@ -710,19 +707,26 @@ __device__ __forceinline__ void prefetch_block_rows(const StepParams& p, uint32_
     hi = min(hi, base + plane_bytes);
     if (hi > lo) l2_prefetch_bulk(reinterpret_cast<const void*>(lo), (uint32_t)(hi - lo));
 }
+// the same for block b of a launch in linear order over a gx x gy x . grid
+template <int Q, int ST, int MODE>
+__device__ __forceinline__ void prefetch_block_rows(const StepParams& p, uint32_t b, int lane, int tile,
+                                                    uint32_t gx = gridDim.x, uint32_t gy = gridDim.y) {
+    if (lane >= Q) return;
+    const uint32_t bx = b % gx, yz = b / gx;
+    prefetch_rows_at<Q, ST, MODE>(p, bx, (int)(yz % gy), (int)(yz / gy), lane, tile);
+}
 
 // Thermal flow: lanes Q .. Q + QT - 1 of the calling warp prefetch into L2
-// thermal plane (lane - Q) over block b's row (the cell's own row: the
+// thermal plane (lane - Q) over row yz of x-block bx (the cell's own row: the
 // thermal populations are read at the cell and pushed at the write), with
 // the flow planes' alignment rule (thermal planes are FP32 and share their
 // plane stride, so they start and end on 16-byte boundaries too).
 template <int Q>
-__device__ __forceinline__ void prefetch_block_thermal_rows(const StepParams& p, uint32_t b, int lane, int tile,
-                                                            uint32_t gx, uint32_t gy) {
+__device__ __forceinline__ void prefetch_thermal_rows_at(const StepParams& p, uint32_t bx, uint32_t yz, int lane,
+                                                         int tile) {
     constexpr int QT = Lattice<Q>::D == 2 ? 5 : 7;
     const int k = lane - Q;
     if (k < 0 || k >= QT) return;
-    const uint32_t bx = b % gx, yz = b / gx;
     const int x0 = (int)bx * tile;
     const int xhi = min(x0 + tile, p.nx);
     const uintptr_t plane_bytes = (uintptr_t)p.n_cells * sizeof(float);
@@ -731,7 +735,6 @@ __device__ __forceinline__ void prefetch_block_thermal_rows(const StepParams& p,
     const uintptr_t lo = (base + (row + (uintptr_t)x0) * sizeof(float)) & ~(uintptr_t)15;
     uintptr_t hi = (base + (row + (uintptr_t)xhi) * sizeof(float) + 15) & ~(uintptr_t)15;
     hi = min(hi, base + plane_bytes);
-    (void)gy;
     if (hi > lo) l2_prefetch_bulk(reinterpret_cast<const void*>(lo), (uint32_t)(hi - lo));
 }
 
@@ -1639,22 +1642,24 @@ template <int Q, int ST, int MODE, bool TRT, bool FORCED, bool THERMAL>
 __global__ void __launch_bounds__(kStepBlock, BF_MIXED_MIN_BLOCKS) masked_mixed_kernel(const __grid_constant__ StepParams p) {
     const uint32_t nx = (uint32_t)p.nx, ny = (uint32_t)p.ny;
     const uint32_t e = __ldg(p.sched + blockIdx.x);
+    // a plain entry: bx | y << sched_shy | z << sched_shz
+    const uint32_t shy = p.sched_shy, shz = p.sched_shz;
+    const uint32_t mx = (1u << shy) - 1u, my = (1u << (shz - shy)) - 1u;
     if (!(e >> 31)) {
-        const uint32_t gx = (nx + blockDim.x - 1) / blockDim.x;
         // the first warp prefetches the rows of the plain block pf_blocks
         // entries ahead in the schedule (one plane per lane)
         if (p.pf_blocks != 0u && threadIdx.x < 32 && blockIdx.x + p.pf_blocks < p.n_sched) {
             const uint32_t ahead = __ldg(p.sched + blockIdx.x + p.pf_blocks);
             if (!(ahead >> 31)) {
-                prefetch_block_rows<Q, ST, MODE>(p, ahead, (int)threadIdx.x, (int)blockDim.x, gx, ny);
+                const uint32_t abx = ahead & mx, ay = (ahead >> shy) & my, az = ahead >> shz;
+                prefetch_rows_at<Q, ST, MODE>(p, abx, (int)ay, (int)az, (int)threadIdx.x, (int)blockDim.x);
                 if (THERMAL && ST != ST_FP64 && p.th_src)
-                    prefetch_block_thermal_rows<Q>(p, ahead, (int)threadIdx.x, (int)blockDim.x, gx, ny);
+                    prefetch_thermal_rows_at<Q>(p, abx, ay + ny * az, (int)threadIdx.x, (int)blockDim.x);
             }
         }
-        const uint32_t mb = e;
-        const uint32_t yz = mb / gx;
-        const int x = (int)((mb - yz * gx) * blockDim.x + threadIdx.x);
-        const int y = (int)(yz % ny), z = (int)(yz / ny);
+        const int x = (int)((e & mx) * blockDim.x + threadIdx.x);
+        const int y = (int)((e >> shy) & my), z = (int)(e >> shz);
+        const uint32_t yz = (uint32_t)y + ny * (uint32_t)z;
         if (x >= p.nx) return;
         using T = typename Codec<ST>::T;
         auto load = [&](int i, auto&& ptr_of) -> T { return *ptr_of(i); };

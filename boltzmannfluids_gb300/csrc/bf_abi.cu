@@ -781,9 +781,11 @@ int bf_create(bf_solver** out) {
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
     s->pf_blocks = (uint32_t)std::max(sms, 1) * 4u;
-    // the boundary-aware step: half a wave (flow past a sphere 256x128x128:
-    // 0.5 / 1 / 1.5 / 2 waves measured 35.1k / 34.8k / 34.3k / 33.6k MLUPs)
-    s->pf_blocks_masked = (uint32_t)std::max(sms, 1) * 2u;
+    // the boundary-aware step: one wave of schedule entries, issued once the
+    // first warp's own loads are in flight (flow past a sphere 256x128x128:
+    // 0.5 / 0.75 / 1 / 1.5 waves measured 34.9k / 37.9k / 38.7k / 38.3k MLUPs,
+    // Rayleigh-Benard 256x256x130 26.3k / 27.2k / 27.3k / 26.9k)
+    s->pf_blocks_masked = (uint32_t)std::max(sms, 1) * 4u;
     if (const char* env = std::getenv("BF_PREFETCH_BLOCKS"))
         s->pf_blocks = s->pf_blocks_masked = (uint32_t)std::strtoul(env, nullptr, 10);
     // BF_TWO_CELL=0 keeps the 16-bit fast step at one cell per thread (A/B comparisons)

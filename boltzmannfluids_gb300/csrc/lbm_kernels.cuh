@@ -659,6 +659,10 @@ __device__ __forceinline__ void collide_fixed(const R (&f)[Q], const MomentsT<R>
     }
 }
 
+struct NoHook {
+    __device__ __forceinline__ void operator()() const {}
+};
+
 // L2 prefetch of a byte range with the bulk-copy engine (no registers held,
 // no completion to wait for).  The range must be 16-byte aligned and sized.
 __device__ __forceinline__ void l2_prefetch_bulk(const void* ptr, uint32_t bytes) {
@@ -1053,9 +1057,9 @@ __device__ __forceinline__ void thermal_collide_push(const StepParams& p, uint32
 // periodic addresses stay inside the lattice), so that the mask costs no
 // round trip of its own; returns whether the cell was updated.
 template <int Q, int ST, int MODE, bool TRT, bool FORCED, bool MP, bool EDGE, bool THERMAL = false,
-          bool GUARD = false, class Load>
+          bool GUARD = false, class Load, class AfterLoads = NoHook>
 __device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepParams& p, int x, int y, int z,
-                                                                     Load&& load) {
+                                                                     Load&& load, AfterLoads after_loads = {}) {
     using L = Lattice<Q>;
     using C = Codec<ST>;
     using T = typename C::T;
@@ -1133,6 +1137,8 @@ __device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepP
 #pragma unroll
         for (int i = 0; i < QT; i++) th[i] = __ldg(p.th_src + (uint64_t)i * p.stride + n);
     }
+    // work the caller issues while the loads are in flight
+    after_loads();
     if (GUARD && guard_mask != 0u) return cs;
     // the update runs on the stored values times 1/SCALE implied: G = g * SCALE
     constexpr int SCE = C::SCALE_EXP;
@@ -1645,18 +1651,20 @@ __global__ void __launch_bounds__(kStepBlock, BF_MIXED_MIN_BLOCKS) masked_mixed_
     // a plain entry: bx | y << sched_shy | z << sched_shz
     const uint32_t shy = p.sched_shy, shz = p.sched_shz;
     const uint32_t mx = (1u << shy) - 1u, my = (1u << (shz - shy)) - 1u;
+    // the entry pf_blocks ahead, loaded beside this block's own entry
+    const bool has_ahead = p.pf_blocks != 0u && threadIdx.x < 32 && blockIdx.x + p.pf_blocks < p.n_sched;
+    const uint32_t ahead = has_ahead ? __ldg(p.sched + blockIdx.x + p.pf_blocks) : 0x80000000u;
     if (!(e >> 31)) {
-        // the first warp prefetches the rows of the plain block pf_blocks
-        // entries ahead in the schedule (one plane per lane)
-        if (p.pf_blocks != 0u && threadIdx.x < 32 && blockIdx.x + p.pf_blocks < p.n_sched) {
-            const uint32_t ahead = __ldg(p.sched + blockIdx.x + p.pf_blocks);
+        // the first warp prefetches the rows of that plain block (one plane
+        // per lane) once its own cell's loads are in flight
+        auto prefetch_ahead = [&]() {
             if (!(ahead >> 31)) {
                 const uint32_t abx = ahead & mx, ay = (ahead >> shy) & my, az = ahead >> shz;
                 prefetch_rows_at<Q, ST, MODE>(p, abx, (int)ay, (int)az, (int)threadIdx.x, (int)blockDim.x);
                 if (THERMAL && ST != ST_FP64 && p.th_src)
                     prefetch_thermal_rows_at<Q>(p, abx, ay + ny * az, (int)threadIdx.x, (int)blockDim.x);
             }
-        }
+        };
         const int x = (int)((e & mx) * blockDim.x + threadIdx.x);
         const int y = (int)((e >> shy) & my), z = (int)(e >> shz);
         const uint32_t yz = (uint32_t)y + ny * (uint32_t)z;
@@ -1664,8 +1672,8 @@ __global__ void __launch_bounds__(kStepBlock, BF_MIXED_MIN_BLOCKS) masked_mixed_
         using T = typename Codec<ST>::T;
         auto load = [&](int i, auto&& ptr_of) -> T { return *ptr_of(i); };
         const bool edge = MODE == AA_EVEN && (y == 0 || y == p.ny - 1 || (Lattice<Q>::D == 3 && (z == 0 || z == p.nz - 1)));
-        if (edge) fast_cell<Q, ST, MODE, TRT, FORCED, false, true, THERMAL, true>(p, x, y, z, load);
-        else fast_cell<Q, ST, MODE, TRT, FORCED, false, false, THERMAL, true>(p, x, y, z, load);
+        if (edge) fast_cell<Q, ST, MODE, TRT, FORCED, false, true, THERMAL, true>(p, x, y, z, load, prefetch_ahead);
+        else fast_cell<Q, ST, MODE, TRT, FORCED, false, false, THERMAL, true>(p, x, y, z, load, prefetch_ahead);
         if ((p.flags & F_SAVE) && p.bnd_tex) {
             const uint32_t n = (uint32_t)x + nx * yz;
             if (__ldg(p.nmask + n) == 0u) p.bnd_tex[n] = 0;

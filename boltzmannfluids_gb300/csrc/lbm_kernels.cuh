@@ -1207,10 +1207,19 @@ template <int Q, int ST, int MODE, bool TRT, bool FORCED, bool MP>
 __global__ void __launch_bounds__(kStepBlock,
                                   ST == ST_FP64 ? 2 : ((ST == ST_FP32 || Q == 27) ? kFastMinBlocks : kFastMinBlocks16))
     fast_step_kernel(const __grid_constant__ StepParams p) {
-    if (p.pf_blocks != 0u && threadIdx.x < 32) {
-        const uint32_t b = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z) + p.pf_blocks;
-        if (b < gridDim.x * gridDim.y * gridDim.z) prefetch_block_rows<Q, ST, MODE>(p, b, (int)threadIdx.x, (int)blockDim.x);
-    }
+    // the first warp prefetches the rows of the block pf_blocks ahead: once
+    // its own cell's loads are in flight, or (Shan-Chen flow, whose psi
+    // stencil loads come after) before them -- each measured the faster
+    auto prefetch = [&]() {
+        if (p.pf_blocks != 0u && threadIdx.x < 32) {
+            const uint32_t b = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z) + p.pf_blocks;
+            if (b < gridDim.x * gridDim.y * gridDim.z) prefetch_block_rows<Q, ST, MODE>(p, b, (int)threadIdx.x, (int)blockDim.x);
+        }
+    };
+    if constexpr (MP) prefetch();
+    auto prefetch_ahead = [&]() {
+        if constexpr (!MP) prefetch();
+    };
     using R = typename Codec<ST>::R;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y, z = blockIdx.z;
@@ -1221,8 +1230,8 @@ __global__ void __launch_bounds__(kStepBlock,
                           (y == 0 || y == p.ny - 1 || (Lattice<Q>::D == 3 && (z == 0 || z == p.nz - 1)));
         using T = typename Codec<ST>::T;
         auto load = [&](int i, auto&& ptr_of) -> T { return *ptr_of(i); };
-        if (edge) cs = fast_cell<Q, ST, MODE, TRT, FORCED, MP, true>(p, x, y, z, load);
-        else cs = fast_cell<Q, ST, MODE, TRT, FORCED, MP, false>(p, x, y, z, load);
+        if (edge) cs = fast_cell<Q, ST, MODE, TRT, FORCED, MP, true, false, false>(p, x, y, z, load, prefetch_ahead);
+        else cs = fast_cell<Q, ST, MODE, TRT, FORCED, MP, false, false, false>(p, x, y, z, load, prefetch_ahead);
     }
     if (p.flags & F_REDUCE) block_reduce_store(cs, p.red_partials);
 }
@@ -1235,9 +1244,9 @@ __global__ void __launch_bounds__(kStepBlock,
 // two 16-bit values through one address.  The arithmetic of each cell is the
 // one-cell kernel's (fast_cell), so results agree bit for bit.
 // ---------------------------------------------------------------------------
-template <int Q, int ST, int MODE, bool TRT, bool FORCED, bool MP, bool EDGE>
+template <int Q, int ST, int MODE, bool TRT, bool FORCED, bool MP, bool EDGE, class AfterLoads = NoHook>
 __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, int z, const float* tile = nullptr,
-                                            int pitch = 0, int lx = 0) {
+                                            int pitch = 0, int lx = 0, AfterLoads after_loads = {}) {
     using L = Lattice<Q>;
     using C = Codec<ST>;
     using T = typename C::T;
@@ -1288,10 +1297,14 @@ __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, i
     // the populations are in flight, and both cells' stencil sums, so that
     // six sums stay live through the first cell's update instead of the stencil
     ScSum sc_pair[2];
+    float pv[kPsiRows<Q>][4];
+    if constexpr (MP) {
+        if (!tile) psi_pair_load<Q>(p.psi_src, n, x, nx, oym, oyp, ozm, ozp, pv);
+    }
+    // work the caller issues while the loads are in flight
+    after_loads();
     if constexpr (MP) {
         if (!tile) {
-            float pv[kPsiRows<Q>][4];
-            psi_pair_load<Q>(p.psi_src, n, x, nx, oym, oyp, ozm, ozp, pv);
             sc_pair[0] = sc_sums<Q, C::SHIFTED>([&](const Dir c) { return pv[psi_row<Q>(c)][c.x + 1]; });
             sc_pair[1] = sc_sums<Q, C::SHIFTED>([&](const Dir c) { return pv[psi_row<Q>(c)][c.x + 2]; });
         }
@@ -1393,10 +1406,20 @@ __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, i
 template <int Q, int ST, int MODE, bool TRT, bool FORCED, bool MP>
 __global__ void __launch_bounds__(kStepBlock, MP ? BF_FAST2_MP_MIN_BLOCKS : BF_FAST2_MIN_BLOCKS)
     fast2_step_kernel(const __grid_constant__ StepParams p) {
-    if (p.pf_blocks != 0u && threadIdx.x < 32) {
-        const uint32_t b = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z) + p.pf_blocks;
-        if (b < gridDim.x * gridDim.y * gridDim.z) prefetch_block_rows<Q, ST, MODE>(p, b, (int)threadIdx.x, 2 * (int)blockDim.x);
-    }
+    // the first warp prefetches the rows of the block pf_blocks ahead: once
+    // its own cells' loads are in flight, or (Shan-Chen flow) before them --
+    // each measured the faster
+    auto prefetch = [&]() {
+        if (p.pf_blocks != 0u && threadIdx.x < 32) {
+            const uint32_t b = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z) + p.pf_blocks;
+            if (b < gridDim.x * gridDim.y * gridDim.z)
+                prefetch_block_rows<Q, ST, MODE>(p, b, (int)threadIdx.x, 2 * (int)blockDim.x);
+        }
+    };
+    if constexpr (MP) prefetch();
+    auto prefetch_ahead = [&]() {
+        if constexpr (!MP) prefetch();
+    };
     const int x = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
     const int y = blockIdx.y, z = blockIdx.z;
     const float* tile = nullptr;
@@ -1432,8 +1455,8 @@ __global__ void __launch_bounds__(kStepBlock, MP ? BF_FAST2_MP_MIN_BLOCKS : BF_F
     if (x >= p.nx) return;
     const int lx = x - 2 * (int)(blockIdx.x * blockDim.x);
     const bool edge = MODE == AA_EVEN && (y == 0 || y == p.ny - 1 || (Lattice<Q>::D == 3 && (z == 0 || z == p.nz - 1)));
-    if (edge) fast2_cells<Q, ST, MODE, TRT, FORCED, MP, true>(p, x, y, z, tile, kPitch, lx);
-    else fast2_cells<Q, ST, MODE, TRT, FORCED, MP, false>(p, x, y, z, tile, kPitch, lx);
+    if (edge) fast2_cells<Q, ST, MODE, TRT, FORCED, MP, true>(p, x, y, z, tile, kPitch, lx, prefetch_ahead);
+    else fast2_cells<Q, ST, MODE, TRT, FORCED, MP, false>(p, x, y, z, tile, kPitch, lx, prefetch_ahead);
 }
 
 // ---------------------------------------------------------------------------

@@ -438,7 +438,11 @@ def run_fp64_error_leg(bf, cavity_steps=10000, sphere_res=(128, 64, 64), sphere_
         f = fields[name][fluid]
         out["cavity"][name] = {"u_err_max_over_umax": float(np.abs(f[:, :3] - ref[:, :3]).max() / scale),
                                "rho_err_max": float(np.abs(f[:, 3] - ref[:, 3]).max())}
-    rho, u, ids3, objs = sphere_channel(sphere_res, radius=8.0, center=(32.0, 32.0, 32.0))
+    # r = ny/8 centred at (ny/2, ny/2, nz/2): r 8 at (32, 32, 32) in 128x64x64, r 16 at (64, 64, 64)
+    # in the configuration's 256x128x128
+    r_s = sphere_res[1] / 8.0
+    rho, u, ids3, objs = sphere_channel(sphere_res, radius=r_s, center=(sphere_res[1] / 2.0, sphere_res[1] / 2.0,
+                                                                       sphere_res[2] / 2.0))
     fields = {}
     for name in ("fp64", "fp32", "fp16s", "fp16c"):
         s = bf.LBM()
@@ -456,7 +460,7 @@ def run_fp64_error_leg(bf, cavity_steps=10000, sphere_res=(128, 64, 64), sphere_
     fluid = ids3 == 0
     ref = fields["fp64"][fluid]
     scale = np.abs(ref[:, :3]).max()
-    out["sphere"] = {"workload": f"D3Q19 TRT flow past a sphere r8, {sphere_res[0]}x{sphere_res[1]}x{sphere_res[2]}, "
+    out["sphere"] = {"workload": f"D3Q19 TRT flow past a sphere r{r_s:g}, {sphere_res[0]}x{sphere_res[1]}x{sphere_res[2]}, "
                                  f"inlet 0.05, {sphere_steps} steps"}
     for name in ("fp32", "fp16s", "fp16c"):
         f = fields[name][fluid]
@@ -631,7 +635,8 @@ def run_gpu(args):
         multi = run_multiphysics_leg(bf)
     fp64err = None
     if not args.no_fp64_errors:
-        fp64err = run_fp64_error_leg(bf)
+        fp64err = (run_fp64_error_leg(bf, sphere_res=(256, 128, 128), sphere_steps=5000) if args.fp64_sphere_full
+                   else run_fp64_error_leg(bf))
     sphere = None
     if not args.no_sphere:
         sphere = run_sphere_leg(bf, args.sphere_steps)
@@ -695,6 +700,8 @@ def main():
     ap.add_argument("--precision-steps", type=int, default=2000)
     ap.add_argument("--no-multiphysics", action="store_true", help="skip the Shan-Chen / Rayleigh-Benard leg")
     ap.add_argument("--no-fp64-errors", action="store_true", help="skip the cavity / sphere errors against FP64")
+    ap.add_argument("--fp64-sphere-full", action="store_true",
+                    help="the sphere's FP64 comparison at the configuration's own size (256x128x128, r 16, 5000 steps)")
     ap.add_argument("--multiphysics-throughput-steps", type=int, default=0,
                     help="instead of the multiphysics leg, only its full-size throughput part with this many timed steps")
     ap.add_argument("--no-sphere", action="store_true", help="skip the flow-past-a-sphere leg")

@@ -247,15 +247,6 @@ __device__ __forceinline__ R pair_sum(const R (&f)[Q], int i) { return FADD(f[i]
 template <int Q, class R>
 __device__ __forceinline__ R pair_diff(const R (&f)[Q], int i) { return FSUB(f[i], f[i + 1]); }
 
-// shifted storage: rho = 1 + (g_0 + s_1 + s_2 + ...) (pairwise order), the
-// populations held times 2^SCE: rho = fma(sum, 2^-SCE, 1)
-template <int Q, int SCE, class R>
-__device__ __forceinline__ R density_shifted(const R (&f)[Q]) {
-    R rho = f[0];
-#pragma unroll
-    for (int i = 1; i < Q; i += 2) rho = FADD(rho, pair_sum<Q>(f, i));
-    return SCE ? FFMA(rho, R(1.0 / (double)(1 << SCE)), R(1)) : FADD(R(1), rho);
-}
 // compute_density (collide.comp:383-388): the populations in order
 template <int Q, class R>
 __device__ __forceinline__ R density_lit(const R (&f)[Q]) {
@@ -264,14 +255,12 @@ __device__ __forceinline__ R density_lit(const R (&f)[Q]) {
     for (int i = 1; i < Q; i++) rho = FADD(rho, f[i]);
     return rho;
 }
-template <int Q, bool SH, int SCE, class R>
-__device__ __forceinline__ R density_of(const R (&f)[Q]) {
-    if constexpr (SH) return density_shifted<Q, SCE>(f);
-    else return density_lit<Q>(f);
-}
-// m.rho (and, shifted, m.drho = the population sum itself, times 2^-SCE)
-// clamped to max(rho, 0.01) with NaN kept; a clamped shifted cell takes
-// drho = 0.01 - 1.  Flags NaN densities in *err.
+// m.rho: unshifted storage compute_density as written; shifted storage
+// rho = 1 + (g_0 + s_1 + s_2 + ...) in pairwise order (s_k the opposite
+// pairs' sums), the populations held times 2^SCE: rho = fma(sum, 2^-SCE, 1);
+// m.drho = the population sum itself, times 2^-SCE.  rho is clamped to
+// max(rho, 0.01) with NaN kept; a clamped shifted cell takes drho = 0.01 - 1.
+// Flags NaN densities in *err.
 template <int Q, bool SH, int SCE, class R>
 __device__ __forceinline__ void density_into(const R (&f)[Q], MomentsT<R>& m, uint32_t* err) {
     if constexpr (SH) {
@@ -920,14 +909,6 @@ __device__ __forceinline__ float thermal_buoyancy_of(const float (&th)[Lattice<Q
     const float k = FMUL(-beta, FSUB(temperature, 1.0f));
     m.Fx = FADD(m.Fx, FMUL(k, m.Fx)); m.Fy = FADD(m.Fy, FMUL(k, m.Fy)); m.Fz = FADD(m.Fz, FMUL(k, m.Fz));
     return temperature;
-}
-template <int Q>
-__device__ __forceinline__ float thermal_buoyancy(const StepParams& p, uint32_t n, Moments& m) {
-    constexpr int QT = Lattice<Q>::D == 2 ? 5 : 7;
-    float th[QT];
-#pragma unroll
-    for (int i = 0; i < QT; i++) th[i] = __ldg(p.th_src + (uint64_t)i * p.stride + n);
-    return thermal_buoyancy_of<Q>(th, p.beta, m);
 }
 
 // thermal BGK towards g_eq(T, u) as written (collide.comp:771-782, :634-651,

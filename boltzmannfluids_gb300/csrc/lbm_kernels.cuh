@@ -911,6 +911,16 @@ __device__ __forceinline__ float thermal_buoyancy_of(const float (&th)[Lattice<Q
     return temperature;
 }
 
+// the same with the cell's thermal populations loaded here (special cells)
+template <int Q>
+__device__ __forceinline__ float thermal_buoyancy(const StepParams& p, uint32_t n, Moments& m) {
+    constexpr int QT = Lattice<Q>::D == 2 ? 5 : 7;
+    float th[QT];
+#pragma unroll
+    for (int i = 0; i < QT; i++) th[i] = __ldg(p.th_src + (uint64_t)i * p.stride + n);
+    return thermal_buoyancy_of<Q>(th, p.beta, m);
+}
+
 // thermal BGK towards g_eq(T, u) as written (collide.comp:771-782, :634-651,
 // :668-670): g + (-(g - g_eq)/tau_T)
 __device__ __forceinline__ float thermal_relax(const StepParams& p, float g, float geq) {

@@ -1652,14 +1652,20 @@ __global__ void __launch_bounds__(kStepBlock, Q == 27 ? 3 : kFastMinBlocks)
 // updated right after their neighbours streamed the same 32-byte sectors
 // through L2, in short blocks of their own, however dense they lie (a wall
 // plane is a run of special blocks).
-// 4 blocks per SM (64 registers; some even-step variants spill 12-56 bytes):
+// 4 blocks per SM (64 registers; some even-step variants spill 12-64 bytes):
 // 3 blocks without spills measured 31.4k against 35.1k MLUPs on flow past a
-// sphere, 18.6k against 20.8k on Rayleigh-Benard
+// sphere, 18.6k against 20.8k on Rayleigh-Benard.  Thermal flow: 5 blocks
+// (48 registers; the spills cost less than the latency they hide: 27.2k ->
+// 28.9k on Rayleigh-Benard; flow past a sphere at 5: 38.6k -> 37.8k)
 #ifndef BF_MIXED_MIN_BLOCKS
 #define BF_MIXED_MIN_BLOCKS kFastMinBlocks
 #endif
+#ifndef BF_MIXED_MIN_BLOCKS_THERMAL
+#define BF_MIXED_MIN_BLOCKS_THERMAL 5
+#endif
 template <int Q, int ST, int MODE, bool TRT, bool FORCED, bool THERMAL>
-__global__ void __launch_bounds__(kStepBlock, BF_MIXED_MIN_BLOCKS) masked_mixed_kernel(const __grid_constant__ StepParams p) {
+__global__ void __launch_bounds__(kStepBlock, THERMAL ? BF_MIXED_MIN_BLOCKS_THERMAL : BF_MIXED_MIN_BLOCKS)
+    masked_mixed_kernel(const __grid_constant__ StepParams p) {
     const uint32_t nx = (uint32_t)p.nx, ny = (uint32_t)p.ny;
     const uint32_t e = __ldg(p.sched + blockIdx.x);
     // a plain entry: bx | y << sched_shy | z << sched_shz

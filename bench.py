@@ -388,14 +388,16 @@ def run_multiphysics_leg(bf, sc_res=(256, 256, 256), sc_steps=20000, rb_res=(256
           **rb_run(rb_res, rb_steps, 0.02, bf.FloatingPointAccuracy.fp32, rb_steps // 5, rb_steps // 100)}
     ref = {}
     for name in ("fp64", "fp32", "fp16s", "fp16c"):
+        # the second half of the run: past the onset transient (~10,000 steps at this size) the
+        # convection is statistically steady, and 100 samples average its 6-9 % fluctuation
         ref[name] = rb_run(ref_rb_res, ref_rb_steps, 0.008, getattr(bf.FloatingPointAccuracy, name),
-                           ref_rb_steps // 5, ref_rb_steps // 200)
+                           ref_rb_steps // 2, ref_rb_steps // 200)
     ref["nusselt_rel_err_fp32"] = abs(ref["fp32"]["nusselt"] - ref["fp64"]["nusselt"]) / ref["fp64"]["nusselt"]
     for name in ("fp32", "fp16s", "fp16c"):
         ref[f"nusselt_mean_rel_err_{name}"] = (abs(ref[name]["nusselt_mean"] - ref["fp64"]["nusselt_mean"]) /
                                                ref["fp64"]["nusselt_mean"])
     rb["vs_fp64"] = {"workload": f"{ref_rb_res[0]}x{ref_rb_res[1]}x{ref_rb_res[2]} x {ref_rb_steps} steps, "
-                                 f"Nusselt mean over the last {ref_rb_steps // 5} steps, every {ref_rb_steps // 200}",
+                                 f"Nusselt mean over the last {ref_rb_steps // 2} steps, every {ref_rb_steps // 200}",
                      **ref}
     out["rayleigh_benard"] = rb
     out["throughput_full_size"] = multiphysics_throughput(bf)

@@ -119,6 +119,7 @@ struct bf_solver {
     DeviceBuf vel_den, force_temp, bnd_tex, partials, red_out, err, decode_tmp;
     DeviceBuf nmask;  // per-cell masks of the boundary-aware fast step
     DeviceBuf special;        // the cells with a nonzero mask, in index order
+    DeviceBuf special_mask;   // their masks, in the same order
     DeviceBuf sched;          // launch schedule of the boundary-aware step (StepParams::sched)
     uint32_t n_special = 0, n_sched = 0, special_chunk = 0;
     uint32_t sched_shy = 0, sched_shz = 0;  // bit positions of y and z in a plain schedule entry
@@ -184,9 +185,12 @@ __global__ void special_flags_kernel(const uint32_t* __restrict__ mask, uint64_t
 }
 
 __global__ void special_scatter_kernel(const uint32_t* __restrict__ mask, const uint32_t* __restrict__ offset,
-                                       uint64_t n, uint32_t* __restrict__ list) {
+                                       uint64_t n, uint32_t* __restrict__ list, uint32_t* __restrict__ list_mask) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n && mask[i] != 0u) list[offset[i]] = (uint32_t)i;
+    if (i < n && mask[i] != 0u) {
+        list[offset[i]] = (uint32_t)i;
+        list_mask[offset[i]] = mask[i];
+    }
 }
 
 // first list position of each block of the cell grid (lower bound of the
@@ -210,6 +214,7 @@ __global__ void special_ptr_kernel(const uint32_t* __restrict__ list, uint32_t c
 // and each cell-grid block's range of it
 cudaError_t build_special_list(bf_solver* s, uint64_t n) {
     s->special.release();
+    s->special_mask.release();
     s->sched.release();
     s->n_special = 0;
     s->n_sched = 0;
@@ -228,8 +233,10 @@ cudaError_t build_special_list(bf_solver* s, uint64_t n) {
     const uint32_t count = last[0] + (last[1] != 0u ? 1u : 0u);
     if (e == cudaSuccess && count > 0) {
         e = s->special.alloc((size_t)count * sizeof(uint32_t));
+        if (e == cudaSuccess) e = s->special_mask.alloc((size_t)count * sizeof(uint32_t));
         if (e == cudaSuccess) {
-            special_scatter_kernel<<<blocks, 256, 0, s->stream>>>(mask, scan.levels[0], n, s->special.as<uint32_t>());
+            special_scatter_kernel<<<blocks, 256, 0, s->stream>>>(mask, scan.levels[0], n, s->special.as<uint32_t>(),
+                                                                  s->special_mask.as<uint32_t>());
             e = cudaGetLastError();
         }
         if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
@@ -309,7 +316,7 @@ void release_all(bf_solver* s) {
     DeviceBuf* bufs[] = {&s->lat[0], &s->lat[1], &s->bnd, &s->objs, &s->kinds, &s->force, &s->bvals,
                          &s->th[0], &s->th[1], &s->psi[0], &s->psi[1], &s->vel_den, &s->force_temp,
                          &s->bnd_tex, &s->partials, &s->red_out, &s->err, &s->decode_tmp, &s->nmask,
-                         &s->special, &s->sched};
+                         &s->special, &s->special_mask, &s->sched};
     for (auto* b : bufs) b->release();
     s->n_special = 0;
     s->n_sched = 0;
@@ -524,6 +531,7 @@ cudaError_t collide(bf_solver* s, bool save, bool update, bool reduce, bool meas
     p.nmask = s->nmask.as<uint32_t>();
     if (s->masked_split && s->n_special > 0 && s->n_sched > 0) {
         p.special = s->special.as<uint32_t>();
+        p.special_mask = s->special_mask.as<uint32_t>();
         p.sched = s->sched.as<uint32_t>();
         p.n_special = s->n_special;
         p.n_sched = s->n_sched;
@@ -1075,6 +1083,7 @@ int bf_initialize_fields(bf_solver* s, const bf_init_desc* d, const float* densi
         mp.bnd = s->bnd.as<uint32_t>();
         mp.bits = s->bits;
         mp.obj_kind = s->kinds.as<uint8_t>();
+        mp.objects = s->objs.as<float4>();
         switch (Q) {
         case 9: e = launch_build_mask<9>(mp, s->nmask.as<uint32_t>(), s->stream); break;
         case 15: e = launch_build_mask<15>(mp, s->nmask.as<uint32_t>(), s->stream); break;

@@ -283,6 +283,7 @@ struct alignas(16) StepParams {
     // special[k * special_chunk ..] (special_chunk of them, one per thread).
     // When set, the boundary-aware step runs this way.
     const uint32_t* special;
+    const uint32_t* special_mask;  // the mask of each listed cell
     const uint32_t* sched;
     uint32_t n_special, n_sched, special_chunk;
     // a plain entry of the schedule packs its block as bx | y << sched_shy |

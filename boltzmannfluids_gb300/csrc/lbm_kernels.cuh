@@ -1459,6 +1459,14 @@ __global__ void __launch_bounds__(kStepBlock, MP ? BF_FAST2_MP_MIN_BLOCKS : BF_F
 // addressing, and the arithmetic is the generic kernel's, so results agree
 // bit for bit.
 // ---------------------------------------------------------------------------
+// per-cell mask of the boundary-aware step: bit i (1 <= i < Q) marks a
+// direction whose AA source is outside the domain or solid under bounce-back;
+// bit 31 a solid cell, bit 30 an equilibrium-boundary cell with its object
+// kind in bits 27-28 (1 velocity, 2 density); bit 29, on a cell with a
+// solid source: every solid source's object moves with velocity (+0, +0, +0)
+// (the bounce-back wall term needs no object lookup).  Q - 1 <= 26 direction bits stay below bit 27.
+constexpr int kMaskKindShift = 27;
+constexpr int kMaskRestingBit = 29;
 template <int Q>
 __global__ void build_mask_kernel(const __grid_constant__ StepParams p, uint32_t* __restrict__ mask) {
     using L = Lattice<Q>;
@@ -1470,7 +1478,8 @@ __global__ void build_mask_kernel(const __grid_constant__ StepParams p, uint32_t
     const uint32_t bid = (flags & F_BOUNDARIES) ? boundary_id(p.bnd, p.bits, n) : 0u;
     uint32_t m = 0u;
     if (solid_id(p.obj_kind, bid)) m |= 1u << 31;
-    else if (bid != 0u) m |= 1u << 30;
+    else if (bid != 0u) m |= (1u << 30) | ((uint32_t)__ldg(p.obj_kind + bid) & 3u) << kMaskKindShift;
+    bool resting = true, solid_source = false;  // every solid source's wall velocity is (+0, +0, +0)
 #pragma unroll
     for (int i = 1; i < Q; i++) {
         const Dir c = L::c(i);
@@ -1480,10 +1489,19 @@ __global__ void build_mask_kernel(const __grid_constant__ StepParams p, uint32_t
         bool special = sopen;
         if (!sopen && (flags & F_BOUNCE_BACK) && (flags & F_BOUNDARIES)) {
             const uint32_t sn = (uint32_t)sx + (uint32_t)nx * ((uint32_t)sy + (uint32_t)ny * (uint32_t)sz);
-            special = solid_id(p.obj_kind, boundary_id(p.bnd, p.bits, sn));
+            const uint32_t sid = boundary_id(p.bnd, p.bits, sn);
+            special = solid_id(p.obj_kind, sid);
+            if (special) {
+                solid_source = true;
+                const float4 uw = __ldg(p.objects + 3u * sid);
+                if ((__float_as_uint(uw.x) | __float_as_uint(uw.y) | __float_as_uint(uw.z)) != 0u) resting = false;
+            }
         }
         if (special) m |= 1u << i;
     }
+    // only on a cell the direction bits already make special (a zero mask
+    // means a plain cell)
+    if (solid_source && resting) m |= 1u << kMaskRestingBit;
     mask[n] = m;
 }
 
@@ -1505,7 +1523,7 @@ __device__ __forceinline__ CellSum masked_cell(const StepParams& p, int x, int y
         return cs;
     }
     const bool eqb = (mask >> 30) & 1u;
-    const uint32_t bid = eqb ? boundary_id(p.bnd, p.bits, n) : 0u;
+    const bool resting = (mask >> kMaskRestingBit) & 1u;
     float4 bv = make_float4(1.f, 0.f, 0.f, 0.f);
     if (eqb && p.bvals) bv = __ldg(p.bvals + n);
     T* const base = static_cast<T*>(p.plane[0]);
@@ -1527,7 +1545,7 @@ __device__ __forceinline__ CellSum masked_cell(const StepParams& p, int x, int y
 #pragma unroll
     for (int i = 0; i < Q; i++) {
         const float w = L::w(i);
-        if (i == 0 || !((mask >> i) & 1u)) {
+        if (i == 0 || !((mask >> i) & 1u)) {  // direction bits only (i < 27)
             f[i] = C::dec(base[slot(i, n, oxm, oxp)], w);
             continue;
         }
@@ -1543,8 +1561,8 @@ __device__ __forceinline__ CellSum masked_cell(const StepParams& p, int x, int y
             const float br = bracket(cu, one_mb, p.R2, p.R4h);
             f[i] = C::SHIFTED ? FFMA(FMUL(w, bv.x), br, -w) : FMUL(FMUL(w, bv.x), br);
         } else if (!sopen) {  // solid source under bounce-back (stream.comp:487-496, rho_wall = 1)
-            const uint32_t sid = boundary_id(p.bnd, p.bits, sn);
-            const float4 uw = __ldg(p.objects + 3u * sid);
+            // resting walls: the same expression on the (+0, +0, +0) velocity the object holds
+            const float4 uw = resting ? make_float4(0.f, 0.f, 0.f, 0.f) : __ldg(p.objects + 3u * boundary_id(p.bnd, p.bits, sn));
             const Dir co = L::c(opp(i));
             const float wall = FMUL(FMUL(-2.f * w, co.x * uw.x + co.y * uw.y + co.z * uw.z), 3.f);
             const float v = (MODE == AA_EVEN) ? C::dec(base[(uint32_t)opp(i) * S + n], w)
@@ -1572,8 +1590,8 @@ __device__ __forceinline__ CellSum masked_cell(const StepParams& p, int x, int y
     if constexpr (C::SHIFTED) velocity_and_limit<Q>(f, m, FRC, p.vlim, p.t_lim, p.t_ext);
     else velocity_literal<Q>(f, m, FRC, p.vlim, p.t_lim, p.t_ext);
     if (eqb) {
-        const int kind = __ldg(p.obj_kind + bid);
-        if (kind == 1) { m.ux = bv.y; m.uy = bv.z; m.uz = bv.w; } else { m.rho = bv.x; }
+        const uint32_t kind = (mask >> kMaskKindShift) & 3u;
+        if (kind == 1u) { m.ux = bv.y; m.uy = bv.z; m.uz = bv.w; } else { m.rho = bv.x; }
         m.Fx = m.Fy = m.Fz = 0.f;
     }
     if (flags & F_UPDATE) {
@@ -1600,7 +1618,7 @@ __device__ __forceinline__ CellSum masked_cell(const StepParams& p, int x, int y
     if (flags & F_SAVE) {
         p.vel_den[n] = make_float4(m.ux, m.uy, m.uz, m.rho);
         p.force_temp[n] = make_float4(m.Fx, m.Fy, m.Fz, temperature);
-        if (p.bnd_tex) p.bnd_tex[n] = (uint8_t)bid;
+        if (p.bnd_tex) p.bnd_tex[n] = eqb ? (uint8_t)boundary_id(p.bnd, p.bits, n) : (uint8_t)0;
     }
     if (flags & F_REDUCE) {
         const float uu = uu_of(m.ux, m.uy, m.uz);
@@ -1703,12 +1721,13 @@ __global__ void __launch_bounds__(kStepBlock, THERMAL ? BF_MIXED_MIN_BLOCKS_THER
     if (threadIdx.x < p.special_chunk) {
         const uint32_t k = (e & 0x7fffffffu) * p.special_chunk + threadIdx.x;
         if (k >= p.n_special) return;
-        const uint32_t n = __ldg(p.special + k);
+        // the cell and its mask, listed side by side (one round trip)
+        const uint32_t n = __ldg(p.special + k), cell_mask = __ldg(p.special_mask + k);
         const uint32_t yz = n / nx;
         const int x = (int)(n - yz * nx), y = (int)(yz % ny), z = (int)(yz / ny);
         // the face-row variant computes every neighbour offset with its wrap,
         // which is right for any row
-        masked_cell<Q, ST, MODE, TRT, FORCED, THERMAL, true>(p, x, y, z, __ldg(p.nmask + n));
+        masked_cell<Q, ST, MODE, TRT, FORCED, THERMAL, true>(p, x, y, z, cell_mask);
     }
 }
 

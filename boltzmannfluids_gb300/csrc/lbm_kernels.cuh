@@ -1235,7 +1235,7 @@ __global__ void __launch_bounds__(kStepBlock,
 // two 16-bit values through one address.  The arithmetic of each cell is the
 // one-cell kernel's (fast_cell), so results agree bit for bit.
 // ---------------------------------------------------------------------------
-template <int Q, int ST, int MODE, bool TRT, bool FORCED, bool MP, bool EDGE, class AfterLoads = NoHook>
+template <int Q, int ST, int MODE, bool TRT, bool FORCED, bool MP, bool EDGE, bool TILE, class AfterLoads = NoHook>
 __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, int z, const float* tile = nullptr,
                                             int pitch = 0, int lx = 0, AfterLoads after_loads = {}) {
     using L = Lattice<Q>;
@@ -1289,16 +1289,12 @@ __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, i
     // six sums stay live through the first cell's update instead of the stencil
     ScSum sc_pair[2];
     float pv[kPsiRows<Q>][4];
-    if constexpr (MP) {
-        if (!tile) psi_pair_load<Q>(p.psi_src, n, x, nx, oym, oyp, ozm, ozp, pv);
-    }
+    if constexpr (MP && !TILE) psi_pair_load<Q>(p.psi_src, n, x, nx, oym, oyp, ozm, ozp, pv);
     // work the caller issues while the loads are in flight
     after_loads();
-    if constexpr (MP) {
-        if (!tile) {
-            sc_pair[0] = sc_sums<Q, C::SHIFTED>([&](const Dir c) { return pv[psi_row<Q>(c)][c.x + 1]; });
-            sc_pair[1] = sc_sums<Q, C::SHIFTED>([&](const Dir c) { return pv[psi_row<Q>(c)][c.x + 2]; });
-        }
+    if constexpr (MP && !TILE) {
+        sc_pair[0] = sc_sums<Q, C::SHIFTED>([&](const Dir c) { return pv[psi_row<Q>(c)][c.x + 1]; });
+        sc_pair[1] = sc_sums<Q, C::SHIFTED>([&](const Dir c) { return pv[psi_row<Q>(c)][c.x + 2]; });
     }
     // the stores recompute their addresses from opaque copies of the pointers
     char *c0s = c0, *cms = cm, *cqs = cq;
@@ -1325,6 +1321,7 @@ __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, i
     const Coef<float> k = coef_of(p, 0.0f);
     // the update runs on the stored values: G = g * SCALE for scaled storage
     constexpr int SCE = C::SCALE_EXP;
+    float psi_first = 0.f;  // the first cell's psi, stored with the second's
 #pragma unroll
     for (int half = 0; half < 2; half++) {
         float f[Q];
@@ -1337,7 +1334,7 @@ __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, i
         m.Fz = FORCED ? p.fconst[2] : 0.f;
         float psi_self = 0.f;
         if constexpr (MP) {
-            if (tile) psi_self = sc_force_tile<Q, C::SHIFTED>(p.G, tile, pitch, lx + half, m);
+            if constexpr (TILE) psi_self = sc_force_tile<Q, C::SHIFTED>(p.G, tile, pitch, lx + half, m);
             else psi_self = sc_apply(p.G, m, sc_pair[half]);
         }
         if constexpr (C::SHIFTED) velocity_and_limit<Q, SCE>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
@@ -1375,8 +1372,11 @@ __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, i
         if (m.out_ext) collide_fixed<Q, TRT, FORCED, true, C::SHIFTED, SCE>(f, m, k, emit);
         else collide_fixed<Q, TRT, FORCED, false, C::SHIFTED, SCE>(f, m, k, emit);
         if constexpr (MP) {
-            // psi of this step's density for the next step (collide.comp:763-769)
-            if (!(p.flags & F_MEASURE)) p.psi_tgt[n + half] = psi_self;
+            // psi of this step's density for the next step (collide.comp:763-769):
+            // both cells' values as one aligned float2 (n even)
+            if (half == 0) psi_first = psi_self;
+            else if (!(p.flags & F_MEASURE))
+                *reinterpret_cast<float2*>(p.psi_tgt + n) = make_float2(psi_first, psi_self);
         }
         if (p.flags & F_SAVE) {
             p.vel_den[n + half] = make_float4(m.ux, m.uy, m.uz, m.rho);
@@ -1394,7 +1394,8 @@ __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, i
 #ifndef BF_FAST2_MP_MIN_BLOCKS
 #define BF_FAST2_MP_MIN_BLOCKS BF_FAST2_MIN_BLOCKS
 #endif
-template <int Q, int ST, int MODE, bool TRT, bool FORCED, bool MP>
+// TILE (Shan-Chen only): the psi stencil staged in shared memory (p.psi_tile)
+template <int Q, int ST, int MODE, bool TRT, bool FORCED, bool MP, bool TILE>
 __global__ void __launch_bounds__(kStepBlock, MP ? BF_FAST2_MP_MIN_BLOCKS : BF_FAST2_MIN_BLOCKS)
     fast2_step_kernel(const __grid_constant__ StepParams p) {
     // the first warp prefetches the rows of the block pf_blocks ahead: once
@@ -1424,7 +1425,7 @@ __global__ void __launch_bounds__(kStepBlock, MP ? BF_FAST2_MP_MIN_BLOCKS : BF_F
         // cached-load variant keeps its L1 share)
         constexpr int ROWS = Lattice<Q>::D == 2 ? 3 : 9;
         extern __shared__ float s_psi[];
-        if (p.psi_tile) {
+        if constexpr (TILE) {
             const int nx = p.nx, ny = p.ny, nz = p.nz;
             const int x0 = 2 * (int)(blockIdx.x * blockDim.x);
             const int span = min(2 * (int)blockDim.x, nx - x0) + 2;
@@ -1446,8 +1447,8 @@ __global__ void __launch_bounds__(kStepBlock, MP ? BF_FAST2_MP_MIN_BLOCKS : BF_F
     if (x >= p.nx) return;
     const int lx = x - 2 * (int)(blockIdx.x * blockDim.x);
     const bool edge = MODE == AA_EVEN && (y == 0 || y == p.ny - 1 || (Lattice<Q>::D == 3 && (z == 0 || z == p.nz - 1)));
-    if (edge) fast2_cells<Q, ST, MODE, TRT, FORCED, MP, true>(p, x, y, z, tile, kPitch, lx, prefetch_ahead);
-    else fast2_cells<Q, ST, MODE, TRT, FORCED, MP, false>(p, x, y, z, tile, kPitch, lx, prefetch_ahead);
+    if (edge) fast2_cells<Q, ST, MODE, TRT, FORCED, MP, true, TILE>(p, x, y, z, tile, kPitch, lx, prefetch_ahead);
+    else fast2_cells<Q, ST, MODE, TRT, FORCED, MP, false, TILE>(p, x, y, z, tile, kPitch, lx, prefetch_ahead);
 }
 
 // ---------------------------------------------------------------------------
@@ -2206,14 +2207,17 @@ cudaError_t launch_step_st(const StepParams& p, int mode, int path, cudaStream_t
             // the Shan-Chen variant's psi tile (p.psi_tile): ROWS x (2 x block + 2) floats
             const size_t tile_bytes =
                 (mp && p.psi_tile) ? (size_t)(Lattice<Q>::D == 2 ? 3 : 9) * (2 * kStepBlock + 2) * sizeof(float) : 0;
-#define BF_FAST2(MODE_, TRT_, F_, MP_) fast2_step_kernel<Q, ST, MODE_, TRT_, F_, MP_><<<g2, threads, tile_bytes, st>>>(p)
+#define BF_FAST2(MODE_, TRT_, F_, MP_) fast2_step_kernel<Q, ST, MODE_, TRT_, F_, MP_, false><<<g2, threads, tile_bytes, st>>>(p)
+#define BF_FAST2T(MODE_, TRT_) fast2_step_kernel<Q, ST, MODE_, TRT_, true, true, true><<<g2, threads, tile_bytes, st>>>(p)
 #define BF_FAST2_MODE(MODE_)                                                                                  \
-    if (mp) { if (trt) BF_FAST2(MODE_, true, true, true); else BF_FAST2(MODE_, false, true, true); }          \
+    if (mp && p.psi_tile) { if (trt) BF_FAST2T(MODE_, true); else BF_FAST2T(MODE_, false); }                  \
+    else if (mp) { if (trt) BF_FAST2(MODE_, true, true, true); else BF_FAST2(MODE_, false, true, true); }     \
     else if (trt) { if (forced) BF_FAST2(MODE_, true, true, false); else BF_FAST2(MODE_, true, false, false); } \
     else { if (forced) BF_FAST2(MODE_, false, true, false); else BF_FAST2(MODE_, false, false, false); }
             if (mode == AA_EVEN) { BF_FAST2_MODE(AA_EVEN) }
             else { BF_FAST2_MODE(AA_ODD) }
 #undef BF_FAST2_MODE
+#undef BF_FAST2T
 #undef BF_FAST2
             return cudaGetLastError();
         }

@@ -420,7 +420,9 @@ __device__ __forceinline__ Coef<double> coef_of(const StepParams& p, double) {
 // which is, term by term, g + omega+-(g_eq - g) + P+- w S+- of the update on
 // g = f - w (g_eq = w rho bracket - w) with the omega+ rho - omega+ of the
 // equilibrium taken as omega+ delta.  SCE: weights times 2^SCE (the
-// populations are held times 2^SCE; delta is unscaled).
+// populations are held times 2^SCE; delta is unscaled).  Above the extreme
+// velocity limit the populations become the equilibrium: the same tree with
+// omega+- = 1 and P+- = 0.
 template <int Q, bool TRT, int SCE, class R, class Emit>
 __device__ __forceinline__ void shifted_source_collide(const R (&f)[Q], const MomentsT<R>& m, const Coef<R>& k,
                                                        Emit emit) {
@@ -428,10 +430,11 @@ __device__ __forceinline__ void shifted_source_collide(const R (&f)[Q], const Mo
     struct W {
         __device__ __forceinline__ static constexpr R w(int i) { return LatticeW<Q, R>::w(i) * R(1 << SCE); }
     };
-    const R op = k.Rtau;
-    const R om = TRT ? k.Wm : k.Rtau;
-    const R pp = TRT ? k.Pp : k.P;
-    const R pm = TRT ? k.Pm : k.P;
+    const bool ext = m.out_ext;
+    const R op = ext ? R(1) : k.Rtau;
+    const R om = ext ? R(1) : (TRT ? k.Wm : k.Rtau);
+    const R pp = ext ? R(0) : (TRT ? k.Pp : k.P);
+    const R pm = ext ? R(0) : (TRT ? k.Pm : k.P);
     const R fuR2 = FMUL(FFMA(m.Fz, m.uz, FFMA(m.Fy, m.uy, FMUL(m.Fx, m.ux))), k.R2);
     const R wp = FMUL(op, m.rho), wm = FMUL(om, m.rho);
     const R A = FFMA(op, m.drho, -FFMA(wp, FMUL(uu_of(m.ux, m.uy, m.uz), k.R2h), FMUL(pp, fuR2)));
@@ -466,7 +469,7 @@ __device__ __forceinline__ void collide_emit(const R (&f)[Q], const MomentsT<R>&
     using L = Lattice<Q>;
     using W = LatticeW<Q, R>;
     if constexpr (SH) {
-        if (src && !to_equilibrium && !m.out_ext) {
+        if (src && !to_equilibrium) {
             if (trt) shifted_source_collide<Q, true, 0>(f, m, k, emit);
             else shifted_source_collide<Q, false, 0>(f, m, k, emit);
             return;
@@ -560,7 +563,7 @@ __device__ __forceinline__ void collide_fixed(const R (&f)[Q], const MomentsT<R>
         __device__ __forceinline__ static constexpr R w(int i) { return LatticeW<Q, R>::w(i) * R(1 << SCE); }
     };
     static_assert(SH || SCE == 0, "scaled populations are shifted");
-    if constexpr (SH && SRC && !EXT) {
+    if constexpr (SH && SRC) {  // the extreme case is taken inside, from m.out_ext
         shifted_source_collide<Q, TRT, SCE>(f, m, k, emit);
         return;
     }
@@ -1168,7 +1171,8 @@ __device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepP
                 *ptr_st(opp(i)) = C::raw_enc(v);
             }
         };
-        if (m.out_ext) collide_fixed<Q, TRT, FORCED, true, C::SHIFTED, SCE>(f, m, k, emit);
+        if constexpr (C::SHIFTED && FORCED) shifted_source_collide<Q, TRT, SCE>(f, m, k, emit);
+        else if (m.out_ext) collide_fixed<Q, TRT, FORCED, true, C::SHIFTED, SCE>(f, m, k, emit);
         else collide_fixed<Q, TRT, FORCED, false, C::SHIFTED, SCE>(f, m, k, emit);
     }
     if constexpr (MP && !F64) {
@@ -1369,7 +1373,8 @@ __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, i
                 *reinterpret_cast<unsigned short*>(half ? dst_b(i) : dst_a(i)) = (unsigned short)e;
             }
         };
-        if (m.out_ext) collide_fixed<Q, TRT, FORCED, true, C::SHIFTED, SCE>(f, m, k, emit);
+        if constexpr (C::SHIFTED && FORCED) shifted_source_collide<Q, TRT, SCE>(f, m, k, emit);
+        else if (m.out_ext) collide_fixed<Q, TRT, FORCED, true, C::SHIFTED, SCE>(f, m, k, emit);
         else collide_fixed<Q, TRT, FORCED, false, C::SHIFTED, SCE>(f, m, k, emit);
         if constexpr (MP) {
             // psi of this step's density for the next step (collide.comp:763-769):
@@ -1609,6 +1614,7 @@ __device__ __forceinline__ CellSum masked_cell(const StepParams& p, int x, int y
             base[slot(opp(i), n_st, oxm_st, oxp_st)] = C::enc(v, L::w(i));
         };
         if (eqb) collide_fixed<Q, false, false, true, C::SHIFTED>(f, m, k, emit);  // f_eq of the cell
+        else if constexpr (C::SHIFTED && FRC) shifted_source_collide<Q, TRT, 0>(f, m, k, emit);
         else if (m.out_ext) collide_fixed<Q, TRT, FRC, true, C::SHIFTED>(f, m, k, emit);
         else collide_fixed<Q, TRT, FRC, false, C::SHIFTED>(f, m, k, emit);
     }

@@ -592,7 +592,7 @@ static void collide(orc_t* s, int save, int update) {
         if (update) {
             REAL fn[QMAX];
             const REAL fuR2 = FMA(force.z, vel.z, FMA(force.y, vel.y, force.x * vel.x)) * s->R2;
-            if (sh && s->src_on && !eqb && !out_ext) {
+            if (sh && s->src_on && !eqb) {
                 /* shifted storage with a source term: relaxation and source
                  * folded into one polynomial per opposite pair (extension):
                  *   A = fma(w+, delta, -fma(w+ rho, u.u R2/2, P+ (F.u) R2))
@@ -601,10 +601,12 @@ static void collide(orc_t* s, int save, int update) {
                  *   BGK: g_i <- fma(w, E +- c.U, (1 - w) g_i)
                  *   TRT: g_i <- fma(w, E +- c.U, fma(a, g_i, b g_opp)),
                  *        a = 1 - (w+ + w-)/2, b = (w- - w+)/2
-                 * (w+- the relaxation rates, P+- = 1 - w+-/2; BGK: w- = w+) */
+                 * (w+- the relaxation rates, P+- = 1 - w+-/2; BGK: w- = w+).
+                 * Above the extreme velocity limit: the equilibrium, the same
+                 * tree with w+- = 1 and P+- = 0. */
                 const int trt = s->d.collision == ORC_TRT;
-                const REAL op = s->Rtau, om = trt ? s->Wm : s->Rtau;
-                const REAL pp = trt ? s->Pp : s->P, pm = trt ? s->Pm : s->P;
+                const REAL op = out_ext ? (REAL)1 : s->Rtau, om = out_ext ? (REAL)1 : (trt ? s->Wm : s->Rtau);
+                const REAL pp = out_ext ? (REAL)0 : (trt ? s->Pp : s->P), pm = out_ext ? (REAL)0 : (trt ? s->Pm : s->P);
                 const REAL wp = op * density, wm = om * density;
                 const REAL A = FMA(op, delta, -FMA(wp, uu_of(vel) * s->R2h, pp * fuR2));
                 const REAL wph = wp * (REAL)0.5;

@@ -148,6 +148,24 @@ def test_velocity_limiter_paths():
     step_and_compare(s, o, [1, 2, 10])
 
 
+@pytest.mark.parametrize("storage,collision,q,res,field", [
+    (2, 0, 2, (32, 16, 1), False), (3, 1, 4, (24, 10, 8), False), (2, 1, 4, (24, 10, 8), False),
+    (3, 0, 4, (24, 10, 8), True), (2, 1, 2, (32, 16, 1), True)])
+def test_velocity_limiter_paths_16bit_forced(storage, collision, q, res, field):
+    """The limiter and the extreme-velocity equilibrium of the shifted 16-bit
+    storages with a source term (the folded collision with omega = 1 and no
+    source above the extreme limit): a uniform force (the two-cell kernel)
+    and a force field (the generic kernel)."""
+    n = res[0] * res[1] * res[2]
+    rho, u = seeded_fields(res, seed=3, dims=2 if res[2] == 1 else 3)
+    u[:, 0] = np.linspace(0.0, 0.4, n)
+    force = np.zeros((n, 3), np.float32)
+    force[:, 1] = 1e-5 * (1.0 + (np.arange(n) % 7 if field else 0))
+    s, o = make_pair(res, 0.7, q, density=rho, velocity=u, force=force, storage=storage, collision=collision)
+    step_and_compare(s, o, [1, 2, 10])
+    assert np.array_equal(s.get_populations(), o.lattice().astype(np.float32))
+
+
 def test_trt_collision():
     res = (20, 16, 12)
     rho, u = seeded_fields(res, seed=8)

@@ -133,6 +133,7 @@ struct bf_solver {
     std::map<int, cudaGraphExec_t> graphs;
     bool graphs_enabled = true;
     uint32_t pf_blocks = 0;  // L2 prefetch distance of the fast kernel, in blocks (0 = off)
+    uint32_t pf_blocks32 = 0;  // the same for FP32 storage
     uint32_t pf_blocks_masked = 0;  // the same for the boundary-aware step, in schedule entries
     bool tma_step = false;   // 16-bit fast step with loads staged by bulk copies
     bool psi_tile = false;   // two-cell Shan-Chen step with psi staged in shared memory
@@ -552,7 +553,8 @@ cudaError_t collide(bf_solver* s, bool save, bool update, bool reduce, bool meas
     // the plane only when every plane starts and ends on a 16-byte boundary
     const size_t plane_bytes = (size_t)s->N * storage_bytes(s->desc.storage);
     if ((!generic || p.sched) && plane_bytes % 16 == 0 && reinterpret_cast<uintptr_t>(lat_src(s)) % 16 == 0)
-        p.pf_blocks = generic ? s->pf_blocks_masked : s->pf_blocks;
+        p.pf_blocks = generic ? s->pf_blocks_masked
+                              : (s->desc.storage == BF_STORE_FP32 ? s->pf_blocks32 : s->pf_blocks);
     p.tma = s->tma_step ? 1u : 0u;
     p.two_cell = s->two_cell ? 1u : 0u;
     p.psi_tile = s->psi_tile ? 1u : 0u;
@@ -783,19 +785,23 @@ int bf_create(bf_solver** out) {
     fluid.effective_density = 1.0f;
     s->objects.push_back(fluid);
     bf_init_desc_default(&s->desc);
-    // fast-kernel L2 prefetch distance: one wave of resident blocks (4 blocks
-    // of 256 threads per SM; longer distances measured slower for FP32 at
-    // 512^3); BF_PREFETCH_BLOCKS overrides (0 = off)
+    // fast-kernel L2 prefetch distance, in blocks: 4 per SM for the 16-bit
+    // two-cell step (half a wave of its 128-thread blocks), 2 per SM for FP32
+    // (half a wave of 256-thread blocks; 512^3 D3Q19 TRT with the prefetch
+    // issued after the warp's own loads: 1/2 / 1 / 1.5 / 2 waves 46.0k / 45.7k
+    // / 44.6k / 42.8k MLUPs; fp16s 83.1k / 86.5k / 84.1k / 80.3k at 1/4 / 1/2 /
+    // 3/4 / 1 wave); BF_PREFETCH_BLOCKS overrides (0 = off)
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
     s->pf_blocks = (uint32_t)std::max(sms, 1) * 4u;
+    s->pf_blocks32 = (uint32_t)std::max(sms, 1) * 2u;
     // the boundary-aware step: one wave of schedule entries, issued once the
     // first warp's own loads are in flight (flow past a sphere 256x128x128:
     // 0.5 / 0.75 / 1 / 1.5 waves measured 34.9k / 37.9k / 38.7k / 38.3k MLUPs,
     // Rayleigh-Benard 256x256x130 26.3k / 27.2k / 27.3k / 26.9k)
     s->pf_blocks_masked = (uint32_t)std::max(sms, 1) * 4u;
     if (const char* env = std::getenv("BF_PREFETCH_BLOCKS"))
-        s->pf_blocks = s->pf_blocks_masked = (uint32_t)std::strtoul(env, nullptr, 10);
+        s->pf_blocks = s->pf_blocks32 = s->pf_blocks_masked = (uint32_t)std::strtoul(env, nullptr, 10);
     // BF_TWO_CELL=0 keeps the 16-bit fast step at one cell per thread (A/B comparisons)
     if (const char* env = std::getenv("BF_TWO_CELL")) s->two_cell = std::strtoul(env, nullptr, 10) != 0;
     // BF_MASKED_STEP=0 sends objects and open faces to the generic kernel (A/B comparisons)

@@ -23,6 +23,7 @@
 // so the update is race free in place.
 #pragma once
 #include "lbm_common.cuh"
+#include "lbm_async.cuh"
 
 #include <algorithm>
 #include <type_traits>
@@ -849,17 +850,6 @@ __device__ __forceinline__ float sc_force(const StepParams& p, uint32_t n, int o
         return __ldg(p.psi_src + a);
     });
 }
-// The same force with psi read from a shared-memory tile of the block's
-// rows: row (c_y + 1) * 3 + (c_z + 1) (3D; c_y + 1 in 2D) of `pitch` floats,
-// column lx + 1 + c_x for the cell at tile column lx (one halo cell each side)
-template <int Q, bool GROUPED>
-__device__ __forceinline__ float sc_force_tile(float G, const float* tile, int pitch, int lx, Moments& m) {
-    return sc_force_nb<Q, GROUPED>(G, m, [&](const Dir c) {
-        const int row = Lattice<Q>::D == 2 ? c.y + 1 : (c.y + 1) * 3 + (c.z + 1);
-        return tile[row * pitch + lx + 1 + c.x];
-    });
-}
-
 // psi of a cell pair's stencil (cells x and x + 1, x even, nx even): the
 // row (y + dy, z + dz) of a direction with c = (., dy, dz) at x - 1, x, x + 1
 // and x + 2 (slots 0..3), x and x + 1 as one aligned float2, x - 1 and x + 2
@@ -896,6 +886,24 @@ __device__ __forceinline__ void psi_pair_load(const float* __restrict__ ps, uint
         // element indices wrap in 32 bits before they meet the pointer
         if (xs & 1u) pv[r][0] = __ldg(ps + (rb + (uint32_t)oxm));
         if (xs & 4u) pv[r][3] = __ldg(ps + (rb + (uint32_t)oxq));
+    }
+}
+
+// The same stencil from a shared-memory tile of whole rows: row r (as
+// psi_row) of nx floats at tile + r * nx, the x wrap inside the row.
+template <int Q>
+__device__ __forceinline__ void psi_pair_load_tile(const float* tile, int x, int nx, float (&pv)[kPsiRows<Q>][4]) {
+    const int xm = x == 0 ? nx - 1 : x - 1, xq = x + 2 == nx ? 0 : x + 2;
+#pragma unroll
+    for (int r = 0; r < kPsiRows<Q>; r++) {
+        const uint32_t xs = psi_row_xs<Q>(r);
+        if (xs == 0u) continue;
+        const float* row = tile + r * nx;
+        const float2 mid = *reinterpret_cast<const float2*>(row + x);
+        pv[r][1] = mid.x;
+        pv[r][2] = mid.y;
+        if (xs & 1u) pv[r][0] = row[xm];
+        if (xs & 4u) pv[r][3] = row[xq];
     }
 }
 
@@ -1241,7 +1249,7 @@ __global__ void __launch_bounds__(kStepBlock,
 // ---------------------------------------------------------------------------
 template <int Q, int ST, int MODE, bool TRT, bool FORCED, bool MP, bool EDGE, bool TILE, class AfterLoads = NoHook>
 __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, int z, const float* tile = nullptr,
-                                            int pitch = 0, int lx = 0, AfterLoads after_loads = {}) {
+                                            uint32_t tile_bar = 0u, AfterLoads after_loads = {}) {
     using L = Lattice<Q>;
     using C = Codec<ST>;
     using T = typename C::T;
@@ -1296,7 +1304,14 @@ __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, i
     if constexpr (MP && !TILE) psi_pair_load<Q>(p.psi_src, n, x, nx, oym, oyp, ozm, ozp, pv);
     // work the caller issues while the loads are in flight
     after_loads();
-    if constexpr (MP && !TILE) {
+    if constexpr (MP && TILE) {
+        // the block's psi rows arrive by bulk copy on tile_bar (bounded
+        // wait; past the limit bit 1 of the error word is set and the step's
+        // results are not to be used)
+        if (!mbar_wait_bounded(tile_bar, 0u)) atomicOr(p.err, 2u);
+        psi_pair_load_tile<Q>(tile, x, nx, pv);
+    }
+    if constexpr (MP) {
         sc_pair[0] = sc_sums<Q, C::SHIFTED>([&](const Dir c) { return pv[psi_row<Q>(c)][c.x + 1]; });
         sc_pair[1] = sc_sums<Q, C::SHIFTED>([&](const Dir c) { return pv[psi_row<Q>(c)][c.x + 2]; });
     }
@@ -1338,8 +1353,7 @@ __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, i
         m.Fz = FORCED ? p.fconst[2] : 0.f;
         float psi_self = 0.f;
         if constexpr (MP) {
-            if constexpr (TILE) psi_self = sc_force_tile<Q, C::SHIFTED>(p.G, tile, pitch, lx + half, m);
-            else psi_self = sc_apply(p.G, m, sc_pair[half]);
+            psi_self = sc_apply(p.G, m, sc_pair[half]);
         }
         if constexpr (C::SHIFTED) velocity_and_limit<Q, SCE>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
         else velocity_literal<Q>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
@@ -1420,40 +1434,39 @@ __global__ void __launch_bounds__(kStepBlock, MP ? BF_FAST2_MP_MIN_BLOCKS : BF_F
     const int x = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
     const int y = blockIdx.y, z = blockIdx.z;
     const float* tile = nullptr;
-    constexpr int kPitch = 2 * kStepBlock + 2;
-    if constexpr (MP) {
-        // p.psi_tile: the block stages the psi rows its cells' stencils read
-        // -- (y + dy, z + dz) for dy, dz in {-1, 0, 1} (dz = 0 in 2D) over its
-        // x range plus one halo cell each side, wrapped -- in shared memory
-        // with plain loads, and the force reads them from there
-        // (dynamic shared memory, sized by the launch only when tiling, so the
-        // cached-load variant keeps its L1 share)
-        constexpr int ROWS = Lattice<Q>::D == 2 ? 3 : 9;
-        extern __shared__ float s_psi[];
-        if constexpr (TILE) {
+    uint32_t tile_bar = 0u;
+    if constexpr (MP && TILE) {
+        // the block's row is the whole row (nx <= 2 x block, nx % 4 == 0): the
+        // psi rows (y + dy, z + dz), dy, dz in {-1, 0, 1} (dz = 0 in 2D), come
+        // into shared memory as one bulk copy each, completing on an mbarrier
+        // that the cells wait on after issuing their population loads
+        constexpr int ROWS = kPsiRows<Q>;
+        extern __shared__ __align__(16) float s_psi[];
+        __shared__ __align__(8) uint64_t s_bar;
+        tile_bar = smem_addr(&s_bar);
+        if (threadIdx.x == 0) {
+            mbar_init(tile_bar, 1);
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
             const int nx = p.nx, ny = p.ny, nz = p.nz;
-            const int x0 = 2 * (int)(blockIdx.x * blockDim.x);
-            const int span = min(2 * (int)blockDim.x, nx - x0) + 2;
+            const uint32_t row_bytes = (uint32_t)nx * (uint32_t)sizeof(float);
+            mbar_arrive_expect_tx(tile_bar, (uint32_t)ROWS * row_bytes);
             for (int r = 0; r < ROWS; r++) {
                 const int dy = Lattice<Q>::D == 2 ? r - 1 : r / 3 - 1, dz = Lattice<Q>::D == 2 ? 0 : r % 3 - 1;
                 const int yy = y + dy < 0 ? y + dy + ny : (y + dy >= ny ? y + dy - ny : y + dy);
                 const int zz = z + dz < 0 ? z + dz + nz : (z + dz >= nz ? z + dz - nz : z + dz);
-                const float* row = p.psi_src + (size_t)nx * ((size_t)yy + (size_t)ny * (size_t)zz);
-                for (int t = threadIdx.x; t < span; t += blockDim.x) {
-                    int xx = x0 - 1 + t;
-                    xx = xx < 0 ? xx + nx : (xx >= nx ? xx - nx : xx);
-                    s_psi[r * kPitch + t] = __ldg(row + xx);
-                }
+                bulk_g2s(smem_addr(s_psi + r * nx), p.psi_src + (size_t)nx * ((size_t)yy + (size_t)ny * (size_t)zz),
+                         row_bytes, tile_bar);
             }
-            __syncthreads();
-            tile = s_psi;
         }
+        tile = s_psi;
     }
     if (x >= p.nx) return;
-    const int lx = x - 2 * (int)(blockIdx.x * blockDim.x);
     const bool edge = MODE == AA_EVEN && (y == 0 || y == p.ny - 1 || (Lattice<Q>::D == 3 && (z == 0 || z == p.nz - 1)));
-    if (edge) fast2_cells<Q, ST, MODE, TRT, FORCED, MP, true, TILE>(p, x, y, z, tile, kPitch, lx, prefetch_ahead);
-    else fast2_cells<Q, ST, MODE, TRT, FORCED, MP, false, TILE>(p, x, y, z, tile, kPitch, lx, prefetch_ahead);
+    if (edge) fast2_cells<Q, ST, MODE, TRT, FORCED, MP, true, TILE>(p, x, y, z, tile, tile_bar, prefetch_ahead);
+    else fast2_cells<Q, ST, MODE, TRT, FORCED, MP, false, TILE>(p, x, y, z, tile, tile_bar, prefetch_ahead);
 }
 
 // ---------------------------------------------------------------------------
@@ -2210,13 +2223,15 @@ cudaError_t launch_step_st(const StepParams& p, int mode, int path, cudaStream_t
             // multiphase flow is forced (the pseudopotential) with the source term on
             const bool trt = (p.flags & F_TRT) != 0, mp = (p.flags & F_MULTIPHASE) != 0;
             const bool forced = (p.flags & F_FORCE_CONST) != 0 || mp;
-            // the Shan-Chen variant's psi tile (p.psi_tile): ROWS x (2 x block + 2) floats
-            const size_t tile_bytes =
-                (mp && p.psi_tile) ? (size_t)(Lattice<Q>::D == 2 ? 3 : 9) * (2 * kStepBlock + 2) * sizeof(float) : 0;
+            // the Shan-Chen variant with the psi rows staged by bulk copies
+            // (p.psi_tile): one block per row (nx <= 2 x kStepBlock) and rows
+            // of whole 16-byte units (nx % 4 == 0); ROWS x nx floats
+            const bool tile = mp && p.psi_tile && g2.x == 1u && p.nx % 4 == 0;
+            const size_t tile_bytes = tile ? (size_t)kPsiRows<Q> * (size_t)p.nx * sizeof(float) : 0;
 #define BF_FAST2(MODE_, TRT_, F_, MP_) fast2_step_kernel<Q, ST, MODE_, TRT_, F_, MP_, false><<<g2, threads, tile_bytes, st>>>(p)
 #define BF_FAST2T(MODE_, TRT_) fast2_step_kernel<Q, ST, MODE_, TRT_, true, true, true><<<g2, threads, tile_bytes, st>>>(p)
 #define BF_FAST2_MODE(MODE_)                                                                                  \
-    if (mp && p.psi_tile) { if (trt) BF_FAST2T(MODE_, true); else BF_FAST2T(MODE_, false); }                  \
+    if (tile) { if (trt) BF_FAST2T(MODE_, true); else BF_FAST2T(MODE_, false); }                              \
     else if (mp) { if (trt) BF_FAST2(MODE_, true, true, true); else BF_FAST2(MODE_, false, true, true); }     \
     else if (trt) { if (forced) BF_FAST2(MODE_, true, true, false); else BF_FAST2(MODE_, true, false, false); } \
     else { if (forced) BF_FAST2(MODE_, false, true, false); else BF_FAST2(MODE_, false, false, false); }

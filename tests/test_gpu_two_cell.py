@@ -103,14 +103,17 @@ def test_two_cell_shan_chen_equals_one_cell(monkeypatch, product_lib):
 
 @pytest.mark.parametrize("vs,res,storage", [
     (bf.VelocitySet.D3Q19, (24, 20, 16), bf.FloatingPointAccuracy.fp16s),
+    (bf.VelocitySet.D3Q19, (512, 3, 4), bf.FloatingPointAccuracy.fp16c),   # the widest row one block stages
+    (bf.VelocitySet.D3Q15, (36, 6, 4), bf.FloatingPointAccuracy.fp16s),
+    (bf.VelocitySet.D2Q9, (40, 24, 1), bf.FloatingPointAccuracy.fp16s),
+    # rows the bulk copies cannot stage (several blocks; nx % 4 != 0): the cached-load kernel
     (bf.VelocitySet.D3Q19, (600, 3, 4), bf.FloatingPointAccuracy.fp16c),
     (bf.VelocitySet.D3Q15, (34, 6, 4), bf.FloatingPointAccuracy.fp16s),
-    (bf.VelocitySet.D2Q9, (40, 24, 1), bf.FloatingPointAccuracy.fp16s),
 ])
 def test_two_cell_shan_chen_psi_tile_matches_oracle(vs, res, storage, monkeypatch, product_lib):
-    """The Shan-Chen step with psi staged in a shared-memory tile of the
-    block's rows (BF_PSI_TILE=1; x wrap through the halo, rows of several
-    blocks with a partly filled last one) against the oracle, bit for bit."""
+    """The Shan-Chen step with the psi rows staged in shared memory by bulk
+    copies (BF_PSI_TILE=1; the x wrap inside the staged row) against the
+    oracle, bit for bit, and the fallback where a row cannot be staged."""
     monkeypatch.setenv("BF_PSI_TILE", "1")
     n = res[0] * res[1] * res[2]
     rng = np.random.default_rng(33)

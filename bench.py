@@ -473,21 +473,26 @@ def run_fp64_error_leg(bf, cavity_steps=10000, sphere_res=(128, 64, 64), sphere_
 
 def multiphysics_throughput(bf, steps=300):
     """MLUPs of the multiphysics configuration's step at its own sizes
-    (Shan-Chen 256^3 in each storage -- fp16s also with the psi stencil staged
-    in shared memory -- and Rayleigh-Benard 256x256x130), a few hundred timed
-    steps each after the start-up steps."""
+    (Shan-Chen 256^3 in each storage -- the 16-bit ones also with the psi rows
+    staged in shared memory and with cached stencil loads -- and
+    Rayleigh-Benard 256x256x130), a few hundred timed steps each after the
+    start-up steps."""
     from boltzmannfluids_gb300.workloads import rayleigh_benard, spinodal
     res = (256, 256, 256)
     n = res[0] * res[1] * res[2]
     out = {"steps_timed": steps}
     rho = spinodal(res, 0.69, 0.01, 4)
-    for name, tile in (("fp32", "0"), ("fp16s", "0"), ("fp16c", "0"), ("fp16s", "1"), ("fp16c", "1")):
-        os.environ["BF_PSI_TILE"] = tile
+    # the library's default per storage, then each 16-bit storage with the psi rows staged in
+    # shared memory by bulk copies (psi_tile) and with cached stencil loads (cached)
+    for name, tile in (("fp32", None), ("fp16s", None), ("fp16c", None), ("fp16s", "1"), ("fp16c", "1"),
+                       ("fp16s", "0"), ("fp16c", "0")):
+        if tile is not None:
+            os.environ["BF_PSI_TILE"] = tile
         s = spinodal_solver(bf, res, getattr(bf.FloatingPointAccuracy, name), rho)
-        os.environ.pop("BF_PSI_TILE")
+        os.environ.pop("BF_PSI_TILE", None)
         s.iterate_time(steps=4, save=False)
         ms = s.benchmark_steps(steps)
-        key = f"shan_chen_256^3_{name}" + ("_psi_tile" if tile == "1" else "") + "_mlups"
+        key = f"shan_chen_256^3_{name}" + {None: "", "1": "_psi_tile", "0": "_cached"}[tile] + "_mlups"
         out[key] = round(n * steps / (ms * 1e-3) / 1e6, 1)
         del s
     rres = (256, 256, 130)

@@ -1427,7 +1427,7 @@ __global__ void __launch_bounds__(kStepBlock, MP ? BF_FAST2_MP_MIN_BLOCKS : BF_F
                 prefetch_block_rows<Q, ST, MODE>(p, b, (int)threadIdx.x, 2 * (int)blockDim.x);
         }
     };
-    if constexpr (MP) prefetch();
+    if constexpr (MP && !TILE) prefetch();
     auto prefetch_ahead = [&]() {
         if constexpr (!MP) prefetch();
     };
@@ -1461,6 +1461,8 @@ __global__ void __launch_bounds__(kStepBlock, MP ? BF_FAST2_MP_MIN_BLOCKS : BF_F
                          row_bytes, tile_bar);
             }
         }
+        // the look-ahead prefetch after the block barrier, which it would delay
+        prefetch();
         tile = s_psi;
     }
     if (x >= p.nx) return;

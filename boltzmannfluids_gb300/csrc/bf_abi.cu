@@ -137,10 +137,10 @@ struct bf_solver {
     uint32_t pf_blocks_masked = 0;  // the same for the boundary-aware step, in schedule entries
     bool tma_step = false;   // 16-bit fast step with loads staged by bulk copies
     // two-cell Shan-Chen step with the psi rows staged in shared memory by bulk
-    // copies: -1 the storage's default (fp16c on, fp16s off: 256^3 D3Q19
-    // 59.4k against 58.5k MLUPs for fp16c, 58.1k against 58.8k for fp16s),
-    // 0 off, 1 on (BF_PSI_TILE)
-    int psi_tile = -1;
+    // copies: 0 off (the default: 256^3 D3Q19 with cached stencil loads 61.6k
+    // MLUPs for fp16s and 61.4k for fp16c, staged 60.4k and 61.0k), 1 on
+    // (BF_PSI_TILE)
+    int psi_tile = 0;
     bool masked_step = true; // boundary-aware fast step for objects and open faces
     bool two_cell = true;    // 16-bit fast step with two cells per thread
     bool masked_split = true; // boundary-aware step with the special cells in blocks of their own
@@ -561,7 +561,7 @@ cudaError_t collide(bf_solver* s, bool save, bool update, bool reduce, bool meas
                               : (s->desc.storage == BF_STORE_FP32 ? s->pf_blocks32 : s->pf_blocks);
     p.tma = s->tma_step ? 1u : 0u;
     p.two_cell = s->two_cell ? 1u : 0u;
-    p.psi_tile = (s->psi_tile < 0 ? s->desc.storage == BF_STORE_FP16C : s->psi_tile != 0) ? 1u : 0u;
+    p.psi_tile = s->psi_tile != 0 ? 1u : 0u;
     switch (s->Q) {
     case 9: fill_uoff<9>(p, storage_bytes(s->desc.storage)); break;
     case 15: fill_uoff<15>(p, storage_bytes(s->desc.storage)); break;

@@ -281,6 +281,18 @@ __device__ __forceinline__ void density_into(const R (&f)[Q], MomentsT<R>& m, ui
     }
 }
 
+// 16-bit multiphase storage, mass-conserving rounding: the mass a cell's
+// populations carry after the collision, as stored (times 2^SCE).  The
+// relaxation and the source term conserve the population sum in exact
+// arithmetic, so T = drho 2^SCE, the cell's own sum (a clamped cell keeps the
+// clamped density's, (0.01 - 1) 2^SCE).  Populations 0..Q-2 are stored
+// rounded, population Q-1 as the rounding of T less their stored values, so
+// the stored populations sum to T up to that one rounding.
+template <int SCE, class R>
+__device__ __forceinline__ R collided_sum(const MomentsT<R>& m) {
+    return SCE ? FMUL(m.drho, R(1 << SCE)) : m.drho;
+}
+
 // shifted storage: u = j/rho (+ F/(2 rho)) and the velocity limiter
 // (collide.comp:722-725): j from the pair differences, r = 1/rho once,
 // u = j r, u = fma(F, r/2, u).
@@ -1164,16 +1176,15 @@ __device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepP
     else velocity_literal<Q>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
     if (p.flags & F_UPDATE) {
         const Coef<R> k = coef_of(p, R(0));
-        // 16-bit multiphase flow: mass-conserving rounding -- each population
-        // is stored with the rounding error of the ones emitted before it
-        // (population order) added first, so that the cell's stored
-        // populations sum to its computed ones up to the last rounding
-        R carry = R(0);
+        // 16-bit multiphase flow: mass-conserving rounding (collided_sum);
+        // rest is T less the stored values of the populations emitted so far
+        R rest = R(0);
+        if constexpr (MP && C::SHIFTED) rest = collided_sum<SCE>(m);
         auto emit = [&](int i, R v) {
             if constexpr (MP && C::SHIFTED) {
-                const R vv = FADD(v, carry);
-                const T h = C::raw_enc(vv);
-                carry = FSUB(vv, C::raw_dec(h));
+                if (i == Q - 1) return;  // stored below, from rest
+                const T h = C::raw_enc(v);
+                rest = FSUB(rest, C::raw_dec(h));
                 *ptr_st(opp(i)) = h;
             } else {
                 *ptr_st(opp(i)) = C::raw_enc(v);
@@ -1182,6 +1193,7 @@ __device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepP
         if constexpr (C::SHIFTED && FORCED) shifted_source_collide<Q, TRT, SCE>(f, m, k, emit);
         else if (m.out_ext) collide_fixed<Q, TRT, FORCED, true, C::SHIFTED, SCE>(f, m, k, emit);
         else collide_fixed<Q, TRT, FORCED, false, C::SHIFTED, SCE>(f, m, k, emit);
+        if constexpr (MP && C::SHIFTED) *ptr_st(opp(Q - 1)) = C::raw_enc(rest);
     }
     if constexpr (MP && !F64) {
         // psi of this step's density for the next step (collide.comp:763-769)
@@ -1358,16 +1370,62 @@ __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, i
         if constexpr (C::SHIFTED) velocity_and_limit<Q, SCE>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
         else velocity_literal<Q>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
         // multiphase: the mass-conserving rounding of the one-cell kernel
-        // (each population carries the rounding error of the ones before it)
-        float carry = 0.f;
+        // (collided_sum; rest is T less the stored values emitted so far)
+        float rest = 0.f;
+        if constexpr (MP && C::SHIFTED) rest = collided_sum<SCE>(m);
+        // store of this cell's encoded population i (a paired slot keeps the
+        // first cell's half until the second cell's is known)
+        auto put = [&](int i, uint32_t e) {
+            if (paired(opp(i))) {
+                if (half == 0) keep[i] = e;
+                else *reinterpret_cast<unsigned int*>(dst_a(i)) = keep[i] | (e << 16);
+            } else {
+                *reinterpret_cast<unsigned short*>(half ? dst_b(i) : dst_a(i)) = (unsigned short)e;
+            }
+        };
+        // both populations of the opposite pair (i, i + 1) of this cell, packed
+        // lo | hi << 16 (a paired slot keeps the first cell's word in keep[i])
+        auto put2 = [&](int i, uint32_t w2) {
+            if (paired(opp(i))) {
+                if (half == 0) {
+                    keep[i] = w2;
+                } else {
+                    *reinterpret_cast<unsigned int*>(dst_a(i)) = __byte_perm(keep[i], w2, 0x5410u);
+                    *reinterpret_cast<unsigned int*>(dst_a(i + 1)) = __byte_perm(keep[i], w2, 0x7632u);
+                }
+            } else {
+                *reinterpret_cast<unsigned short*>(half ? dst_b(i) : dst_a(i)) = (unsigned short)w2;
+                *reinterpret_cast<unsigned short*>(half ? dst_b(i + 1) : dst_a(i + 1)) = (unsigned short)(w2 >> 16);
+            }
+        };
+        float pend = 0.f;  // the first population of an opposite pair until the second is emitted
         auto emit = [&](int i, float v) {
-            const int o = opp(i);
             if constexpr (MP && C::SHIFTED) {
-                v = FADD(v, carry);
-                carry = FSUB(v, C::raw_dec(C::raw_enc(v)));
+                // populations 1..Q-1 come as opposite pairs (i, i + 1), i odd:
+                // one cvt.rn.f16x2.f32 rounds both (each as its own conversion
+                // would); population Q-1 is stored after the collision, from rest
+                if (i == 0) {
+                    const T h = C::raw_enc(v);
+                    rest = FSUB(rest, C::raw_dec(h));
+                    put(0, bits16(h));
+                } else if (i & 1) {
+                    pend = v;
+                } else if (i == Q - 1) {
+                    const T h = C::raw_enc(pend);
+                    rest = FSUB(rest, C::raw_dec(h));
+                    put(i - 1, bits16(h));
+                } else {
+                    const __half2 h2 = __floats2half2_rn(pend, v);
+                    rest = FSUB(rest, __low2float(h2));
+                    rest = FSUB(rest, __high2float(h2));
+                    uint32_t w2;
+                    memcpy(&w2, &h2, 4);
+                    put2(i - 1, w2);
+                }
+                return;
             }
             if constexpr (std::is_same<T, __half>::value) {
-                if (paired(o)) {
+                if (paired(opp(i))) {
                     if (half == 0) {
                         keep[i] = __float_as_uint(v);
                     } else {
@@ -1379,17 +1437,12 @@ __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, i
                     return;
                 }
             }
-            const uint32_t e = bits16(C::raw_enc(v));
-            if (paired(o)) {
-                if (half == 0) keep[i] = e;
-                else *reinterpret_cast<unsigned int*>(dst_a(i)) = keep[i] | (e << 16);
-            } else {
-                *reinterpret_cast<unsigned short*>(half ? dst_b(i) : dst_a(i)) = (unsigned short)e;
-            }
+            put(i, bits16(C::raw_enc(v)));
         };
         if constexpr (C::SHIFTED && FORCED) shifted_source_collide<Q, TRT, SCE>(f, m, k, emit);
         else if (m.out_ext) collide_fixed<Q, TRT, FORCED, true, C::SHIFTED, SCE>(f, m, k, emit);
         else collide_fixed<Q, TRT, FORCED, false, C::SHIFTED, SCE>(f, m, k, emit);
+        if constexpr (MP && C::SHIFTED) put(Q - 1, bits16(C::raw_enc(rest)));
         if constexpr (MP) {
             // psi of this step's density for the next step (collide.comp:763-769):
             // both cells' values as one aligned float2 (n even)
@@ -1874,21 +1927,14 @@ __device__ __forceinline__ CellSumT<typename Codec<ST>::R> cell_update(const Ste
 
     // ---- collision + AA store (collide.comp:727-760) ----
     if (flags & F_UPDATE) {
-        // 16-bit multiphase flow: the mass-conserving rounding (each population
-        // carries the rounding error of the ones before it, written or not)
+        // 16-bit multiphase flow: the mass-conserving rounding (collided_sum;
+        // an equilibrium boundary cell's populations sum to rho - 1); rest is
+        // T less the stored values of the populations emitted so far, written or not
         const bool carry_on = C::SHIFTED && (flags & F_MULTIPHASE);
-        R carry = R(0);
-        collide_emit<Q, C::SHIFTED>(f, m, k, (flags & F_TRT) != 0, (flags & F_SOURCE) != 0, eqb, [&](int i, R v) {
+        R rest = R(0);
+        if (carry_on) rest = eqb ? FSUB(m.rho, R(1)) : collided_sum<0>(m);
+        auto store = [&](int i, T h) {
             const Dir c = L::c(i);
-            const R w = W::w(i);
-            T h;
-            if (carry_on) {
-                const R vv = FADD(v, carry);
-                h = C::enc(vv, w);
-                carry = FSUB(vv, C::dec(h, w));
-            } else {
-                h = C::enc(v, w);
-            }
             if (MODE == AA_EVEN) {
                 int dx = x + c.x, dy = y + c.y, dz = z + c.z;
                 bool dopen;
@@ -1898,7 +1944,19 @@ __device__ __forceinline__ CellSumT<typename Codec<ST>::R> cell_update(const Ste
             } else {
                 plane(i)[n] = h;
             }
+        };
+        collide_emit<Q, C::SHIFTED>(f, m, k, (flags & F_TRT) != 0, (flags & F_SOURCE) != 0, eqb, [&](int i, R v) {
+            const R w = W::w(i);
+            if (carry_on) {
+                if (i == Q - 1) return;  // stored after the collision, from rest
+                const T h = C::enc(v, w);
+                rest = FSUB(rest, C::dec(h, w));
+                store(i, h);
+            } else {
+                store(i, C::enc(v, w));
+            }
         });
+        if (carry_on) store(Q - 1, C::enc(rest, W::w(Q - 1)));
     }
 
     if ((flags & F_MULTIPHASE) && !(flags & F_MEASURE)) {  // collide.comp:763-769, psi of the effective density

@@ -697,19 +697,23 @@ static void collide(orc_t* s, int save, int update) {
                 }
             }
             if (sh && s->d.multiphase) {
-                /* 16-bit storage of multiphase flow: mass-conserving rounding.
-                 * Each population is rounded with the rounding error of the
-                 * ones before it (in population order) added first, so the
-                 * stored populations of a cell sum to the computed ones up to
-                 * the last rounding (an error diffusion; Shan-Chen interfaces
-                 * otherwise gain mass at ~1e-5 per step from rounding). */
-                REAL carry = 0;
-                for (int i = 0; i < Q; i++) {
-                    const REAL v = fn[i] + carry;
-                    const REAL h = lat_store(s, v, i);
-                    carry = v - h;
+                /* 16-bit storage of multiphase flow: mass-conserving rounding
+                 * (extension; Shan-Chen interfaces otherwise gain mass at
+                 * ~1e-5 per step from rounding).  The relaxation and the
+                 * source term conserve the population sum in exact
+                 * arithmetic, so the cell's populations carry T = delta, its
+                 * own sum (a clamped cell the clamped density's); an
+                 * equilibrium boundary cell's rho - 1.  Populations
+                 * 0..Q-2 are stored rounded, population Q-1 as the rounding of
+                 * T less their stored values, so the stored populations sum to
+                 * T up to that one rounding. */
+                REAL rest = eqb ? density - (REAL)1 : delta;
+                for (int i = 0; i < Q - 1; i++) {
+                    const REAL h = lat_store(s, fn[i], i);
+                    rest = rest - h;
                     fn[i] = h;
                 }
+                fn[Q - 1] = lat_store(s, rest, Q - 1);
             }
             for (int i = 0; i < Q; i++) {
                 size_t wc; int ws;

@@ -378,32 +378,56 @@ float sqrt_threshold(float lim) {
     return y;
 }
 
-// Whether x / y == fma(fma(-q, y, x), r, q) with q = x * r, r = RN(1/y), for
-// every significand of x (so for every x whose quotient and remainder stay
-// normal): the fast kernels then divide by the launch-uniform y in three
-// operations.  Results are kept per divisor (the knobs change rarely).
-bool division_checked(float y) {
+// Whether x / y == fma(x, r, RN(x l)) with r = RN(1/y), for every
+// significand of x (so for every x whose quotient and x l stay normal), l the
+// low part of the split reciprocal: RN(1/y - r) from the double reciprocal,
+// else the first of its float neighbours up to four steps away (nearer
+// first) for which the sequence passes.  Split reciprocals give the correctly
+// rounded quotient for most divisors (Brisebarre, Muller and Raina, IEEE
+// Trans. Computers 53(8), 2004); the exhaustive check decides for each one.
+// The fast kernels then divide by the launch-uniform y in two operations.
+// Results are kept per divisor (the knobs change rarely).
+bool division_checked(float y, float* lo) {
     static std::mutex mu;
-    static std::map<uint32_t, bool> seen;
+    static std::map<uint32_t, std::pair<bool, float>> seen;
     uint32_t key;
     std::memcpy(&key, &y, 4);
     {
         std::lock_guard<std::mutex> lock(mu);
         auto it = seen.find(key);
-        if (it != seen.end()) return it->second;
+        if (it != seen.end()) {
+            *lo = it->second.second;
+            return it->second.first;
+        }
     }
-    bool ok = std::isfinite(y) && y != 0.0f;
-    const float r = 1.0f / y;
-    for (uint32_t m = 0; ok && m < (1u << 23); m++) {
-        const uint32_t xb = 0x3f800000u | m;
-        float x;
-        std::memcpy(&x, &xb, 4);
-        const float q = x * r;
-        const float e = std::fma(-q, y, x);
-        ok = std::fma(e, r, q) == x / y;
+    bool ok = false;
+    float l_ok = 0.0f;
+    if (std::isfinite(y) && y != 0.0f) {
+        const float r = 1.0f / y;
+        const float l0 = (float)(1.0 / (double)y - (double)r);
+        auto passes = [&](float l) {
+            for (uint32_t m = 0; m < (1u << 23); m++) {
+                const uint32_t xb = 0x3f800000u | m;
+                float x;
+                std::memcpy(&x, &xb, 4);
+                const float t = x * l;
+                if (std::fma(x, r, t) != x / y) return false;
+            }
+            return true;
+        };
+        // l0, then one float up, one down, two up, two down, ...
+        for (int k = 0; k <= 8 && !ok; k++) {
+            float l = l0;
+            for (int j = 0; j < (k + 1) / 2; j++) l = std::nextafter(l, (k & 1) ? INFINITY : -INFINITY);
+            if (passes(l)) {
+                ok = true;
+                l_ok = l;
+            }
+        }
     }
     std::lock_guard<std::mutex> lock(mu);
-    seen[key] = ok;
+    seen[key] = {ok, l_ok};
+    *lo = l_ok;
     return ok;
 }
 
@@ -418,8 +442,8 @@ void fill_constants(bf_solver* s, StepParams& p) {
     p.cs4 = cs4;
     p.tau = tau;
     p.tau_t = s->desc.thermal_relaxation_time;
-    p.div_ok = (division_checked(cs2) ? 1u : 0u) | (division_checked(cs4) ? 2u : 0u) |
-               (division_checked(tau) ? 4u : 0u) | (division_checked(p.tau_t) ? 8u : 0u);
+    p.div_ok = (division_checked(cs2, &p.L2) ? 1u : 0u) | (division_checked(cs4, &p.L4) ? 2u : 0u) |
+               (division_checked(tau, &p.Ltau) ? 4u : 0u) | (division_checked(p.tau_t, &p.Ltau_t) ? 8u : 0u);
     p.R2h = p.R2 * 0.5f;
     p.R4h = p.R4 * 0.5f;
     p.Rtau = 1.0f / tau;
@@ -525,7 +549,7 @@ cudaError_t collide(bf_solver* s, bool save, bool update, bool reduce, bool meas
     // multiphase flow: the boundary-aware fast kernel, with its masks
     const uint32_t masked_excl = F_FORCE_FIELD | F_MULTIPHASE;
     // the fast and boundary-aware kernels divide by the launch's divisors in
-    // three operations, which the host has checked for every divisor
+    // two operations, which the host has checked for every divisor
     // (fill_constants); a divisor that failed the check sends the step to the
     // generic kernel, which divides by it in full
     const bool div_checked = f64 || p.div_ok == 0xFu;

@@ -314,10 +314,11 @@ struct alignas(16) StepParams {
     // shim of pow(cs, 2) / pow(cs, 4)), tau, tau_T
     float cs2, cs4, tau, tau_t;
     // divisors among cs^2 (bit 0), cs^4 (bit 1), tau (bit 2), tau_T (bit 3)
-    // for which the host has checked the three-operation division by the
-    // reciprocal (R2, R4, Rtau, Rtau_t) against IEEE division for every
-    // significand; the fast kernels run only when all four passed
+    // for which the host has checked the two-operation division by the split
+    // reciprocal (R2 + L2, R4 + L4, Rtau + Ltau, Rtau_t + Ltau_t) against IEEE
+    // division for every significand; the fast kernels run only when all four passed
     uint32_t div_ok;
+    float L2, L4, Ltau, Ltau_t;  // low parts of 1/cs2, 1/cs4, 1/tau, 1/tau_T (div_m)
     // launch constants, FP32, computed on the host exactly as the oracle
     // does: cs = float(1/sqrt(3)), cs2 = cs*cs, cs4 = cs2*cs2
     float R2;                 // 1/cs2

@@ -143,30 +143,32 @@ __device__ __forceinline__ R bracket(R cu, R one_m, R R2, R R4h) {
     return FFMA(FMUL(cu, cu), R4h, FFMA(cu, R2, one_m));
 }
 
-// x / y for a launch-uniform divisor y with r = RN(1/y): q = RN(x r), the
-// exact remainder e = fma(-q, y, x), then q + e r with one rounding
-// (Markstein's correction) -- the correctly rounded quotient, three
-// operations.  The host checks the sequence against IEEE division for every
-// significand of x with each launch divisor (StepParams::div_ok); the fast
-// and boundary-aware kernels use it only when every check passed (div_m),
-// the generic kernel per divisor (div_u).  Double: the full division.
-__device__ __forceinline__ float div_m(float x, float y, float r) {
-    const float q = __fmul_rn(x, r);
-    return __fmaf_rn(__fmaf_rn(-q, y, x), r, q);
+// x / y for a launch-uniform divisor y, from the reciprocal split as
+// r = RN(1/y) and a low part l close to 1/y - r: q = fma(x, r, RN(x l)), two
+// operations (Brisebarre, Muller and Raina, "Accelerating correctly rounded
+// floating-point division when the divisor is known in advance", IEEE Trans.
+// Computers 53(8), 2004).  The host takes l = RN(1/y - r), or the nearest
+// float to it for which the sequence passes, and checks the sequence against
+// IEEE division for every significand of x with each launch divisor
+// (StepParams::div_ok); the fast and boundary-aware kernels use it only when
+// every check passed (div_m), the generic kernel per divisor (div_u).
+// Double: the full division.
+__device__ __forceinline__ float div_m(float x, float, float r, float l) {
+    return __fmaf_rn(x, r, __fmul_rn(x, l));
 }
-__device__ __forceinline__ double div_m(double x, double y, double) { return __ddiv_rn(x, y); }
-__device__ __forceinline__ float div_u(float x, float y, float r, bool ok) {
-    return ok ? div_m(x, y, r) : __fdiv_rn(x, y);
+__device__ __forceinline__ double div_m(double x, double y, double, double) { return __ddiv_rn(x, y); }
+__device__ __forceinline__ float div_u(float x, float y, float r, float l, bool ok) {
+    return ok ? div_m(x, y, r, l) : __fdiv_rn(x, y);
 }
-__device__ __forceinline__ double div_u(double x, double y, double, bool) { return __ddiv_rn(x, y); }
+__device__ __forceinline__ double div_u(double x, double y, double, double, bool) { return __ddiv_rn(x, y); }
 template <bool MK, class R>
-__device__ __forceinline__ R div_k(R x, R y, R r, bool ok) {
-    if constexpr (MK) return div_m(x, y, r);
-    else return div_u(x, y, r, ok);
+__device__ __forceinline__ R div_k(R x, R y, R r, R l, bool ok) {
+    if constexpr (MK) return div_m(x, y, r, l);
+    else return div_u(x, y, r, l, ok);
 }
 // the divisors cs^2 and cs^4 of the literal evaluation, their reciprocals
 // and checks
-template <class R> struct Div { R cs2, rcs2, cs4, rcs4; bool ok2, ok4; };
+template <class R> struct Div { R cs2, rcs2, lcs2, cs4, rcs4, lcs4; bool ok2, ok4; };
 
 // GLSL's dot(a, b) as written: a.x*b.x + a.y*b.y + a.z*b.z
 template <class R>
@@ -177,13 +179,13 @@ __device__ __forceinline__ R dot_lit(R ax, R ay, R az, R bx, R by, R bz) {
 // (w p) (((1 + cu/cs2) + cu^2/2/cs4) - uuh), uuh = (u.u/2)/cs2 of the cell
 template <bool MK, class R>
 __device__ __forceinline__ R feq_lit(R wp, R cu, const Div<R>& d, R uuh) {
-    return FMUL(wp, FSUB(FADD(FADD(R(1), div_k<MK>(cu, d.cs2, d.rcs2, d.ok2)),
-                              div_k<MK>(FMUL(FMUL(cu, cu), R(0.5)), d.cs4, d.rcs4, d.ok4)),
+    return FMUL(wp, FSUB(FADD(FADD(R(1), div_k<MK>(cu, d.cs2, d.rcs2, d.lcs2, d.ok2)),
+                              div_k<MK>(FMUL(FMUL(cu, cu), R(0.5)), d.cs4, d.rcs4, d.lcs4, d.ok4)),
                          uuh));
 }
 template <bool MK, class R>
 __device__ __forceinline__ R uuh_of(R ux, R uy, R uz, const Div<R>& d) {
-    return div_k<MK>(FMUL(dot_lit(ux, uy, uz, ux, uy, uz), R(0.5)), d.cs2, d.rcs2, d.ok2);
+    return div_k<MK>(FMUL(dot_lit(ux, uy, uz, ux, uy, uz), R(0.5)), d.cs2, d.rcs2, d.lcs2, d.ok2);
 }
 
 template <int Q>
@@ -406,16 +408,17 @@ template <class R> struct Coef {
     Div<R> d;
     R tau;
     bool ok_tau;
+    R ltau;  // low part of 1/tau (div_m)
 };
 __device__ __forceinline__ Coef<float> coef_of(const StepParams& p, float) {
     return Coef<float>{p.R2, p.R4, p.R2h, p.R4h, p.Rtau, p.P, p.Wm, p.Pp, p.Pm,
-                       Div<float>{p.cs2, p.R2, p.cs4, p.R4, (p.div_ok & 1u) != 0, (p.div_ok & 2u) != 0},
-                       p.tau, (p.div_ok & 4u) != 0};
+                       Div<float>{p.cs2, p.R2, p.L2, p.cs4, p.R4, p.L4, (p.div_ok & 1u) != 0, (p.div_ok & 2u) != 0},
+                       p.tau, (p.div_ok & 4u) != 0, p.Ltau};
 }
 __device__ __forceinline__ Coef<double> coef_of(const StepParams& p, double) {
     return Coef<double>{p.k64.R2, p.k64.R4, p.k64.R2h, p.k64.R4h, p.k64.Rtau, p.k64.P, p.k64.Wm, p.k64.Pp,
-                        p.k64.Pm, Div<double>{p.k64.cs2, p.k64.R2, p.k64.cs4, p.k64.R4, false, false},
-                        p.k64.tau, false};
+                        p.k64.Pm, Div<double>{p.k64.cs2, p.k64.R2, 0.0, p.k64.cs4, p.k64.R4, 0.0, false, false},
+                        p.k64.tau, false, 0.0};
 }
 
 // Shifted storage with a source term (Guo forcing, Shan-Chen, buoyancy): the
@@ -492,18 +495,18 @@ __device__ __forceinline__ void collide_emit(const R (&f)[Q], const MomentsT<R>&
         // collide.comp:727-745 with :589-629 as written: f + (-(f - feq)/tau) + source
         const Div<R>& d = k.d;
         const R uuh = uuh_of<false>(m.ux, m.uy, m.uz, d);
-        const R fuc = src ? div_u(dot_lit(m.Fx, m.Fy, m.Fz, m.ux, m.uy, m.uz), d.cs2, d.rcs2, d.ok2) : R(0);
+        const R fuc = src ? div_u(dot_lit(m.Fx, m.Fy, m.Fz, m.ux, m.uy, m.uz), d.cs2, d.rcs2, d.lcs2, d.ok2) : R(0);
 #pragma unroll
         for (int i = 0; i < Q; i++) {
             const Dir c = L::c(i);
             const R w = W::w(i);
             const R cu = cdot_rt(c, m.ux, m.uy, m.uz);
             const R fe = feq_lit<false>(FMUL(w, m.rho), cu, d, uuh);
-            R v = FSUB(f[i], div_u(FSUB(f[i], fe), k.tau, k.Rtau, k.ok_tau));
+            R v = FSUB(f[i], div_u(FSUB(f[i], fe), k.tau, k.Rtau, k.ltau, k.ok_tau));
             if (src) {
                 const R fc = cdot_rt(c, m.Fx, m.Fy, m.Fz);
-                v = FADD(v, FMUL(FMUL(k.P, w), FADD(div_u(fc, d.cs2, d.rcs2, d.ok2),
-                                                    FSUB(div_u(FMUL(fc, cu), d.cs4, d.rcs4, d.ok4), fuc))));
+                v = FADD(v, FMUL(FMUL(k.P, w), FADD(div_u(fc, d.cs2, d.rcs2, d.lcs2, d.ok2),
+                                                    FSUB(div_u(FMUL(fc, cu), d.cs4, d.rcs4, d.lcs4, d.ok4), fuc))));
             }
             emit(i, (to_equilibrium || m.out_ext) ? fe : v);
         }
@@ -584,7 +587,7 @@ __device__ __forceinline__ void collide_fixed(const R (&f)[Q], const MomentsT<R>
         // collide.comp:727-745 with :589-629 as written: f + (-(f - feq)/tau) + source
         const Div<R>& d = k.d;
         const R uuh = uuh_of<true>(m.ux, m.uy, m.uz, d);
-        const R fuc = SRC ? div_m(dot_lit(m.Fx, m.Fy, m.Fz, m.ux, m.uy, m.uz), d.cs2, d.rcs2) : R(0);
+        const R fuc = SRC ? div_m(dot_lit(m.Fx, m.Fy, m.Fz, m.ux, m.uy, m.uz), d.cs2, d.rcs2, d.lcs2) : R(0);
 #pragma unroll
         for (int i = 0; i < Q; i++) {
             const Dir c = L::c(i);
@@ -592,11 +595,11 @@ __device__ __forceinline__ void collide_fixed(const R (&f)[Q], const MomentsT<R>
             const R cu = cdot_rt(c, m.ux, m.uy, m.uz);
             const R fe = feq_lit<true>(FMUL(w, m.rho), cu, d, uuh);
             if (EXT) { emit(i, fe); continue; }
-            R v = FSUB(f[i], div_m(FSUB(f[i], fe), k.tau, k.Rtau));
+            R v = FSUB(f[i], div_m(FSUB(f[i], fe), k.tau, k.Rtau, k.ltau));
             if (SRC) {
                 const R fc = cdot_rt(c, m.Fx, m.Fy, m.Fz);
-                v = FADD(v, FMUL(FMUL(k.P, w), FADD(div_m(fc, d.cs2, d.rcs2),
-                                                    FSUB(div_m(FMUL(fc, cu), d.cs4, d.rcs4), fuc))));
+                v = FADD(v, FMUL(FMUL(k.P, w), FADD(div_m(fc, d.cs2, d.rcs2, d.lcs2),
+                                                    FSUB(div_m(FMUL(fc, cu), d.cs4, d.rcs4, d.lcs4), fuc))));
             }
             emit(i, v);
         }
@@ -947,10 +950,10 @@ __device__ __forceinline__ float thermal_buoyancy(const StepParams& p, uint32_t 
 // thermal BGK towards g_eq(T, u) as written (collide.comp:771-782, :634-651,
 // :668-670): g + (-(g - g_eq)/tau_T)
 __device__ __forceinline__ float thermal_relax(const StepParams& p, float g, float geq) {
-    return FSUB(g, div_m(FSUB(g, geq), p.tau_t, p.Rtau_t));
+    return FSUB(g, div_m(FSUB(g, geq), p.tau_t, p.Rtau_t, p.Ltau_t));
 }
 __device__ __forceinline__ Div<float> div_of(const StepParams& p) {
-    return Div<float>{p.cs2, p.R2, p.cs4, p.R4, (p.div_ok & 1u) != 0, (p.div_ok & 2u) != 0};
+    return Div<float>{p.cs2, p.R2, p.L2, p.cs4, p.R4, p.L4, (p.div_ok & 1u) != 0, (p.div_ok & 2u) != 0};
 }
 template <int Q>
 __device__ __forceinline__ void thermal_collide(const StepParams& p, uint32_t n, const Moments& m, float temperature) {
@@ -997,6 +1000,7 @@ __device__ __forceinline__ void thermal_collide_r(const StepParams& p, uint32_t 
     const R* src = th_src_of(p, R(0));
     R* tgt = th_tgt_of(p, R(0));
     const R rtau_t = sizeof(R) == 4 ? R(p.Rtau_t) : R(0);
+    const R ltau_t = sizeof(R) == 4 ? R(p.Ltau_t) : R(0);
     const bool ok_t = sizeof(R) == 4 && (p.div_ok & 8u) != 0;
 #pragma unroll
     for (int i = 0; i < QT; i++) {
@@ -1005,7 +1009,7 @@ __device__ __forceinline__ void thermal_collide_r(const StepParams& p, uint32_t 
         const R cu = cdot_rt(c, m.ux, m.uy, m.uz);
         const R geq = feq_lit<false>(FMUL(w, temperature), cu, k.d, uuh);
         const R g = __ldg(src + (uint64_t)i * p.stride + n);
-        tgt[(uint64_t)i * p.stride + n] = FSUB(g, div_u(FSUB(g, geq), tau_t, rtau_t, ok_t));
+        tgt[(uint64_t)i * p.stride + n] = FSUB(g, div_u(FSUB(g, geq), tau_t, rtau_t, ltau_t, ok_t));
     }
 }
 

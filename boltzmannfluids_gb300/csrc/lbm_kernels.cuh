@@ -344,8 +344,10 @@ __device__ __forceinline__ void velocity_and_limit(const float (&f)[Q], Moments&
 // decided on the literal u.u (float: against the square-root thresholds,
 // which decides exactly as sqrt(u.u) > limit; double: on the square root);
 // a limited u becomes (u/|u|) * limit.  Forced: the force term is compiled in
-// (adding F/(2 rho) = +0 would change nothing but the sign of a zero).
-template <int Q, class R>
+// (adding F/(2 rho) = +0 would change nothing but the sign of a zero).  ZF:
+// zero force components skip their division (bit for bit the same; kernels
+// whose forces are rarely exactly zero, Shan-Chen's, leave the test out).
+template <int Q, bool ZF = true, class R>
 __device__ __forceinline__ void velocity_literal(const R (&f)[Q], MomentsT<R>& m, bool forced, R vlim, R t_lim,
                                                  R t_ext) {
     using L = Lattice<Q>;
@@ -363,10 +365,15 @@ __device__ __forceinline__ void velocity_literal(const R (&f)[Q], MomentsT<R>& m
     m.uy = FDIV(jy, m.rho);
     m.uz = FDIV(jz, m.rho);
     if (forced) {
+        // d2 >= 0.02 (the clamped density) or NaN: a zero force component's
+        // quotient is that signed zero, so it is added without the division,
+        // whose slow path takes zero dividends (a force along one axis leaves
+        // two components zero in every cell); with d2 NaN, u is NaN already
         const R d2 = FMUL(R(2), m.rho);
-        m.ux = FADD(m.ux, FDIV(m.Fx, d2));
-        m.uy = FADD(m.uy, FDIV(m.Fy, d2));
-        m.uz = FADD(m.uz, FDIV(m.Fz, d2));
+        auto half_f = [&](R F) -> R { return (ZF && F == R(0)) ? F : FDIV(F, d2); };
+        m.ux = FADD(m.ux, half_f(m.Fx));
+        m.uy = FADD(m.uy, half_f(m.Fy));
+        m.uz = FADD(m.uz, half_f(m.Fz));
     }
     const R uu = dot_lit(m.ux, m.uy, m.uz, m.ux, m.uy, m.uz);
     bool lim;
@@ -1175,9 +1182,9 @@ __device__ __forceinline__ CellSumT<typename Codec<ST>::R> fast_cell(const StepP
         static_assert(FORCED, "thermal flow runs with the source term on");
         temperature = thermal_buoyancy_of<Q>(th, p.beta, m);
     }
-    if constexpr (F64) velocity_literal<Q>(f, m, FORCED, p.k64.vlim, p.k64.vlim, p.k64.vlim_ext);
+    if constexpr (F64) velocity_literal<Q, !MP>(f, m, FORCED, p.k64.vlim, p.k64.vlim, p.k64.vlim_ext);
     else if constexpr (C::SHIFTED) velocity_and_limit<Q, SCE>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
-    else velocity_literal<Q>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
+    else velocity_literal<Q, !MP>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
     if (p.flags & F_UPDATE) {
         const Coef<R> k = coef_of(p, R(0));
         // 16-bit multiphase flow: mass-conserving rounding (collided_sum);
@@ -1372,7 +1379,7 @@ __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, i
             psi_self = sc_apply(p.G, m, sc_pair[half]);
         }
         if constexpr (C::SHIFTED) velocity_and_limit<Q, SCE>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
-        else velocity_literal<Q>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
+        else velocity_literal<Q, !MP>(f, m, FORCED, p.vlim, p.t_lim, p.t_ext);
         // multiphase: the mass-conserving rounding of the one-cell kernel
         // (collided_sum; rest is T less the stored values emitted so far)
         float rest = 0.f;

@@ -1473,7 +1473,8 @@ __device__ __forceinline__ void fast2_cells(const StepParams& p, int x, int y, i
 #endif
 // 64 registers (4 blocks of 256 per SM): a thread holds both cells' loads; a few
 // TRT and forced variants spill a handful of words, which measured cheaper than
-// the latency of running at 3 blocks
+// the latency of running at 3 blocks (Shan-Chen 256^3 at 3 blocks, 80 registers
+// and no spills: fp16s 60.2k / fp16c 59.2k MLUPs against 61.8k / 61.6k)
 #ifndef BF_FAST2_MP_MIN_BLOCKS
 #define BF_FAST2_MP_MIN_BLOCKS BF_FAST2_MIN_BLOCKS
 #endif

@@ -112,6 +112,32 @@ def test_shan_chen_16bit_clamped_and_extreme_cells_match_oracle(storage, two_cel
     assert np.array_equal(s.get_populations(), o.lattice().astype(np.float32))
 
 
+@pytest.mark.parametrize("storage,collision,tau", [(bf.FloatingPointAccuracy.fp16s, 0, 1.0),
+                                                   (bf.FloatingPointAccuracy.fp16c, 1, 0.8)])
+def test_shan_chen_16bit_with_objects_matches_oracle(storage, collision, tau, product_lib):
+    """16-bit Shan-Chen with a velocity inlet and a density outlet (equilibrium
+    objects: the rounding's target is the prescribed density's mass) and a
+    solid obstacle under bounce-back, through the generic step, against the
+    oracle, bit for bit."""
+    nx, ny, nz = 24, 12, 10
+    ids = np.zeros((nz, ny, nx), np.uint32)
+    ids[:, :, 0] = 1
+    ids[:, :, -1] = 2
+    z, y, x = np.mgrid[0:nz, 0:ny, 0:nx]
+    ids[(x - 9) ** 2 + (y - 6) ** 2 + (z - 5) ** 2 < 6] = 3
+    objs = {1: dict(kind=1), 2: dict(kind=2), 3: dict()}
+    n = nx * ny * nz
+    rng = np.random.default_rng(36)
+    rho = (0.69 + 0.01 * rng.uniform(-1, 1, n)).astype(np.float32)
+    u = np.zeros((n, 3), np.float32)
+    u[:, 0] = 0.02
+    s, o = make_pair((nx, ny, nz), tau, bf.VelocitySet.D3Q19, density=rho, velocity=u, ids=ids.reshape(-1),
+                     objects=objs, periodic=(False, True, True), boundary_mode=1, collision=collision,
+                     storage=storage, multiphase=True, G=-5.0, esoteric=True)
+    fluid = ids.reshape(-1) != 3
+    step_and_compare(s, o, [1, 2, 3, 8, 17], mask=fluid)
+
+
 def test_two_cell_shan_chen_equals_one_cell(monkeypatch, product_lib):
     res = (64, 12, 10)
     n = res[0] * res[1] * res[2]

@@ -147,3 +147,22 @@ def test_shan_chen_conserves_mass_and_separates():
     vd, _ = o.fields()
     assert abs(o.lattice().sum() - m0) < 1e-9 * m0
     assert vd[:, 3].max() - vd[:, 3].min() > 0.1  # spinodal decomposition started
+
+
+@pytest.mark.parametrize("res,storage", [((24, 24, 24), 2), ((48, 48, 1), 3)])
+def test_shan_chen_16bit_rounding_conserves_mass(res, storage):
+    """16-bit storage (2 fp16s, 3 fp16c) of multiphase flow stores each
+    cell's last population as the rounding of the cell's mass less the
+    others' stored values, so the mass stays within ~1e-6 over 400 steps of
+    spinodal decomposition (rounded independently, the populations of a
+    phase-separated flow gain ~1e-2 over 2000 steps at 48^3)."""
+    n = res[0] * res[1] * res[2]
+    rng = np.random.default_rng(4)
+    rho = (0.69 + 0.01 * rng.uniform(-1, 1, n)).astype(np.float32)
+    o = Oracle(res, 1.0, density=rho, velocity_set=4 if res[2] > 1 else 2, esoteric=True, multiphase=True,
+               G=-5.0, storage=storage)
+    m0 = o.reduce()[0]
+    o.iterate(400)
+    vd, _ = o.fields()
+    assert abs(o.reduce()[0] - m0) < 1e-5 * m0
+    assert vd[:, 3].max() - vd[:, 3].min() > 1.0  # the phases separated
